@@ -1,0 +1,324 @@
+"""Benchmark of the usx imaging path on one GB300.
+
+Workload (the headline configuration): 128-element 5 MHz linear probe, 75
+plane waves at -16..16 deg, 100,000-scatterer seeded speckle phantom with three
+2-4 mm cysts, 60 mm depth (2073 samples at 20 MHz), IQ (75, 128, 2073)
+complex64 beamformed onto a 512 x 1024 grid with minimum variance (subarray
+64, diagonal loading tr(R)/(100 L), range averaging +/-2, f-number 1.5).
+
+A step is one frame. `value` is frames/s with the IQ resident in HBM (159 MB,
+larger than the 129 MB L2, so no flush is needed between steps); `e2e` is the
+same metric through the public API (`usx.ImagingPipeline.process_frame` on a
+host RF ChannelData: host-to-device copy of the RF, demodulation, beamforming,
+device-to-host copy of the frame). The phantom is simulated on the GPU by the
+project's own simulator at start-up (synthetic data; no dataset is used).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's own CPU implementation of the same
+beamformer (the reference library built from its sources where present, else
+the CPU oracle port) on all host cores over a bounded sample of lines.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "ultrasound-engine_gb300"
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(PKG / "python"))
+
+METRIC = "frames/s, 128ch 75-PW 512×1024: learned vs plain MV on 1 GB300 at ΔgCNR≤0.01"
+N_EL, N_TX, N_SMP = 128, 75, 2073
+N0, N1 = 512, 1024
+FS, F0, C0 = 20e6, 5e6, 1540.0
+MV_KW = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01, mv_range_average=2)
+CYSTS = ((-0.010, 0.025, 0.002), (0.0, 0.035, 0.003), (0.010, 0.045, 0.004))
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def workload_setup():
+    """Probe, acquisition, transmits, grid and phantom of the headline workload (host objects)."""
+    import usx
+    probe = usx.Probe()
+    probe.n_elements, probe.pitch, probe.element_width = N_EL, 300e-6, 270e-6
+    probe.center_frequency, probe.bandwidth = F0, 0.6
+    medium = usx.Medium()
+    acq = usx.presets.acquisition(probe, depth=0.06, medium=medium, samples_per_wavelength=FS / F0)
+    assert acq.n_samples == N_SMP
+    cfg = usx.SimulatorConfig()
+    sim = usx.Simulator(probe, medium, acq, cfg)
+    txs = sim.make_plane_waves(usx.angles_deg(-16, 16, N_TX))
+    half = 0.5 * probe.aperture_width()
+    ph = usx.Phantom.speckle_box(-half * 1.1, half * 1.1, 0.004, 0.062, 0.0, 100_000, 2026)
+    for x, z, r in CYSTS:
+        ph.scale_amplitude_in_circle(usx.Vec3(x, 0.0, z), r, 0.0)
+    grid = usx.grid_for(probe, 0.005, 0.060, N0, N1)
+    return usx, probe, medium, acq, sim, txs, ph, grid
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([v.strip() for v in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def mv_flops_per_frame(grid_pts: np.ndarray, cfg: dict) -> float:
+    """Algorithmic FLOPs of minimum variance over the grid: covariance
+    4 L^2 n_snap + Cholesky (4/3) L^3 + solves and apply 16 L^2 per pixel, with
+    L and n_snap from the reference's clamp rule and the pixel's aperture."""
+    z = grid_pts[:, 2]
+    x = grid_pts[:, 0]
+    ex = (np.arange(N_EL) - 0.5 * (N_EL - 1)) * 300e-6
+    half = 0.5 * z / cfg["f_number"]
+    n_act = (np.abs(ex[None, :] - x[:, None]) < half[:, None]).sum(1)
+    L = np.clip(np.minimum(cfg["mv_subarray"], np.maximum(2, n_act // 2)), 2, None).astype(np.float64)
+    n_snap = (2 * cfg["mv_range_average"] + 1) * (n_act - L + 1)
+    ok = n_act >= 4
+    f = 4 * L ** 2 * n_snap + (4.0 / 3.0) * L ** 3 + 16 * L ** 2
+    return float(np.sum(f[ok]))
+
+
+def cpu_baseline_mv(iq: np.ndarray, pts: np.ndarray, txs, probe, acq, lines: int, threads: int):
+    """Time the CPU minimum variance on `lines` lateral lines; returns (s, kind)."""
+    from oracle import oracle as O
+    pr = O.probe(N_EL, probe.pitch, probe.element_width, 5e-3, F0, probe.bandwidth)
+    oacq = O.acquisition(fs=acq.sampling_frequency, n_samples=acq.n_samples, t0=acq.t0, prf=acq.prf)
+    tx = O.TxSet(np.ones(len(txs), np.int32), np.asarray([t.angle for t in txs], np.float32),
+                 np.tile([0, 0, 0.03], (len(txs), 1)).astype(np.float32), np.zeros((len(txs), 3), np.float32),
+                 np.asarray([t.delays for t in txs], np.float32), np.asarray([t.apodization for t in txs], np.float32))
+    cd = O.channel_desc(pr, O.medium(), oacq, tx, is_iq=True, fdem=F0)
+    idx = np.linspace(0, N0 - 1, lines).astype(int)
+    sub = pts.reshape(N0, N1, 3)[idx].reshape(-1, 3)
+    if O.REF_SO.exists():
+        ref = O.RefLib()
+        kind = "reference"
+        axis1 = sub.reshape(lines, N1, 3)[0, :, 2]
+        t = time.perf_counter()
+        ref.beamform(cd, iq, 0, sub[::N1, 0], axis1, (0, 0, 0), sub, O.bf_config(**MV_KW))
+        dt = time.perf_counter() - t
+    else:
+        orc = O.Lib("oracle")
+        orc.set_threads(threads)
+        kind = "port"
+        t = time.perf_counter()
+        orc.beamform(cd, iq, sub, lines, N1, O.bf_config(**MV_KW))
+        dt = time.perf_counter() - t
+    return dt, kind
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    threads = int(os.environ["OMP_NUM_THREADS"])
+    usx, probe, medium, acq, sim, txs, ph, grid = workload_setup()
+    rng = np.random.default_rng(1)
+    # The CPU path's cost does not depend on the sample values; random IQ of the workload's shape.
+    iq = (rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)
+          + 1j * rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)).astype(np.complex64)
+    pts = np.asarray(grid.points)
+    lines = 2
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, kind = cpu_baseline_mv(iq, pts, txs, probe, acq, lines, threads)
+        if i >= args.warmup:
+            times.append(dt)
+    sec_per_frame = float(np.mean(times)) * N0 / lines
+    v = 1.0 / sec_per_frame
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "mv_l64_75pw_512x1024", "combiner": "mv"},
+            "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": kind,
+                             "sample": f"{lines} of {N0} lateral lines per step, scaled to a frame"},
+            "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args) -> None:
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    os.environ["USX_DEVICE"] = str(local)
+    from usx import capi
+
+    usx, probe, medium, acq, sim, txs, ph, grid = workload_setup()
+    # Synthetic acquisition through the public API (GPU simulator + host copy).
+    raw = sim.simulate(txs, ph)
+    rf_host = np.asarray(raw.rf)
+    ctx = capi.Context(local)
+    tx = [dict(type=1, angle=t.angle, delays=t.delays, apodization=t.apodization) for t in txs]
+    ch_rf = capi.Channel(capi.Probe(N_EL, probe.pitch, probe.element_width, probe.elevation_height, F0,
+                                    probe.bandwidth),
+                         capi.Medium(medium.speed_of_sound, medium.attenuation, medium.density),
+                         capi.Acquisition(acq.sampling_frequency, acq.n_samples, acq.t0, acq.prf), tx)
+    ch_iq = capi.Channel(ch_rf.desc.probe, ch_rf.desc.medium, ch_rf.desc.acq, tx, is_iq=True, fdem=F0)
+    d_rf = torch.from_numpy(rf_host).cuda()
+    d_iq = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    ctx.demodulate(ch_rf, capi.demod_config(), d_rf.data_ptr(), d_iq.data_ptr())
+    ctx.synchronize()
+    pts = np.asarray(grid.points)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), pts)
+    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
+    frame = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        plan.execute(d_iq.data_ptr(), frame.data_ptr())
+    ctx.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    capi.profile(ctx, True)
+    capi.profile_reset(ctx)
+    with ClockSampler(local) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.execute(d_iq.data_ptr(), frame.data_ptr())
+        ev1.record(stream)
+        ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    prof = capi.profile_read(ctx)
+    capi.profile(ctx, False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * args.steps / (ms / 1e3)
+
+    # Dominant kernel and its roofline (algorithmic FLOPs over live device time).
+    peaks = load_peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 0))
+    launches_in_region = sum(n for _, n in prof.values())
+    mv_flops = mv_flops_per_frame(pts, MV_KW)
+    kname, (kms, kn) = top
+    achieved_tflops = mv_flops / (kms / kn / 1e3) / 1e12 if kn and kname == "mv_kernel" else None
+    roofline = {"kernel": kname, "bound": "tensor", "achieved": achieved_tflops,
+                "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
+                "frac": (achieved_tflops / peaks["bf16_tflops_sustained"]) if achieved_tflops else None,
+                "traffic": None, "peak_source": peaks["source"],
+                "kernels_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in prof.items()},
+                "algorithmic_gflop_per_frame": mv_flops / 1e9}
+
+    # End to end through the public API on host RF.
+    pcfg = usx.PipelineConfig()
+    b = pcfg.beamformer
+    b.f_number, b.combiner, b.mv_subarray = 1.5, usx.Combiner.MV, 64
+    b.mv_diagonal_loading, b.mv_range_average = 0.01, 2
+    pcfg.beamformer = b
+    pipe = usx.ImagingPipeline(grid, pcfg)
+    pipe.process_frame(raw)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        fr = pipe.process_frame(raw)
+    e2e_s = (time.perf_counter() - t) / e2e_steps
+    e2e = {"value": world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": int(rf_host.nbytes),
+           "d2h_bytes_per_step": int(N0 * N1 * 8), "api": "usx.ImagingPipeline.process_frame(RF ChannelData)"}
+
+    if rank == 0:
+        cpu = None
+        if world == 1:
+            threads = os.cpu_count() or 1
+            iq_host = d_iq.cpu().numpy()
+            dt, kind = cpu_baseline_mv(iq_host, pts, txs, probe, acq, 2, threads)
+            cpu = {"value": 1.0 / (dt * N0 / 2), "unit": "frames/s", "cores": threads, "kind": kind,
+                   "sample": f"2 of {N0} lateral lines, scaled to a frame"}
+        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-simulated 100k-scatterer cyst phantom)",
+                "config": {"workload": "mv_l64_75pw_512x1024", "combiner": "mv (plain, fp32)", "n_tx": N_TX,
+                           "n_ch": N_EL, "grid": [N0, N1], "iq_bytes": int(d_iq.numel() * 8),
+                           "l2": "inputs larger than L2 (159 MB IQ), no flush"},
+                "gpu_launches": launches_in_region, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks.summary()}
+        print(json.dumps(line))
+    plan.close()
+    ctx.close()
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

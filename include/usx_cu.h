@@ -1,0 +1,202 @@
+/* usx_cu.h — C-ABI of the GB300 (sm_103a) imaging path.
+ *
+ * This is the boundary the host layer (the C++ classes behind the `_usx`
+ * module, or any FFI: ctypes, cgo, JNI) calls. It takes plain pointers, sizes
+ * and the POD descriptors of usx_types.h; no C++ or torch types cross it.
+ *
+ * Conventions
+ *  - Every entry point returns USX_OK (0) or a USX_ERR_* code; the message of
+ *    the last failure on the calling thread is usx_cu_last_error(). Invalid
+ *    arguments map to USX_ERR_INVALID, the way the reference throws
+ *    std::invalid_argument (types.cpp:8-124, beamformer.cpp:218-225).
+ *  - Sample and image buffers are DEVICE pointers on the context's device;
+ *    descriptors (transmits, grid axes) are HOST memory read during the call.
+ *  - Work is enqueued on the context's stream; calls return without waiting
+ *    unless they must read a device result back (documented per function).
+ *  - Complex data is interleaved float (re, im), i.e. std::complex<float>.
+ *  - Layouts follow the reference: channel data [event][channel][sample],
+ *    frames [axis0][axis1] with axis1 fastest, grid points [pixel][x,y,z].
+ */
+#ifndef USX_CU_H
+#define USX_CU_H
+
+#include "usx_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  USX_OK = 0,
+  USX_ERR_INVALID = 1,      /* bad argument (reference: std::invalid_argument) */
+  USX_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+  USX_ERR_NOMEM = 3,        /* device allocation failed */
+  USX_ERR_NUMERIC = 4,      /* a kernel reported a numeric failure */
+  USX_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  USX_ERR_UNSUPPORTED = 6   /* configuration outside what the kernels implement */
+};
+
+#define USX_CU_ABI_VERSION 1
+
+typedef struct usx_ctx usx_ctx;
+typedef struct usx_bf_plan usx_bf_plan;
+
+/* ----------------------------------------------------------- context, memory */
+
+int usx_cu_abi_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* usx_cu_last_error(void);
+
+/* One context per device and host thread of use. The context owns a stream
+ * (or adopts `stream` if non-NULL; a cudaStream_t) and a grow-only scratch
+ * arena. */
+int usx_cu_ctx_create(int device, void* stream, usx_ctx** out);
+int usx_cu_ctx_destroy(usx_ctx* ctx);
+void* usx_cu_ctx_stream(usx_ctx* ctx);
+int usx_cu_ctx_set_stream(usx_ctx* ctx, void* stream);
+int usx_cu_synchronize(usx_ctx* ctx);
+
+int usx_cu_malloc(usx_ctx* ctx, size_t bytes, void** dev);
+int usx_cu_free(usx_ctx* ctx, void* dev);
+/* Page-locked host memory, for host buffers that are copied every frame. */
+int usx_cu_host_alloc(usx_ctx* ctx, size_t bytes, void** host);
+int usx_cu_host_free(usx_ctx* ctx, void* host);
+/* Copies on the context's stream; *_sync variants wait for completion. */
+int usx_cu_memcpy_h2d(usx_ctx* ctx, void* dst_dev, const void* src_host, size_t bytes);
+int usx_cu_memcpy_d2h(usx_ctx* ctx, void* dst_host, const void* src_dev, size_t bytes);
+int usx_cu_memcpy_d2d(usx_ctx* ctx, void* dst_dev, const void* src_dev, size_t bytes);
+int usx_cu_memset(usx_ctx* ctx, void* dst_dev, int value, size_t bytes);
+
+/* Per-kernel timing with CUDA events recorded on the context's stream around
+ * every launch (off by default; no counterpart in the reference, whose only
+ * timing is PipelineStats' wall clock, pipeline.cpp:25-46). profile_read
+ * returns the index-th distinct kernel name with its summed device time and
+ * launch count, and USX_ERR_INVALID past the last one. */
+int usx_cu_profile_enable(usx_ctx* ctx, int on);
+int usx_cu_profile_reset(usx_ctx* ctx);
+int usx_cu_profile_read(usx_ctx* ctx, int index, char* name, int name_cap, double* total_ms,
+                        int64_t* launches);
+
+/* ------------------------------------------------------------------ simulator */
+
+/* Simulator::simulate (reference simulator.cpp:213-419): point scatterers ->
+ * RF [n_events][n_elements][n_samples] float, overwritten. `scat` is a device
+ * array of n_scat usx_scatterer. `noise_z` is NULL (no receive noise) or a
+ * device array of n_events*n_elements*n_samples standard normals, the draws of
+ * std::normal_distribution<float> seeded noise_seed+event (simulator.cpp:
+ * 406-415); each event adds z * peak * 10^(noise_db/20). `stats` (host, may be
+ * NULL) receives {scatterer-element-samples accumulated, flops} of the call
+ * and forces a synchronisation when given. */
+int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd, const usx_simulator_config* cfg,
+                    const usx_scatterer* scat, int64_t n_scat, const float* noise_z, float* rf,
+                    double* stats);
+
+/* Simulator::pulse (simulator.cpp:140-154), computed on the host: writes up to
+ * `cap` taps to `out` (host) and returns the tap count via *n_taps. */
+int usx_cu_pulse(const usx_probe* probe, const usx_acquisition* acq,
+                 const usx_simulator_config* cfg, float* out, int cap, int* n_taps,
+                 float* half_duration);
+
+/* ---------------------------------------------------------------- demodulator */
+
+/* demodulate (reference demodulate.cpp:36-121): RF [E][C][N] float ->
+ * IQ [E][C][ceil(N/dec)] complex. *out_fdem receives the demodulation
+ * frequency used (config value, else the probe centre frequency). */
+int usx_cu_demodulate(usx_ctx* ctx, const usx_channel_desc* cd, const usx_demod_config* cfg,
+                      const float* rf, float* iq, float* out_fdem);
+
+/* design_lowpass (demodulate.cpp:13-34), host-side; returns taps via *n_taps. */
+int usx_cu_design_lowpass(int n_taps, float normalized_cutoff, float* h, int cap, int* n_out);
+
+/* ----------------------------------------------------------------- beamformer */
+
+/* A beamforming plan: the channel metadata, grid and config of
+ * Beamformer::beamform (reference beamformer.cpp:297-549) frozen on the device
+ * (transmit tables, pixel positions), so that executing it only launches
+ * kernels and can be captured in a CUDA graph. `points_host` is the grid's
+ * point list [n_axis0*n_axis1][3] (host memory, copied). */
+int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_grid_desc* grid,
+                          const float* points_host, const usx_beamformer_config* cfg,
+                          int event_begin, int event_end, usx_bf_plan** out);
+int usx_cu_bf_plan_destroy(usx_bf_plan* plan);
+/* Device bytes of scratch one execution of the plan needs (MV snapshots). */
+int usx_cu_bf_plan_workspace(const usx_bf_plan* plan, size_t* bytes);
+/* Beamform one acquisition: `data` is RF float or IQ complex as the plan's
+ * channel descriptor says; `frame` receives n_axis0*n_axis1 complex. */
+int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame);
+/* Beamform `n_frames` acquisitions laid out back to back (strides in
+ * elements of the data type: floats for RF, complex for IQ; frames in complex)
+ * in one launch sequence. */
+int usx_cu_bf_execute_batch(usx_bf_plan* plan, int n_frames, const void* data,
+                            int64_t data_stride, float* frames, int64_t frame_stride);
+
+/* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one
+ * launch: frame f uses the plan's events [first + f*events_per_frame,
+ * first + (f+1)*events_per_frame) of the single acquisition `data`; frames
+ * are written frame_stride complex apart. This is how a Doppler ensemble is
+ * formed. */
+int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_frames,
+                               const void* data, float* frames, int64_t frame_stride);
+
+/* One-shot convenience: plan, execute, destroy (not graph-capturable). */
+int usx_cu_beamform(usx_ctx* ctx, const usx_channel_desc* cd, const void* data,
+                    const usx_grid_desc* grid, const float* points_host,
+                    const usx_beamformer_config* cfg, int event_begin, int event_end,
+                    float* frame);
+
+/* ------------------------------------------------------------- post-process */
+
+/* envelope (postprocess.cpp:67-82): |z| when fdem > 0, else the modulus of
+ * the analytic signal of the real part along axis 1 (radix-2 FFT Hilbert). */
+int usx_cu_envelope(usx_ctx* ctx, const float* frame, int n0, int n1, float fdem, float* env);
+/* apply_tgc (postprocess.cpp:84-98); points device [n0*n1][3]. */
+int usx_cu_apply_tgc(usx_ctx* ctx, const float* env, int n0, int n1, const float* points,
+                     float attenuation_db_cm_mhz, float center_frequency_hz, float* out);
+/* log_compress (postprocess.cpp:100-117); reference <= 0 uses the maximum
+ * (found on the device). */
+int usx_cu_log_compress(usx_ctx* ctx, const float* env, int64_t n, float dynamic_range_db,
+                        float gain_db, float reference, float* out);
+/* Maximum of a float array (device) into *out_host (synchronises). */
+int usx_cu_max(usx_ctx* ctx, const float* x, int64_t n, float* out_host);
+/* scan_convert (postprocess.cpp:119-178). `grid` gives type, axes (host) and
+ * apex; points device [n0*n1][3]; pixels device [height][width];
+ * extent (host) receives x_min, x_max, z_min, z_max. */
+int usx_cu_scan_convert(usx_ctx* ctx, const float* image, const usx_grid_desc* grid,
+                        const float* points_host, int width, int height, float fill,
+                        float* pixels, float* extent);
+
+/* ------------------------------------------------------- Doppler / strain */
+
+/* apply_wall_filter (doppler.cpp:51-75): ensemble [n_frames][n_pix] complex. */
+int usx_cu_wall_filter(usx_ctx* ctx, const float* ens, int n_frames, int64_t n_pix, int type,
+                       int order, float* out);
+/* color_flow (doppler.cpp:77-176). Outputs device [n0*n1]; *nyquist (host). */
+int usx_cu_color_flow(usx_ctx* ctx, const float* ens, int n_frames, int n0, int n1,
+                      const float* axis1_host, float fdem, float prf, float speed_of_sound,
+                      const usx_doppler_config* cfg, float* velocity, float* power,
+                      float* variance, uint8_t* valid, float* nyquist);
+/* Many colour-flow ensembles of uneven length in one launch sequence:
+ * ensemble e has n_frames[e] frames starting at frame offset frame_offset[e]
+ * of `ens` (all the same grid); outputs are [n_ens][n0*n1]. */
+int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int* n_frames_host,
+                            const int64_t* frame_offset_host, int n0, int n1,
+                            const float* axis1_host, float fdem, float prf,
+                            float speed_of_sound, const usx_doppler_config* cfg, float* velocity,
+                            float* power, float* variance, uint8_t* valid);
+/* power_doppler (doppler.cpp:178-186). */
+int usx_cu_power_doppler(usx_ctx* ctx, const float* ens, int n_frames, int64_t n_pix, int type,
+                         int order, float* power);
+/* estimate_axial_displacement (doppler.cpp:188-273). */
+int usx_cu_axial_displacement(usx_ctx* ctx, const float* before, const float* after, int n0,
+                              int n1, const float* axis1_host, float fdem, float speed_of_sound,
+                              int kernel_axial, int kernel_lateral, int max_lag, float* axial,
+                              float* correlation);
+/* axial_strain (doppler.cpp:275-305). */
+int usx_cu_axial_strain(usx_ctx* ctx, const float* axial, int n0, int n1,
+                        const float* axis1_host, int fit_length, float* strain);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* USX_CU_H */

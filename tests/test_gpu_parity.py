@@ -1,0 +1,388 @@
+"""CUDA kernels against the reference (golden fixtures) and the CPU oracle,
+called through the C-ABI (libusx_cu.so via usx.capi), device memory from torch.
+
+Tolerances (relative L2 unless stated):
+  FP32 paths (demodulation, DAS/CF/DMAS in every compounding mode, RF
+  beamforming, the simulator, envelope, TGC, log compression, scan conversion,
+  wall filter, power Doppler, displacement, strain):           <= 1e-5
+  minimum variance (FP32 covariance and Cholesky in the reference's order;
+  a Cholesky solve amplifies rounding by the condition number): <= 1e-4
+  colour-flow velocity: equal validity masks except at most 1% of pixels at
+  a gate boundary, velocities where both valid within 1e-4 relative.
+The kernels follow the reference's operation order without FMA contraction,
+so most of these agree to the last ulp of the device's sincosf/cosf/atan2f.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from gold import BF_CASES, rel_l2, sim_setup, txset
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+TOL_MV = 1e-4
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    return t
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from usx import capi as c
+    return c
+
+
+@pytest.fixture(scope="module")
+def ctx(capi, torch):
+    c = capi.Context(0, stream=torch.cuda.current_stream().cuda_stream)
+    yield c
+    c.close()
+
+
+def dev(torch, a):
+    a = np.ascontiguousarray(a)
+    return torch.from_numpy(a).cuda()
+
+
+def host(torch, t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def c_probe(capi, p):
+    return capi.Probe(p.n_elements, p.pitch, p.element_width, p.elevation_height, p.center_frequency, p.bandwidth)
+
+
+def c_channel(capi, pr, med, acq, txs: O.TxSet, is_iq=False, fdem=0.0):
+    tx = [dict(type=int(txs.types[e]), angle=float(txs.angles[e]), focus=txs.focus[e], origin=txs.origin[e],
+               delays=txs.delays[e], apodization=txs.apod[e]) for e in range(len(txs))]
+    return capi.Channel(c_probe(capi, pr), capi.Medium(med.speed_of_sound, med.attenuation, med.density),
+                        capi.Acquisition(acq.sampling_frequency, acq.n_samples, acq.t0, acq.prf), tx, is_iq, fdem)
+
+
+# --------------------------------------------------------------- simulator
+
+def test_simulate_matches_reference(capi, ctx, torch, golden):
+    g = golden("sim")
+    pr, med, acq = sim_setup(g)
+    ch = c_channel(capi, pr, med, acq, txset(g, "pw"))
+    scat = dev(torch, g["scat"])
+    z = dev(torch, g["noise_z"])
+    rf = torch.empty(g["rf"].shape, dtype=torch.float32, device="cuda")
+    stats = ctx.simulate(ch, capi.sim_config(noise_db=-60.0, noise_seed=7), scat.data_ptr(), len(g["scat"]),
+                         z.data_ptr(), rf.data_ptr(), want_stats=True)
+    assert rel_l2(host(torch, rf), g["rf"]) < TOL
+    assert stats[0] > 0
+    ctx.simulate(ch, capi.sim_config(noise_db=-200.0, incident_trim_db=-30.0, enable_motion=0), scat.data_ptr(),
+                 len(g["scat"]), None, rf.data_ptr())
+    assert rel_l2(host(torch, rf), g["rf_quiet"]) < TOL
+
+
+def test_simulate_focused_and_no_diffraction_match_oracle(capi, ctx, torch, golden, oracle):
+    g = golden("sim")
+    b = golden("bf")
+    pr, med, acq = sim_setup(g)
+    for txs, cfg in ((txset(b, "foc"), dict(noise_db=-200.0)),
+                     (txset(g, "pw"), dict(noise_db=-200.0, full_transmit_diffraction=0, apply_attenuation=0)),
+                     (txset(b, "div"), dict(noise_db=-200.0, apply_directivity=0, oversampling=2))):
+        ch = c_channel(capi, pr, med, acq, txs)
+        rf = torch.empty((len(txs), pr.n_elements, acq.n_samples), dtype=torch.float32, device="cuda")
+        ctx.simulate(ch, capi.sim_config(**cfg), dev(torch, g["scat"]).data_ptr(), len(g["scat"]), None, rf.data_ptr())
+        want = oracle.simulate(O.channel_desc(pr, med, acq, txs), O.sim_config(**cfg), g["scat"])
+        assert rel_l2(host(torch, rf), want) < TOL
+
+
+def test_simulate_empty_phantom_and_zero_amplitudes(capi, ctx, torch, golden):
+    g = golden("sim")
+    pr, med, acq = sim_setup(g)
+    ch = c_channel(capi, pr, med, acq, txset(g, "pw"))
+    rf = torch.full(g["rf"].shape, 7.0, dtype=torch.float32, device="cuda")
+    ctx.simulate(ch, capi.sim_config(noise_db=-200.0), 0, 0, None, rf.data_ptr())
+    assert float(host(torch, rf).__abs__().max()) == 0.0
+    scat = g["scat"].copy()
+    scat[:, 3] = 0.0
+    ctx.simulate(ch, capi.sim_config(noise_db=-60.0), dev(torch, scat).data_ptr(), len(scat),
+                 dev(torch, g["noise_z"]).data_ptr(), rf.data_ptr())
+    assert float(np.abs(host(torch, rf)).max()) == 0.0  # zero peak: no noise either
+
+
+# ------------------------------------------------------------- demodulator
+
+@pytest.mark.parametrize("key,kw", [("iq", {}), ("iq_dec2", dict(decimation=2, filter_taps=21, cutoff_fraction=0.45))])
+def test_demodulate_matches_reference(capi, ctx, torch, golden, key, kw):
+    g = golden("sim")
+    pr, med, acq = sim_setup(g)
+    ch = c_channel(capi, pr, med, acq, txset(g, "pw"))
+    want = g[key]
+    iq = torch.empty(want.shape, dtype=torch.complex64, device="cuda")
+    fdem = ctx.demodulate(ch, capi.demod_config(**kw), dev(torch, g["rf"]).data_ptr(), iq.data_ptr())
+    assert fdem == pytest.approx(5e6)
+    assert rel_l2(host(torch, iq), want) < TOL
+
+
+def test_demodulate_rejects_iq_input(capi, ctx, torch, golden):
+    g = golden("sim")
+    pr, med, acq = sim_setup(g)
+    ch = c_channel(capi, pr, med, acq, txset(g, "pw"), is_iq=True, fdem=5e6)
+    buf = torch.empty(16, device="cuda")
+    with pytest.raises(ValueError):
+        ctx.demodulate(ch, capi.demod_config(), buf.data_ptr(), buf.data_ptr())
+
+
+# --------------------------------------------------------------- beamformer
+
+def _bf(capi, ctx, torch, ch, grid, cfg, data, ev_begin=0, ev_end=-1):
+    plan = ctx.plan(ch, grid, cfg, ev_begin, ev_end)
+    out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
+    plan.execute(dev(torch, data).data_ptr(), out.data_ptr())
+    res = host(torch, out)
+    plan.close()
+    return res
+
+
+@pytest.mark.parametrize("name", sorted(BF_CASES))
+def test_beamform_matches_reference(capi, ctx, torch, golden, name):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    out = _bf(capi, ctx, torch, ch, grid, capi.bf_config(**BF_CASES[name]), g["iq"])
+    tol = TOL_MV if name.startswith("mv") else TOL
+    assert rel_l2(out, g[f"bf_{name}"]) < tol
+
+
+def test_beamform_geometries_match_reference(capi, ctx, torch, golden):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    assert rel_l2(_bf(capi, ctx, torch, ch, grid, capi.bf_config(f_number=1.5), g["iq"], 1, 2), g["bf_das_ev1"]) < TOL
+    chr_ = c_channel(capi, pr, med, acq, txset(s, "pw"))
+    assert rel_l2(_bf(capi, ctx, torch, chr_, grid, capi.bf_config(f_number=1.5), s["rf"]), g["bf_rf"]) < TOL
+    chf = c_channel(capi, pr, med, acq, txset(g, "foc"), is_iq=True, fdem=5e6)
+    assert rel_l2(_bf(capi, ctx, torch, chf, grid, capi.bf_config(f_number=1.5, compounding=2), g["foc_iq"]),
+                  g["bf_foc_select"]) < TOL
+    assert rel_l2(_bf(capi, ctx, torch, chf, grid, capi.bf_config(f_number=1.5), g["foc_iq"]), g["bf_foc_coh"]) < TOL
+    chd = c_channel(capi, pr, med, acq, txset(g, "div"), is_iq=True, fdem=5e6)
+    sgrid = capi.Grid(1, g["sax0"], g["sax1"], g["spts"])
+    assert rel_l2(_bf(capi, ctx, torch, chd, sgrid, capi.bf_config(f_number=1.5), g["div_iq"]), g["bf_div_sector"]) < TOL
+    assert rel_l2(_bf(capi, ctx, torch, chd, sgrid, capi.bf_config(f_number=1.5, combiner=2, mv_subarray=12),
+                      g["div_iq"]), g["bf_div_mv"]) < TOL_MV
+
+
+def test_batch_and_sequence_equal_single_frames(capi, ctx, torch, golden):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    for cfg in (capi.bf_config(f_number=1.5), capi.bf_config(f_number=1.5, combiner=2, mv_subarray=8)):
+        ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+        plan = ctx.plan(ch, grid, cfg)
+        iq = g["iq"]
+        stack = np.stack([iq, iq * (0.5 + 0.25j), iq[::-1].copy()])
+        d = dev(torch, stack)
+        n_pix = grid.shape[0] * grid.shape[1]
+        out = torch.empty((3, n_pix), dtype=torch.complex64, device="cuda")
+        plan.execute_batch(3, d.data_ptr(), iq.size, out.data_ptr(), n_pix)
+        got = host(torch, out)
+        for f in range(3):
+            one = torch.empty(n_pix, dtype=torch.complex64, device="cuda")
+            plan.execute(d[f].data_ptr(), one.data_ptr())
+            assert np.array_equal(host(torch, one), got[f])
+        plan.close()
+    # Sequence: each frame beamforms one event; equals beamforming that event alone.
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    plan = ctx.plan(ch, grid, capi.bf_config(f_number=1.5))
+    n_pix = grid.shape[0] * grid.shape[1]
+    out = torch.empty((3, n_pix), dtype=torch.complex64, device="cuda")
+    plan.execute_sequence(1, 3, dev(torch, g["iq"]).data_ptr(), out.data_ptr(), n_pix)
+    got = host(torch, out)
+    assert rel_l2(got[1].reshape(grid.shape), g["bf_das_ev1"]) < TOL
+
+
+def test_beamform_edge_cases(capi, ctx, torch, golden, oracle):
+    """Pixels above the face, outside the record and a 4-element probe (n_active
+    < 4 falls back to DAS in MV); all against the oracle."""
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    txs = txset(s, "pw")
+    n0, n1 = 6, 50
+    ax0 = np.linspace(-0.02, 0.02, n0).astype(np.float32)
+    ax1 = np.linspace(-0.002, 0.05, n1).astype(np.float32)
+    pts = np.stack(np.meshgrid(ax0, [0.0], ax1, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    grid = capi.Grid(0, ax0, ax1, pts)
+    for kw in (dict(), dict(combiner=2, mv_subarray=16), dict(combiner=1, coherence_factor=1)):
+        ch = c_channel(capi, pr, med, acq, txs, is_iq=True, fdem=5e6)
+        got = _bf(capi, ctx, torch, ch, grid, capi.bf_config(**kw), s["iq"])
+        want = oracle.beamform(O.channel_desc(pr, med, acq, txs, is_iq=True, fdem=5e6), s["iq"], pts, n0, n1,
+                               O.bf_config(**kw))
+        assert rel_l2(got, want) < TOL_MV
+    small = O.probe(n_elements=4, pitch=300e-6, element_width=270e-6)
+    iq4 = np.ascontiguousarray(s["iq"][:, :4, :])
+    t4 = O.TxSet(txs.types, txs.angles, txs.focus, txs.origin, txs.delays[:, :4], txs.apod[:, :4])
+    ch = c_channel(capi, small, med, acq, t4, is_iq=True, fdem=5e6)
+    got = _bf(capi, ctx, torch, ch, grid, capi.bf_config(combiner=2), iq4)
+    want = oracle.beamform(O.channel_desc(small, med, acq, t4, is_iq=True, fdem=5e6), iq4, pts, n0, n1,
+                           O.bf_config(combiner=2))
+    assert rel_l2(got, want) < TOL
+
+
+def test_beamform_invalid_config_raises(capi, ctx, golden):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    with pytest.raises(ValueError):
+        ctx.plan(ch, grid, capi.bf_config(f_number=0.0))
+    with pytest.raises(ValueError):
+        ctx.plan(ch, grid, capi.bf_config(mv_subarray=1))
+    bad = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=0.0)
+    with pytest.raises(ValueError):
+        ctx.plan(bad, grid, capi.bf_config())
+
+
+# ------------------------------------------------------------ post-process
+
+def test_postprocess_matches_reference(capi, ctx, torch, golden):
+    g = golden("post")
+    b = golden("bf")
+    n0, n1 = g["frame"].shape
+    env = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    ctx.envelope(dev(torch, g["frame"]).data_ptr(), n0, n1, 5e6, env.data_ptr())
+    assert rel_l2(host(torch, env), g["env_iq"]) < TOL
+    ctx.envelope(dev(torch, g["rf_frame"]).data_ptr(), n0, n1, 0.0, env.data_ptr())
+    assert rel_l2(host(torch, env), g["env_rf"]) < TOL
+    out = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    ctx.apply_tgc(dev(torch, g["env_iq"]).data_ptr(), n0, n1, dev(torch, b["pts"]).data_ptr(), 0.5, 5e6, out.data_ptr())
+    assert rel_l2(host(torch, out), g["tgc"]) < TOL
+    ctx.log_compress(dev(torch, g["tgc"]).data_ptr(), n0 * n1, 50.0, 2.0, -1.0, out.data_ptr())
+    assert rel_l2(host(torch, out), g["log"]) < TOL
+    ctx.log_compress(dev(torch, g["tgc"]).data_ptr(), n0 * n1, 40.0, 0.0, float(g["tgc"].max() * 0.5), out.data_ptr())
+    assert rel_l2(host(torch, out), g["log_ref"]) < TOL
+    sgrid = capi.Grid(1, b["sax0"], b["sax1"], b["spts"])
+    px = torch.empty((40, 50), dtype=torch.float32, device="cuda")
+    ext = ctx.scan_convert(dev(torch, g["sc_img"]).data_ptr(), sgrid, 50, 40, -1.0, px.data_ptr())
+    assert rel_l2(host(torch, px), g["sc_sector"]) < TOL
+    assert np.array_equal(ext, g["sc_sector_ext"])
+    cgrid = capi.Grid(0, b["ax0"], b["ax1"], b["pts"])
+    px = torch.empty((47, 33), dtype=torch.float32, device="cuda")
+    ctx.scan_convert(dev(torch, g["env_iq"]).data_ptr(), cgrid, 33, 47, 0.0, px.data_ptr())
+    assert rel_l2(host(torch, px), g["sc_cart"]) < TOL
+
+
+# ---------------------------------------------------------- Doppler / strain
+
+@pytest.mark.parametrize("key,wt,order", [("w0o1", 0, 1), ("w1o1", 1, 1), ("w1o2", 1, 2), ("w2o0", 2, 0)])
+def test_doppler_matches_reference(capi, ctx, torch, golden, key, wt, order):
+    g = golden("doppler")
+    ens = g["ens"]
+    n, n0, n1 = ens.shape
+    d = dev(torch, ens)
+    out = torch.empty_like(d)
+    ctx.wall_filter(d.data_ptr(), n, n0 * n1, wt, order, out.data_ptr())
+    assert rel_l2(host(torch, out), g[f"wall_{key}"]) < TOL
+    pw = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    ctx.power_doppler(d.data_ptr(), n, n0 * n1, wt, order, pw.data_ptr())
+    assert rel_l2(host(torch, pw), g[f"pd_{key}"]) < TOL
+    vel, pwr, var = (torch.empty((n0, n1), dtype=torch.float32, device="cuda") for _ in range(3))
+    valid = torch.empty((n0, n1), dtype=torch.uint8, device="cuda")
+    nyq = ctx.color_flow(d.data_ptr(), n, n0, n1, g["ax1"], 5e6, 5000.0, 1540.0,
+                         capi.doppler_config(wall_filter=wt, polynomial_order=order),
+                         vel.data_ptr(), pwr.data_ptr(), var.data_ptr(), valid.data_ptr())
+    assert np.float32(nyq) == g[f"cf_nyq_{key}"]
+    v, vd = host(torch, vel), host(torch, valid)
+    assert rel_l2(host(torch, pwr), g[f"cf_pow_{key}"]) < TOL
+    assert np.mean(vd != g[f"cf_valid_{key}"]) <= 0.01
+    both = (vd == 1) & (g[f"cf_valid_{key}"] == 1)
+    assert rel_l2(v[both], g[f"cf_vel_{key}"][both]) < 1e-4
+
+
+def test_color_flow_batch_of_uneven_ensembles(capi, ctx, torch, golden, oracle):
+    g = golden("doppler")
+    ens = g["ens"]
+    n, n0, n1 = ens.shape
+    lens = [4, 10, 6, 2]
+    frames = np.concatenate([ens[:k] for k in lens])
+    offs = np.cumsum([0] + lens[:-1])
+    d = dev(torch, frames)
+    cfg = capi.doppler_config(wall_filter=1, polynomial_order=1)
+    vel, pwr, var = (torch.empty((len(lens), n0, n1), dtype=torch.float32, device="cuda") for _ in range(3))
+    valid = torch.empty((len(lens), n0, n1), dtype=torch.uint8, device="cuda")
+    ctx.color_flow_batch(d.data_ptr(), lens, offs, n0, n1, g["ax1"], 5e6, 5000.0, 1540.0, cfg, vel.data_ptr(),
+                         pwr.data_ptr(), var.data_ptr(), valid.data_ptr())
+    P = host(torch, pwr)
+    for e, k in enumerate(lens):
+        _, p, _, _, _ = oracle.color_flow(ens[:k], g["ax1"], 5e6, 5000.0, 1540.0, O.doppler_config())
+        assert rel_l2(P[e], p) < TOL
+
+
+def test_displacement_and_strain_match_reference(capi, ctx, torch, golden):
+    g = golden("doppler")
+    a, b = g["disp_a"], g["disp_b"]
+    n0, n1 = a.shape
+    ax = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    cr = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    ctx.axial_displacement(dev(torch, a).data_ptr(), dev(torch, b).data_ptr(), n0, n1, g["disp_ax1"], 5e6, 1540.0,
+                           4, 1, 5, ax.data_ptr(), cr.data_ptr())
+    assert rel_l2(host(torch, ax), g["disp_axial"]) < TOL
+    assert rel_l2(host(torch, cr), g["disp_corr"]) < TOL
+    st = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
+    ctx.axial_strain(dev(torch, g["disp_axial"]).data_ptr(), n0, n1, g["disp_ax1"], 9, st.data_ptr())
+    assert rel_l2(host(torch, st), g["strain"]) < TOL
+
+
+# ------------------------------------------------ full-size, size-independent
+
+def test_full_size_das_is_linear_and_matches_oracle_on_lines(capi, ctx, torch, oracle):
+    """75 plane waves, 128 channels, 512 x 1024 pixels: the frame is linear in
+    the IQ data (checked on random inputs), and a sample of lines matches the
+    oracle exactly as at small sizes."""
+    pr = O.probe()
+    med = O.medium()
+    acq = O.acquisition(fs=20e6, n_samples=2073, prf=5000.0)
+    ang = np.deg2rad(np.linspace(-16, 16, 75)).astype(np.float32)
+    n_el = 128
+    ex = ((np.arange(n_el, dtype=np.float32) - np.float32(0.5 * (n_el - 1))) * np.float32(300e-6)).astype(np.float32)
+    delays = (ex[None, :] * np.sin(ang)[:, None] / np.float32(1540.0)).astype(np.float32)
+    apod = np.ones((75, n_el), np.float32)
+    txs = O.TxSet(np.ones(75, np.int32), ang, np.tile([0, 0, 0.03], (75, 1)).astype(np.float32),
+                  np.zeros((75, 3), np.float32), delays, apod)
+    rng = np.random.default_rng(3)
+    shape = (75, n_el, 2073)
+    x = (rng.standard_normal(shape, dtype=np.float32) + 1j * rng.standard_normal(shape, dtype=np.float32)).astype(np.complex64)
+    y = (rng.standard_normal(shape, dtype=np.float32) + 1j * rng.standard_normal(shape, dtype=np.float32)).astype(np.complex64)
+    half = 0.5 * (127 * 300e-6 + 270e-6)
+    ax0 = np.linspace(-half, half, 512).astype(np.float32)
+    ax1 = np.linspace(0.005, 0.060, 1024).astype(np.float32)
+    pts = np.stack(np.meshgrid(ax0, [0.0], ax1, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    ch = c_channel(capi, pr, med, acq, txs, is_iq=True, fdem=5e6)
+    grid = capi.Grid(0, ax0, ax1, pts)
+    plan = ctx.plan(ch, grid, capi.bf_config(f_number=1.5))
+    dx, dy = dev(torch, x), dev(torch, y)
+    fx = torch.empty((512, 1024), dtype=torch.complex64, device="cuda")
+    fy = torch.empty_like(fx)
+    fz = torch.empty_like(fx)
+    plan.execute(dx.data_ptr(), fx.data_ptr())
+    plan.execute(dy.data_ptr(), fy.data_ptr())
+    dz = (2.0 * dx - 0.5j * dy).contiguous()
+    plan.execute(dz.data_ptr(), fz.data_ptr())
+    lin = 2.0 * fx - 0.5j * fy
+    assert rel_l2(host(torch, fz), host(torch, lin)) < 1e-5
+    lines = [0, 100, 255, 511]
+    sub = pts.reshape(512, 1024, 3)[lines].reshape(-1, 3)
+    want = oracle.beamform(O.channel_desc(pr, med, acq, txs, is_iq=True, fdem=5e6), x, sub, len(lines), 1024,
+                           O.bf_config(f_number=1.5))
+    got = host(torch, fx)[lines]
+    assert rel_l2(got, want) < TOL
+    plan.close()

@@ -1,0 +1,669 @@
+// beamform.cu — delay-and-sum with dynamic receive aperture, plane-wave /
+// focused / diverging transmit compounding, and the DAS, DMAS, coherence-factor
+// and minimum-variance combiners (reference beamformer.cpp:297-549).
+//
+// Kernel structure (das_kernel): one thread per pixel, pixels ordered with the
+// depth axis fastest so a warp is 32 consecutive depths of one line; at a fixed
+// (event, channel) its 32 delayed reads fall in one ~45-sample window of the
+// trace, i.e. 2-3 cache lines, so the gather is served by L1/L2 with little
+// waste. Channels are processed in groups of kGroup: for a group the receive
+// geometry (aperture weight, receive delay, receive phasor) is computed once
+// into registers, then every transmit event is visited in order and its
+// geometry (illumination weight, transmit delay, transmit phasor) computed
+// once per group; the kGroup per-channel sums stay in registers. This keeps
+// the reference's summation order exactly — each channel sums its events in
+// ascending order, channels are then combined in ascending order — so DAS,
+// DMAS and CF reproduce the reference C++ bit for bit (to the last ulp of
+// the device's sincosf/cosf), and it lets the non-linear combiners consume one
+// finished channel at a time.
+//
+// Minimum variance exports the compounded per-channel samples Y[pixel][ch]
+// and runs mv_kernel on them (one warp per pixel): spatially smoothed and
+// range-averaged covariance, diagonal loading, Cholesky solve of R w = 1 and
+// the weighted subarray average, in the reference's operation order.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "usx_internal.cuh"
+
+namespace usxcu {
+namespace {
+
+constexpr int kGroup = 8;
+constexpr int kBfThreads = 128;
+constexpr int kMaxL = 64;
+constexpr int kMaxCh = 256;
+constexpr int kMvWarps = 2;
+constexpr int kMaxRangeAvg = 4;
+
+struct BfArgs {
+  const float2* iq;      // IQ path: [ev][ch][smp]
+  const float* rf;       // RF path
+  long data_stride;      // elements between frames of a batch
+  const float* points;   // [pix][3]
+  const TxDev* tx;       // [n_events]
+  float2* out;           // [pix] per frame
+  long out_stride;
+  float2* y_out;         // MV: [frame][pix][n_ch]
+  float* acc_out;        // incoherent MV: per-pixel |out|^2 accumulator
+  int n_ch, n_smp, n_pix, n1;
+  int ev_begin, ev_end;
+  int seq_epf;           // > 0: frame f uses events ev_begin + [f*seq_epf, (f+1)*seq_epf)
+  int pass;              // >= 0: export only event (first event of the frame) + pass
+  float c, fs, t0, fdem, two_pi_f, lambda, pitch, half_nm1;
+  float f_number, tukey_alpha;
+  int rx_window, combiner, compounding, tx_weighting, cf, is_mv;
+  int mv_subarray, mv_range_average;
+  float mv_loading;
+};
+
+__device__ __forceinline__ float elem_x(const BfArgs& a, int ch) {
+  return (static_cast<float>(ch) - a.half_nm1) * a.pitch;
+}
+
+template <bool IQ>
+__global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
+  const int pix = blockIdx.x * kBfThreads + threadIdx.x;
+  if (pix >= a.n_pix) return;
+  const long frame = blockIdx.y;
+  const float px = __ldg(a.points + 3 * pix), py = __ldg(a.points + 3 * pix + 1),
+              pz = __ldg(a.points + 3 * pix + 2);
+  int ev_first = a.ev_begin, ev_last = a.ev_end;
+  if (a.seq_epf > 0) {
+    ev_first = a.ev_begin + static_cast<int>(frame) * a.seq_epf;
+    ev_last = ev_first + a.seq_epf;
+  }
+  if (a.pass >= 0) {
+    ev_first += a.pass;
+    ev_last = ev_first + 1;
+  }
+  const bool incoherent = a.compounding == USX_COMP_INCOHERENT && a.pass < 0;
+  const bool select = a.compounding == USX_COMP_SELECT;
+
+  int best_ev = -1;
+  float best_w = 0.0f;
+  if (select) {
+    for (int ev = ev_first; ev < ev_last; ++ev) {
+      const float tw = tx_sensitivity(a.tx[ev], px, pz, a.lambda, a.pitch);
+      if (tw > best_w) {
+        best_w = tw;
+        best_ev = ev;
+      }
+    }
+  }
+
+  const int n_pass = incoherent ? (ev_last - ev_first) : 1;
+  float inc_acc = 0.0f;
+  cplx result = mk(0.f, 0.f);
+  const float2* iq = IQ ? a.iq + frame * a.data_stride : nullptr;
+  const float* rf = IQ ? nullptr : a.rf + frame * a.data_stride;
+
+  for (int pass = 0; pass < max(1, n_pass); ++pass) {
+    const int ev_lo = incoherent ? ev_first + pass : ev_first;
+    const int ev_hi = incoherent ? ev_lo + 1 : ev_last;
+    cplx das = mk(0.f, 0.f), s = mk(0.f, 0.f), q = mk(0.f, 0.f), coh = mk(0.f, 0.f);
+    float incs = 0.0f;
+    int n_active = 0;
+
+    for (int g = 0; g < a.n_ch; g += kGroup) {
+      float ap[kGroup], rt[kGroup], rc[kGroup], rs[kGroup];
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) {
+        const int ch = g + k;
+        ap[k] = 0.0f;
+        rt[k] = 0.0f;
+        rc[k] = 1.0f;
+        rs[k] = 0.0f;
+        if (ch < a.n_ch) {
+          const float ex = elem_x(a, ch);
+          const float w = aperture_weight(ex, px, pz, a.f_number, a.rx_window, a.tukey_alpha);
+          ap[k] = a.is_mv ? (w > 0.0f ? 1.0f : 0.0f) : w;
+          if (w > 0.0f) {
+            any = true;
+            rt[k] = dist3(ex, 0.0f, 0.0f, px, py, pz) / a.c;
+            if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs[k], &rc[k]);
+          }
+        }
+      }
+      cplx Y[kGroup];
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) Y[k] = mk(0.f, 0.f);
+
+      if (any) {
+        for (int ev = ev_lo; ev < ev_hi; ++ev) {
+          const TxDev& t = a.tx[ev];
+          float tw;
+          if (select) {
+            tw = (best_ev == ev) ? best_w : 0.0f;
+            if (tw > 0.0f) tw = 1.0f;
+          } else if (a.tx_weighting) {
+            tw = tx_sensitivity(t, px, pz, a.lambda, a.pitch);
+          } else {
+            tw = 1.0f;
+          }
+          if (tw <= 0.0f) continue;
+          const float tau = tx_arrival(t, px, py, pz, a.c);
+          float tc = 1.0f, ts = 0.0f;
+          if (a.fdem > 0.0f) sincosf(a.two_pi_f * tau, &ts, &tc);
+          const long trace0 = (static_cast<long>(ev) * a.n_ch + g) * a.n_smp;
+#pragma unroll
+          for (int k = 0; k < kGroup; ++k) {
+            if (ap[k] <= 0.0f) continue;
+            const float idx = (tau + rt[k] - a.t0) * a.fs;
+            const int kk = static_cast<int>(floorf(idx));
+            const float wt = ap[k] * tw;
+            if (IQ) {
+              cplx v = mk(0.f, 0.f);
+              if (kk >= 0 && kk + 1 < a.n_smp) {
+                const float f = idx - static_cast<float>(kk);
+                const float2* tr = iq + trace0 + static_cast<long>(k) * a.n_smp;
+                const float2 s0 = __ldg(tr + kk), s1 = __ldg(tr + kk + 1);
+                const float w0 = 1.0f - f;
+                v = mk(s0.x * w0 + s1.x * f, s0.y * w0 + s1.y * f);
+              }
+              const cplx rot = mk(tc * rc[k] - ts * rs[k], ts * rc[k] + tc * rs[k]);
+              Y[k] = cadd(Y[k], cscale(cmul(v, rot), wt));
+            } else {
+              float v = 0.0f;
+              if (kk >= 0 && kk + 1 < a.n_smp) {
+                const float f = idx - static_cast<float>(kk);
+                const float* tr = rf + trace0 + static_cast<long>(k) * a.n_smp;
+                v = __ldg(tr + kk) * (1.0f - f) + __ldg(tr + kk + 1) * f;
+              }
+              Y[k] = cadd(Y[k], mk(v * wt, 0.0f * wt));
+            }
+          }
+        }
+      }
+
+      // Combine the finished channels of this group in ascending order.
+#pragma unroll
+      for (int k = 0; k < kGroup; ++k) {
+        const int ch = g + k;
+        if (ch >= a.n_ch) break;
+        const bool act = ap[k] > 0.0f;
+        const cplx y = act ? Y[k] : mk(0.f, 0.f);
+        if (a.is_mv) {
+          a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = make_float2(y.re, y.im);
+          continue;
+        }
+        n_active += act ? 1 : 0;
+        if (a.combiner == USX_COMB_DMAS) {
+          const float m = cabsf_(y);
+          if (m > 0.0f) {
+            const cplx v = cdivr(y, sqrtf(m));
+            s = cadd(s, v);
+            q = cadd(q, cmul(v, v));
+          }
+        } else {
+          das = cadd(das, y);
+        }
+        if (a.cf && act) {
+          coh = cadd(coh, y);
+          incs += cnorm(y);
+        }
+      }
+    }
+    if (a.is_mv) continue;
+
+    cplx out;
+    if (n_active == 0) {
+      out = mk(0.f, 0.f);
+      if (incoherent) continue;
+    } else if (a.combiner == USX_COMB_DMAS) {
+      const cplx acc = cscale(csub(cmul(s, s), q), 0.5f);
+      const float norm = 0.5f * fmaxf(1.0f, static_cast<float>(n_active - 1));
+      out = cdivr(acc, norm);
+    } else {
+      out = das;
+    }
+    if (a.cf && n_active > 0)
+      out = cscale(out, (incs > 0.0f) ? cnorm(coh) / (static_cast<float>(n_active) * incs) : 0.0f);
+    if (incoherent)
+      inc_acc += cnorm(out);
+    else
+      result = out;
+  }
+  if (a.is_mv) return;
+  if (incoherent) result = mk(sqrtf(inc_acc), 0.0f);
+  a.out[frame * a.out_stride + pix] = make_float2(result.re, result.im);
+}
+
+// ------------------------------------------------------------------------
+// Minimum variance (reference beamformer.cpp:137-214, Cholesky :47-79).
+//
+// One warp per pixel. Shared memory per warp: the compacted active-channel
+// samples of the pixel and its range neighbours, and the L x L covariance.
+// The covariance entries are spread over the lanes, each entry summed over
+// (range offset, subarray) in the reference's order. The Cholesky follows the
+// reference's row-oriented recurrence; entries on one anti-diagonal i + j are
+// independent and are computed in parallel, each with its inner product in
+// the reference's order, so the factor is bit-identical to a serial one.
+struct MvShared {
+  cplx ys[2 * kMaxRangeAvg + 1][kMaxCh];  // [d + ra][active index]
+  cplx R[kMaxL * kMaxL];
+  cplx w[kMaxL];
+  int act[kMaxCh];
+  int fail;
+};
+
+__global__ void __launch_bounds__(32 * kMvWarps) mv_kernel(const BfArgs a) {
+  extern __shared__ float4 mv_smem_raw[];
+  MvShared* sh_all = reinterpret_cast<MvShared*>(mv_smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  MvShared& S = sh_all[warp];
+  const long gw = static_cast<long>(blockIdx.x) * kMvWarps + warp;
+  if (gw >= a.n_pix) return;
+  const int pix = static_cast<int>(gw);
+  const long frame = blockIdx.y;
+  const int j = pix % a.n1;
+  const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+  const float2* Y = a.y_out + frame * static_cast<long>(a.n_pix) * a.n_ch;
+  const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
+
+  // Active channels of this pixel, compacted in ascending channel order.
+  int n_act = 0;
+  for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+    const int ch = c0 + lane;
+    bool act = false;
+    if (ch < a.n_ch)
+      act = aperture_weight(elem_x(a, ch), px, pz, a.f_number, a.rx_window, a.tukey_alpha) > 0.0f;
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (act) S.act[n_act + __popc(m & ((1u << lane) - 1u))] = ch;
+    n_act += __popc(m);
+  }
+  __syncwarp();
+
+  const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+  auto finish = [&](cplx out) {
+    if (lane != 0) return;
+    if (a.cf && n_act > 0) {
+      cplx coh = mk(0.f, 0.f);
+      float inc = 0.0f;
+      for (int q = 0; q < n_act; ++q) {
+        const float2 v = yc[S.act[q]];
+        coh = cadd(coh, mk(v.x, v.y));
+        inc += cnorm(mk(v.x, v.y));
+      }
+      out = cscale(out, (inc > 0.0f) ? cnorm(coh) / (static_cast<float>(n_act) * inc) : 0.0f);
+    }
+    if (incoherent)
+      a.acc_out[frame * a.n_pix + pix] += cnorm(out);
+    else
+      a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+  };
+  auto das_of_center = [&]() {
+    cplx acc = mk(0.f, 0.f);
+    for (int q = 0; q < n_act; ++q) {
+      const float2 v = yc[S.act[q]];
+      acc = cadd(acc, mk(v.x, v.y));
+    }
+    return acc;
+  };
+
+  if (n_act == 0) {
+    if (!incoherent && lane == 0) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
+    return;
+  }
+  if (n_act < 4) {
+    finish(das_of_center());
+    return;
+  }
+  int L = a.mv_subarray;
+  const int hi = max(2, n_act / 2);
+  if (L < 2) L = 2;
+  if (L > hi) L = hi;
+  const int n_sub = n_act - L + 1;
+  const int ra = a.mv_range_average;
+
+  // Stage the active samples of the valid range neighbours.
+  int n_d = 0;
+  for (int d = -ra; d <= ra; ++d) {
+    const int jj = j + d;
+    if (jj < 0 || jj >= a.n1) continue;
+    const float2* yr = Y + static_cast<long>(pix + d) * a.n_ch;
+    for (int q = lane; q < n_act; q += 32) {
+      const float2 v = yr[S.act[q]];
+      S.ys[n_d][q] = mk(v.x, v.y);
+    }
+    ++n_d;
+  }
+  __syncwarp();
+  const int n_snap = n_d * n_sub;
+
+  // Covariance, upper triangle, entry (r, c) with c >= r.
+  const int n_ent = L * (L + 1) / 2;
+  const float inv = 1.0f / static_cast<float>(n_snap);
+  for (int e = lane; e < n_ent; e += 32) {
+    // Decode packed upper-triangle index e -> (r, c).
+    int r = 0, rem = e;
+    while (rem >= L - r) {
+      rem -= L - r;
+      ++r;
+    }
+    const int c = r + rem;
+    cplx acc = mk(0.f, 0.f);
+    for (int d = 0; d < n_d; ++d)
+      for (int s0 = 0; s0 < n_sub; ++s0) acc = cadd(acc, cmul(S.ys[d][s0 + r], cconj(S.ys[d][s0 + c])));
+    acc = cscale(acc, inv);
+    S.R[r * L + c] = acc;
+    if (c != r) S.R[c * L + r] = cconj(acc);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    float trace = 0.0f;
+    for (int r = 0; r < L; ++r) trace += S.R[r * L + r].re;
+    const float eps = fmaxf(a.mv_loading * trace / static_cast<float>(L), 1e-20f);
+    for (int r = 0; r < L; ++r) S.R[r * L + r] = cadd(S.R[r * L + r], mk(eps, 0.0f));
+    S.fail = 0;
+  }
+  __syncwarp();
+
+  // Cholesky by anti-diagonals t = i + j of the lower triangle.
+  for (int t = 0; t <= 2 * (L - 1); ++t) {
+    const int j_lo = max(0, t - (L - 1));
+    const int j_hi = t / 2;
+    for (int jc = j_lo + lane; jc <= j_hi; jc += 32) {
+      const int i = t - jc;
+      cplx sum = S.R[i * L + jc];
+      for (int k = 0; k < jc; ++k) sum = csub(sum, cmul(S.R[i * L + k], cconj(S.R[jc * L + k])));
+      if (i == jc) {
+        const float d = sum.re;
+        if (!(d > 0.0f)) S.fail = 1;
+        S.R[i * L + jc] = mk(sqrtf(d), 0.0f);
+      } else {
+        S.R[i * L + jc] = cdiv_wide(sum, S.R[jc * L + jc]);
+      }
+    }
+    __syncwarp();
+  }
+  if (S.fail) {
+    finish(das_of_center());
+    return;
+  }
+  // Forward and back substitution for R w = 1 (serial, reference order).
+  if (lane == 0) {
+    for (int i = 0; i < L; ++i) {
+      cplx sum = mk(1.0f, 0.0f);
+      for (int k = 0; k < i; ++k) sum = csub(sum, cmul(S.R[i * L + k], S.w[k]));
+      S.w[i] = cdiv_wide(sum, S.R[i * L + i]);
+    }
+    for (int i = L - 1; i >= 0; --i) {
+      cplx sum = S.w[i];
+      for (int k = i + 1; k < L; ++k) sum = csub(sum, cmul(cconj(S.R[k * L + i]), S.w[k]));
+      S.w[i] = cdiv_wide(sum, S.R[i * L + i]);
+    }
+    cplx denom = mk(0.f, 0.f);
+    for (int q = 0; q < L; ++q) denom = cadd(denom, S.w[q]);
+    cplx out;
+    if (cabsf_(denom) < 1e-30f) {
+      out = das_of_center();
+    } else {
+      out = mk(0.f, 0.f);
+      // Weighted subarray average of the centre pixel (its row in ys).
+      int dc = 0;
+      for (int d = -ra; d < 0; ++d)
+        if (j + d >= 0) ++dc;
+      for (int q = 0; q < L; ++q) {
+        cplx avg = mk(0.f, 0.f);
+        for (int s0 = 0; s0 < n_sub; ++s0) avg = cadd(avg, S.ys[dc][s0 + q]);
+        avg = cdivr(avg, static_cast<float>(n_sub));
+        out = cadd(out, cmul(cconj(S.w[q]), avg));
+      }
+      out = cscale(cdiv_wide(out, denom), static_cast<float>(n_act));
+    }
+    finish(out);
+  }
+}
+
+__global__ void sqrt_acc_kernel(const float* acc, float2* out, long n_pix, long out_stride,
+                                int n_frames) {
+  const long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (i >= n_pix * n_frames) return;
+  const long f = i / n_pix, p = i - f * n_pix;
+  out[f * out_stride + p] = make_float2(sqrtf(acc[i]), 0.0f);
+}
+
+}  // namespace
+}  // namespace usxcu
+
+using namespace usxcu;
+
+struct usx_bf_plan {
+  usx_ctx* ctx = nullptr;
+  usx_channel_desc cd{};
+  usx_beamformer_config cfg{};
+  int n0 = 0, n1 = 0;
+  float* d_points = nullptr;
+  TxDev* d_tx = nullptr;
+  int ev_begin = 0, ev_end = 0;
+};
+
+namespace {
+
+int validate_bf_config(const usx_beamformer_config& c) {
+  if (!(c.f_number > 0)) return fail(USX_ERR_INVALID, "BeamformerConfig.f_number must be > 0");
+  if (c.mv_subarray < 2) return fail(USX_ERR_INVALID, "BeamformerConfig.mv_subarray must be >= 2");
+  if (c.mv_diagonal_loading < 0)
+    return fail(USX_ERR_INVALID, "BeamformerConfig.mv_diagonal_loading must be >= 0");
+  if (c.mv_range_average < 0)
+    return fail(USX_ERR_INVALID, "BeamformerConfig.mv_range_average must be >= 0");
+  return USX_OK;
+}
+
+BfArgs make_args(const usx_bf_plan* p) {
+  BfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const usx_channel_desc& cd = p->cd;
+  a.points = p->d_points;
+  a.tx = p->d_tx;
+  a.n_ch = cd.probe.n_elements;
+  a.n_smp = cd.acq.n_samples;
+  a.n1 = p->n1;
+  a.n_pix = p->n0 * p->n1;
+  a.ev_begin = p->ev_begin;
+  a.ev_end = p->ev_end;
+  a.c = cd.medium.speed_of_sound;
+  a.fs = cd.acq.sampling_frequency;
+  a.t0 = cd.acq.t0;
+  a.fdem = cd.is_iq ? cd.demodulation_frequency : 0.0f;
+  a.two_pi_f = 2.0f * kPi * a.fdem;
+  a.lambda = cd.medium.speed_of_sound / cd.probe.center_frequency;
+  a.pitch = cd.probe.pitch;
+  a.half_nm1 = 0.5f * static_cast<float>(cd.probe.n_elements - 1);
+  a.f_number = p->cfg.f_number;
+  a.tukey_alpha = p->cfg.tukey_alpha;
+  a.rx_window = p->cfg.rx_window;
+  a.combiner = p->cfg.combiner;
+  a.compounding = p->cfg.compounding;
+  a.tx_weighting = p->cfg.transmit_weighting;
+  a.cf = p->cfg.coherence_factor;
+  a.is_mv = p->cfg.combiner == USX_COMB_MV;
+  a.mv_subarray = p->cfg.mv_subarray;
+  a.mv_range_average = a.is_mv ? p->cfg.mv_range_average : 0;
+  a.mv_loading = p->cfg.mv_diagonal_loading;
+  a.seq_epf = 0;
+  a.pass = -1;
+  return a;
+}
+
+
+int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_stride,
+               float* frames, int64_t frame_stride, int seq_epf) {
+  if (!plan || !data || !frames) return fail(USX_ERR_INVALID, "usx_cu_bf_execute: null argument");
+  if (n_frames <= 0) return USX_OK;
+  if (n_frames > 65535) return fail(USX_ERR_UNSUPPORTED, "beamforming more than 65535 frames per call");
+  usx_ctx* ctx = plan->ctx;
+  BfArgs a = make_args(plan);
+  if (plan->cd.is_iq)
+    a.iq = static_cast<const float2*>(data);
+  else
+    a.rf = static_cast<const float*>(data);
+  a.data_stride = data_stride;
+  a.out = reinterpret_cast<float2*>(frames);
+  a.out_stride = frame_stride;
+  a.seq_epf = seq_epf;
+  const long n_pix = a.n_pix;
+  const int ev_per_frame = seq_epf > 0 ? seq_epf : (a.ev_end - a.ev_begin);
+  if (ev_per_frame <= 0) {
+    // No events: the reference returns an all-zero frame.
+    for (int f = 0; f < n_frames; ++f)
+      USX_CUDA(cudaMemsetAsync(frames + 2 * f * frame_stride, 0, sizeof(float2) * n_pix, ctx->stream));
+    return USX_OK;
+  }
+  const dim3 grid_das(ceil_div(n_pix, kBfThreads), n_frames);
+  if (!a.is_mv) {
+    prof_begin(ctx, "das_kernel");
+    if (plan->cd.is_iq)
+      das_kernel<true><<<grid_das, kBfThreads, 0, ctx->stream>>>(a);
+    else
+      das_kernel<false><<<grid_das, kBfThreads, 0, ctx->stream>>>(a);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("das_kernel");
+    return USX_OK;
+  }
+  // Minimum variance: per pass, export compounded channel samples, then solve.
+  const size_t y_bytes = static_cast<size_t>(n_frames) * n_pix * a.n_ch * sizeof(float2);
+  const size_t acc_bytes = static_cast<size_t>(n_frames) * n_pix * sizeof(float);
+  void* ws = nullptr;
+  if (int rc = scratch(ctx, y_bytes + acc_bytes + 256, &ws)) return rc;
+  a.y_out = static_cast<float2*>(ws);
+  a.acc_out = reinterpret_cast<float*>(static_cast<char*>(ws) + ((y_bytes + 255) / 256) * 256);
+  const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
+  const size_t smem = sizeof(MvShared) * kMvWarps;
+  USX_CUDA(cudaFuncSetAttribute(mv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem)));
+  const dim3 grid_mv(ceil_div(n_pix, kMvWarps), n_frames);
+  if (incoherent) USX_CUDA(cudaMemsetAsync(a.acc_out, 0, acc_bytes, ctx->stream));
+  const int n_pass = incoherent ? ev_per_frame : 1;
+  for (int pass = 0; pass < n_pass; ++pass) {
+    BfArgs b = a;
+    b.pass = incoherent ? pass : -1;
+    prof_begin(ctx, "das_kernel(mv export)");
+    if (plan->cd.is_iq)
+      das_kernel<true><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
+    else
+      das_kernel<false><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("das_kernel(mv export)");
+    prof_begin(ctx, "mv_kernel");
+    mv_kernel<<<grid_mv, 32 * kMvWarps, smem, ctx->stream>>>(b);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("mv_kernel");
+  }
+  if (incoherent) {
+    const long n = n_pix * n_frames;
+    sqrt_acc_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(a.acc_out, a.out, n_pix, frame_stride,
+                                                              n_frames);
+    USX_CHECK_LAUNCH("sqrt_acc_kernel");
+  }
+  return USX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_grid_desc* grid,
+                          const float* points_host, const usx_beamformer_config* cfg,
+                          int event_begin, int event_end, usx_bf_plan** out) {
+  if (!ctx || !cd || !grid || !points_host || !cfg || !out)
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_create: null argument");
+  if (int rc = validate_channel(*cd)) return rc;
+  if (int rc = validate_bf_config(*cfg)) return rc;
+  if (grid->n_axis0 <= 0 || grid->n_axis1 <= 0)
+    return fail(USX_ERR_INVALID, "ScanGrid dimensions must be > 0");
+  if (cfg->combiner != USX_COMB_DAS && cfg->combiner != USX_COMB_DMAS && cfg->combiner != USX_COMB_MV)
+    return fail(USX_ERR_UNSUPPORTED, "usx_cu_bf_plan_create: unknown combiner");
+  if (cfg->combiner == USX_COMB_MV) {
+    if (cd->probe.n_elements > kMaxCh)
+      return fail(USX_ERR_UNSUPPORTED, "minimum variance supports at most 256 channels");
+    if (std::min(cfg->mv_subarray, std::max(2, cd->probe.n_elements / 2)) > kMaxL)
+      return fail(USX_ERR_UNSUPPORTED, "minimum variance supports subarrays up to 64");
+    if (cfg->mv_range_average > kMaxRangeAvg)
+      return fail(USX_ERR_UNSUPPORTED, "minimum variance supports range averaging up to +/-4");
+  }
+  const long n_pix = static_cast<long>(grid->n_axis0) * grid->n_axis1;
+  if (n_pix > 0x7fffffffL / 2) return fail(USX_ERR_UNSUPPORTED, "grid too large");
+  const int n_ev = cd->n_events;
+  if (event_end < 0) event_end = n_ev;
+  event_begin = std::min(std::max(event_begin, 0), n_ev);
+  event_end = std::min(std::max(event_end, event_begin), n_ev);
+
+  usx_bf_plan* p = new usx_bf_plan();
+  p->ctx = ctx;
+  p->cd = *cd;
+  p->cd.transmits = nullptr;
+  p->cfg = *cfg;
+  p->n0 = grid->n_axis0;
+  p->n1 = grid->n_axis1;
+  p->ev_begin = event_begin;
+  p->ev_end = event_end;
+  std::vector<TxDev> txs(static_cast<size_t>(n_ev));
+  for (int e = 0; e < n_ev; ++e) txs[static_cast<size_t>(e)] = make_txdev(cd->probe, cd->transmits[e]);
+  cudaError_t e1 = cudaMalloc(&p->d_points, sizeof(float) * 3 * n_pix);
+  cudaError_t e2 = cudaMalloc(&p->d_tx, sizeof(TxDev) * std::max(1, n_ev));
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    cudaFree(p->d_points);
+    cudaFree(p->d_tx);
+    delete p;
+    return fail(USX_ERR_NOMEM, "usx_cu_bf_plan_create: device allocation failed");
+  }
+  cudaMemcpy(p->d_points, points_host, sizeof(float) * 3 * n_pix, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_tx, txs.data(), sizeof(TxDev) * n_ev, cudaMemcpyHostToDevice);
+  *out = p;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_destroy(usx_bf_plan* plan) {
+  if (!plan) return USX_OK;
+  cudaStreamSynchronize(plan->ctx->stream);
+  cudaFree(plan->d_points);
+  cudaFree(plan->d_tx);
+  delete plan;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_workspace(const usx_bf_plan* plan, size_t* bytes) {
+  if (!plan || !bytes) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_workspace: null argument");
+  const size_t n_pix = static_cast<size_t>(plan->n0) * plan->n1;
+  *bytes = 0;
+  if (plan->cfg.combiner == USX_COMB_MV)
+    *bytes = n_pix * plan->cd.probe.n_elements * sizeof(float2) + n_pix * sizeof(float);
+  return USX_OK;
+}
+
+int usx_cu_bf_execute_batch(usx_bf_plan* plan, int n_frames, const void* data,
+                            int64_t data_stride, float* frames, int64_t frame_stride) {
+  return bf_execute(plan, n_frames, data, data_stride, frames, frame_stride, 0);
+}
+
+int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_frames,
+                               const void* data, float* frames, int64_t frame_stride) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_execute_sequence: null plan");
+  if (events_per_frame <= 0)
+    return fail(USX_ERR_INVALID, "beamform_sequence: events_per_frame must be > 0");
+  if (plan->ev_begin + static_cast<long>(events_per_frame) * n_frames > plan->ev_end)
+    return fail(USX_ERR_INVALID, "beamform_sequence: frames exceed the plan's events");
+  return bf_execute(plan, n_frames, data, 0, frames, frame_stride, events_per_frame);
+}
+
+int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame) {
+  return usx_cu_bf_execute_batch(plan, 1, data, 0, frame, 0);
+}
+
+int usx_cu_beamform(usx_ctx* ctx, const usx_channel_desc* cd, const void* data,
+                    const usx_grid_desc* grid, const float* points_host,
+                    const usx_beamformer_config* cfg, int event_begin, int event_end,
+                    float* frame) {
+  usx_bf_plan* plan = nullptr;
+  if (int rc = usx_cu_bf_plan_create(ctx, cd, grid, points_host, cfg, event_begin, event_end, &plan))
+    return rc;
+  const int rc = usx_cu_bf_execute(plan, data, frame);
+  usx_cu_bf_plan_destroy(plan);
+  return rc;
+}
+
+}  // extern "C"

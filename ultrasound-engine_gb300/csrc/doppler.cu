@@ -1,0 +1,434 @@
+// doppler.cu — polynomial-regression wall filter, colour flow (Kasai/Loupas
+// autocorrelation with coherence and power gates), power Doppler, two-stage
+// axial displacement tracking and least-squares strain (reference
+// doppler.cpp:15-305).
+//
+// Ensembles are [frame][pixel] complex. The (I - P) clutter projector depends
+// only on the ensemble length and is built on the host with the reference's
+// float Gram-Schmidt (bit-identical), then applied per pixel on the device.
+// Every per-pixel sum runs in the reference's loop order (lateral offset,
+// axial offset, frame), so the maps match the reference to the last ulp of
+// the device's atan2f/hypotf.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "usx_internal.cuh"
+
+namespace usxcu {
+namespace {
+
+constexpr int kMaxEns = 64;
+
+// doppler.cpp:15-47, host float arithmetic.
+std::vector<float> reject_matrix(int n, int order) {
+  order = std::min(std::max(order, 0), n - 1);
+  const int p = order + 1;
+  std::vector<std::vector<float>> basis;
+  for (int d = 0; d < p; ++d) {
+    std::vector<float> v(static_cast<size_t>(n));
+    for (int k = 0; k < n; ++k) {
+      const float x = (n == 1) ? 0.0f : 2.0f * static_cast<float>(k) / static_cast<float>(n - 1) - 1.0f;
+      v[static_cast<size_t>(k)] = static_cast<float>(std::pow(static_cast<double>(x), static_cast<double>(d)));
+    }
+    for (const auto& b : basis) {
+      float dot = 0;
+      for (int k = 0; k < n; ++k) dot += v[static_cast<size_t>(k)] * b[static_cast<size_t>(k)];
+      for (int k = 0; k < n; ++k) v[static_cast<size_t>(k)] -= dot * b[static_cast<size_t>(k)];
+    }
+    float norm = 0;
+    for (float x : v) norm += x * x;
+    norm = std::sqrt(norm);
+    if (norm < 1e-8f) continue;
+    for (float& x : v) x /= norm;
+    basis.push_back(v);
+  }
+  std::vector<float> M(static_cast<size_t>(n) * n, 0.0f);
+  for (int i = 0; i < n; ++i) M[static_cast<size_t>(i) * n + i] = 1.0f;
+  for (const auto& b : basis)
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        M[static_cast<size_t>(i) * n + j] -= b[static_cast<size_t>(i)] * b[static_cast<size_t>(j)];
+  return M;
+}
+
+struct WallArgs {
+  const float2* ens;
+  float2* out;          // filtered ensemble, or nullptr
+  float* power;         // power Doppler sum, or nullptr
+  long n_pix;
+  int n;
+  int identity;         // WallFilter::None: copy through
+  float M[kMaxEns * kMaxEns];
+};
+
+__global__ void wall_kernel(const WallArgs a) {
+  extern __shared__ float2 zs[];   // [n][blockDim]
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= a.n_pix) return;
+  for (int j = 0; j < a.n; ++j) zs[j * blockDim.x + threadIdx.x] = a.ens[j * a.n_pix + k];
+  float p = 0.0f;
+  for (int i = 0; i < a.n; ++i) {
+    cplx acc;
+    if (a.identity) {
+      const float2 z = zs[i * blockDim.x + threadIdx.x];
+      acc = mk(z.x, z.y);
+    } else {
+      acc = mk(0.f, 0.f);
+      for (int j = 0; j < a.n; ++j) {
+        const float2 z = zs[j * blockDim.x + threadIdx.x];
+        acc = cadd(acc, cscale(mk(z.x, z.y), a.M[i * a.n + j]));
+      }
+    }
+    if (a.out) a.out[i * a.n_pix + k] = make_float2(acc.re, acc.im);
+    p += cnorm(acc);
+  }
+  if (a.power) a.power[k] = p;
+}
+
+struct FlowArgs {
+  const float2* filt;   // [n][n0*n1]
+  int n, n0, n1, ka, kl, loupas;
+  float dz, fdem, prf, c, coh_thr;
+  float* velocity;
+  float* power;
+  float* variance;
+  uint8_t* valid;
+  unsigned* pmax_bits;
+};
+
+__global__ void flow_kernel(const FlowArgs a) {
+  const long k0 = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  const long n_pix = static_cast<long>(a.n0) * a.n1;
+  // Out-of-range lanes evaluate the last pixel but do not store, so that the
+  // whole warp reaches the max reduction below.
+  const bool in_range = k0 < n_pix;
+  const long k = in_range ? k0 : n_pix - 1;
+  const int i = static_cast<int>(k / a.n1), j = static_cast<int>(k - static_cast<long>(i) * a.n1);
+  cplx R01 = mk(0.f, 0.f), R10 = mk(0.f, 0.f);
+  float R00 = 0.0f;
+  for (int di = -a.kl; di <= a.kl; ++di) {
+    const int ii = i + di;
+    if (ii < 0 || ii >= a.n0) continue;
+    for (int dj = -a.ka; dj <= a.ka; ++dj) {
+      const int jj = j + dj;
+      if (jj < 0 || jj >= a.n1) continue;
+      const long kk = static_cast<long>(ii) * a.n1 + jj;
+      for (int e = 0; e < a.n; ++e) {
+        const float2 zf = a.filt[e * n_pix + kk];
+        const cplx z = mk(zf.x, zf.y);
+        R00 += cnorm(z);
+        if (e + 1 < a.n) {
+          const float2 w = a.filt[(e + 1) * n_pix + kk];
+          R01 = cadd(R01, cmul(cconj(z), mk(w.x, w.y)));
+        }
+        if (jj + 1 < a.n1) {
+          const float2 w = a.filt[e * n_pix + kk + 1];
+          R10 = cadd(R10, cmul(cconj(z), mk(w.x, w.y)));
+        }
+      }
+    }
+  }
+  float vel = 0.0f, var = 0.0f;
+  uint8_t ok = 0;
+  if (R00 > 0.0f) {
+    const float coherence = cabsf_(R01) / R00;
+    var = fclamp(2.0f * (1.0f - coherence), 0.0f, 1.0f);
+    if (!(coherence < a.coh_thr)) {
+      const float phase_slow = atan2f(R01.im, R01.re);
+      float f_centre = a.fdem;
+      if (a.loupas) {
+        const float phase_fast = atan2f(R10.im, R10.re);
+        const float f_est = phase_fast * a.c / (4.0f * kPi * a.dz);
+        if (f_est > 0.25f * a.fdem && f_est < 2.0f * a.fdem) f_centre = f_est;
+      }
+      if (f_centre > 0.0f) {
+        vel = -phase_slow * a.c * a.prf / (4.0f * kPi * f_centre);
+        ok = 1;
+      }
+    }
+  }
+  if (in_range) {
+    a.velocity[k] = vel;
+    a.power[k] = R00;
+    a.variance[k] = var;
+    a.valid[k] = ok;
+  }
+  // Power is non-negative, so its bit pattern orders like its value.
+  unsigned m = __float_as_uint(fmaxf(R00, 0.0f));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(a.pmax_bits, m);
+}
+
+__global__ void power_gate_kernel(const float* power, uint8_t* valid, long n, float ratio,
+                                  const unsigned* pmax_bits) {
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  const float pmax = __uint_as_float(*pmax_bits);
+  if (pmax > 0.0f) {
+    const float thr = pmax * ratio;
+    if (power[k] < thr) valid[k] = 0;
+  }
+}
+
+struct DispArgs {
+  const float2* a;
+  const float2* b;
+  int n0, n1, ka, kl, lag_max;
+  float dz, fdem, c;
+  float* axial;
+  float* corr;
+};
+
+__global__ void displacement_kernel(const DispArgs p) {
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= static_cast<long>(p.n0) * p.n1) return;
+  const int i = static_cast<int>(k / p.n1), j = static_cast<int>(k - static_cast<long>(i) * p.n1);
+  p.axial[k] = 0.0f;
+  p.corr[k] = 0.0f;
+  cplx R10 = mk(0.f, 0.f);
+  for (int di = -p.kl; di <= p.kl; ++di) {
+    const int ii = i + di;
+    if (ii < 0 || ii >= p.n0) continue;
+    for (int dj = -p.ka; dj <= p.ka; ++dj) {
+      const int jj = j + dj;
+      if (jj < 0 || jj + 1 >= p.n1) continue;
+      const long kk = static_cast<long>(ii) * p.n1 + jj;
+      const float2 u = p.a[kk], v = p.a[kk + 1];
+      R10 = cadd(R10, cmul(cconj(mk(u.x, u.y)), mk(v.x, v.y)));
+    }
+  }
+  float f_centre = p.fdem;
+  const float f_est = atan2f(R10.im, R10.re) * p.c / (4.0f * kPi * p.dz);
+  if (f_est > 0.25f * p.fdem && f_est < 2.0f * p.fdem) f_centre = f_est;
+  if (f_centre <= 0.0f) return;
+  cplx best_R = mk(0.f, 0.f);
+  float best_corr = -1.0f;
+  int best_lag = 0;
+  for (int lag = -p.lag_max; lag <= p.lag_max; ++lag) {
+    cplx R = mk(0.f, 0.f);
+    float ea = 0.0f, eb = 0.0f;
+    for (int di = -p.kl; di <= p.kl; ++di) {
+      const int ii = i + di;
+      if (ii < 0 || ii >= p.n0) continue;
+      for (int dj = -p.ka; dj <= p.ka; ++dj) {
+        const int jj = j + dj;
+        const int jl = jj + lag;
+        if (jj < 0 || jj >= p.n1 || jl < 0 || jl >= p.n1) continue;
+        const float2 u = p.a[static_cast<long>(ii) * p.n1 + jj];
+        const float2 v = p.b[static_cast<long>(ii) * p.n1 + jl];
+        const cplx A = mk(u.x, u.y), B = mk(v.x, v.y);
+        R = cadd(R, cmul(cconj(A), B));
+        ea += cnorm(A);
+        eb += cnorm(B);
+      }
+    }
+    if (ea <= 0.0f || eb <= 0.0f) continue;
+    const float cr = cabsf_(R) / sqrtf(ea * eb);
+    if (cr > best_corr) {
+      best_corr = cr;
+      best_R = R;
+      best_lag = lag;
+    }
+  }
+  if (best_corr < 0.0f) return;
+  p.corr[k] = fclamp(best_corr, 0.0f, 1.0f);
+  const float residual = -atan2f(best_R.im, best_R.re) * p.c / (4.0f * kPi * f_centre);
+  p.axial[k] = static_cast<float>(best_lag) * p.dz + residual;
+}
+
+__global__ void strain_kernel(const float* axial, int n0, int n1, float dz, int half, float* strain) {
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= static_cast<long>(n0) * n1) return;
+  const int i = static_cast<int>(k / n1), j = static_cast<int>(k - static_cast<long>(i) * n1);
+  float sx = 0, sy = 0, sxx = 0, sxy = 0;
+  int n = 0;
+  for (int d = -half; d <= half; ++d) {
+    const int jj = j + d;
+    if (jj < 0 || jj >= n1) continue;
+    const float x = static_cast<float>(d) * dz;
+    const float y = axial[static_cast<long>(i) * n1 + jj];
+    sx += x;
+    sy += y;
+    sxx += x * x;
+    sxy += x * y;
+    ++n;
+  }
+  float out = 0.0f;
+  if (n >= 2) {
+    const float denom = static_cast<float>(n) * sxx - sx * sx;
+    if (!(fabsf(denom) < 1e-20f)) out = (static_cast<float>(n) * sxy - sx * sy) / denom;
+  }
+  strain[k] = out;
+}
+
+float axial_step(const float* axis1, int n1) {
+  float dz = 1e-4f;
+  if (n1 > 1 && axis1) dz = std::abs(axis1[1] - axis1[0]);
+  return dz;
+}
+
+int launch_wall(usx_ctx* ctx, const float* ens, int n, long n_pix, int type, int order, float* out,
+                float* power) {
+  if (n > kMaxEns) return fail(USX_ERR_UNSUPPORTED, "ensembles longer than 64 frames are not supported");
+  WallArgs a;
+  a.ens = reinterpret_cast<const float2*>(ens);
+  a.out = reinterpret_cast<float2*>(out);
+  a.power = power;
+  a.n_pix = n_pix;
+  a.n = n;
+  a.identity = type == USX_WALL_NONE;
+  if (!a.identity) {
+    const std::vector<float> M = reject_matrix(n, type == USX_WALL_MEAN ? 0 : order);
+    std::copy(M.begin(), M.end(), a.M);
+  }
+  const int threads = 128;
+  const size_t smem = sizeof(float2) * n * threads;
+  if (smem > 48 * 1024)
+    USX_CUDA(cudaFuncSetAttribute(wall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem)));
+  wall_kernel<<<ceil_div(n_pix, threads), threads, smem, ctx->stream>>>(a);
+  USX_CHECK_LAUNCH("wall_kernel");
+  return USX_OK;
+}
+
+int launch_flow(usx_ctx* ctx, const float* filt, int n, int n0, int n1, float dz, float fdem,
+                float prf, float c, const usx_doppler_config& cfg, float* velocity, float* power,
+                float* variance, uint8_t* valid, unsigned* pmax_bits) {
+  FlowArgs a;
+  a.filt = reinterpret_cast<const float2*>(filt);
+  a.n = n;
+  a.n0 = n0;
+  a.n1 = n1;
+  a.ka = std::max(0, cfg.kernel_axial);
+  a.kl = std::max(0, cfg.kernel_lateral);
+  a.loupas = cfg.loupas;
+  a.dz = dz;
+  a.fdem = fdem;
+  a.prf = prf;
+  a.c = c;
+  a.coh_thr = cfg.coherence_threshold;
+  a.velocity = velocity;
+  a.power = power;
+  a.variance = variance;
+  a.valid = valid;
+  a.pmax_bits = pmax_bits;
+  const long n_pix = static_cast<long>(n0) * n1;
+  USX_CUDA(cudaMemsetAsync(pmax_bits, 0, sizeof(unsigned), ctx->stream));
+  flow_kernel<<<ceil_div(n_pix, 128), 128, 0, ctx->stream>>>(a);
+  USX_CHECK_LAUNCH("flow_kernel");
+  const float ratio = std::pow(10.0f, cfg.power_threshold_db / 10.0f);
+  power_gate_kernel<<<ceil_div(n_pix, 256), 256, 0, ctx->stream>>>(power, valid, n_pix, ratio, pmax_bits);
+  USX_CHECK_LAUNCH("power_gate_kernel");
+  return USX_OK;
+}
+
+}  // namespace
+}  // namespace usxcu
+
+using namespace usxcu;
+
+extern "C" {
+
+int usx_cu_wall_filter(usx_ctx* ctx, const float* ens, int n_frames, int64_t n_pix, int type,
+                       int order, float* out) {
+  if (!ctx || !ens || !out) return fail(USX_ERR_INVALID, "usx_cu_wall_filter: null argument");
+  if (n_frames <= 0 || n_pix <= 0) return USX_OK;
+  return launch_wall(ctx, ens, n_frames, n_pix, type, order, out, nullptr);
+}
+
+int usx_cu_power_doppler(usx_ctx* ctx, const float* ens, int n_frames, int64_t n_pix, int type,
+                         int order, float* power) {
+  if (!ctx || !ens || !power) return fail(USX_ERR_INVALID, "usx_cu_power_doppler: null argument");
+  if (n_frames <= 0 || n_pix <= 0) return USX_OK;
+  return launch_wall(ctx, ens, n_frames, n_pix, type, order, nullptr, power);
+}
+
+int usx_cu_color_flow(usx_ctx* ctx, const float* ens, int n_frames, int n0, int n1,
+                      const float* axis1_host, float fdem, float prf, float speed_of_sound,
+                      const usx_doppler_config* cfg, float* velocity, float* power,
+                      float* variance, uint8_t* valid, float* nyquist) {
+  if (!ctx || !ens || !cfg || !velocity || !power || !variance || !valid)
+    return fail(USX_ERR_INVALID, "usx_cu_color_flow: null argument");
+  if (n_frames < 2) return fail(USX_ERR_INVALID, "color_flow: need at least 2 frames in the ensemble");
+  if (n0 <= 0 || n1 <= 0) return fail(USX_ERR_INVALID, "color_flow: empty grid");
+  const long n_pix = static_cast<long>(n0) * n1;
+  void* ws = nullptr;
+  if (int rc = scratch(ctx, sizeof(float2) * n_pix * n_frames, &ws)) return rc;
+  float* filt = static_cast<float*>(ws);
+  if (int rc = launch_wall(ctx, ens, n_frames, n_pix, cfg->wall_filter, cfg->polynomial_order, filt, nullptr))
+    return rc;
+  if (nyquist) *nyquist = (fdem > 0.0f) ? speed_of_sound * prf / (4.0f * fdem) : 0.0f;
+  return launch_flow(ctx, filt, n_frames, n0, n1, axial_step(axis1_host, n1), fdem, prf,
+                     speed_of_sound, *cfg, velocity, power, variance, valid,
+                     reinterpret_cast<unsigned*>(ctx->d_status + 10));
+}
+
+int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int* n_frames_host,
+                            const int64_t* frame_offset_host, int n0, int n1,
+                            const float* axis1_host, float fdem, float prf,
+                            float speed_of_sound, const usx_doppler_config* cfg, float* velocity,
+                            float* power, float* variance, uint8_t* valid) {
+  if (!ctx || !ens || !n_frames_host || !frame_offset_host || !cfg)
+    return fail(USX_ERR_INVALID, "usx_cu_color_flow_batch: null argument");
+  const long n_pix = static_cast<long>(n0) * n1;
+  long max_frames = 0;
+  for (int e = 0; e < n_ens; ++e) {
+    if (n_frames_host[e] < 2) return fail(USX_ERR_INVALID, "color_flow: need at least 2 frames in the ensemble");
+    max_frames = std::max<long>(max_frames, n_frames_host[e]);
+  }
+  void* ws = nullptr;
+  if (int rc = scratch(ctx, sizeof(float2) * n_pix * max_frames + 256, &ws)) return rc;
+  float* filt = static_cast<float*>(ws);
+  for (int e = 0; e < n_ens; ++e) {
+    const float* src = ens + 2 * frame_offset_host[e] * n_pix;
+    if (int rc = launch_wall(ctx, src, n_frames_host[e], n_pix, cfg->wall_filter, cfg->polynomial_order,
+                             filt, nullptr))
+      return rc;
+    if (int rc = launch_flow(ctx, filt, n_frames_host[e], n0, n1, axial_step(axis1_host, n1), fdem, prf,
+                             speed_of_sound, *cfg, velocity + e * n_pix, power + e * n_pix,
+                             variance + e * n_pix, valid + e * n_pix,
+                             reinterpret_cast<unsigned*>(ctx->d_status + 10)))
+      return rc;
+  }
+  return USX_OK;
+}
+
+int usx_cu_axial_displacement(usx_ctx* ctx, const float* before, const float* after, int n0,
+                              int n1, const float* axis1_host, float fdem, float speed_of_sound,
+                              int kernel_axial, int kernel_lateral, int max_lag, float* axial,
+                              float* correlation) {
+  if (!ctx || !before || !after || !axial || !correlation)
+    return fail(USX_ERR_INVALID, "usx_cu_axial_displacement: null argument");
+  const long n = static_cast<long>(n0) * n1;
+  if (n <= 0) return USX_OK;
+  DispArgs p;
+  p.a = reinterpret_cast<const float2*>(before);
+  p.b = reinterpret_cast<const float2*>(after);
+  p.n0 = n0;
+  p.n1 = n1;
+  p.ka = std::max(1, kernel_axial);
+  p.kl = std::max(0, kernel_lateral);
+  p.lag_max = std::max(0, max_lag);
+  p.dz = axial_step(axis1_host, n1);
+  p.fdem = fdem;
+  p.c = speed_of_sound;
+  p.axial = axial;
+  p.corr = correlation;
+  displacement_kernel<<<ceil_div(n, 128), 128, 0, ctx->stream>>>(p);
+  USX_CHECK_LAUNCH("displacement_kernel");
+  return USX_OK;
+}
+
+int usx_cu_axial_strain(usx_ctx* ctx, const float* axial, int n0, int n1,
+                        const float* axis1_host, int fit_length, float* strain) {
+  if (!ctx || !axial || !strain) return fail(USX_ERR_INVALID, "usx_cu_axial_strain: null argument");
+  const long n = static_cast<long>(n0) * n1;
+  if (n <= 0) return USX_OK;
+  strain_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(axial, n0, n1, axial_step(axis1_host, n1),
+                                                           std::max(1, fit_length / 2), strain);
+  USX_CHECK_LAUNCH("strain_kernel");
+  return USX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,224 @@
+// beamformer.cpp — host front end of the GPU beamformer (behaviour of the
+// reference's core/src/beamformer.cpp:218-569). A Beamformer keeps a small
+// cache of device plans (channel metadata, grid and config frozen on the GPU)
+// so that repeated frames with the same geometry pay only for the transfer of
+// their samples and the kernels.
+#include "usx/beamformer.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <list>
+#include <mutex>
+
+#include "desc.hpp"
+#include "usx/geometry.hpp"
+#include "usx/runtime.hpp"
+
+namespace usx {
+
+void BeamformerConfig::validate() const {
+  if (f_number <= 0) throw std::invalid_argument("BeamformerConfig.f_number must be > 0");
+  if (mv_subarray < 2) throw std::invalid_argument("BeamformerConfig.mv_subarray must be >= 2");
+  if (mv_diagonal_loading < 0)
+    throw std::invalid_argument("BeamformerConfig.mv_diagonal_loading must be >= 0");
+  if (mv_range_average < 0)
+    throw std::invalid_argument("BeamformerConfig.mv_range_average must be >= 0");
+}
+
+// The key of a plan is everything that is frozen into it.
+struct PlanKey {
+  usx_ctx* ctx = nullptr;
+  std::vector<unsigned char> meta;   // POD bytes of probe/medium/acq/config/tx geometry
+  std::vector<real> points;
+  bool operator==(const PlanKey& o) const {
+    return ctx == o.ctx && meta == o.meta && points == o.points;
+  }
+};
+
+class PlanCache {
+ public:
+  ~PlanCache() {
+    for (auto& e : entries_) usx_cu_bf_plan_destroy(e.second);
+  }
+  usx_bf_plan* get(const ChannelData& data, const ScanGrid& grid, const BeamformerConfig& cfg,
+                   int ev_begin, int ev_end) {
+    PlanKey key;
+    key.ctx = rt::ctx();
+    const usx_probe p = desc::probe(data.probe);
+    const usx_medium m = desc::medium(data.medium);
+    const usx_acquisition a = desc::acq(data.acq);
+    const usx_beamformer_config b = desc::bf(cfg);
+    auto put = [&](const void* x, std::size_t n) {
+      const auto* c = static_cast<const unsigned char*>(x);
+      key.meta.insert(key.meta.end(), c, c + n);
+    };
+    put(&p, sizeof p);
+    put(&m, sizeof m);
+    put(&a, sizeof a);
+    put(&b, sizeof b);
+    const int iq = data.is_iq ? 1 : 0;
+    put(&iq, sizeof iq);
+    put(&data.demodulation_frequency, sizeof(real));
+    put(&ev_begin, sizeof ev_begin);
+    put(&ev_end, sizeof ev_end);
+    const int gt = static_cast<int>(grid.type);
+    put(&gt, sizeof gt);
+    put(&grid.n_axis0, sizeof(int));
+    put(&grid.n_axis1, sizeof(int));
+    for (const Transmit& t : data.transmits) {
+      const int ty = static_cast<int>(t.type);
+      put(&ty, sizeof ty);
+      put(&t.angle, sizeof(real));
+      put(&t.focus, sizeof(Vec3));
+      put(&t.origin, sizeof(Vec3));
+      const int na = static_cast<int>(t.apodization.size());
+      put(&na, sizeof na);
+      if (na) put(t.apodization.data(), sizeof(real) * t.apodization.size());
+    }
+    key.points.assign(desc::points(grid), desc::points(grid) + 3 * grid.points.size());
+
+    std::lock_guard<std::mutex> lock(mu_);
+    for (auto it = entries_.begin(); it != entries_.end(); ++it) {
+      if (it->first == key) {
+        entries_.splice(entries_.begin(), entries_, it);
+        return entries_.front().second;
+      }
+    }
+    desc::Channel ch(data);
+    const usx_grid_desc g = desc::grid(grid);
+    usx_bf_plan* plan = nullptr;
+    rt::check(usx_cu_bf_plan_create(key.ctx, &ch.cd, &g, desc::points(grid), &b, ev_begin, ev_end, &plan),
+              "beamformer plan");
+    entries_.emplace_front(std::move(key), plan);
+    while (entries_.size() > kMaxPlans) {
+      usx_cu_bf_plan_destroy(entries_.back().second);
+      entries_.pop_back();
+    }
+    return plan;
+  }
+
+ private:
+  static constexpr std::size_t kMaxPlans = 4;
+  std::mutex mu_;
+  std::list<std::pair<PlanKey, usx_bf_plan*>> entries_;
+};
+
+Beamformer::Beamformer(BeamformerConfig config) : config_(config), plans_(std::make_shared<PlanCache>()) {
+  config_.validate();
+}
+Beamformer::~Beamformer() = default;
+Beamformer::Beamformer(const Beamformer& o) : config_(o.config_), plans_(std::make_shared<PlanCache>()) {}
+Beamformer& Beamformer::operator=(const Beamformer& o) {
+  config_ = o.config_;
+  plans_ = std::make_shared<PlanCache>();
+  return *this;
+}
+
+namespace {
+const void* upload(const ChannelData& data) {
+  if (data.is_iq) {
+    if (data.iq.size() != data.size()) throw std::invalid_argument("ChannelData has no IQ samples");
+    void* d = rt::slot(3, data.iq.size() * sizeof(cplx));
+    rt::h2d(d, data.iq.data(), data.iq.size() * sizeof(cplx));
+    return d;
+  }
+  if (data.rf.size() != data.size()) throw std::invalid_argument("ChannelData has no RF samples");
+  void* d = rt::slot(3, data.rf.size() * sizeof(float));
+  rt::h2d(d, data.rf.data(), data.rf.size() * sizeof(float));
+  return d;
+}
+}  // namespace
+
+Frame Beamformer::beamform(const ChannelData& data, const ScanGrid& grid, int event_begin,
+                           int event_end) const {
+  data.validate();
+  grid.validate();
+  config_.validate();
+  return beamform_device(data, upload(data), grid, event_begin, event_end);
+}
+
+Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, const ScanGrid& grid,
+                                  int event_begin, int event_end) const {
+  data.validate();
+  grid.validate();
+  config_.validate();
+  const int n_ev = data.n_events();
+  if (event_end < 0) event_end = n_ev;
+  event_begin = std::clamp(event_begin, 0, n_ev);
+  event_end = std::clamp(event_end, event_begin, n_ev);
+  Frame frame;
+  frame.grid = grid;
+  frame.demodulation_frequency = data.is_iq ? data.demodulation_frequency : 0.0f;
+  frame.allocate();
+  usx_bf_plan* plan = plans_->get(data, grid, config_, event_begin, event_end);
+  void* d_out = rt::slot(4, frame.data.size() * sizeof(cplx));
+  rt::check(usx_cu_bf_execute(plan, d_in, static_cast<float*>(d_out)), "beamform");
+  rt::d2h(frame.data.data(), d_out, frame.data.size() * sizeof(cplx));
+  return frame;
+}
+
+std::vector<Frame> Beamformer::beamform_sequence(const ChannelData& data, const ScanGrid& grid,
+                                                 int events_per_frame) const {
+  if (events_per_frame <= 0)
+    throw std::invalid_argument("beamform_sequence: events_per_frame must be > 0");
+  data.validate();
+  grid.validate();
+  config_.validate();
+  const int n_ev = data.n_events();
+  const int n_frames = n_ev / events_per_frame;
+  if (n_frames == 0) throw std::invalid_argument("beamform_sequence: fewer events than events_per_frame");
+  usx_bf_plan* plan = plans_->get(data, grid, config_, 0, n_ev);
+  const void* d_in = upload(data);
+  const std::size_t n_pix = static_cast<std::size_t>(grid.n_pixels());
+  void* d_out = rt::slot(4, n_pix * n_frames * sizeof(cplx));
+  rt::check(usx_cu_bf_execute_sequence(plan, events_per_frame, n_frames, d_in,
+                                       static_cast<float*>(d_out), static_cast<int64_t>(n_pix)),
+            "beamform_sequence");
+  std::vector<Frame> frames(static_cast<std::size_t>(n_frames));
+  std::vector<cplx> all(n_pix * n_frames);
+  rt::d2h(all.data(), d_out, all.size() * sizeof(cplx));
+  for (int f = 0; f < n_frames; ++f) {
+    Frame& fr = frames[static_cast<std::size_t>(f)];
+    fr.grid = grid;
+    fr.demodulation_frequency = data.is_iq ? data.demodulation_frequency : 0.0f;
+    fr.data.assign(all.begin() + static_cast<std::ptrdiff_t>(n_pix * f),
+                   all.begin() + static_cast<std::ptrdiff_t>(n_pix * (f + 1)));
+    fr.sequence = f;
+    fr.timestamp = static_cast<double>(f) * events_per_frame / data.acq.prf;
+  }
+  return frames;
+}
+
+real transmit_sensitivity(const Probe& probe, const Transmit& tx, const Vec3& point, real wavelength) {
+  // Scalar restatement of the illumination weight (beamformer.cpp:238-295).
+  bool valid = false;
+  real x_lo = 0, x_hi = 0;
+  for (int i = 0; i < probe.n_elements; ++i) {
+    if (!tx.apodization.empty() && tx.apodization[static_cast<std::size_t>(i)] == 0.0f) continue;
+    const real x = probe.element_position(i).x;
+    if (!valid) { x_lo = x_hi = x; valid = true; }
+    else { x_lo = std::min(x_lo, x); x_hi = std::max(x_hi, x); }
+  }
+  if (!valid || point.z <= 0.0f) return 0.0f;
+  real a, b;
+  if (tx.type == TransmitType::PlaneWave) {
+    const real shift = point.z * std::tan(tx.angle);
+    a = x_lo + shift;
+    b = x_hi + shift;
+  } else {
+    const real zf = tx.focus.z;
+    if (std::abs(zf) < 1e-9f) return 1.0f;
+    a = x_lo + (tx.focus.x - x_lo) * point.z / zf;
+    b = x_hi + (tx.focus.x - x_hi) * point.z / zf;
+    if (a > b) std::swap(a, b);
+  }
+  const real aperture = std::max(x_hi - x_lo, probe.pitch);
+  const real diffraction = std::clamp(point.z / aperture, 0.5f, 20.0f) * wavelength;
+  a -= diffraction;
+  b += diffraction;
+  const real centre = 0.5f * (a + b), half = 0.5f * (b - a);
+  if (half <= 0.0f) return 0.0f;
+  return window_value(Window::Tukey, (point.x - centre) / half, 0.4f);
+}
+
+}  // namespace usx

@@ -1,0 +1,336 @@
+"""ctypes binding of the C-ABI in include/usx_cu.h (libusx_cu.so).
+
+This is the device-resident door into the kernels: every data argument is a
+device address (an int, e.g. `torch.Tensor.data_ptr()`), descriptors are
+ctypes structures mirroring include/usx_types.h, and each call maps a non-zero
+status to an exception (ValueError for USX_ERR_INVALID, as the reference maps
+std::invalid_argument; RuntimeError otherwise). It is also the template for a
+binding from another language: every call here is one C function.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parents[2] / "lib" / "libusx_cu.so"
+
+USX_OK, USX_ERR_INVALID = 0, 1
+
+f32p = C.POINTER(C.c_float)
+vp = C.c_void_p
+
+
+class Probe(C.Structure):
+    _fields_ = [("n_elements", C.c_int32), ("pitch", C.c_float), ("element_width", C.c_float),
+                ("elevation_height", C.c_float), ("center_frequency", C.c_float), ("bandwidth", C.c_float)]
+
+
+class Medium(C.Structure):
+    _fields_ = [("speed_of_sound", C.c_float), ("attenuation", C.c_float), ("density", C.c_float)]
+
+
+class Acquisition(C.Structure):
+    _fields_ = [("sampling_frequency", C.c_float), ("n_samples", C.c_int32), ("t0", C.c_float), ("prf", C.c_float)]
+
+
+class Transmit(C.Structure):
+    _fields_ = [("type", C.c_int32), ("angle", C.c_float), ("focus", C.c_float * 3), ("origin", C.c_float * 3),
+                ("delays", f32p), ("apodization", f32p)]
+
+
+class ChannelDesc(C.Structure):
+    _fields_ = [("probe", Probe), ("medium", Medium), ("acq", Acquisition), ("n_events", C.c_int32),
+                ("transmits", C.POINTER(Transmit)), ("is_iq", C.c_int32), ("demodulation_frequency", C.c_float)]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("n_axis0", C.c_int32), ("n_axis1", C.c_int32), ("apex", C.c_float * 3),
+                ("axis0", f32p), ("axis1", f32p)]
+
+
+class BeamformerConfig(C.Structure):
+    _fields_ = [("f_number", C.c_float), ("rx_window", C.c_int32), ("tukey_alpha", C.c_float),
+                ("combiner", C.c_int32), ("compounding", C.c_int32), ("transmit_weighting", C.c_int32),
+                ("coherence_factor", C.c_int32), ("mv_subarray", C.c_int32), ("mv_diagonal_loading", C.c_float),
+                ("mv_range_average", C.c_int32)]
+
+
+class DemodConfig(C.Structure):
+    _fields_ = [("demodulation_frequency", C.c_float), ("cutoff_fraction", C.c_float),
+                ("filter_taps", C.c_int32), ("decimation", C.c_int32)]
+
+
+class SimulatorConfig(C.Structure):
+    _fields_ = [("pulse_cycles", C.c_float), ("tx_window", C.c_int32), ("tx_f_number", C.c_float),
+                ("oversampling", C.c_int32), ("full_transmit_diffraction", C.c_int32),
+                ("incident_trim_db", C.c_float), ("max_incident_window_us", C.c_float),
+                ("apply_attenuation", C.c_int32), ("apply_directivity", C.c_int32),
+                ("apply_spreading", C.c_int32), ("noise_db", C.c_float), ("noise_seed", C.c_uint32),
+                ("enable_motion", C.c_int32)]
+
+
+class DopplerConfig(C.Structure):
+    _fields_ = [("wall_filter", C.c_int32), ("polynomial_order", C.c_int32), ("loupas", C.c_int32),
+                ("kernel_axial", C.c_int32), ("kernel_lateral", C.c_int32), ("power_threshold_db", C.c_float),
+                ("coherence_threshold", C.c_float)]
+
+
+def bf_config(**kw) -> BeamformerConfig:
+    d = dict(f_number=1.75, rx_window=1, tukey_alpha=0.5, combiner=0, compounding=0, transmit_weighting=1,
+             coherence_factor=0, mv_subarray=16, mv_diagonal_loading=1e-2, mv_range_average=2)
+    d.update(kw)
+    return BeamformerConfig(**d)
+
+
+def demod_config(**kw) -> DemodConfig:
+    d = dict(demodulation_frequency=0.0, cutoff_fraction=0.5, filter_taps=33, decimation=1)
+    d.update(kw)
+    return DemodConfig(**d)
+
+
+def sim_config(**kw) -> SimulatorConfig:
+    d = dict(pulse_cycles=2.5, tx_window=1, tx_f_number=2.0, oversampling=4, full_transmit_diffraction=1,
+             incident_trim_db=-40.0, max_incident_window_us=30.0, apply_attenuation=1, apply_directivity=1,
+             apply_spreading=1, noise_db=-60.0, noise_seed=7, enable_motion=1)
+    d.update(kw)
+    return SimulatorConfig(**d)
+
+
+def doppler_config(**kw) -> DopplerConfig:
+    d = dict(wall_filter=1, polynomial_order=1, loupas=1, kernel_axial=4, kernel_lateral=1,
+             power_threshold_db=-35.0, coherence_threshold=0.35)
+    d.update(kw)
+    return DopplerConfig(**d)
+
+
+class Channel:
+    """A usx_channel_desc with its transmit arrays kept alive.
+
+    `transmits`: list of dicts with keys type, angle, focus, origin, delays, apodization."""
+
+    def __init__(self, probe: Probe, medium: Medium, acq: Acquisition, transmits, is_iq=False, fdem=0.0):
+        n = len(transmits)
+        self._arrays = []
+        self.tx = (Transmit * max(n, 1))()
+        for e, t in enumerate(transmits):
+            x = self.tx[e]
+            x.type = int(t.get("type", 1))
+            x.angle = float(t.get("angle", 0.0))
+            for k in range(3):
+                x.focus[k] = float(t.get("focus", (0, 0, 0.03))[k])
+                x.origin[k] = float(t.get("origin", (0, 0, 0))[k])
+            for name, field in (("delays", "delays"), ("apodization", "apodization")):
+                arr = t.get(name)
+                if arr is None or len(arr) == 0:
+                    setattr(x, field, None)
+                else:
+                    a = np.ascontiguousarray(arr, dtype=np.float32)
+                    self._arrays.append(a)
+                    setattr(x, field, a.ctypes.data_as(f32p))
+        self.desc = ChannelDesc(probe, medium, acq, n, C.cast(self.tx, C.POINTER(Transmit)), int(is_iq), float(fdem))
+
+
+class Grid:
+    """A usx_grid_desc plus its host point list (n_axis0*n_axis1, 3) float32."""
+
+    def __init__(self, gtype, axis0, axis1, points, apex=(0.0, 0.0, 0.0)):
+        self.axis0 = np.ascontiguousarray(axis0, dtype=np.float32)
+        self.axis1 = np.ascontiguousarray(axis1, dtype=np.float32)
+        self.points = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+        ap = (C.c_float * 3)(*[float(v) for v in apex])
+        self.desc = GridDesc(int(gtype), len(self.axis0), len(self.axis1), ap,
+                             self.axis0.ctypes.data_as(f32p), self.axis1.ctypes.data_as(f32p))
+
+    @property
+    def shape(self):
+        return (len(self.axis0), len(self.axis1))
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is not built; run ultrasound-engine_gb300/build.py")
+        _lib = C.CDLL(str(LIB_PATH))
+        _lib.usx_cu_last_error.restype = C.c_char_p
+        _lib.usx_cu_ctx_stream.restype = vp
+    return _lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc == USX_OK:
+        return
+    msg = lib().usx_cu_last_error().decode()
+    if rc == USX_ERR_INVALID:
+        raise ValueError(f"{what}: {msg}")
+    raise RuntimeError(f"{what} failed ({rc}): {msg}")
+
+
+class Context:
+    """usx_ctx on one device; adopts `stream` (an int cudaStream_t) if given."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = vp()
+        check(lib().usx_cu_ctx_create(int(device), vp(stream) if stream else None, C.byref(self._h)),
+              "usx_cu_ctx_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def stream(self) -> int:
+        return lib().usx_cu_ctx_stream(self._h) or 0
+
+    def synchronize(self):
+        check(lib().usx_cu_synchronize(self._h), "synchronize")
+
+    def close(self):
+        if self._h:
+            lib().usx_cu_ctx_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------- kernels
+    def simulate(self, ch: Channel, cfg: SimulatorConfig, scat_ptr: int, n_scat: int, noise_ptr: int | None,
+                 rf_ptr: int, want_stats: bool = False):
+        stats = (C.c_double * 2)()
+        check(lib().usx_cu_simulate(self._h, C.byref(ch.desc), C.byref(cfg), vp(scat_ptr), C.c_int64(n_scat),
+                                    vp(noise_ptr) if noise_ptr else None, vp(rf_ptr),
+                                    stats if want_stats else None), "simulate")
+        return (stats[0], stats[1]) if want_stats else None
+
+    def demodulate(self, ch: Channel, cfg: DemodConfig, rf_ptr: int, iq_ptr: int) -> float:
+        f = C.c_float()
+        check(lib().usx_cu_demodulate(self._h, C.byref(ch.desc), C.byref(cfg), vp(rf_ptr), vp(iq_ptr),
+                                      C.byref(f)), "demodulate")
+        return f.value
+
+    def plan(self, ch: Channel, grid: Grid, cfg: BeamformerConfig, ev_begin=0, ev_end=-1) -> "Plan":
+        return Plan(self, ch, grid, cfg, ev_begin, ev_end)
+
+    def envelope(self, frame_ptr, n0, n1, fdem, env_ptr):
+        check(lib().usx_cu_envelope(self._h, vp(frame_ptr), n0, n1, C.c_float(fdem), vp(env_ptr)), "envelope")
+
+    def apply_tgc(self, env_ptr, n0, n1, points_ptr, atten, f0, out_ptr):
+        check(lib().usx_cu_apply_tgc(self._h, vp(env_ptr), n0, n1, vp(points_ptr), C.c_float(atten),
+                                     C.c_float(f0), vp(out_ptr)), "apply_tgc")
+
+    def log_compress(self, env_ptr, n, dr, gain, ref, out_ptr):
+        check(lib().usx_cu_log_compress(self._h, vp(env_ptr), C.c_int64(n), C.c_float(dr), C.c_float(gain),
+                                        C.c_float(ref), vp(out_ptr)), "log_compress")
+
+    def scan_convert(self, img_ptr, grid: Grid, width, height, fill, px_ptr):
+        ext = (C.c_float * 4)()
+        check(lib().usx_cu_scan_convert(self._h, vp(img_ptr), C.byref(grid.desc), grid.points.ctypes.data_as(f32p),
+                                        width, height, C.c_float(fill), vp(px_ptr), ext), "scan_convert")
+        return np.array(ext[:], np.float32)
+
+    def wall_filter(self, ens_ptr, n_frames, n_pix, wtype, order, out_ptr):
+        check(lib().usx_cu_wall_filter(self._h, vp(ens_ptr), n_frames, C.c_int64(n_pix), wtype, order,
+                                       vp(out_ptr)), "wall_filter")
+
+    def power_doppler(self, ens_ptr, n_frames, n_pix, wtype, order, out_ptr):
+        check(lib().usx_cu_power_doppler(self._h, vp(ens_ptr), n_frames, C.c_int64(n_pix), wtype, order,
+                                         vp(out_ptr)), "power_doppler")
+
+    def color_flow(self, ens_ptr, n_frames, n0, n1, axis1, fdem, prf, c, cfg: DopplerConfig, vel, pw, var, valid):
+        ax = np.ascontiguousarray(axis1, dtype=np.float32)
+        nyq = C.c_float()
+        check(lib().usx_cu_color_flow(self._h, vp(ens_ptr), n_frames, n0, n1, ax.ctypes.data_as(f32p),
+                                      C.c_float(fdem), C.c_float(prf), C.c_float(c), C.byref(cfg), vp(vel), vp(pw),
+                                      vp(var), vp(valid), C.byref(nyq)), "color_flow")
+        return nyq.value
+
+    def color_flow_batch(self, ens_ptr, n_frames, frame_offset, n0, n1, axis1, fdem, prf, c,
+                         cfg: DopplerConfig, vel, pw, var, valid):
+        nf = np.ascontiguousarray(n_frames, dtype=np.int32)
+        off = np.ascontiguousarray(frame_offset, dtype=np.int64)
+        ax = np.ascontiguousarray(axis1, dtype=np.float32)
+        check(lib().usx_cu_color_flow_batch(self._h, vp(ens_ptr), len(nf), nf.ctypes.data_as(C.POINTER(C.c_int)),
+                                            off.ctypes.data_as(C.POINTER(C.c_int64)), n0, n1,
+                                            ax.ctypes.data_as(f32p), C.c_float(fdem), C.c_float(prf), C.c_float(c),
+                                            C.byref(cfg), vp(vel), vp(pw), vp(var), vp(valid)),
+              "color_flow_batch")
+
+    def axial_displacement(self, a_ptr, b_ptr, n0, n1, axis1, fdem, c, ka, kl, max_lag, axial_ptr, corr_ptr):
+        ax = np.ascontiguousarray(axis1, dtype=np.float32)
+        check(lib().usx_cu_axial_displacement(self._h, vp(a_ptr), vp(b_ptr), n0, n1, ax.ctypes.data_as(f32p),
+                                              C.c_float(fdem), C.c_float(c), ka, kl, max_lag, vp(axial_ptr),
+                                              vp(corr_ptr)), "axial_displacement")
+
+    def axial_strain(self, axial_ptr, n0, n1, axis1, fit, out_ptr):
+        ax = np.ascontiguousarray(axis1, dtype=np.float32)
+        check(lib().usx_cu_axial_strain(self._h, vp(axial_ptr), n0, n1, ax.ctypes.data_as(f32p), fit,
+                                        vp(out_ptr)), "axial_strain")
+
+
+class Plan:
+    """usx_bf_plan: a frozen beamforming configuration on the device."""
+
+    def __init__(self, ctx: Context, ch: Channel, grid: Grid, cfg: BeamformerConfig, ev_begin=0, ev_end=-1):
+        self.ctx = ctx
+        self._h = vp()
+        self._keep = (ch, grid, cfg)
+        check(lib().usx_cu_bf_plan_create(ctx.handle, C.byref(ch.desc), C.byref(grid.desc),
+                                          grid.points.ctypes.data_as(f32p), C.byref(cfg), ev_begin, ev_end,
+                                          C.byref(self._h)), "bf_plan_create")
+
+    def execute(self, data_ptr: int, frame_ptr: int):
+        check(lib().usx_cu_bf_execute(self._h, vp(data_ptr), vp(frame_ptr)), "bf_execute")
+
+    def execute_batch(self, n_frames, data_ptr, data_stride, frames_ptr, frame_stride):
+        check(lib().usx_cu_bf_execute_batch(self._h, n_frames, vp(data_ptr), C.c_int64(data_stride),
+                                            vp(frames_ptr), C.c_int64(frame_stride)), "bf_execute_batch")
+
+    def execute_sequence(self, events_per_frame, n_frames, data_ptr, frames_ptr, frame_stride):
+        check(lib().usx_cu_bf_execute_sequence(self._h, events_per_frame, n_frames, vp(data_ptr), vp(frames_ptr),
+                                               C.c_int64(frame_stride)), "bf_execute_sequence")
+
+    def workspace_bytes(self) -> int:
+        n = C.c_size_t()
+        check(lib().usx_cu_bf_plan_workspace(self._h, C.byref(n)), "bf_plan_workspace")
+        return n.value
+
+    def close(self):
+        if self._h:
+            lib().usx_cu_bf_plan_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def profile(ctx: Context, on: bool = True) -> None:
+    """Record CUDA events around every launch on ctx's stream."""
+    check(lib().usx_cu_profile_enable(ctx.handle, 1 if on else 0), "profile_enable")
+
+
+def profile_reset(ctx: Context) -> None:
+    check(lib().usx_cu_profile_reset(ctx.handle), "profile_reset")
+
+
+def profile_read(ctx: Context) -> dict:
+    """{kernel name: (total device ms, launches)} since the last reset."""
+    out = {}
+    name = C.create_string_buffer(128)
+    ms = C.c_double()
+    n = C.c_int64()
+    i = 0
+    while lib().usx_cu_profile_read(ctx.handle, i, name, 128, C.byref(ms), C.byref(n)) == USX_OK:
+        out[name.value.decode()] = (ms.value, n.value)
+        i += 1
+    return out
