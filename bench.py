@@ -43,6 +43,12 @@ N_EL, N_TX, N_SMP = 128, 75, 2073
 N0, N1 = 512, 1024
 FS, F0, C0 = 20e6, 5e6, 1540.0
 MV_KW = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01, mv_range_average=2)
+WORKLOADS = {
+    "mv": MV_KW,
+    "das": dict(f_number=1.5),
+    "cf": dict(f_number=1.5, coherence_factor=1),
+    "dmas": dict(f_number=1.5, combiner=1),
+}
 CYSTS = ((-0.010, 0.025, 0.002), (0.0, 0.035, 0.003), (0.010, 0.045, 0.004))
 
 
@@ -176,7 +182,7 @@ def run_reference(args) -> None:
     iq = (rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)
           + 1j * rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)).astype(np.complex64)
     pts = np.asarray(grid.points)
-    lines = 2
+    lines = max(2, min(threads, 16))  # the reference parallelises over lines: one per core
     times = []
     for i in range(args.warmup + args.steps):
         dt, kind = cpu_baseline_mv(iq, pts, txs, probe, acq, lines, threads)
@@ -220,12 +226,15 @@ def run_ours(args) -> None:
     ch_iq = capi.Channel(ch_rf.desc.probe, ch_rf.desc.medium, ch_rf.desc.acq, tx, is_iq=True, fdem=F0)
     d_rf = torch.from_numpy(rf_host).cuda()
     d_iq = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()  # the context works on its own stream
     ctx.demodulate(ch_rf, capi.demod_config(), d_rf.data_ptr(), d_iq.data_ptr())
     ctx.synchronize()
-    pts = np.asarray(grid.points)
-    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), pts)
-    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
-    frame = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
+    n0 = args.lines
+    pts = np.asarray(grid.points).reshape(N0, N1, 3)[:n0].reshape(-1, 3)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0)[:n0], np.asarray(grid.axis1), pts)
+    bkw = WORKLOADS[args.workload]
+    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
+    frame = torch.empty((n0, N1), dtype=torch.complex64, device="cuda")
 
     stream = torch.cuda.ExternalStream(ctx.stream())
     for _ in range(args.warmup):
@@ -260,7 +269,7 @@ def run_ours(args) -> None:
     launches_in_region = sum(n for _, n in prof.values())
     mv_flops = mv_flops_per_frame(pts, MV_KW)
     kname, (kms, kn) = top
-    achieved_tflops = mv_flops / (kms / kn / 1e3) / 1e12 if kn and kname == "mv_kernel" else None
+    achieved_tflops = mv_flops / (kms / kn / 1e3) / 1e12 if kn and kname.startswith("mv") else None
     roofline = {"kernel": kname, "bound": "tensor", "achieved": achieved_tflops,
                 "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
                 "frac": (achieved_tflops / peaks["bf16_tflops_sustained"]) if achieved_tflops else None,
@@ -268,36 +277,28 @@ def run_ours(args) -> None:
                 "kernels_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in prof.items()},
                 "algorithmic_gflop_per_frame": mv_flops / 1e9}
 
-    # End to end through the public API on host RF.
-    pcfg = usx.PipelineConfig()
-    b = pcfg.beamformer
-    b.f_number, b.combiner, b.mv_subarray = 1.5, usx.Combiner.MV, 64
-    b.mv_diagonal_loading, b.mv_range_average = 0.01, 2
-    pcfg.beamformer = b
-    pipe = usx.ImagingPipeline(grid, pcfg)
-    pipe.process_frame(raw)
-    e2e_steps = max(1, min(args.steps, 5))
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for _ in range(e2e_steps):
-        fr = pipe.process_frame(raw)
-    e2e_s = (time.perf_counter() - t) / e2e_steps
-    e2e = {"value": world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": int(rf_host.nbytes),
-           "d2h_bytes_per_step": int(N0 * N1 * 8), "api": "usx.ImagingPipeline.process_frame(RF ChannelData)"}
+    e2e = None
+    if args.no_e2e:
+        pass
+    else:
+        e2e = run_e2e(usx, grid, raw, rf_host, args, world)
 
     if rank == 0:
         cpu = None
-        if world == 1:
+        if world == 1 and not args.no_cpu:
             threads = os.cpu_count() or 1
             iq_host = d_iq.cpu().numpy()
-            dt, kind = cpu_baseline_mv(iq_host, pts, txs, probe, acq, 2, threads)
-            cpu = {"value": 1.0 / (dt * N0 / 2), "unit": "frames/s", "cores": threads, "kind": kind,
-                   "sample": f"2 of {N0} lateral lines, scaled to a frame"}
-        line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-simulated 100k-scatterer cyst phantom)",
-                "config": {"workload": "mv_l64_75pw_512x1024", "combiner": "mv (plain, fp32)", "n_tx": N_TX,
-                           "n_ch": N_EL, "grid": [N0, N1], "iq_bytes": int(d_iq.numel() * 8),
+            lines = max(2, min(threads, 16))
+            dt, kind = cpu_baseline_mv(iq_host, np.asarray(grid.points), txs, probe, acq, lines, threads)
+            cpu = {"value": 1.0 / (dt * N0 / lines), "unit": "frames/s", "cores": threads, "kind": kind,
+                   "sample": f"{lines} of {N0} lateral lines (one per core), scaled to a frame"}
+        frames_per_s = value * N0 / n0
+        line = {"metric": METRIC, "value": frames_per_s, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step * N0 / n0, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (GPU-simulated 100k-scatterer cyst phantom)",
+                "config": {"workload": f"{args.workload}_75pw_512x1024", "beamformer": bkw, "n_tx": N_TX,
+                           "n_ch": N_EL, "grid": [N0, N1], "lines_timed": n0, "iq_bytes": int(d_iq.numel() * 8),
                            "l2": "inputs larger than L2 (159 MB IQ), no flush"},
                 "gpu_launches": launches_in_region, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}
@@ -306,12 +307,41 @@ def run_ours(args) -> None:
     ctx.close()
 
 
+def run_e2e(usx, grid, raw, rf_host, args, world):
+    """The same frame through the public API with host buffers: RF up, frame back."""
+    import torch
+    pcfg = usx.PipelineConfig()
+    b = pcfg.beamformer
+    kw = WORKLOADS[args.workload]
+    b.f_number = kw["f_number"]
+    b.combiner = usx.Combiner(kw.get("combiner", 0))
+    b.coherence_factor = bool(kw.get("coherence_factor", 0))
+    b.mv_subarray = kw.get("mv_subarray", 16)
+    b.mv_diagonal_loading = kw.get("mv_diagonal_loading", 0.01)
+    b.mv_range_average = kw.get("mv_range_average", 2)
+    pcfg.beamformer = b
+    pipe = usx.ImagingPipeline(grid, pcfg)
+    pipe.process_frame(raw)
+    e2e_steps = max(1, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(e2e_steps):
+        pipe.process_frame(raw)
+    e2e_s = (time.perf_counter() - t) / e2e_steps
+    return {"value": world / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": int(rf_host.nbytes),
+            "d2h_bytes_per_step": int(N0 * N1 * 8), "api": "usx.ImagingPipeline.process_frame(RF ChannelData)"}
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="mv", choices=sorted(WORKLOADS))
+    ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

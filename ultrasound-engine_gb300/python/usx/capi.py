@@ -172,11 +172,21 @@ def check(rc: int, what: str) -> None:
     raise RuntimeError(f"{what} failed ({rc}): {msg}")
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the stream torch calls "default" (handle 0)
+
+
 class Context:
-    """usx_ctx on one device; adopts `stream` (an int cudaStream_t) if given."""
+    """usx_ctx on one device.
+
+    stream=None: the context creates its own non-blocking stream (callers must
+    order their own copies against it, e.g. with synchronize()).
+    stream=int: the context adopts that cudaStream_t; 0 (torch's default
+    stream) means the legacy default stream, so work is ordered with torch's."""
 
     def __init__(self, device: int = 0, stream: int | None = None):
         self._h = vp()
+        if stream is not None and stream == 0:
+            stream = CUDA_STREAM_LEGACY
         check(lib().usx_cu_ctx_create(int(device), vp(stream) if stream else None, C.byref(self._h)),
               "usx_cu_ctx_create")
 
