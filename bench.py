@@ -44,7 +44,8 @@ N0, N1 = 512, 1024
 FS, F0, C0 = 20e6, 5e6, 1540.0
 MV_KW = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01, mv_range_average=2)
 WORKLOADS = {
-    "mv": MV_KW,
+    "mv": MV_KW,             # tensor-core covariance (the fast plain MV)
+    "mv_exact": MV_KW,       # FP32 in the reference's operation order
     "das": dict(f_number=1.5),
     "cf": dict(f_number=1.5, coherence_factor=1),
     "dmas": dict(f_number=1.5, combiner=1),
@@ -234,6 +235,8 @@ def run_ours(args) -> None:
     cgrid = capi.Grid(0, np.asarray(grid.axis0)[:n0], np.asarray(grid.axis1), pts)
     bkw = WORKLOADS[args.workload]
     plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
+    if args.workload == "mv":
+        plan.set_mv_mode(1)
     frame = torch.empty((n0, N1), dtype=torch.complex64, device="cuda")
 
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -282,6 +285,10 @@ def run_ours(args) -> None:
         pass
     else:
         e2e = run_e2e(usx, grid, raw, rf_host, args, world)
+    if bkw.get("combiner") == 2:
+        fp64, failed = plan.mv_stats()
+        roofline["mv_fp64_resolves_per_frame"] = fp64 / max(1, args.steps + args.warmup)
+        roofline["mv_factorization_failures"] = failed
 
     if rank == 0:
         cpu = None
@@ -310,6 +317,7 @@ def run_ours(args) -> None:
 def run_e2e(usx, grid, raw, rf_host, args, world):
     """The same frame through the public API with host buffers: RF up, frame back."""
     import torch
+    os.environ["USX_MV_SOLVER"] = "exact" if args.workload == "mv_exact" else "tensor"
     pcfg = usx.PipelineConfig()
     b = pcfg.beamformer
     kw = WORKLOADS[args.workload]

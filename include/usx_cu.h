@@ -130,6 +130,20 @@ int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame);
 int usx_cu_bf_execute_batch(usx_bf_plan* plan, int n_frames, const void* data,
                             int64_t data_stride, float* frames, int64_t frame_stride);
 
+/* Minimum-variance solver of a plan (no counterpart in the reference, whose
+ * one solver is combine_mv_windowed, beamformer.cpp:137-214):
+ *   USX_MV_EXACT   FP32, the reference's operation order (default);
+ *   USX_MV_TENSOR  BF16 covariance on the tensor cores with FP32 accumulation,
+ *                  FP32 Cholesky, one refinement step against the FP32
+ *                  covariance, FP64 re-solve where the refined residual fails.
+ * Results of the two agree within 1e-3 relative L2. */
+enum { USX_MV_EXACT = 0, USX_MV_TENSOR = 1 };
+int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode);
+/* Counts since the last call (synchronises): pixels re-solved in FP64 and
+ * pixels whose factorisation failed (these take the DAS sum). */
+int usx_cu_bf_plan_mv_stats(usx_bf_plan* plan, int64_t* fp64_resolves,
+                            int64_t* factorization_failures);
+
 /* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one
  * launch: frame f uses the plan's events [first + f*events_per_frame,
  * first + (f+1)*events_per_frame) of the single acquisition `data`; frames

@@ -95,7 +95,8 @@ def test_simulate_focused_and_no_diffraction_match_oracle(capi, ctx, torch, gold
                      (txset(b, "div"), dict(noise_db=-200.0, apply_directivity=0, oversampling=2))):
         ch = c_channel(capi, pr, med, acq, txs)
         rf = torch.empty((len(txs), pr.n_elements, acq.n_samples), dtype=torch.float32, device="cuda")
-        ctx.simulate(ch, capi.sim_config(**cfg), dev(torch, g["scat"]).data_ptr(), len(g["scat"]), None, rf.data_ptr())
+        sc = dev(torch, g["scat"])
+        ctx.simulate(ch, capi.sim_config(**cfg), sc.data_ptr(), len(g["scat"]), None, rf.data_ptr())
         want = oracle.simulate(O.channel_desc(pr, med, acq, txs), O.sim_config(**cfg), g["scat"])
         assert rel_l2(host(torch, rf), want) < TOL
 
@@ -109,8 +110,8 @@ def test_simulate_empty_phantom_and_zero_amplitudes(capi, ctx, torch, golden):
     assert float(host(torch, rf).__abs__().max()) == 0.0
     scat = g["scat"].copy()
     scat[:, 3] = 0.0
-    ctx.simulate(ch, capi.sim_config(noise_db=-60.0), dev(torch, scat).data_ptr(), len(scat),
-                 dev(torch, g["noise_z"]).data_ptr(), rf.data_ptr())
+    sc, z = dev(torch, scat), dev(torch, g["noise_z"])
+    ctx.simulate(ch, capi.sim_config(noise_db=-60.0), sc.data_ptr(), len(scat), z.data_ptr(), rf.data_ptr())
     assert float(np.abs(host(torch, rf)).max()) == 0.0  # zero peak: no noise either
 
 
@@ -123,7 +124,8 @@ def test_demodulate_matches_reference(capi, ctx, torch, golden, key, kw):
     ch = c_channel(capi, pr, med, acq, txset(g, "pw"))
     want = g[key]
     iq = torch.empty(want.shape, dtype=torch.complex64, device="cuda")
-    fdem = ctx.demodulate(ch, capi.demod_config(**kw), dev(torch, g["rf"]).data_ptr(), iq.data_ptr())
+    rf = dev(torch, g["rf"])
+    fdem = ctx.demodulate(ch, capi.demod_config(**kw), rf.data_ptr(), iq.data_ptr())
     assert fdem == pytest.approx(5e6)
     assert rel_l2(host(torch, iq), want) < TOL
 
@@ -142,7 +144,8 @@ def test_demodulate_rejects_iq_input(capi, ctx, torch, golden):
 def _bf(capi, ctx, torch, ch, grid, cfg, data, ev_begin=0, ev_end=-1):
     plan = ctx.plan(ch, grid, cfg, ev_begin, ev_end)
     out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
-    plan.execute(dev(torch, data).data_ptr(), out.data_ptr())
+    d = dev(torch, data)
+    plan.execute(d.data_ptr(), out.data_ptr())
     res = host(torch, out)
     plan.close()
     return res
@@ -158,6 +161,41 @@ def test_beamform_matches_reference(capi, ctx, torch, golden, name):
     out = _bf(capi, ctx, torch, ch, grid, capi.bf_config(**BF_CASES[name]), g["iq"])
     tol = TOL_MV if name.startswith("mv") else TOL
     assert rel_l2(out, g[f"bf_{name}"]) < tol
+
+
+@pytest.mark.parametrize("name", ["mv", "mv_l4", "mv_cf"])
+def test_mv_tensor_cores_match_reference(capi, ctx, torch, golden, name):
+    """BF16 tensor-core covariance + FP32 refinement: within 1e-3 of the reference."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    plan = ctx.plan(ch, grid, capi.bf_config(**BF_CASES[name]))
+    plan.set_mv_mode(1)
+    out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
+    d = dev(torch, g["iq"])
+    plan.execute(d.data_ptr(), out.data_ptr())
+    got = host(torch, out)
+    fp64, failed = plan.mv_stats()
+    plan.close()
+    assert rel_l2(got, g[f"bf_{name}"]) < 1e-3
+    assert failed == 0
+
+
+def test_mv_tensor_cores_on_sector_grid(capi, ctx, torch, golden):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    chd = c_channel(capi, pr, med, acq, txset(g, "div"), is_iq=True, fdem=5e6)
+    sgrid = capi.Grid(1, g["sax0"], g["sax1"], g["spts"])
+    plan = ctx.plan(chd, sgrid, capi.bf_config(f_number=1.5, combiner=2, mv_subarray=12))
+    plan.set_mv_mode(1)
+    out = torch.empty(sgrid.shape, dtype=torch.complex64, device="cuda")
+    d = dev(torch, g["div_iq"])
+    plan.execute(d.data_ptr(), out.data_ptr())
+    assert rel_l2(host(torch, out), g["bf_div_mv"]) < 1e-3
+    plan.close()
 
 
 def test_beamform_geometries_match_reference(capi, ctx, torch, golden):
@@ -205,7 +243,8 @@ def test_batch_and_sequence_equal_single_frames(capi, ctx, torch, golden):
     plan = ctx.plan(ch, grid, capi.bf_config(f_number=1.5))
     n_pix = grid.shape[0] * grid.shape[1]
     out = torch.empty((3, n_pix), dtype=torch.complex64, device="cuda")
-    plan.execute_sequence(1, 3, dev(torch, g["iq"]).data_ptr(), out.data_ptr(), n_pix)
+    diq = dev(torch, g["iq"])
+    plan.execute_sequence(1, 3, diq.data_ptr(), out.data_ptr(), n_pix)
     got = host(torch, out)
     assert rel_l2(got[1].reshape(grid.shape), g["bf_das_ev1"]) < TOL
 
@@ -259,25 +298,30 @@ def test_postprocess_matches_reference(capi, ctx, torch, golden):
     b = golden("bf")
     n0, n1 = g["frame"].shape
     env = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
-    ctx.envelope(dev(torch, g["frame"]).data_ptr(), n0, n1, 5e6, env.data_ptr())
+    fr, rfr = dev(torch, g["frame"]), dev(torch, g["rf_frame"])
+    ctx.envelope(fr.data_ptr(), n0, n1, 5e6, env.data_ptr())
     assert rel_l2(host(torch, env), g["env_iq"]) < TOL
-    ctx.envelope(dev(torch, g["rf_frame"]).data_ptr(), n0, n1, 0.0, env.data_ptr())
+    ctx.envelope(rfr.data_ptr(), n0, n1, 0.0, env.data_ptr())
     assert rel_l2(host(torch, env), g["env_rf"]) < TOL
+    # Inputs are held in named tensors: a temporary's memory would be reused by
+    # torch's caching allocator for the next upload while the kernel reads it.
     out = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
-    ctx.apply_tgc(dev(torch, g["env_iq"]).data_ptr(), n0, n1, dev(torch, b["pts"]).data_ptr(), 0.5, 5e6, out.data_ptr())
+    env_iq, pts, tgc = dev(torch, g["env_iq"]), dev(torch, b["pts"]), dev(torch, g["tgc"])
+    ctx.apply_tgc(env_iq.data_ptr(), n0, n1, pts.data_ptr(), 0.5, 5e6, out.data_ptr())
     assert rel_l2(host(torch, out), g["tgc"]) < TOL
-    ctx.log_compress(dev(torch, g["tgc"]).data_ptr(), n0 * n1, 50.0, 2.0, -1.0, out.data_ptr())
+    ctx.log_compress(tgc.data_ptr(), n0 * n1, 50.0, 2.0, -1.0, out.data_ptr())
     assert rel_l2(host(torch, out), g["log"]) < TOL
-    ctx.log_compress(dev(torch, g["tgc"]).data_ptr(), n0 * n1, 40.0, 0.0, float(g["tgc"].max() * 0.5), out.data_ptr())
+    ctx.log_compress(tgc.data_ptr(), n0 * n1, 40.0, 0.0, float(g["tgc"].max() * 0.5), out.data_ptr())
     assert rel_l2(host(torch, out), g["log_ref"]) < TOL
     sgrid = capi.Grid(1, b["sax0"], b["sax1"], b["spts"])
     px = torch.empty((40, 50), dtype=torch.float32, device="cuda")
-    ext = ctx.scan_convert(dev(torch, g["sc_img"]).data_ptr(), sgrid, 50, 40, -1.0, px.data_ptr())
+    img = dev(torch, g["sc_img"])
+    ext = ctx.scan_convert(img.data_ptr(), sgrid, 50, 40, -1.0, px.data_ptr())
     assert rel_l2(host(torch, px), g["sc_sector"]) < TOL
     assert np.array_equal(ext, g["sc_sector_ext"])
     cgrid = capi.Grid(0, b["ax0"], b["ax1"], b["pts"])
     px = torch.empty((47, 33), dtype=torch.float32, device="cuda")
-    ctx.scan_convert(dev(torch, g["env_iq"]).data_ptr(), cgrid, 33, 47, 0.0, px.data_ptr())
+    ctx.scan_convert(env_iq.data_ptr(), cgrid, 33, 47, 0.0, px.data_ptr())
     assert rel_l2(host(torch, px), g["sc_cart"]) < TOL
 
 
@@ -333,12 +377,14 @@ def test_displacement_and_strain_match_reference(capi, ctx, torch, golden):
     n0, n1 = a.shape
     ax = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
     cr = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
-    ctx.axial_displacement(dev(torch, a).data_ptr(), dev(torch, b).data_ptr(), n0, n1, g["disp_ax1"], 5e6, 1540.0,
-                           4, 1, 5, ax.data_ptr(), cr.data_ptr())
+    da, db = dev(torch, a), dev(torch, b)
+    ctx.axial_displacement(da.data_ptr(), db.data_ptr(), n0, n1, g["disp_ax1"], 5e6, 1540.0, 4, 1, 5,
+                           ax.data_ptr(), cr.data_ptr())
     assert rel_l2(host(torch, ax), g["disp_axial"]) < TOL
     assert rel_l2(host(torch, cr), g["disp_corr"]) < TOL
     st = torch.empty((n0, n1), dtype=torch.float32, device="cuda")
-    ctx.axial_strain(dev(torch, g["disp_axial"]).data_ptr(), n0, n1, g["disp_ax1"], 9, st.data_ptr())
+    dax = dev(torch, g["disp_axial"])
+    ctx.axial_strain(dax.data_ptr(), n0, n1, g["disp_ax1"], 9, st.data_ptr())
     assert rel_l2(host(torch, st), g["strain"]) < TOL
 
 

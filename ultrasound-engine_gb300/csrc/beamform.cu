@@ -439,6 +439,8 @@ struct usx_bf_plan {
   float* d_points = nullptr;
   TxDev* d_tx = nullptr;
   int ev_begin = 0, ev_end = 0;
+  int mv_mode = USX_MV_EXACT;
+  int* d_mv_stats = nullptr;   // [0] FP64 re-solves, [1] factorisation failures
 };
 
 namespace {
@@ -527,10 +529,17 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
   // Minimum variance: per pass, export compounded channel samples, then solve.
   const size_t y_bytes = static_cast<size_t>(n_frames) * n_pix * a.n_ch * sizeof(float2);
   const size_t acc_bytes = static_cast<size_t>(n_frames) * n_pix * sizeof(float);
+  const size_t fb_bytes = static_cast<size_t>(n_frames) * n_pix * sizeof(int2);
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   void* ws = nullptr;
-  if (int rc = scratch(ctx, y_bytes + acc_bytes + 256, &ws)) return rc;
-  a.y_out = static_cast<float2*>(ws);
-  a.acc_out = reinterpret_cast<float*>(static_cast<char*>(ws) + ((y_bytes + 255) / 256) * 256);
+  if (int rc = scratch(ctx, up(y_bytes) + up(acc_bytes) + up(fb_bytes) + 256, &ws)) return rc;
+  char* wsb = static_cast<char*>(ws);
+  a.y_out = reinterpret_cast<float2*>(wsb);
+  a.acc_out = reinterpret_cast<float*>(wsb + up(y_bytes));
+  int2* fb_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes));
+  int* fb_count = reinterpret_cast<int*>(wsb + up(y_bytes) + up(acc_bytes) + up(fb_bytes));
+  const bool tensor = plan->mv_mode == USX_MV_TENSOR &&
+                      mv_tc_supported(a.n_ch, a.mv_subarray, a.mv_range_average);
   const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
   const size_t smem = sizeof(MvShared) * kMvWarps;
   USX_CUDA(cudaFuncSetAttribute(mv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -548,10 +557,19 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       das_kernel<false><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
     prof_end(ctx);
     USX_CHECK_LAUNCH("das_kernel(mv export)");
-    prof_begin(ctx, "mv_kernel");
-    mv_kernel<<<grid_mv, 32 * kMvWarps, smem, ctx->stream>>>(b);
-    prof_end(ctx);
-    USX_CHECK_LAUNCH("mv_kernel");
+    if (tensor) {
+      USX_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(int), ctx->stream));
+      if (int rc = launch_mv_tc(ctx, b.y_out, b.points, b.out, b.out_stride, b.acc_out, b.n_ch, b.n_pix, b.n1,
+                                n_frames, b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number,
+                                b.tukey_alpha, b.rx_window, b.half_nm1, b.pitch, b.cf, incoherent ? 1 : 0,
+                                plan->d_mv_stats, fb_count, fb_list, static_cast<int>(n_frames * n_pix)))
+        return rc;
+    } else {
+      prof_begin(ctx, "mv_kernel");
+      mv_kernel<<<grid_mv, 32 * kMvWarps, smem, ctx->stream>>>(b);
+      prof_end(ctx);
+      USX_CHECK_LAUNCH("mv_kernel");
+    }
   }
   if (incoherent) {
     const long n = n_pix * n_frames;
@@ -605,12 +623,15 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
   for (int e = 0; e < n_ev; ++e) txs[static_cast<size_t>(e)] = make_txdev(cd->probe, cd->transmits[e]);
   cudaError_t e1 = cudaMalloc(&p->d_points, sizeof(float) * 3 * n_pix);
   cudaError_t e2 = cudaMalloc(&p->d_tx, sizeof(TxDev) * std::max(1, n_ev));
-  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+  cudaError_t e3 = cudaMalloc(&p->d_mv_stats, sizeof(int) * 4);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     cudaFree(p->d_points);
     cudaFree(p->d_tx);
+    cudaFree(p->d_mv_stats);
     delete p;
     return fail(USX_ERR_NOMEM, "usx_cu_bf_plan_create: device allocation failed");
   }
+  cudaMemset(p->d_mv_stats, 0, sizeof(int) * 4);
   cudaMemcpy(p->d_points, points_host, sizeof(float) * 3 * n_pix, cudaMemcpyHostToDevice);
   cudaMemcpy(p->d_tx, txs.data(), sizeof(TxDev) * n_ev, cudaMemcpyHostToDevice);
   *out = p;
@@ -622,6 +643,7 @@ int usx_cu_bf_plan_destroy(usx_bf_plan* plan) {
   cudaStreamSynchronize(plan->ctx->stream);
   cudaFree(plan->d_points);
   cudaFree(plan->d_tx);
+  cudaFree(plan->d_mv_stats);
   delete plan;
   return USX_OK;
 }
@@ -648,6 +670,28 @@ int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_fr
   if (plan->ev_begin + static_cast<long>(events_per_frame) * n_frames > plan->ev_end)
     return fail(USX_ERR_INVALID, "beamform_sequence: frames exceed the plan's events");
   return bf_execute(plan, n_frames, data, 0, frames, frame_stride, events_per_frame);
+}
+
+int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: null plan");
+  if (mode != USX_MV_EXACT && mode != USX_MV_TENSOR)
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: unknown mode");
+  if (mode == USX_MV_TENSOR &&
+      !mv_tc_supported(plan->cd.probe.n_elements, plan->cfg.mv_subarray, plan->cfg.mv_range_average))
+    return fail(USX_ERR_UNSUPPORTED, "tensor-core minimum variance supports <= 128 channels, L <= 64, range +/-4");
+  plan->mv_mode = mode;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_mv_stats(usx_bf_plan* plan, int64_t* fp64_resolves, int64_t* factorization_failures) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_mv_stats: null plan");
+  int h[2] = {0, 0};
+  USX_CUDA(cudaMemcpyAsync(h, plan->d_mv_stats, sizeof(h), cudaMemcpyDeviceToHost, plan->ctx->stream));
+  USX_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  USX_CUDA(cudaMemsetAsync(plan->d_mv_stats, 0, sizeof(h), plan->ctx->stream));
+  if (fp64_resolves) *fp64_resolves = h[0];
+  if (factorization_failures) *factorization_failures = h[1];
+  return USX_OK;
 }
 
 int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame) {

@@ -1,0 +1,737 @@
+// mv_tc.cu — minimum variance with the covariance on the tensor cores
+// (reference beamformer.cpp:137-214 is the algorithm; this is the fast
+// formulation, selected with USX_MV_TENSOR).
+//
+// Per pixel, with the active channels a_0 < ... < a_{n-1}, subarray length L,
+// n_sub = n - L + 1 subarrays and n_d valid range offsets, the spatially
+// smoothed covariance is R = X X^H / K with the K = n_d * n_sub snapshot
+// columns x_(d,s)[i] = y_d[s + i] (Hankel in (s, i)). Stacking real and
+// imaginary parts as interleaved rows of a 2L x K real matrix A, G = A A^T
+// holds every product R needs:
+//     R[a][b] = (G[2a][2b] + G[2a+1][2b+1]) + i (G[2a+1][2b] - G[2a][2b+1]).
+// G is computed with mma.sync m16n8k16 (BF16 operands, FP32 accumulation),
+// upper block-triangle only; A is never materialised: each fragment element is
+// fetched from a per-pixel shared staging of the snapshots (scaled by a power
+// of two so the scale is exact) in pairs laid out so that any two consecutive
+// snapshot entries are one aligned 32-bit load.
+//
+// The Capon solve then runs in FP32 on the BF16 covariance R~ (+ diagonal
+// loading from the exact FP32 trace), followed by one step of iterative
+// refinement against the exact FP32 covariance, applied as R w = X (X^H w)/K
+// directly from the FP32 snapshots (O(K L), no second covariance):
+//     w0 = R~^-1 1,  r = 1 - (R + eps I) w0,  w = w0 + R~^-1 r.
+// If the refined residual |1 - (R + eps I) w| / sqrt(L) still exceeds 1e-3,
+// the pixel is re-solved in FP64 (covariance and Cholesky) on the GPU.
+// Fallback rules are the reference's: n_active < 4 or a failed factorisation
+// or |sum w| < 1e-30 give the DAS sum.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "usx_internal.cuh"
+
+namespace usxcu {
+
+namespace {
+
+constexpr int kTcWarps = 4;
+constexpr int kTcMaxL = 64;
+constexpr int kTcMaxCh = 128;
+constexpr float kRefineGate = 1e-3f;
+
+struct MvTcLayout {
+  int n_ch, n_dmax, lmax;
+  int words;          // 32-bit words per (part, parity, d) staging row
+  size_t off_act, off_yf, off_yb, off_r, off_w, off_t, bytes;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~static_cast<size_t>(15); }
+
+__host__ __device__ inline MvTcLayout mv_tc_layout(int n_ch, int n_dmax, int lmax) {
+  MvTcLayout l;
+  l.n_ch = n_ch;
+  l.n_dmax = n_dmax;
+  l.lmax = lmax;
+  l.words = n_ch / 2 + 10;  // pairs up to index n_ch + 16 (masked subarray starts)
+  size_t o = 0;
+  l.off_act = o;  o = align16(o + sizeof(int) * n_ch);
+  l.off_yf = o;   o = align16(o + sizeof(float2) * n_dmax * n_ch);
+  l.off_yb = o;   o = align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);
+  l.off_r = o;    o = align16(o + sizeof(float2) * (lmax * (lmax + 1) / 2));
+  l.off_w = o;    o = align16(o + sizeof(float2) * 4 * lmax);
+  l.off_t = o;    o = align16(o + sizeof(float2) * n_dmax * n_ch);
+  l.bytes = o;
+  return l;
+}
+
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }  // lower, i >= j
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
+  return static_cast<uint32_t>(__bfloat16_as_ushort(l)) | (static_cast<uint32_t>(__bfloat16_as_ushort(h)) << 16);
+}
+
+// Pair (v[q], v[q+1]) of part p (0 re, 1 im) of staged row d, as one word.
+__device__ __forceinline__ uint32_t pair_at(const uint32_t* yb, int words, int n_dmax, int p, int d, int q) {
+  const int par = q & 1;
+  return yb[((p * 2 + par) * n_dmax + d) * words + (q >> 1)];
+}
+
+// Zero the halves of a pair whose subarray start s (for the low half) or s+1
+// (for the high half) is past the last subarray.
+__device__ __forceinline__ uint32_t mask_pair(uint32_t w, int s, int n_sub) {
+  if (s + 1 < n_sub) return w;
+  if (s < n_sub) return w & 0x0000ffffu;
+  return 0u;
+}
+
+struct MvTcArgs {
+  const float2* y;        // [frame][pix][n_ch] compounded channel samples
+  const float* points;
+  float2* out;
+  long out_stride;
+  float* acc_out;
+  int n_ch, n_pix, n1;
+  int mv_subarray, range_avg;
+  float loading, f_number, tukey_alpha, half_nm1, pitch;
+  int rx_window, cf, incoherent;
+  int n_dmax, lmax;
+  int* stats;             // [0] FP64 fallbacks, [1] factorisation failures
+  int* fallback_count;    // pixels whose refined residual failed
+  int2* fallback;         // (pixel, frame) of each, up to fallback_cap
+  int fallback_cap;
+};
+
+__global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) {
+  extern __shared__ float4 tc_smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const MvTcLayout lay = mv_tc_layout(a.n_ch, a.n_dmax, a.lmax);
+  char* base = reinterpret_cast<char*>(tc_smem_raw) + warp * lay.bytes;
+  int* act = reinterpret_cast<int*>(base + lay.off_act);
+  float2* yf = reinterpret_cast<float2*>(base + lay.off_yf);
+  uint32_t* yb = reinterpret_cast<uint32_t*>(base + lay.off_yb);
+  float2* Rl = reinterpret_cast<float2*>(base + lay.off_r);
+  float2* wv = reinterpret_cast<float2*>(base + lay.off_w);   // w0 | r | w1 | scratch
+  float2* tk = reinterpret_cast<float2*>(base + lay.off_t);
+
+  const long gw = static_cast<long>(blockIdx.x) * kTcWarps + warp;
+  if (gw >= a.n_pix) return;
+  const int pix = static_cast<int>(gw);
+  const long frame = blockIdx.y;
+  const int j = pix % a.n1;
+  const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+  const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+  const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+
+  // Active channels in ascending order.
+  int n_act = 0;
+  for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+    const int ch = c0 + lane;
+    bool on = false;
+    if (ch < a.n_ch)
+      on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                           a.tukey_alpha) > 0.0f;
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    if (on) act[n_act + __popc(m & ((1u << lane) - 1u))] = ch;
+    n_act += __popc(m);
+  }
+  __syncwarp();
+
+  auto center_das = [&]() {
+    cplx acc = mk(0.f, 0.f);
+    for (int q = 0; q < n_act; ++q) {
+      const float2 v = yc[act[q]];
+      acc = cadd(acc, mk(v.x, v.y));
+    }
+    return acc;
+  };
+  auto finish = [&](cplx out) {
+    if (lane != 0) return;
+    if (a.cf && n_act > 0) {
+      cplx coh = mk(0.f, 0.f);
+      float inc = 0.0f;
+      for (int q = 0; q < n_act; ++q) {
+        const float2 v = yc[act[q]];
+        coh = cadd(coh, mk(v.x, v.y));
+        inc += cnorm(mk(v.x, v.y));
+      }
+      out = cscale(out, (inc > 0.0f) ? cnorm(coh) / (static_cast<float>(n_act) * inc) : 0.0f);
+    }
+    if (a.incoherent)
+      a.acc_out[frame * a.n_pix + pix] += cnorm(out);
+    else
+      a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+  };
+
+  if (n_act == 0) {
+    if (!a.incoherent && lane == 0) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
+    return;
+  }
+  if (n_act < 4) {
+    const cplx o = center_das();
+    finish(o);
+    return;
+  }
+  int L = a.mv_subarray;
+  const int hi = max(2, n_act / 2);
+  if (L < 2) L = 2;
+  if (L > hi) L = hi;
+  const int n_sub = n_act - L + 1;
+  const int ra = a.range_avg;
+
+  // Stage the FP32 snapshots and their magnitude bound.
+  int n_d = 0, dc = 0;
+  float amax = 0.0f;
+  for (int d = -ra; d <= ra; ++d) {
+    const int jj = j + d;
+    if (jj < 0 || jj >= a.n1) continue;
+    if (d == 0) dc = n_d;
+    const float2* yr = Y + static_cast<long>(pix + d) * a.n_ch;
+    for (int q = lane; q < n_act; q += 32) {
+      const float2 v = yr[act[q]];
+      yf[n_d * a.n_ch + q] = v;
+      amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    ++n_d;
+  }
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if (!(amax > 0.0f)) {
+    finish(mk(0.f, 0.f));
+    return;
+  }
+  // Power-of-two scale: exact, and brings the largest magnitude to [0.5, 1).
+  int e2;
+  frexpf(amax, &e2);
+  const float sc = ldexpf(1.0f, -e2), inv_sc = ldexpf(1.0f, e2);
+  for (int k = lane; k < n_d * a.n_ch; k += 32) {
+    const int q = k % a.n_ch;
+    if (q < n_act) {
+      const float2 v = yf[k];
+      yf[k] = make_float2(v.x * sc, v.y * sc);
+    }
+  }
+  __syncwarp();
+  // BF16 pair staging: word (p, par, d, w) = (v[2w+par], v[2w+par+1]) of part p.
+  for (int k = lane; k < 4 * n_d * lay.words; k += 32) {
+    const int w = k % lay.words;
+    const int d = (k / lay.words) % n_d;
+    const int pp = k / (lay.words * n_d);  // p * 2 + par
+    const int p = pp >> 1, par = pp & 1;
+    const int q0 = 2 * w + par, q1 = q0 + 1;
+    const float2 v0 = q0 < n_act ? yf[d * a.n_ch + q0] : make_float2(0.f, 0.f);
+    const float2 v1 = q1 < n_act ? yf[d * a.n_ch + q1] : make_float2(0.f, 0.f);
+    yb[(pp * a.n_dmax + d) * lay.words + w] = pack_bf16(p ? v0.y : v0.x, p ? v1.y : v1.x);
+  }
+  __syncwarp();
+
+  // ---- G = A A^T on the tensor cores, upper block-triangle ------------------
+  const int g = lane >> 2, t4 = lane & 3;
+  const int two_l = 2 * L;
+  const int MT = (two_l + 15) / 16, NT = (two_l + 7) / 8;
+  const int n_kstep = (n_sub + 15) / 16;
+  const float inv_k = 1.0f / static_cast<float>(n_d * n_sub);
+  for (int mt = 0; mt < MT; ++mt) {
+    float acc[16][4];
+#pragma unroll
+    for (int x = 0; x < 16; ++x) acc[x][0] = acc[x][1] = acc[x][2] = acc[x][3] = 0.f;
+    const int r0 = mt * 16 + g, r1 = r0 + 8;      // A rows of this lane
+    for (int d = 0; d < n_d; ++d) {
+      for (int ks = 0; ks < n_kstep; ++ks) {
+        const int s_lo = ks * 16 + 2 * t4;        // subarray starts of this lane's k pairs
+        const int s_hi = s_lo + 8;
+        uint32_t af[4];
+        // Row r = 2i + p reads y[s + i] of part p; rows past 2L are zero.
+        af[0] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_lo + (r0 >> 1)), s_lo, n_sub) : 0u;
+        af[1] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_lo + (r1 >> 1)), s_lo, n_sub) : 0u;
+        af[2] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_hi + (r0 >> 1)), s_hi, n_sub) : 0u;
+        af[3] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_hi + (r1 >> 1)), s_hi, n_sub) : 0u;
+#pragma unroll
+        for (int x = 0; x < 16; ++x) {
+          const int nt = 2 * mt + x;
+          if (nt < NT) {
+            const int c = nt * 8 + g;               // B column = A row c
+            uint32_t b0 = 0u, b1 = 0u;
+            if (c < two_l) {
+              b0 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_lo + (c >> 1)), s_lo, n_sub);
+              b1 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_hi + (c >> 1)), s_hi, n_sub);
+            }
+            mma16816(acc[x], af, b0, b1);
+          }
+        }
+      }
+    }
+    // Fold the real-embedding blocks into complex entries R[a][b], b >= a.
+#pragma unroll
+    for (int x = 0; x < 16; ++x) {
+      const int nt = 2 * mt + x;
+      if (nt >= NT) continue;
+      // acc[x][0..1]: row r0, cols c0, c0+1; acc[x][2..3]: row r1.
+      const float o0 = __shfl_xor_sync(0xffffffffu, acc[x][0], 4);
+      const float o1 = __shfl_xor_sync(0xffffffffu, acc[x][1], 4);
+      const float o2 = __shfl_xor_sync(0xffffffffu, acc[x][2], 4);
+      const float o3 = __shfl_xor_sync(0xffffffffu, acc[x][3], 4);
+      if ((g & 1) == 0) {
+        const int c0 = nt * 8 + 2 * t4;
+        const int bcol = c0 >> 1;
+        // rows (r0, r0+1) and (r1, r1+1) are complex rows ar0 = r0/2, ar1 = r1/2.
+        const int ar0 = r0 >> 1, ar1 = r1 >> 1;
+        if (bcol < L && ar0 < L && bcol >= ar0) {
+          const float re = acc[x][0] + o1, im = o0 - acc[x][1];
+          Rl[tri(bcol, ar0)] = make_float2(re * inv_k, -im * inv_k);
+        }
+        if (bcol < L && ar1 < L && bcol >= ar1) {
+          const float re = acc[x][2] + o3, im = o2 - acc[x][3];
+          Rl[tri(bcol, ar1)] = make_float2(re * inv_k, -im * inv_k);
+        }
+      }
+    }
+  }
+  __syncwarp();
+
+  // ---- exact trace and diagonal loading ------------------------------------
+  float tr = 0.0f;
+  for (int k = lane; k < n_d * n_sub; k += 32) {
+    const int d = k / n_sub, s = k - d * n_sub;
+    for (int i = 0; i < L; ++i) {
+      const float2 v = yf[d * a.n_ch + s + i];
+      tr += v.x * v.x + v.y * v.y;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+  tr *= inv_k;
+  const float eps = fmaxf(a.loading * tr / static_cast<float>(L), 1e-20f);
+  for (int i = lane; i < L; i += 32) Rl[tri(i, i)].x += eps;
+  __syncwarp();
+
+  // ---- Cholesky of R~ (lower, in place), right-looking ---------------------
+  bool ok = true;
+  for (int c = 0; c < L; ++c) {
+    const float dgl = Rl[tri(c, c)].x;
+    if (!(dgl > 0.0f)) {
+      ok = false;
+      break;
+    }
+    const float ljj = sqrtf(dgl);
+    const float inv = 1.0f / ljj;
+    __syncwarp();
+    for (int i = c + 1 + lane; i < L; i += 32) {
+      const float2 v = Rl[tri(i, c)];
+      Rl[tri(i, c)] = make_float2(v.x * inv, v.y * inv);
+    }
+    if (lane == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
+    __syncwarp();
+    for (int i = c + 1 + lane; i < L; i += 32) {
+      const float2 lic = Rl[tri(i, c)];
+      for (int k = c + 1; k <= i; ++k) {
+        const float2 lkc = Rl[tri(k, c)];
+        float2 v = Rl[tri(i, k)];
+        // v -= lic * conj(lkc)
+        v.x -= lic.x * lkc.x + lic.y * lkc.y;
+        v.y -= lic.y * lkc.x - lic.x * lkc.y;
+        Rl[tri(i, k)] = v;
+      }
+    }
+    __syncwarp();
+  }
+  if (!ok) {
+    if (a.stats && lane == 0) atomicAdd(a.stats + 1, 1);
+    const cplx o = center_das();
+    finish(o);
+    return;
+  }
+
+  // Triangular solves with the factor, vector in registers (rows lane, lane+32).
+  auto solve = [&](float2 (&v)[2]) {
+    for (int c = 0; c < L; ++c) {  // L y = v
+      const int own = c & 31, sl = c >> 5;
+      float2 vc = make_float2(0.f, 0.f);
+      if (lane == own) {
+        const float ljj = Rl[tri(c, c)].x;
+        v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+      }
+      vc.x = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+      vc.y = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        if (i > c && i < L) {
+          const float2 lic = Rl[tri(i, c)];
+          v[s2].x -= lic.x * vc.x - lic.y * vc.y;
+          v[s2].y -= lic.x * vc.y + lic.y * vc.x;
+        }
+      }
+    }
+    for (int c = L - 1; c >= 0; --c) {  // L^H x = y
+      const int own = c & 31, sl = c >> 5;
+      if (lane == own) {
+        const float ljj = Rl[tri(c, c)].x;
+        v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+      }
+      float2 vc;
+      vc.x = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+      vc.y = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        if (i < c) {
+          const float2 lci = Rl[tri(c, i)];  // (L^H)[i][c] = conj(L[c][i])
+          v[s2].x -= lci.x * vc.x + lci.y * vc.y;
+          v[s2].y -= lci.x * vc.y - lci.y * vc.x;
+        }
+      }
+    }
+  };
+  // Residual 1 - (R + eps I) w with R = X X^H / K from the FP32 snapshots.
+  auto residual = [&](const float2 (&w)[2], float2 (&r)[2]) {
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      if (i < L) wv[i] = w[s2];
+    }
+    __syncwarp();
+    for (int k = lane; k < n_d * n_sub; k += 32) {  // t_k = x_k^H w
+      const int d = k / n_sub, s = k - d * n_sub;  // once per snapshot
+      float tre = 0.f, tim = 0.f;
+      for (int i = 0; i < L; ++i) {
+        const float2 x = yf[d * a.n_ch + s + i];
+        const float2 w_ = wv[i];
+        tre += x.x * w_.x + x.y * w_.y;
+        tim += x.x * w_.y - x.y * w_.x;
+      }
+      tk[k] = make_float2(tre, tim);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      r[s2] = make_float2(0.f, 0.f);
+      if (i < L) {
+        float are = 0.f, aim = 0.f;
+        for (int d = 0; d < n_d; ++d) {
+          const float2* xr = yf + d * a.n_ch + i;
+          const float2* tr = tk + d * n_sub;
+          for (int s = 0; s < n_sub; ++s) {
+            const float2 x = xr[s];
+            const float2 t = tr[s];
+            are += x.x * t.x - x.y * t.y;
+            aim += x.x * t.y + x.y * t.x;
+          }
+        }
+        r[s2] = make_float2(1.0f - (are * inv_k + eps * w[s2].x), -(aim * inv_k + eps * w[s2].y));
+      }
+    }
+    __syncwarp();
+  };
+
+  float2 w[2] = {make_float2(1.f, 0.f), make_float2(1.f, 0.f)};
+  if (lane + 32 >= L) w[1] = make_float2(0.f, 0.f);
+  if (lane >= L) w[0] = make_float2(0.f, 0.f);
+  solve(w);
+  float2 r[2];
+  residual(w, r);
+  solve(r);
+#pragma unroll
+  for (int s2 = 0; s2 < 2; ++s2) {
+    w[s2].x += r[s2].x;
+    w[s2].y += r[s2].y;
+  }
+  residual(w, r);
+  float rn = 0.f;
+#pragma unroll
+  for (int s2 = 0; s2 < 2; ++s2) rn += r[s2].x * r[s2].x + r[s2].y * r[s2].y;
+  for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
+  const bool refine_ok = sqrtf(rn / static_cast<float>(L)) <= kRefineGate;
+
+  if (!refine_ok) {
+    // Re-solved in FP64 by mv_fp64_kernel; nothing is written here.
+    if (lane == 0) {
+      const int slot = atomicAdd(a.fallback_count, 1);
+      if (slot < a.fallback_cap) a.fallback[slot] = make_int2(pix, static_cast<int>(frame));
+    }
+    return;
+  }
+
+  // ---- apply: out = sum conj(w_i) avg_i / sum w * n_act ------------------------
+  float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
+#pragma unroll
+  for (int s2 = 0; s2 < 2; ++s2) {
+    const int i = lane + 32 * s2;
+    if (i < L) {
+      dre += w[s2].x;
+      dim += w[s2].y;
+      float are = 0.f, aim = 0.f;
+      for (int s = 0; s < n_sub; ++s) {
+        const float2 v = yf[dc * a.n_ch + s + i];
+        are += v.x;
+        aim += v.y;
+      }
+      are = are * inv_sc / static_cast<float>(n_sub);
+      aim = aim * inv_sc / static_cast<float>(n_sub);
+      ore += w[s2].x * are + w[s2].y * aim;   // conj(w) * avg
+      oim += w[s2].x * aim - w[s2].y * are;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dre += __shfl_xor_sync(0xffffffffu, dre, o);
+    dim += __shfl_xor_sync(0xffffffffu, dim, o);
+    ore += __shfl_xor_sync(0xffffffffu, ore, o);
+    oim += __shfl_xor_sync(0xffffffffu, oim, o);
+  }
+  cplx out;
+  if (hypotf(dre, dim) < 1e-30f) {
+    out = center_das();
+  } else {
+    out = cscale(cdiv_wide(mk(ore, oim), mk(dre, dim)), static_cast<float>(n_act));
+  }
+  finish(out);
+}
+
+// FP64 re-solve of the pixels whose refined FP32 residual failed: covariance
+// from the snapshots, Cholesky and solves in double, one warp per pixel.
+
+__global__ void __launch_bounds__(32) mv_fp64_kernel(const MvTcArgs a) {
+  extern __shared__ double2 f64_smem[];
+  const int lane = threadIdx.x;
+  const int count = min(*a.fallback_count, a.fallback_cap);
+  double2* Rd = f64_smem;                                    // packed lower L(L+1)/2
+  int* act = reinterpret_cast<int*>(Rd + a.lmax * (a.lmax + 1) / 2);
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    const int2 pf = a.fallback[item];
+    const int pix = pf.x;
+    const long frame = pf.y;
+    const int j = pix % a.n1;
+    const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+    const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+    __syncwarp();
+    int n_act = 0;
+    for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+      const int ch = c0 + lane;
+      bool on = false;
+      if (ch < a.n_ch)
+        on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                             a.tukey_alpha) > 0.0f;
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (on) act[n_act + __popc(m & ((1u << lane) - 1u))] = ch;
+      n_act += __popc(m);
+    }
+    __syncwarp();
+    int L = a.mv_subarray;
+    const int hi = max(2, n_act / 2);
+    if (L < 2) L = 2;
+    if (L > hi) L = hi;
+    const int n_sub = n_act - L + 1;
+    int dlo = -a.range_avg, dhi = a.range_avg;
+    while (j + dlo < 0) ++dlo;
+    while (j + dhi >= a.n1) --dhi;
+    const int n_d = dhi - dlo + 1;
+    const double inv_k = 1.0 / static_cast<double>(n_d * n_sub);
+    for (int e = lane; e < L * (L + 1) / 2; e += 32) {
+      int i = 0, rem = e;
+      while (rem > i) {
+        rem -= i + 1;
+        ++i;
+      }
+      const int jj = rem;
+      double re = 0.0, im = 0.0;
+      for (int d = dlo; d <= dhi; ++d) {
+        const float2* yr = Y + static_cast<long>(pix + d) * a.n_ch;
+        for (int s = 0; s < n_sub; ++s) {
+          const float2 xi = yr[act[s + i]], xj = yr[act[s + jj]];
+          re += static_cast<double>(xi.x) * xj.x + static_cast<double>(xi.y) * xj.y;
+          im += static_cast<double>(xi.y) * xj.x - static_cast<double>(xi.x) * xj.y;
+        }
+      }
+      Rd[e] = make_double2(re * inv_k, im * inv_k);
+    }
+    __syncwarp();
+    double tr = 0.0;
+    for (int i = lane; i < L; i += 32) tr += Rd[tri(i, i)].x;
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    const double eps = fmax(static_cast<double>(a.loading) * tr / L, 1e-20);
+    for (int i = lane; i < L; i += 32) Rd[tri(i, i)].x += eps;
+    __syncwarp();
+    bool ok = true;
+    for (int c = 0; c < L; ++c) {
+      const double dgl = Rd[tri(c, c)].x;
+      if (!(dgl > 0.0)) {
+        ok = false;
+        break;
+      }
+      const double ljj = sqrt(dgl);
+      __syncwarp();
+      for (int i = c + 1 + lane; i < L; i += 32) {
+        const double2 v = Rd[tri(i, c)];
+        Rd[tri(i, c)] = make_double2(v.x / ljj, v.y / ljj);
+      }
+      if (lane == 0) Rd[tri(c, c)] = make_double2(ljj, 0.0);
+      __syncwarp();
+      for (int i = c + 1 + lane; i < L; i += 32) {
+        const double2 lic = Rd[tri(i, c)];
+        for (int k = c + 1; k <= i; ++k) {
+          const double2 lkc = Rd[tri(k, c)];
+          double2 v = Rd[tri(i, k)];
+          v.x -= lic.x * lkc.x + lic.y * lkc.y;
+          v.y -= lic.y * lkc.x - lic.x * lkc.y;
+          Rd[tri(i, k)] = v;
+        }
+      }
+      __syncwarp();
+    }
+    cplx out;
+    if (!ok) {
+      if (a.stats && lane == 0) atomicAdd(a.stats + 1, 1);
+      out = mk(0.f, 0.f);
+      for (int q = 0; q < n_act; ++q) out = cadd(out, mk(yc[act[q]].x, yc[act[q]].y));
+    } else {
+      double2 v[2];
+      for (int s2 = 0; s2 < 2; ++s2) v[s2] = (lane + 32 * s2 < L) ? make_double2(1.0, 0.0) : make_double2(0.0, 0.0);
+      for (int c = 0; c < L; ++c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const double l = Rd[tri(c, c)].x;
+          v[sl] = make_double2(v[sl].x / l, v[sl].y / l);
+        }
+        const double vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const double vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i > c && i < L) {
+            const double2 l = Rd[tri(i, c)];
+            v[s2].x -= l.x * vx - l.y * vy;
+            v[s2].y -= l.x * vy + l.y * vx;
+          }
+        }
+      }
+      for (int c = L - 1; c >= 0; --c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const double l = Rd[tri(c, c)].x;
+          v[sl] = make_double2(v[sl].x / l, v[sl].y / l);
+        }
+        const double vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const double vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i < c) {
+            const double2 l = Rd[tri(c, i)];
+            v[s2].x -= l.x * vx + l.y * vy;
+            v[s2].y -= l.x * vy - l.y * vx;
+          }
+        }
+      }
+      double dre = 0, dim = 0, ore = 0, oim = 0;
+      const float2* ycen = yc;
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        if (i >= L) continue;
+        dre += v[s2].x;
+        dim += v[s2].y;
+        double are = 0, aim = 0;
+        for (int s = 0; s < n_sub; ++s) {
+          are += ycen[act[s + i]].x;
+          aim += ycen[act[s + i]].y;
+        }
+        are /= n_sub;
+        aim /= n_sub;
+        ore += v[s2].x * are + v[s2].y * aim;
+        oim += v[s2].x * aim - v[s2].y * are;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        dre += __shfl_xor_sync(0xffffffffu, dre, o);
+        dim += __shfl_xor_sync(0xffffffffu, dim, o);
+        ore += __shfl_xor_sync(0xffffffffu, ore, o);
+        oim += __shfl_xor_sync(0xffffffffu, oim, o);
+      }
+      const double den = dre * dre + dim * dim;
+      if (sqrt(den) < 1e-30) {
+        out = mk(0.f, 0.f);
+        for (int q = 0; q < n_act; ++q) out = cadd(out, mk(yc[act[q]].x, yc[act[q]].y));
+      } else {
+        out = mk(static_cast<float>((ore * dre + oim * dim) / den * n_act),
+                 static_cast<float>((oim * dre - ore * dim) / den * n_act));
+      }
+    }
+    if (lane == 0) {
+      if (a.cf) {
+        cplx coh = mk(0.f, 0.f);
+        float inc = 0.0f;
+        for (int q = 0; q < n_act; ++q) {
+          const float2 y = yc[act[q]];
+          coh = cadd(coh, mk(y.x, y.y));
+          inc += cnorm(mk(y.x, y.y));
+        }
+        out = cscale(out, (inc > 0.0f) ? cnorm(coh) / (static_cast<float>(n_act) * inc) : 0.0f);
+      }
+      if (a.incoherent)
+        a.acc_out[frame * a.n_pix + pix] += cnorm(out);
+      else
+        a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+    }
+  }
+}
+
+}  // namespace
+
+int mv_tc_supported(int n_ch, int mv_subarray, int range_avg) {
+  const int lmax = std::min(std::max(mv_subarray, 2), std::max(2, n_ch / 2));
+  if (n_ch > kTcMaxCh || lmax > kTcMaxL || range_avg > 4) return 0;
+  const MvTcLayout l = mv_tc_layout(n_ch, 2 * range_avg + 1, lmax);
+  return l.bytes * kTcWarps <= 227 * 1024 ? 1 : 0;
+}
+
+int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,
+                 float* acc_out, int n_ch, int n_pix, int n1, int n_frames, int mv_subarray, int range_avg,
+                 float loading, float f_number, float tukey_alpha, int rx_window, float half_nm1, float pitch,
+                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap) {
+  MvTcArgs a;
+  a.y = y;
+  a.points = points;
+  a.out = out;
+  a.out_stride = out_stride;
+  a.acc_out = acc_out;
+  a.n_ch = n_ch;
+  a.n_pix = n_pix;
+  a.n1 = n1;
+  a.mv_subarray = mv_subarray;
+  a.range_avg = range_avg;
+  a.loading = loading;
+  a.f_number = f_number;
+  a.tukey_alpha = tukey_alpha;
+  a.half_nm1 = half_nm1;
+  a.pitch = pitch;
+  a.rx_window = rx_window;
+  a.cf = cf;
+  a.incoherent = incoherent;
+  a.n_dmax = 2 * range_avg + 1;
+  a.lmax = std::min(std::max(mv_subarray, 2), std::max(2, n_ch / 2));
+  a.stats = stats;
+  a.fallback_count = fallback_count;
+  a.fallback = fallback;
+  a.fallback_cap = fallback_cap;
+  const MvTcLayout l = mv_tc_layout(n_ch, a.n_dmax, a.lmax);
+  const size_t smem = l.bytes * kTcWarps;
+  USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  const dim3 grid(ceil_div(n_pix, kTcWarps), n_frames);
+  prof_begin(ctx, "mv_tc_kernel");
+  mv_tc_kernel<<<grid, 32 * kTcWarps, smem, ctx->stream>>>(a);
+  prof_end(ctx);
+  USX_CHECK_LAUNCH("mv_tc_kernel");
+  // FP64 re-solve of the pixels whose refined residual failed (usually none).
+  const size_t smem64 = sizeof(double2) * (a.lmax * (a.lmax + 1) / 2) + sizeof(int) * n_ch;
+  USX_CUDA(cudaFuncSetAttribute(mv_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem64)));
+  prof_begin(ctx, "mv_fp64_kernel");
+  mv_fp64_kernel<<<ctx->sm_count * 4, 32, smem64, ctx->stream>>>(a);
+  prof_end(ctx);
+  USX_CHECK_LAUNCH("mv_fp64_kernel");
+  return USX_OK;
+}
+
+}  // namespace usxcu

@@ -215,4 +215,11 @@ TxDev make_txdev(const usx_probe& probe, const usx_transmit& tx);
 
 inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); }
 
+// Tensor-core minimum variance (mv_tc.cu).
+int mv_tc_supported(int n_ch, int mv_subarray, int range_avg);
+int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,
+                 float* acc_out, int n_ch, int n_pix, int n1, int n_frames, int mv_subarray, int range_avg,
+                 float loading, float f_number, float tukey_alpha, int rx_window, float half_nm1, float pitch,
+                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap);
+
 }  // namespace usxcu

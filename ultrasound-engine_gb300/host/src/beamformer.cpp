@@ -6,6 +6,7 @@
 #include "usx/beamformer.hpp"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <list>
 #include <mutex>
@@ -89,6 +90,14 @@ class PlanCache {
     usx_bf_plan* plan = nullptr;
     rt::check(usx_cu_bf_plan_create(key.ctx, &ch.cd, &g, desc::points(grid), &b, ev_begin, ev_end, &plan),
               "beamformer plan");
+    // Minimum variance runs on the tensor cores (BF16 covariance, FP32
+    // refinement, FP64 re-solve where needed) unless USX_MV_SOLVER=exact asks
+    // for the reference's FP32 operation order.
+    if (cfg.combiner == Combiner::MV) {
+      const char* solver = std::getenv("USX_MV_SOLVER");
+      const bool exact = solver && std::string(solver) == "exact";
+      if (!exact) usx_cu_bf_plan_set_mv_mode(plan, USX_MV_TENSOR);  // unsupported shapes stay exact
+    }
     entries_.emplace_front(std::move(key), plan);
     while (entries_.size() > kMaxPlans) {
       usx_cu_bf_plan_destroy(entries_.back().second);

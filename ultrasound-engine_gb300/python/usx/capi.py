@@ -307,6 +307,15 @@ class Plan:
         check(lib().usx_cu_bf_execute_sequence(self._h, events_per_frame, n_frames, vp(data_ptr), vp(frames_ptr),
                                                C.c_int64(frame_stride)), "bf_execute_sequence")
 
+    def set_mv_mode(self, mode: int) -> None:
+        """0: FP32 in the reference's order; 1: BF16 tensor-core covariance + refinement."""
+        check(lib().usx_cu_bf_plan_set_mv_mode(self._h, int(mode)), "bf_plan_set_mv_mode")
+
+    def mv_stats(self):
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().usx_cu_bf_plan_mv_stats(self._h, C.byref(a), C.byref(b)), "bf_plan_mv_stats")
+        return a.value, b.value
+
     def workspace_bytes(self) -> int:
         n = C.c_size_t()
         check(lib().usx_cu_bf_plan_workspace(self._h, C.byref(n)), "bf_plan_workspace")
