@@ -130,6 +130,16 @@ int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame);
 int usx_cu_bf_execute_batch(usx_bf_plan* plan, int n_frames, const void* data,
                             int64_t data_stride, float* frames, int64_t frame_stride);
 
+/* Arithmetic of the delay-and-sum stage (no counterpart in the reference):
+ *   USX_BF_FAST   default: the reference's delay indices and phase arguments
+ *                 bit for bit, the rest with FMA and the receive phasor
+ *                 applied once per channel (~1e-7 relative L2 from the
+ *                 reference);
+ *   USX_BF_EXACT  every operation in the reference's order without
+ *                 contraction (agrees to the last ulp of sincosf/cosf). */
+enum { USX_BF_FAST = 0, USX_BF_EXACT = 1 };
+int usx_cu_bf_plan_set_precision(usx_bf_plan* plan, int precision);
+
 /* Minimum-variance solver of a plan (no counterpart in the reference, whose
  * one solver is combine_mv_windowed, beamformer.cpp:137-214):
  *   USX_MV_EXACT   FP32, the reference's operation order (default);

@@ -163,6 +163,25 @@ def test_beamform_matches_reference(capi, ctx, torch, golden, name):
     assert rel_l2(out, g[f"bf_{name}"]) < tol
 
 
+@pytest.mark.parametrize("name", ["das", "cf", "dmas", "incoh", "select", "mv"])
+def test_exact_precision_matches_reference_to_the_ulp(capi, ctx, torch, golden, name):
+    """USX_BF_EXACT evaluates every operation in the reference's order: only the
+    1-ulp differences of the device's sincosf/cosf remain."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    plan = ctx.plan(ch, grid, capi.bf_config(**BF_CASES[name]))
+    plan.set_precision(1)
+    out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
+    d = dev(torch, g["iq"])
+    plan.execute(d.data_ptr(), out.data_ptr())
+    got = host(torch, out)
+    plan.close()
+    assert rel_l2(got, g[f"bf_{name}"]) < (1e-5 if name == "mv" else 1e-6)
+
+
 @pytest.mark.parametrize("name", ["mv", "mv_l4", "mv_cf"])
 def test_mv_tensor_cores_match_reference(capi, ctx, torch, golden, name):
     """BF16 tensor-core covariance + FP32 refinement: within 1e-3 of the reference."""

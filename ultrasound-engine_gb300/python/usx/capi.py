@@ -307,6 +307,10 @@ class Plan:
         check(lib().usx_cu_bf_execute_sequence(self._h, events_per_frame, n_frames, vp(data_ptr), vp(frames_ptr),
                                                C.c_int64(frame_stride)), "bf_execute_sequence")
 
+    def set_precision(self, precision: int) -> None:
+        """0: fast (default); 1: every operation in the reference's order."""
+        check(lib().usx_cu_bf_plan_set_precision(self._h, int(precision)), "bf_plan_set_precision")
+
     def set_mv_mode(self, mode: int) -> None:
         """0: FP32 in the reference's order; 1: BF16 tensor-core covariance + refinement."""
         check(lib().usx_cu_bf_plan_set_mv_mode(self._h, int(mode)), "bf_plan_set_mv_mode")
