@@ -207,6 +207,24 @@ int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int
                             const float* axis1_host, float fdem, float prf,
                             float speed_of_sound, const usx_doppler_config* cfg, float* velocity,
                             float* power, float* variance, uint8_t* valid);
+/* Colour flow that allocates nothing. No counterpart in the reference: this
+ * is for callers that cannot allocate device memory while they run (a
+ * real-time acquisition loop with a fixed memory budget, or a host that owns
+ * the device allocator and only lends this library a stream). It computes
+ * exactly what usx_cu_color_flow computes, on `stream` (a cudaStream_t; NULL is the legacy default stream)
+ * instead of a context, with its working memory in a fixed array that every
+ * device loading this library reserves until the process exits.
+ *   Limit: n_frames * n0 * n1 <= 1048576 complex samples (8 MiB of scratch);
+ *   larger ensembles return USX_ERR_INVALID (use usx_cu_color_flow).
+ *   The first call on each device looks the array up (cudaGetSymbolAddress);
+ *   make that first call before capturing the stream into a graph.
+ *   All calls share the one array: calls whose work overlaps on the GPU (on
+ *   different streams, or from different threads) race and must be
+ *   serialised by the caller. */
+int usx_cu_color_flow_noalloc(void* stream, const float* ens, int n_frames, int n0, int n1,
+                              const float* axis1_host, float fdem, float prf, float speed_of_sound,
+                              const usx_doppler_config* cfg, float* velocity, float* power,
+                              float* variance, uint8_t* valid, float* nyquist);
 /* power_doppler (doppler.cpp:178-186). */
 int usx_cu_power_doppler(usx_ctx* ctx, const float* ens, int n_frames, int64_t n_pix, int type,
                          int order, float* power);

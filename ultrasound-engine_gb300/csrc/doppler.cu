@@ -11,6 +11,7 @@
 // the device's atan2f/hypotf.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "usx_internal.cuh"
@@ -324,6 +325,47 @@ int launch_flow(usx_ctx* ctx, const float* filt, int n, int n0, int n1, float dz
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------------
+// Colour flow without allocation (usx_cu_color_flow_noalloc).
+//
+// For callers that must not allocate device memory once they are running: a
+// scanner's real-time loop with a fixed memory budget, or code that hands this
+// library a stream but owns the device's allocator. Its working
+// memory, the wall-filtered ensemble and the frame's maximum power, is this
+// fixed array, reserved on every device that loads the library for as long
+// as the process lives: kNoAllocSamples complex samples (8 MiB) plus one
+// word. Host code must not pass the array's name to a kernel: on the host it
+// only stands in for the symbol, so its device address is looked up once per
+// device with cudaGetSymbolAddress.
+namespace {
+
+constexpr long kNoAllocSamples = 1L << 20;
+static __device__ __align__(256) float2 g_noalloc_scratch[kNoAllocSamples + 32];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float2* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch on the current device, looked up on the
+// first call for that device.
+int noalloc_scratch(float2** out) {
+  int dev = 0;
+  USX_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return fail(USX_ERR_UNSUPPORTED, "usx_cu_color_flow_noalloc: device index above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    g_noalloc_addr[dev] = static_cast<float2*>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return USX_OK;
+}
+
+}  // namespace
 }  // namespace usxcu
 
 using namespace usxcu;
@@ -391,6 +433,73 @@ int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int
                              reinterpret_cast<unsigned*>(ctx->d_status + 10)))
       return rc;
   }
+  return USX_OK;
+}
+
+int usx_cu_color_flow_noalloc(void* stream, const float* ens, int n_frames, int n0, int n1,
+                              const float* axis1_host, float fdem, float prf, float speed_of_sound,
+                              const usx_doppler_config* cfg, float* velocity, float* power,
+                              float* variance, uint8_t* valid, float* nyquist) {
+  if (!ens || !cfg || !velocity || !power || !variance || !valid)
+    return fail(USX_ERR_INVALID, "usx_cu_color_flow_noalloc: null argument");
+  if (n_frames < 2) return fail(USX_ERR_INVALID, "color_flow: need at least 2 frames in the ensemble");
+  if (n0 <= 0 || n1 <= 0) return fail(USX_ERR_INVALID, "color_flow: empty grid");
+  if (n_frames > kMaxEns) return fail(USX_ERR_UNSUPPORTED, "ensembles longer than 64 frames are not supported");
+  const long n_pix = static_cast<long>(n0) * n1;
+  if (n_pix * n_frames > kNoAllocSamples)
+    return fail(USX_ERR_INVALID,
+                "usx_cu_color_flow_noalloc: n_frames * n0 * n1 exceeds the 1048576 complex samples of its "
+                "static scratch; use usx_cu_color_flow");
+  float2* scratch = nullptr;
+  if (int rc = noalloc_scratch(&scratch)) return rc;
+  float2* filt = scratch;
+  unsigned* pmax_bits = reinterpret_cast<unsigned*>(scratch + kNoAllocSamples);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+  WallArgs w;
+  w.ens = reinterpret_cast<const float2*>(ens);
+  w.out = filt;
+  w.power = nullptr;
+  w.n_pix = n_pix;
+  w.n = n_frames;
+  w.identity = cfg->wall_filter == USX_WALL_NONE;
+  if (!w.identity) {
+    const std::vector<float> M = reject_matrix(n_frames, cfg->wall_filter == USX_WALL_MEAN ? 0 : cfg->polynomial_order);
+    std::copy(M.begin(), M.end(), w.M);
+  }
+  const int threads = 128;
+  const size_t smem = sizeof(float2) * n_frames * threads;
+  if (smem > 48 * 1024)
+    USX_CUDA(cudaFuncSetAttribute(wall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  wall_kernel<<<ceil_div(n_pix, threads), threads, smem, st>>>(w);
+  USX_CHECK_LAUNCH("wall_kernel");
+
+  FlowArgs f;
+  f.filt = filt;
+  f.n = n_frames;
+  f.n0 = n0;
+  f.n1 = n1;
+  f.ka = std::max(0, cfg->kernel_axial);
+  f.kl = std::max(0, cfg->kernel_lateral);
+  f.loupas = cfg->loupas;
+  f.dz = axial_step(axis1_host, n1);
+  f.fdem = fdem;
+  f.prf = prf;
+  f.c = speed_of_sound;
+  f.coh_thr = cfg->coherence_threshold;
+  f.velocity = velocity;
+  f.power = power;
+  f.variance = variance;
+  f.valid = valid;
+  f.pmax_bits = pmax_bits;
+  // The scratch keeps the previous call's contents: the running maximum must start at zero.
+  USX_CUDA(cudaMemsetAsync(pmax_bits, 0, sizeof(unsigned), st));
+  flow_kernel<<<ceil_div(n_pix, 128), 128, 0, st>>>(f);
+  USX_CHECK_LAUNCH("flow_kernel");
+  const float ratio = std::pow(10.0f, cfg->power_threshold_db / 10.0f);
+  power_gate_kernel<<<ceil_div(n_pix, 256), 256, 0, st>>>(power, valid, n_pix, ratio, pmax_bits);
+  USX_CHECK_LAUNCH("power_gate_kernel");
+  if (nyquist) *nyquist = (fdem > 0.0f) ? speed_of_sound * prf / (4.0f * fdem) : 0.0f;
   return USX_OK;
 }
 

@@ -357,3 +357,18 @@ def profile_read(ctx: Context) -> dict:
         out[name.value.decode()] = (ms.value, n.value)
         i += 1
     return out
+
+
+def color_flow_noalloc(stream: int, ens_ptr, n_frames, n0, n1, axis1, fdem, prf, c, cfg: DopplerConfig,
+                       vel, pw, var, valid) -> float:
+    """usx_cu_color_flow_noalloc: colour flow on `stream` (0: legacy default
+    stream) with no device allocation, working memory in the library's fixed
+    8 MiB array (n_frames * n0 * n1 <= 1048576; larger raises ValueError).
+    Calls overlapping on the GPU share that array and must be serialised."""
+    ax = np.ascontiguousarray(axis1, dtype=np.float32)
+    nyq = C.c_float()
+    check(lib().usx_cu_color_flow_noalloc(vp(stream) if stream else None, vp(ens_ptr), n_frames, n0, n1,
+                                          ax.ctypes.data_as(f32p), C.c_float(fdem), C.c_float(prf), C.c_float(c),
+                                          C.byref(cfg), vp(vel), vp(pw), vp(var), vp(valid), C.byref(nyq)),
+          "color_flow_noalloc")
+    return nyq.value
