@@ -39,6 +39,7 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["ctx.cu", "demod.cu", "beamform.cu", "mv_tc.cu", "post.cu", "doppler.cu", "simulate.cu"]
+FMAD_SOURCES = {"mv_tc.cu"}
 HOST_SOURCES = ["types.cpp", "geometry.cpp", "simulator.cpp", "demodulate.cpp", "beamformer.cpp",
                 "postprocess.cpp", "doppler.cpp", "pipeline.cpp", "runtime.cpp"]
 
@@ -71,7 +72,10 @@ def build_cuda(jobs: int) -> Path:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
         if _stale(o, [s, *_headers()]):
-            cmds.append([NVCC, ARCH, "-lineinfo", "-O3", "-std=c++17", "-fmad=false",
+            # Bit-faithful kernels keep every product and sum separately rounded;
+            # the tensor-core MV (1e-3 tolerance) contracts freely.
+            fmad = "-fmad=true" if src in FMAD_SOURCES else "-fmad=false"
+            cmds.append([NVCC, ARCH, "-lineinfo", "-O3", "-std=c++17", fmad,
                          "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                          "-I", str(INCLUDE), "-c", str(s), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

@@ -56,10 +56,13 @@ __host__ __device__ inline MvTcLayout mv_tc_layout(int n_ch, int n_dmax, int lma
   size_t o = 0;
   l.off_act = o;  o = align16(o + sizeof(int) * n_ch);
   l.off_yf = o;   o = align16(o + sizeof(float2) * n_dmax * n_ch);
-  l.off_yb = o;   o = align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);
+  l.off_yb = o;
+  o = align16(o + (sizeof(uint32_t) * 4 * n_dmax * l.words > sizeof(float2) * n_dmax * n_ch
+                       ? sizeof(uint32_t) * 4 * n_dmax * l.words
+                       : sizeof(float2) * n_dmax * n_ch));  // bf16 pairs, then t_k
   l.off_r = o;    o = align16(o + sizeof(float2) * (lmax * (lmax + 1) / 2));
-  l.off_w = o;    o = align16(o + sizeof(float2) * 4 * lmax);
-  l.off_t = o;    o = align16(o + sizeof(float2) * n_dmax * n_ch);
+  l.off_w = o;    o = align16(o + sizeof(float2) * 2 * lmax);
+  l.off_t = l.off_yb;
   l.bytes = o;
   return l;
 }
@@ -110,387 +113,410 @@ struct MvTcArgs {
   int fallback_cap;
 };
 
+// One CTA (kTcWarps warps) per pixel; a grid-stride loop over pixels keeps
+// the shared layout resident.
 __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) {
   extern __shared__ float4 tc_smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const MvTcLayout lay = mv_tc_layout(a.n_ch, a.n_dmax, a.lmax);
-  char* base = reinterpret_cast<char*>(tc_smem_raw) + warp * lay.bytes;
+  char* base = reinterpret_cast<char*>(tc_smem_raw);
   int* act = reinterpret_cast<int*>(base + lay.off_act);
   float2* yf = reinterpret_cast<float2*>(base + lay.off_yf);
   uint32_t* yb = reinterpret_cast<uint32_t*>(base + lay.off_yb);
+  float2* tk = reinterpret_cast<float2*>(base + lay.off_yb);   // aliases yb after the covariance
   float2* Rl = reinterpret_cast<float2*>(base + lay.off_r);
-  float2* wv = reinterpret_cast<float2*>(base + lay.off_w);   // w0 | r | w1 | scratch
-  float2* tk = reinterpret_cast<float2*>(base + lay.off_t);
+  float2* wv = reinterpret_cast<float2*>(base + lay.off_w);     // [0,L): w, [L,2L): r / partial sums
+  __shared__ int s_misc[8];
+  __shared__ float s_red[kTcWarps][4];
 
-  const long gw = static_cast<long>(blockIdx.x) * kTcWarps + warp;
-  if (gw >= a.n_pix) return;
-  const int pix = static_cast<int>(gw);
-  const long frame = blockIdx.y;
-  const int j = pix % a.n1;
-  const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
-  const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
-  const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+  const long total = static_cast<long>(a.n_pix) * gridDim.y;
+  for (long item = blockIdx.x; item < static_cast<long>(a.n_pix); item += gridDim.x) {
+    const int pix = static_cast<int>(item);
+    const long frame = blockIdx.y;
+    (void)total;
+    const int j = pix % a.n1;
+    const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+    const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+    __syncthreads();  // the previous pixel is done with the shared layout
 
-  // Active channels in ascending order.
-  int n_act = 0;
-  for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
-    const int ch = c0 + lane;
-    bool on = false;
-    if (ch < a.n_ch)
-      on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
-                           a.tukey_alpha) > 0.0f;
-    const unsigned m = __ballot_sync(0xffffffffu, on);
-    if (on) act[n_act + __popc(m & ((1u << lane) - 1u))] = ch;
-    n_act += __popc(m);
-  }
-  __syncwarp();
-
-  auto center_das = [&]() {
-    cplx acc = mk(0.f, 0.f);
-    for (int q = 0; q < n_act; ++q) {
-      const float2 v = yc[act[q]];
-      acc = cadd(acc, mk(v.x, v.y));
+    // Active channels (warp 0, ascending).
+    if (warp == 0) {
+      int n = 0;
+      for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+        const int ch = c0 + lane;
+        bool on = false;
+        if (ch < a.n_ch)
+          on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                               a.tukey_alpha) > 0.0f;
+        const unsigned m = __ballot_sync(0xffffffffu, on);
+        if (on) act[n + __popc(m & ((1u << lane) - 1u))] = ch;
+        n += __popc(m);
+      }
+      if (lane == 0) s_misc[0] = n;
     }
-    return acc;
-  };
-  auto finish = [&](cplx out) {
-    if (lane != 0) return;
-    if (a.cf && n_act > 0) {
-      cplx coh = mk(0.f, 0.f);
-      float inc = 0.0f;
+    __syncthreads();
+    const int n_act = s_misc[0];
+
+    auto finish = [&](cplx out) {  // thread 0 only
+      if (a.cf && n_act > 0) {
+        cplx coh = mk(0.f, 0.f);
+        float inc = 0.0f;
+        for (int q = 0; q < n_act; ++q) {
+          const float2 v = yc[act[q]];
+          coh = cadd(coh, mk(v.x, v.y));
+          inc += cnorm(mk(v.x, v.y));
+        }
+        out = cscale(out, (inc > 0.0f) ? cnorm(coh) / (static_cast<float>(n_act) * inc) : 0.0f);
+      }
+      if (a.incoherent)
+        a.acc_out[frame * a.n_pix + pix] += cnorm(out);
+      else
+        a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+    };
+    auto center_das = [&]() {
+      cplx acc = mk(0.f, 0.f);
       for (int q = 0; q < n_act; ++q) {
         const float2 v = yc[act[q]];
-        coh = cadd(coh, mk(v.x, v.y));
-        inc += cnorm(mk(v.x, v.y));
+        acc = cadd(acc, mk(v.x, v.y));
       }
-      out = cscale(out, (inc > 0.0f) ? cnorm(coh) / (static_cast<float>(n_act) * inc) : 0.0f);
+      return acc;
+    };
+    if (n_act == 0) {
+      if (tid == 0 && !a.incoherent) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
+      continue;
     }
-    if (a.incoherent)
-      a.acc_out[frame * a.n_pix + pix] += cnorm(out);
-    else
-      a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
-  };
+    if (n_act < 4) {
+      if (tid == 0) finish(center_das());
+      continue;
+    }
+    int L = a.mv_subarray;
+    const int hi = max(2, n_act / 2);
+    if (L < 2) L = 2;
+    if (L > hi) L = hi;
+    const int n_sub = n_act - L + 1;
+    int dlo = -a.range_avg, dhi = a.range_avg;
+    while (j + dlo < 0) ++dlo;
+    while (j + dhi >= a.n1) --dhi;
+    const int n_d = dhi - dlo + 1, dc = -dlo;
+    const int K = n_d * n_sub;
 
-  if (n_act == 0) {
-    if (!a.incoherent && lane == 0) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
-    return;
-  }
-  if (n_act < 4) {
-    const cplx o = center_das();
-    finish(o);
-    return;
-  }
-  int L = a.mv_subarray;
-  const int hi = max(2, n_act / 2);
-  if (L < 2) L = 2;
-  if (L > hi) L = hi;
-  const int n_sub = n_act - L + 1;
-  const int ra = a.range_avg;
-
-  // Stage the FP32 snapshots and their magnitude bound.
-  int n_d = 0, dc = 0;
-  float amax = 0.0f;
-  for (int d = -ra; d <= ra; ++d) {
-    const int jj = j + d;
-    if (jj < 0 || jj >= a.n1) continue;
-    if (d == 0) dc = n_d;
-    const float2* yr = Y + static_cast<long>(pix + d) * a.n_ch;
-    for (int q = lane; q < n_act; q += 32) {
-      const float2 v = yr[act[q]];
-      yf[n_d * a.n_ch + q] = v;
+    // Stage the FP32 snapshots, then find the largest magnitude.
+    float amax = 0.0f;
+    for (int k = tid; k < n_d * n_act; k += blockDim.x) {
+      const int d = k / n_act, q = k - d * n_act;
+      const float2 v = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[q]];
+      yf[d * a.n_ch + q] = v;
       amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
     }
-    ++n_d;
-  }
-  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  if (!(amax > 0.0f)) {
-    finish(mk(0.f, 0.f));
-    return;
-  }
-  // Power-of-two scale: exact, and brings the largest magnitude to [0.5, 1).
-  int e2;
-  frexpf(amax, &e2);
-  const float sc = ldexpf(1.0f, -e2), inv_sc = ldexpf(1.0f, e2);
-  for (int k = lane; k < n_d * a.n_ch; k += 32) {
-    const int q = k % a.n_ch;
-    if (q < n_act) {
-      const float2 v = yf[k];
-      yf[k] = make_float2(v.x * sc, v.y * sc);
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    if (lane == 0) s_red[warp][0] = amax;
+    __syncthreads();
+    amax = fmaxf(fmaxf(s_red[0][0], s_red[1][0]), fmaxf(s_red[2][0], s_red[3][0]));
+    if (!(amax > 0.0f)) {
+      if (tid == 0) finish(mk(0.f, 0.f));
+      continue;
     }
-  }
-  __syncwarp();
-  // BF16 pair staging: word (p, par, d, w) = (v[2w+par], v[2w+par+1]) of part p.
-  for (int k = lane; k < 4 * n_d * lay.words; k += 32) {
-    const int w = k % lay.words;
-    const int d = (k / lay.words) % n_d;
-    const int pp = k / (lay.words * n_d);  // p * 2 + par
-    const int p = pp >> 1, par = pp & 1;
-    const int q0 = 2 * w + par, q1 = q0 + 1;
-    const float2 v0 = q0 < n_act ? yf[d * a.n_ch + q0] : make_float2(0.f, 0.f);
-    const float2 v1 = q1 < n_act ? yf[d * a.n_ch + q1] : make_float2(0.f, 0.f);
-    yb[(pp * a.n_dmax + d) * lay.words + w] = pack_bf16(p ? v0.y : v0.x, p ? v1.y : v1.x);
-  }
-  __syncwarp();
+    // Power-of-two scale: exact, brings the largest magnitude to [0.5, 1).
+    int e2;
+    frexpf(amax, &e2);
+    const float sc = ldexpf(1.0f, -e2), inv_sc = ldexpf(1.0f, e2);
+    for (int k = tid; k < n_d * n_act; k += blockDim.x) {
+      const int d = k / n_act, q = k - d * n_act;
+      const float2 v = yf[d * a.n_ch + q];
+      yf[d * a.n_ch + q] = make_float2(v.x * sc, v.y * sc);
+    }
+    __syncthreads();
+    // BF16 pair staging: word (p, par, d, w) = (v[2w+par], v[2w+par+1]) of part p.
+    for (int k = tid; k < 4 * n_d * lay.words; k += blockDim.x) {
+      const int w = k % lay.words;
+      const int d = (k / lay.words) % n_d;
+      const int pp = k / (lay.words * n_d);
+      const int p = pp >> 1, par = pp & 1;
+      const int q0 = 2 * w + par, q1 = q0 + 1;
+      const float2 v0 = q0 < n_act ? yf[d * a.n_ch + q0] : make_float2(0.f, 0.f);
+      const float2 v1 = q1 < n_act ? yf[d * a.n_ch + q1] : make_float2(0.f, 0.f);
+      yb[(pp * a.n_dmax + d) * lay.words + w] = pack_bf16(p ? v0.y : v0.x, p ? v1.y : v1.x);
+    }
+    __syncthreads();
 
-  // ---- G = A A^T on the tensor cores, upper block-triangle ------------------
-  const int g = lane >> 2, t4 = lane & 3;
-  const int two_l = 2 * L;
-  const int MT = (two_l + 15) / 16, NT = (two_l + 7) / 8;
-  const int n_kstep = (n_sub + 15) / 16;
-  const float inv_k = 1.0f / static_cast<float>(n_d * n_sub);
-  for (int mt = 0; mt < MT; ++mt) {
-    float acc[16][4];
+    // ---- G = A A^T on the tensor cores, upper block-triangle ----------------
+    // Task = (row strip mt, chunk of up to 8 column tiles), spread over warps.
+    const int g = lane >> 2, t4 = lane & 3;
+    const int two_l = 2 * L;
+    const int MT = (two_l + 15) / 16, NT = (two_l + 7) / 8;
+    const int n_kstep = (n_sub + 15) / 16;
+    const float inv_k = 1.0f / static_cast<float>(K);
+    int task = 0;
+    for (int mt = 0; mt < MT; ++mt) {
+      for (int nt0 = 2 * mt; nt0 < NT; nt0 += 8, ++task) {
+        if (task % kTcWarps != warp) continue;
+        float acc[8][4];
 #pragma unroll
-    for (int x = 0; x < 16; ++x) acc[x][0] = acc[x][1] = acc[x][2] = acc[x][3] = 0.f;
-    const int r0 = mt * 16 + g, r1 = r0 + 8;      // A rows of this lane
-    for (int d = 0; d < n_d; ++d) {
-      for (int ks = 0; ks < n_kstep; ++ks) {
-        const int s_lo = ks * 16 + 2 * t4;        // subarray starts of this lane's k pairs
-        const int s_hi = s_lo + 8;
-        uint32_t af[4];
-        // Row r = 2i + p reads y[s + i] of part p; rows past 2L are zero.
-        af[0] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_lo + (r0 >> 1)), s_lo, n_sub) : 0u;
-        af[1] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_lo + (r1 >> 1)), s_lo, n_sub) : 0u;
-        af[2] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_hi + (r0 >> 1)), s_hi, n_sub) : 0u;
-        af[3] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_hi + (r1 >> 1)), s_hi, n_sub) : 0u;
-#pragma unroll
-        for (int x = 0; x < 16; ++x) {
-          const int nt = 2 * mt + x;
-          if (nt < NT) {
-            const int c = nt * 8 + g;               // B column = A row c
-            uint32_t b0 = 0u, b1 = 0u;
-            if (c < two_l) {
-              b0 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_lo + (c >> 1)), s_lo, n_sub);
-              b1 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_hi + (c >> 1)), s_hi, n_sub);
-            }
-            mma16816(acc[x], af, b0, b1);
-          }
-        }
-      }
-    }
-    // Fold the real-embedding blocks into complex entries R[a][b], b >= a.
-#pragma unroll
-    for (int x = 0; x < 16; ++x) {
-      const int nt = 2 * mt + x;
-      if (nt >= NT) continue;
-      // acc[x][0..1]: row r0, cols c0, c0+1; acc[x][2..3]: row r1.
-      const float o0 = __shfl_xor_sync(0xffffffffu, acc[x][0], 4);
-      const float o1 = __shfl_xor_sync(0xffffffffu, acc[x][1], 4);
-      const float o2 = __shfl_xor_sync(0xffffffffu, acc[x][2], 4);
-      const float o3 = __shfl_xor_sync(0xffffffffu, acc[x][3], 4);
-      if ((g & 1) == 0) {
-        const int c0 = nt * 8 + 2 * t4;
-        const int bcol = c0 >> 1;
-        // rows (r0, r0+1) and (r1, r1+1) are complex rows ar0 = r0/2, ar1 = r1/2.
-        const int ar0 = r0 >> 1, ar1 = r1 >> 1;
-        if (bcol < L && ar0 < L && bcol >= ar0) {
-          const float re = acc[x][0] + o1, im = o0 - acc[x][1];
-          Rl[tri(bcol, ar0)] = make_float2(re * inv_k, -im * inv_k);
-        }
-        if (bcol < L && ar1 < L && bcol >= ar1) {
-          const float re = acc[x][2] + o3, im = o2 - acc[x][3];
-          Rl[tri(bcol, ar1)] = make_float2(re * inv_k, -im * inv_k);
-        }
-      }
-    }
-  }
-  __syncwarp();
-
-  // ---- exact trace and diagonal loading ------------------------------------
-  float tr = 0.0f;
-  for (int k = lane; k < n_d * n_sub; k += 32) {
-    const int d = k / n_sub, s = k - d * n_sub;
-    for (int i = 0; i < L; ++i) {
-      const float2 v = yf[d * a.n_ch + s + i];
-      tr += v.x * v.x + v.y * v.y;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-  tr *= inv_k;
-  const float eps = fmaxf(a.loading * tr / static_cast<float>(L), 1e-20f);
-  for (int i = lane; i < L; i += 32) Rl[tri(i, i)].x += eps;
-  __syncwarp();
-
-  // ---- Cholesky of R~ (lower, in place), right-looking ---------------------
-  bool ok = true;
-  for (int c = 0; c < L; ++c) {
-    const float dgl = Rl[tri(c, c)].x;
-    if (!(dgl > 0.0f)) {
-      ok = false;
-      break;
-    }
-    const float ljj = sqrtf(dgl);
-    const float inv = 1.0f / ljj;
-    __syncwarp();
-    for (int i = c + 1 + lane; i < L; i += 32) {
-      const float2 v = Rl[tri(i, c)];
-      Rl[tri(i, c)] = make_float2(v.x * inv, v.y * inv);
-    }
-    if (lane == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
-    __syncwarp();
-    for (int i = c + 1 + lane; i < L; i += 32) {
-      const float2 lic = Rl[tri(i, c)];
-      for (int k = c + 1; k <= i; ++k) {
-        const float2 lkc = Rl[tri(k, c)];
-        float2 v = Rl[tri(i, k)];
-        // v -= lic * conj(lkc)
-        v.x -= lic.x * lkc.x + lic.y * lkc.y;
-        v.y -= lic.y * lkc.x - lic.x * lkc.y;
-        Rl[tri(i, k)] = v;
-      }
-    }
-    __syncwarp();
-  }
-  if (!ok) {
-    if (a.stats && lane == 0) atomicAdd(a.stats + 1, 1);
-    const cplx o = center_das();
-    finish(o);
-    return;
-  }
-
-  // Triangular solves with the factor, vector in registers (rows lane, lane+32).
-  auto solve = [&](float2 (&v)[2]) {
-    for (int c = 0; c < L; ++c) {  // L y = v
-      const int own = c & 31, sl = c >> 5;
-      float2 vc = make_float2(0.f, 0.f);
-      if (lane == own) {
-        const float ljj = Rl[tri(c, c)].x;
-        v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
-      }
-      vc.x = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
-      vc.y = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
-#pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
-        const int i = lane + 32 * s2;
-        if (i > c && i < L) {
-          const float2 lic = Rl[tri(i, c)];
-          v[s2].x -= lic.x * vc.x - lic.y * vc.y;
-          v[s2].y -= lic.x * vc.y + lic.y * vc.x;
-        }
-      }
-    }
-    for (int c = L - 1; c >= 0; --c) {  // L^H x = y
-      const int own = c & 31, sl = c >> 5;
-      if (lane == own) {
-        const float ljj = Rl[tri(c, c)].x;
-        v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
-      }
-      float2 vc;
-      vc.x = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
-      vc.y = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
-#pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
-        const int i = lane + 32 * s2;
-        if (i < c) {
-          const float2 lci = Rl[tri(c, i)];  // (L^H)[i][c] = conj(L[c][i])
-          v[s2].x -= lci.x * vc.x + lci.y * vc.y;
-          v[s2].y -= lci.x * vc.y - lci.y * vc.x;
-        }
-      }
-    }
-  };
-  // Residual 1 - (R + eps I) w with R = X X^H / K from the FP32 snapshots.
-  auto residual = [&](const float2 (&w)[2], float2 (&r)[2]) {
-    for (int s2 = 0; s2 < 2; ++s2) {
-      const int i = lane + 32 * s2;
-      if (i < L) wv[i] = w[s2];
-    }
-    __syncwarp();
-    for (int k = lane; k < n_d * n_sub; k += 32) {  // t_k = x_k^H w
-      const int d = k / n_sub, s = k - d * n_sub;  // once per snapshot
-      float tre = 0.f, tim = 0.f;
-      for (int i = 0; i < L; ++i) {
-        const float2 x = yf[d * a.n_ch + s + i];
-        const float2 w_ = wv[i];
-        tre += x.x * w_.x + x.y * w_.y;
-        tim += x.x * w_.y - x.y * w_.x;
-      }
-      tk[k] = make_float2(tre, tim);
-    }
-    __syncwarp();
-#pragma unroll
-    for (int s2 = 0; s2 < 2; ++s2) {
-      const int i = lane + 32 * s2;
-      r[s2] = make_float2(0.f, 0.f);
-      if (i < L) {
-        float are = 0.f, aim = 0.f;
+        for (int x = 0; x < 8; ++x) acc[x][0] = acc[x][1] = acc[x][2] = acc[x][3] = 0.f;
+        const int r0 = mt * 16 + g, r1 = r0 + 8;
         for (int d = 0; d < n_d; ++d) {
-          const float2* xr = yf + d * a.n_ch + i;
-          const float2* tr = tk + d * n_sub;
-          for (int s = 0; s < n_sub; ++s) {
-            const float2 x = xr[s];
-            const float2 t = tr[s];
-            are += x.x * t.x - x.y * t.y;
-            aim += x.x * t.y + x.y * t.x;
+          for (int ks = 0; ks < n_kstep; ++ks) {
+            const int s_lo = ks * 16 + 2 * t4, s_hi = s_lo + 8;
+            uint32_t af[4];
+            af[0] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_lo + (r0 >> 1)), s_lo, n_sub) : 0u;
+            af[1] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_lo + (r1 >> 1)), s_lo, n_sub) : 0u;
+            af[2] = r0 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r0 & 1, d, s_hi + (r0 >> 1)), s_hi, n_sub) : 0u;
+            af[3] = r1 < two_l ? mask_pair(pair_at(yb, lay.words, a.n_dmax, r1 & 1, d, s_hi + (r1 >> 1)), s_hi, n_sub) : 0u;
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+              const int nt = nt0 + x;
+              if (nt < NT) {
+                const int c = nt * 8 + g;
+                uint32_t b0 = 0u, b1 = 0u;
+                if (c < two_l) {
+                  b0 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_lo + (c >> 1)), s_lo, n_sub);
+                  b1 = mask_pair(pair_at(yb, lay.words, a.n_dmax, c & 1, d, s_hi + (c >> 1)), s_hi, n_sub);
+                }
+                mma16816(acc[x], af, b0, b1);
+              }
+            }
           }
         }
-        r[s2] = make_float2(1.0f - (are * inv_k + eps * w[s2].x), -(aim * inv_k + eps * w[s2].y));
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+          const int nt = nt0 + x;
+          if (nt >= NT) continue;
+          const float o0 = __shfl_xor_sync(0xffffffffu, acc[x][0], 4);
+          const float o1 = __shfl_xor_sync(0xffffffffu, acc[x][1], 4);
+          const float o2 = __shfl_xor_sync(0xffffffffu, acc[x][2], 4);
+          const float o3 = __shfl_xor_sync(0xffffffffu, acc[x][3], 4);
+          if ((g & 1) == 0) {
+            const int bcol = (nt * 8 + 2 * t4) >> 1;
+            const int ar0 = r0 >> 1, ar1 = r1 >> 1;
+            if (bcol < L && ar0 < L && bcol >= ar0)
+              Rl[tri(bcol, ar0)] = make_float2((acc[x][0] + o1) * inv_k, -(o0 - acc[x][1]) * inv_k);
+            if (bcol < L && ar1 < L && bcol >= ar1)
+              Rl[tri(bcol, ar1)] = make_float2((acc[x][2] + o3) * inv_k, -(o2 - acc[x][3]) * inv_k);
+          }
+        }
       }
     }
-    __syncwarp();
-  };
+    __syncthreads();  // covariance complete; yb is free (tk aliases it)
 
-  float2 w[2] = {make_float2(1.f, 0.f), make_float2(1.f, 0.f)};
-  if (lane + 32 >= L) w[1] = make_float2(0.f, 0.f);
-  if (lane >= L) w[0] = make_float2(0.f, 0.f);
-  solve(w);
-  float2 r[2];
-  residual(w, r);
-  solve(r);
-#pragma unroll
-  for (int s2 = 0; s2 < 2; ++s2) {
-    w[s2].x += r[s2].x;
-    w[s2].y += r[s2].y;
-  }
-  residual(w, r);
-  float rn = 0.f;
-#pragma unroll
-  for (int s2 = 0; s2 < 2; ++s2) rn += r[s2].x * r[s2].x + r[s2].y * r[s2].y;
-  for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
-  const bool refine_ok = sqrtf(rn / static_cast<float>(L)) <= kRefineGate;
-
-  if (!refine_ok) {
-    // Re-solved in FP64 by mv_fp64_kernel; nothing is written here.
-    if (lane == 0) {
-      const int slot = atomicAdd(a.fallback_count, 1);
-      if (slot < a.fallback_cap) a.fallback[slot] = make_int2(pix, static_cast<int>(frame));
+    // ---- exact trace and diagonal loading -----------------------------------
+    float tr = 0.0f;
+    for (int k = tid; k < K; k += blockDim.x) {
+      const int d = k / n_sub, s = k - d * n_sub;
+      const float2* x = yf + d * a.n_ch + s;
+      for (int i = 0; i < L; ++i) tr = fmaf(x[i].x, x[i].x, fmaf(x[i].y, x[i].y, tr));
     }
-    return;
-  }
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    if (lane == 0) s_red[warp][1] = tr;
+    __syncthreads();
+    tr = (s_red[0][1] + s_red[1][1] + s_red[2][1] + s_red[3][1]) * inv_k;
+    const float eps = fmaxf(a.loading * tr / static_cast<float>(L), 1e-20f);
+    for (int i = tid; i < L; i += blockDim.x) Rl[tri(i, i)].x += eps;
+    __syncthreads();
 
-  // ---- apply: out = sum conj(w_i) avg_i / sum w * n_act ------------------------
-  float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
-#pragma unroll
-  for (int s2 = 0; s2 < 2; ++s2) {
-    const int i = lane + 32 * s2;
-    if (i < L) {
-      dre += w[s2].x;
-      dim += w[s2].y;
-      float are = 0.f, aim = 0.f;
-      for (int s = 0; s < n_sub; ++s) {
-        const float2 v = yf[dc * a.n_ch + s + i];
-        are += v.x;
-        aim += v.y;
+    // ---- Cholesky of R~, right-looking; two threads per trailing row ------
+    bool ok = true;
+    for (int c = 0; c < L; ++c) {
+      const float dgl = Rl[tri(c, c)].x;
+      if (!(dgl > 0.0f)) {
+        ok = false;
+        break;
       }
-      are = are * inv_sc / static_cast<float>(n_sub);
-      aim = aim * inv_sc / static_cast<float>(n_sub);
-      ore += w[s2].x * are + w[s2].y * aim;   // conj(w) * avg
-      oim += w[s2].x * aim - w[s2].y * are;
+      const float ljj = sqrtf(dgl), inv = 1.0f / ljj;
+      __syncthreads();  // everyone has read the pivot
+      if (tid == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
+      for (int i = c + 1 + tid; i < L; i += blockDim.x) {
+        const float2 v = Rl[tri(i, c)];
+        Rl[tri(i, c)] = make_float2(v.x * inv, v.y * inv);
+      }
+      __syncthreads();
+      for (int t = tid; t < 2 * (L - c - 1); t += blockDim.x) {
+        const int i = c + 1 + (t >> 1);
+        const float2 lic = Rl[tri(i, c)];
+        const int row = i * (i + 1) / 2;
+        for (int k = c + 1 + (t & 1); k <= i; k += 2) {
+          const float2 lkc = Rl[k * (k + 1) / 2 + c];
+          float2 v = Rl[row + k];
+          v.x -= fmaf(lic.x, lkc.x, lic.y * lkc.y);
+          v.y -= fmaf(lic.y, lkc.x, -lic.x * lkc.y);
+          Rl[row + k] = v;
+        }
+      }
+      __syncthreads();
+    }
+    if (!ok) {
+      if (tid == 0) {
+        if (a.stats) atomicAdd(a.stats + 1, 1);
+        finish(center_das());
+      }
+      continue;
+    }
+
+    // Triangular solves with the factor (warp 0), vector in registers.
+    auto solve = [&](float2 (&v)[2]) {
+      for (int c = 0; c < L; ++c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const float ljj = Rl[tri(c, c)].x;
+          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+        }
+        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i > c && i < L) {
+            const float2 l = Rl[tri(i, c)];
+            v[s2].x -= fmaf(l.x, vx, -l.y * vy);
+            v[s2].y -= fmaf(l.x, vy, l.y * vx);
+          }
+        }
+      }
+      for (int c = L - 1; c >= 0; --c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const float ljj = Rl[tri(c, c)].x;
+          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+        }
+        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        const int row = c * (c + 1) / 2;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i < c) {
+            const float2 l = Rl[row + i];
+            v[s2].x -= fmaf(l.x, vx, l.y * vy);
+            v[s2].y -= fmaf(l.x, vy, -l.y * vx);
+          }
+        }
+      }
+    };
+
+    // r = 1 - (R + eps I) w for the w in wv[0, L), R = X X^H / K applied from
+    // the FP32 snapshots as X (X^H w) / K; written to wv[L, 2L).
+    auto residual = [&]() {
+      for (int k = tid; k < K; k += blockDim.x) {  // t_k = x_k^H w
+        const int d = k / n_sub, s = k - d * n_sub;
+        const float2* x = yf + d * a.n_ch + s;
+        float tre = 0.f, tim = 0.f;
+        for (int i = 0; i < L; ++i) {
+          const float2 xi = x[i], wi = wv[i];
+          tre = fmaf(xi.x, wi.x, fmaf(xi.y, wi.y, tre));
+          tim = fmaf(xi.x, wi.y, fmaf(-xi.y, wi.x, tim));
+        }
+        tk[k] = make_float2(tre, tim);
+      }
+      __syncthreads();
+      {  // (R w)[i]: two threads per i split the snapshots
+        const int i = tid >> 1, half = tid & 1;
+        float are = 0.f, aim = 0.f;
+        if (i < L) {
+          for (int d = 0; d < n_d; ++d) {
+            const float2* xr = yf + d * a.n_ch + i;
+            const float2* tr_ = tk + d * n_sub;
+            for (int s = half; s < n_sub; s += 2) {
+              const float2 x = xr[s], t = tr_[s];
+              are = fmaf(x.x, t.x, fmaf(-x.y, t.y, are));
+              aim = fmaf(x.x, t.y, fmaf(x.y, t.x, aim));
+            }
+          }
+        }
+        are += __shfl_xor_sync(0xffffffffu, are, 1);
+        aim += __shfl_xor_sync(0xffffffffu, aim, 1);
+        if (i < L && half == 0) {
+          const float2 wi = wv[i];
+          wv[L + i] = make_float2(1.0f - fmaf(are, inv_k, eps * wi.x), -fmaf(aim, inv_k, eps * wi.y));
+        }
+      }
+      __syncthreads();
+    };
+
+    float2 w[2];
+    if (warp == 0) {
+      w[0] = lane < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+      w[1] = lane + 32 < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+      solve(w);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2)
+        if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
+    }
+    __syncthreads();
+    residual();
+    // One refinement step: w = w0 + R~^-1 r.
+    if (warp == 0) {
+      float2 r[2];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        r[s2] = i < L ? wv[L + i] : make_float2(0.f, 0.f);
+      }
+      solve(r);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        w[s2].x += r[s2].x;
+        w[s2].y += r[s2].y;
+        if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
+      }
+    }
+    __syncthreads();
+    residual();
+    if (warp == 0) {
+      // The refined residual |1 - (R + eps I) w| / sqrt(L) gates the FP64 re-solve.
+      float rn = 0.f;
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        if (i < L) {
+          const float2 r = wv[L + i];
+          rn = fmaf(r.x, r.x, fmaf(r.y, r.y, rn));
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
+      if (!(sqrtf(rn / static_cast<float>(L)) <= kRefineGate)) {
+        if (lane == 0) {
+          const int slot = atomicAdd(a.fallback_count, 1);
+          if (slot < a.fallback_cap) a.fallback[slot] = make_int2(pix, static_cast<int>(frame));
+          if (a.stats) atomicAdd(a.stats, 1);
+        }
+      } else {
+        // out = sum conj(w_i) avg_i / sum w * n_act, avg from the centre row.
+        float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i < L) {
+            dre += w[s2].x;
+            dim += w[s2].y;
+            float are = 0.f, aim = 0.f;
+            for (int s = 0; s < n_sub; ++s) {
+              const float2 v = yf[dc * a.n_ch + s + i];
+              are += v.x;
+              aim += v.y;
+            }
+            are = are * inv_sc / static_cast<float>(n_sub);
+            aim = aim * inv_sc / static_cast<float>(n_sub);
+            ore += w[s2].x * are + w[s2].y * aim;
+            oim += w[s2].x * aim - w[s2].y * are;
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          dre += __shfl_xor_sync(0xffffffffu, dre, o);
+          dim += __shfl_xor_sync(0xffffffffu, dim, o);
+          ore += __shfl_xor_sync(0xffffffffu, ore, o);
+          oim += __shfl_xor_sync(0xffffffffu, oim, o);
+        }
+        if (lane == 0) {
+          cplx out;
+          if (hypotf(dre, dim) < 1e-30f)
+            out = center_das();
+          else
+            out = cscale(cdiv_wide(mk(ore, oim), mk(dre, dim)), static_cast<float>(n_act));
+          finish(out);
+        }
+      }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    dre += __shfl_xor_sync(0xffffffffu, dre, o);
-    dim += __shfl_xor_sync(0xffffffffu, dim, o);
-    ore += __shfl_xor_sync(0xffffffffu, ore, o);
-    oim += __shfl_xor_sync(0xffffffffu, oim, o);
-  }
-  cplx out;
-  if (hypotf(dre, dim) < 1e-30f) {
-    out = center_das();
-  } else {
-    out = cscale(cdiv_wide(mk(ore, oim), mk(dre, dim)), static_cast<float>(n_act));
-  }
-  finish(out);
 }
 
 // FP64 re-solve of the pixels whose refined FP32 residual failed: covariance
@@ -684,7 +710,7 @@ int mv_tc_supported(int n_ch, int mv_subarray, int range_avg) {
   const int lmax = std::min(std::max(mv_subarray, 2), std::max(2, n_ch / 2));
   if (n_ch > kTcMaxCh || lmax > kTcMaxL || range_avg > 4) return 0;
   const MvTcLayout l = mv_tc_layout(n_ch, 2 * range_avg + 1, lmax);
-  return l.bytes * kTcWarps <= 227 * 1024 ? 1 : 0;
+  return l.bytes <= 200 * 1024 ? 1 : 0;
 }
 
 int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,
@@ -717,9 +743,12 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
   a.fallback = fallback;
   a.fallback_cap = fallback_cap;
   const MvTcLayout l = mv_tc_layout(n_ch, a.n_dmax, a.lmax);
-  const size_t smem = l.bytes * kTcWarps;
+  const size_t smem = l.bytes;
   USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  const dim3 grid(ceil_div(n_pix, kTcWarps), n_frames);
+  int per_sm = 0;
+  USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_tc_kernel, 32 * kTcWarps, smem));
+  const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 4 / std::max(1, n_frames);
+  const dim3 grid(static_cast<unsigned>(std::max(1L, std::min<long>(n_pix, want))), n_frames);
   prof_begin(ctx, "mv_tc_kernel");
   mv_tc_kernel<<<grid, 32 * kTcWarps, smem, ctx->stream>>>(a);
   prof_end(ctx);
