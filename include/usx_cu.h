@@ -40,6 +40,7 @@ enum {
 
 typedef struct usx_ctx usx_ctx;
 typedef struct usx_bf_plan usx_bf_plan;
+typedef struct usx_mlp usx_mlp;
 
 /* ----------------------------------------------------------- context, memory */
 
@@ -153,6 +154,59 @@ int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode);
  * pixels whose factorisation failed (these take the DAS sum). */
 int usx_cu_bf_plan_mv_stats(usx_bf_plan* plan, int64_t* fp64_resolves,
                             int64_t* factorization_failures);
+
+/* ------------------------------------------------- learned minimum variance */
+
+/* The learned minimum variance has no counterpart in the reference; the
+ * method it stands in for is the reference's minimum variance
+ * (combine_mv_windowed, beamformer.cpp:137-214), which stays its per-pixel
+ * fallback.
+ *
+ * A plan whose config has combiner USX_COMB_LEARNED_MV runs, per pixel:
+ * the receive-delayed, compounded channel samples (rectangular apodisation,
+ * as for minimum variance); 256 scale- and phase-free features (normalised
+ * diagonal sums of the spatially smoothed covariance, the subarray-averaged
+ * snapshot, L and the active aperture); the network (256 -> ... -> 128); the
+ * predicted weights w~ = out / L, i < L; the distortionless residual
+ * |1^H w~ - 1|. Pixels above `gate` are solved by the tensor-core minimum
+ * variance; the others output n_act * (w~^H a) / conj(1^H w~), a the
+ * subarray-averaged snapshot. Pixels with fewer than 4 active channels give
+ * the DAS sum, as in the reference. Coherent and select compounding only.
+ * The network is not owned and must outlive the plan's executions. */
+int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate);
+/* Pixels gated to the exact solver and pixels beamformed by the learned path
+ * since the last call (synchronises). */
+int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels);
+/* Training pairs from a coherent minimum-variance plan in USX_MV_TENSOR mode:
+ * every execution also writes, per pixel row r = frame * n_pix + pix,
+ * features[r][256], weights[r][128] = L w_i / sum(w) interleaved (re, im),
+ * zero for i >= L, and valid[r] = 1 where a Capon solve exists (0 for the
+ * DAS rule and failed factorisations). Device buffers; NULLs turn it off. */
+int usx_cu_bf_plan_set_training_export(usx_bf_plan* plan, float* features, float* weights,
+                                       uint8_t* valid);
+
+/* The network: fully connected layers dims[0] -> dims[1] -> ... ->
+ * dims[n_layers], ReLU between layers, FP32 master weights with a BF16 copy
+ * for the GEMMs (mma.sync BF16, FP32 accumulation). Every width must be a
+ * positive multiple of 128. Parameters are laid out per layer as W_l
+ * [dims[l]][dims[l+1]] row-major followed by b_l [dims[l+1]]. Weights start
+ * He-uniform from `seed`, biases at zero. */
+int usx_cu_mlp_create(usx_ctx* ctx, int n_layers, const int* dims, uint64_t seed, usx_mlp** out);
+int usx_cu_mlp_destroy(usx_mlp* mlp);
+int usx_cu_mlp_num_params(const usx_mlp* mlp, int64_t* count);
+/* FP32 parameters to / from host memory (synchronises). */
+int usx_cu_mlp_get_params(usx_mlp* mlp, float* host);
+int usx_cu_mlp_set_params(usx_mlp* mlp, const float* host);
+/* y[rows][dims[n_layers]] = net(x[rows][dims[0]]), FP32 device buffers. */
+int usx_cu_mlp_forward(usx_mlp* mlp, const float* x, int64_t rows, float* y);
+/* One training step on device buffers x[rows][dims[0]], target and mask
+ * [rows][dims[n_layers]] (mask may be NULL): gradients of
+ * sum(mask * (y - target)^2) / (rows * dims[n_layers]), then, when lr > 0,
+ * one Adam step (beta 0.9, 0.999, eps 1e-8). rows must be a multiple of 128.
+ * loss_host and grad_host (n_params floats) are optional host outputs and
+ * make the call synchronise. */
+int usx_cu_mlp_train_step(usx_mlp* mlp, const float* x, const float* target, const float* mask,
+                          int64_t rows, float lr, float* loss_host, float* grad_host);
 
 /* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one
  * launch: frame f uses the plan's events [first + f*events_per_frame,

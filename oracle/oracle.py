@@ -235,6 +235,25 @@ class Lib:
           ev_end, _ptr(out, self._pt(prec)))
         return out[..., 0] + 1j * out[..., 1]
 
+    def mv_training_pairs(self, cd, data, points, n0, n1, bcfg, prec="f32"):
+        """(frame, features [n_pix, 256], weights [n_pix, 128], valid [n_pix]) of
+        the minimum-variance beamform (learned-MV training pairs)."""
+        dt = self._dt(prec)
+        d = np.ascontiguousarray(np.stack([np.real(data), np.imag(data)], -1), dtype=dt)
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        out = np.zeros((n0, n1, 2), dtype=dt)
+        feat = np.zeros((n0 * n1, 256), dtype=dt)
+        w = np.zeros((n0 * n1, 128), dtype=dt)
+        valid = np.zeros(n0 * n1, dtype=np.uint8)
+        f = self._fn("orc_mv_training_pairs", prec)
+        f.argtypes = [C.c_void_p, self._pt(prec), C.c_int, C.c_int, f32p, C.c_void_p, self._pt(prec),
+                      self._pt(prec), self._pt(prec), C.c_void_p]
+        rc = f(C.byref(cd), _ptr(d, self._pt(prec)), n0, n1, _ptr(pts, f32p), C.byref(bcfg),
+               _ptr(out, self._pt(prec)), _ptr(feat, self._pt(prec)), _ptr(w, self._pt(prec)), valid.ctypes.data)
+        if rc != 0:
+            raise ValueError("mv_training_pairs needs a coherent minimum-variance config")
+        return out[..., 0] + 1j * out[..., 1], feat, w, valid
+
     def _cplx(self, a, prec):
         dt = self._dt(prec)
         return np.ascontiguousarray(np.stack([np.real(a), np.imag(a)], -1), dtype=dt)

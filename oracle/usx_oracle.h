@@ -48,6 +48,12 @@ extern "C" {
                        int n_pix_axis1, const float* points,                             \
                        const usx_beamformer_config* cfg, int event_begin, int event_end, \
                        R* frame);                                                        \
+  /* learned minimum variance (no reference counterpart): MV beamform plus per-pixel */ \
+  /* features [n_pix][256], Capon weights L w / sum(w) [n_pix][128] and valid flags */     \
+  int orc_mv_training_pairs_##S(const usx_channel_desc* cd, const R* data, int n_pix_axis0, \
+                                int n_pix_axis1, const float* points,                     \
+                                const usx_beamformer_config* cfg, R* frame, R* feat,      \
+                                R* weights, unsigned char* valid);                        \
   /* beamformer.cpp:249-295 */                                                           \
   R orc_transmit_sensitivity_##S(const usx_probe* probe, const usx_transmit* tx,         \
                                  const float* point, R wavelength);                      \

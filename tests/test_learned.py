@@ -1,0 +1,327 @@
+"""Learned minimum variance: the network's kernels against the CPU oracle
+(forward, gradients, Adam), the feature kernel and the Capon-weight export
+against the C oracle's restatement, the gate and fallback, and what training
+gains over the same combiner with uniform weights.
+
+The network and the learned combiner have no counterpart in the reference;
+the oracle for the network is oracle/mlp_oracle.py and for the features and
+weights oracle/usx_oracle_impl.inc (orc_mv_training_pairs), whose minimum
+variance reproduces the reference's golden frames bit for bit."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from gold import BF_CASES, rel_l2, sim_setup, txset
+from oracle import mlp_oracle as MO
+from oracle import oracle as O
+
+DIMS = (256, 256, 256, 256, 128)
+
+
+# ------------------------------------------------------------------ CPU
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, -2.5, 1e-3, 65504.0], np.float32)
+    got = MO.bf16(x)
+    assert got[0] == 1.0
+    assert got[1] == 1.0                      # tie -> even mantissa
+    assert got[2] == 1.0 + 2.0 ** -6          # tie -> even (up)
+    assert got[3] == -2.5
+    assert abs(got[4] - 1e-3) / 1e-3 < 2.0 ** -8
+    assert got[5] == 65536.0
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    dims = (6, 10, 8, 4)
+    n = sum(a * b + b for a, b in zip(dims[:-1], dims[1:]))
+    p = rng.standard_normal(n) * 0.5
+    x = rng.standard_normal((7, dims[0]))
+    t = rng.standard_normal((7, dims[-1]))
+    m = (rng.random((7, dims[-1])) > 0.3).astype(np.float64)
+    _, g = MO.backward(p, dims, x, t, m, quantize=False)
+    fd = np.empty(n)
+    h = 1e-6
+    for i in range(n):
+        e = np.zeros(n)
+        e[i] = h
+        fd[i] = (MO.loss(p + e, dims, x, t, m) - MO.loss(p - e, dims, x, t, m)) / (2 * h)
+    assert np.max(np.abs(fd - g)) < 1e-7 * max(1.0, np.max(np.abs(g)))
+
+
+def test_weights_file_roundtrip(tmp_path):
+    from usx import learned
+    rng = np.random.default_rng(0)
+    n = sum(a * b + b for a, b in zip(DIMS[:-1], DIMS[1:]))
+    p = rng.standard_normal(n).astype(np.float32)
+    f = tmp_path / "w.bin"
+    learned.save_weights(f, DIMS, p)
+    dims, q = learned.load_weights(f)
+    assert dims == DIMS and np.array_equal(p, q)
+    f.write_bytes(b"nonsense" + f.read_bytes()[8:])
+    with pytest.raises(ValueError):
+        learned.load_weights(f)
+
+
+def _golden_mv_case(golden, name="mv"):
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    return g, s, pr, med, acq
+
+
+def test_oracle_training_pairs_reproduce_the_reference_frame(oracle, golden):
+    """The training export rides on the oracle's minimum variance, which is
+    the reference's to the bit; the exported weights are L w / sum(w)."""
+    g, s, pr, med, acq = _golden_mv_case(golden)
+    cd = O.channel_desc(pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    n0, n1 = len(g["ax0"]), len(g["ax1"])
+    fr, feat, w, valid = oracle.mv_training_pairs(cd, g["iq"], g["pts"], n0, n1, O.bf_config(**BF_CASES["mv"]))
+    assert np.array_equal(fr.astype(np.complex64), g["bf_mv"])
+    ok = valid == 1
+    assert ok.mean() > 0.9
+    L = np.round(feat[:, 0] * 64).astype(int)
+    wc = w[:, 0::2] + 1j * w[:, 1::2]
+    assert np.max(np.abs(wc[ok].sum(1) / L[ok] - 1)) < 1e-5
+    for r in np.nonzero(ok)[0][:50]:
+        assert np.all(wc[r, L[r]:] == 0) and np.all(feat[r, 2 * L[r]:128] == 0)
+    assert np.all(feat[~ok & (L == 0)] == 0)
+
+
+# ------------------------------------------------------------------ GPU
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from usx import capi
+    return capi
+
+
+@pytest.fixture(scope="module")
+def ctx(capi, torch):
+    c = capi.Context(0, stream=0)
+    yield c
+    c.close()
+
+
+def _net_case(capi, ctx, torch, rows=384, seed=5):
+    rng = np.random.default_rng(seed)
+    mlp = capi.Mlp(ctx, DIMS, seed=11)
+    p = mlp.get_params()
+    # Non-zero biases so that their gradients and the bias epilogue are exercised.
+    for w, b in mlp.layers(p):
+        b[:] = rng.standard_normal(b.size).astype(np.float32) * 0.1
+    mlp.set_params(p)
+    x = rng.standard_normal((rows, DIMS[0])).astype(np.float32)
+    t = rng.standard_normal((rows, DIMS[-1])).astype(np.float32)
+    m = (rng.random((rows, DIMS[-1])) > 0.25).astype(np.float32)
+    return mlp, p, x, t, m
+
+
+@pytest.mark.gpu
+def test_mlp_forward_matches_oracle(capi, ctx, torch):
+    mlp, p, x, _, _ = _net_case(capi, ctx, torch, rows=300)  # not a multiple of 128: padded internally
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.empty((x.shape[0], DIMS[-1]), dtype=torch.float32, device="cuda")
+    mlp.forward(dx.data_ptr(), x.shape[0], dy.data_ptr())
+    ctx.synchronize()
+    want, _ = MO.forward(p, DIMS, x, quantize=True)
+    assert rel_l2(dy.cpu().numpy(), want) < 2e-3
+
+
+@pytest.mark.gpu
+def test_mlp_gradients_match_oracle(capi, ctx, torch):
+    """Hand-written backward GEMMs (dW split-K, dX with the ReLU mask) and the
+    bias reduction against the oracle's backward with the same BF16 rounding."""
+    mlp, p, x, t, m = _net_case(capi, ctx, torch)
+    dx, dt, dm = (torch.from_numpy(a).cuda() for a in (x, t, m))
+    loss, grad = mlp.train_step(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), x.shape[0], 0.0, True, True)
+    want_loss, want = MO.backward(p, DIMS, x, t, m, quantize=True)
+    assert abs(loss - want_loss) < 1e-3 * want_loss
+    o = 0
+    for din, dout in zip(DIMS[:-1], DIMS[1:]):
+        gw, ww = grad[o:o + din * dout], want[o:o + din * dout]
+        o += din * dout
+        gb, wb = grad[o:o + dout], want[o:o + dout]
+        o += dout
+        assert rel_l2(gw, ww) < 3e-3
+        assert rel_l2(gb, wb) < 3e-3
+    # Parameters are untouched when lr = 0.
+    assert np.array_equal(mlp.get_params(), p)
+
+
+@pytest.mark.gpu
+def test_adam_step_matches_oracle(capi, ctx, torch):
+    mlp, p, x, t, m = _net_case(capi, ctx, torch)
+    dx, dt, dm = (torch.from_numpy(a).cuda() for a in (x, t, m))
+    _, g = mlp.train_step(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), x.shape[0], 0.0, False, True)
+    lr = 1e-3
+    mlp.train_step(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), x.shape[0], lr)
+    got = mlp.get_params()
+    want, _, _ = MO.adam_step(p.astype(np.float64), g.astype(np.float64), 0.0, 0.0, 1, lr)
+    step = got - p
+    # The first Adam step moves each parameter by ~lr * sign(g); split-K
+    # accumulation order may flip only the tiniest gradients.
+    assert rel_l2(step, want - p) < 1e-2
+    assert np.mean(np.abs(step - (want - p)) > 1e-5) < 1e-3
+
+
+@pytest.mark.gpu
+def test_training_drives_the_loss_down(capi, ctx, torch):
+    """A smooth target (a fixed random network) is learned by the on-device loop."""
+    rng = np.random.default_rng(1)
+    rows = 4096
+    x = rng.standard_normal((rows, DIMS[0])).astype(np.float32)
+    teacher = capi.Mlp(ctx, DIMS, seed=99)
+    dx = torch.from_numpy(x).cuda()
+    dt = torch.empty((rows, DIMS[-1]), dtype=torch.float32, device="cuda")
+    teacher.forward(dx.data_ptr(), rows, dt.data_ptr())
+    student = capi.Mlp(ctx, DIMS, seed=3)
+    first = None
+    for step in range(300):
+        loss, _ = student.train_step(dx.data_ptr(), dt.data_ptr(), None, rows, 1e-3, step % 50 == 0 or step == 299)
+        if loss is not None:
+            first = loss if first is None else first
+            last = loss
+    assert last < 0.5 * first
+
+
+def _learned_setup():
+    from usx import learned
+    return learned, learned.Setup(n_tx=15, depth=0.04, n0=128, n1=256)
+
+
+@pytest.mark.gpu
+def test_features_and_weights_match_oracle(capi, torch, oracle):
+    """Device features (trapezoid-weighted lag products) and tensor-core Capon
+    weights against the oracle's direct definitions, on a simulated phantom."""
+    learned, setup = _learned_setup()
+    im = learned.Imager(setup)
+    try:
+        spec = learned.phantom(7, setup)
+        im.acquire(spec)
+        frame, feat, w, valid = im.export_pairs()
+        iq = im.iq.cpu().numpy()
+        feat, w, valid = feat.cpu().numpy(), w.cpu().numpy(), valid.cpu().numpy()
+        # The oracle on a band of 8 lateral lines (the oracle is a plain CPU loop).
+        lines = np.arange(60, 68)
+        pts = im.grid.points.reshape(setup.n0, setup.n1, 3)[lines].reshape(-1, 3)
+        pr = O.probe(n_elements=setup.n_el, pitch=setup.pitch, element_width=setup.width,
+                     center_frequency=setup.f0, bandwidth=0.6)
+        a = im.ch_iq.desc.acq
+        acq = O.acquisition(fs=a.sampling_frequency, n_samples=a.n_samples, t0=a.t0, prf=a.prf)
+        tx = im.transmits
+        n = len(tx)
+        txs = O.TxSet(np.array([t["type"] for t in tx]), np.array([t["angle"] for t in tx], np.float32),
+                      np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32),
+                      np.stack([np.asarray(t["delays"], np.float32) for t in tx]),
+                      np.stack([np.asarray(t["apodization"], np.float32) for t in tx]))
+        cd = O.channel_desc(pr, O.medium(), acq, txs, is_iq=True, fdem=setup.f0)
+        fr_o, feat_o, w_o, valid_o = oracle.mv_training_pairs(cd, iq, pts, len(lines), setup.n1,
+                                                              O.bf_config(**setup_bf_kw(setup)))
+        rows = (lines[:, None] * setup.n1 + np.arange(setup.n1)[None, :]).ravel()
+        assert np.array_equal(valid[rows], valid_o)
+        ok = valid_o == 1
+        assert np.max(np.abs(feat[rows] - feat_o)) < 2e-3
+        # Weights: the tensor-core solve is within 1e-3 of the exact frame;
+        # normalised weights of well-conditioned pixels agree to ~1e-2.
+        wc, wo = w[rows][ok], w_o[ok]
+        err = np.linalg.norm(wc - wo, axis=1) / np.maximum(np.linalg.norm(wo, axis=1), 1e-12)
+        assert np.median(err) < 1e-2
+        assert rel_l2(frame.cpu().numpy()[lines], fr_o) < 1e-3
+    finally:
+        im.close()
+
+
+def setup_bf_kw(setup):
+    return dict(f_number=setup.f_number, combiner=2, mv_subarray=setup.subarray,
+                mv_diagonal_loading=setup.loading, mv_range_average=setup.range_avg)
+
+
+def _uniform_params(mlp):
+    """All-zero weights, last bias = (1, 0) per output pair: the network that
+    predicts uniform weights w = 1/L (the combiner without learning)."""
+    p = np.zeros(mlp.n_params, np.float32)
+    _, b = mlp.layers(p)[-1]
+    b[0::2] = 1.0
+    return p
+
+
+@pytest.mark.gpu
+def test_gate_zero_falls_back_to_plain_mv_everywhere(capi, torch):
+    learned, setup = _learned_setup()
+    im = learned.Imager(setup)
+    try:
+        im.acquire(learned.phantom(21, setup))
+        mv = im.beamform(learned.COMB_MV).cpu().numpy()
+        mlp = capi.Mlp(im.ctx, DIMS, seed=1)
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        plan.set_learned(mlp, 0.0)
+        plan.learned_stats()
+        out = im.beamform(learned.COMB_LEARNED_MV).cpu().numpy()
+        gated, pixels = plan.learned_stats()
+        assert pixels == setup.n0 * setup.n1
+        assert gated > 0.9 * pixels
+        assert rel_l2(out, mv) < 1e-6
+        # An infinite gate takes every network output (no fallback).
+        plan.set_learned(mlp, float("inf"))
+        im.beamform(learned.COMB_LEARNED_MV)
+        gated, pixels = plan.learned_stats()
+        assert gated == 0 and pixels == setup.n0 * setup.n1
+    finally:
+        im.close()
+
+
+@pytest.mark.gpu
+def test_learned_plan_needs_a_network(capi, torch):
+    learned, setup = _learned_setup()
+    im = learned.Imager(setup)
+    try:
+        im.acquire(learned.phantom(22, setup))
+        with pytest.raises(ValueError, match="no network"):
+            im.beamform(learned.COMB_LEARNED_MV)
+        wrong = capi.Mlp(im.ctx, (128, 128), seed=0)
+        with pytest.raises(ValueError, match="256 features"):
+            im.plan(learned.COMB_LEARNED_MV).set_learned(wrong, 0.05)
+    finally:
+        im.close()
+
+
+@pytest.mark.gpu
+def test_training_gains_over_uniform_weights(capi, torch):
+    """Trained on plain-MV pairs from 12 phantoms, the network's images are
+    closer to plain MV (relative L2, wire lateral FWHM) on held-out phantoms
+    than the same combiner with uniform weights (the method without it)."""
+    learned, setup = _learned_setup()
+    im = learned.Imager(setup)
+    try:
+        X, T, M = learned.make_pairs(im, np.arange(100, 112), per_phantom=8192, log=None)
+        mlp, losses = learned.train(im.ctx, X, T, M, steps=1500, batch=2048, lr=1e-3, log=None)
+        assert losses[-1][1] < 0.5 * losses[0][1]
+        uniform = capi.Mlp(im.ctx, DIMS)
+        uniform.set_params(_uniform_params(uniform))
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        res = {}
+        for name, net in (("trained", mlp), ("uniform", uniform)):
+            plan.set_learned(net, float("inf"))
+            errs, fw = [], []
+            for s in (900, 901):
+                spec = learned.phantom(s, setup)
+                im.acquire(spec)
+                mv = im.beamform(learned.COMB_MV)
+                lf = im.beamform(learned.COMB_LEARNED_MV)
+                errs.append(float((lf - mv).abs().pow(2).sum().sqrt() / mv.abs().pow(2).sum().sqrt()))
+                a, b = learned.image_metrics(mv, im, spec), learned.image_metrics(lf, im, spec)
+                fw += [abs(y - x) / x for x, y in zip(a["lateral_fwhm_mm"], b["lateral_fwhm_mm"])]
+            res[name] = (np.mean(errs), np.mean(fw))
+        assert res["trained"][0] < 0.8 * res["uniform"][0], res
+        assert res["trained"][1] < res["uniform"][1], res
+    finally:
+        im.close()

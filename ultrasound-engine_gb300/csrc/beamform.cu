@@ -617,6 +617,7 @@ using namespace usxcu;
 
 struct usx_bf_plan {
   usx_ctx* ctx = nullptr;
+  int device = 0;
   usx_channel_desc cd{};
   usx_beamformer_config cfg{};
   int n0 = 0, n1 = 0;
@@ -625,7 +626,15 @@ struct usx_bf_plan {
   int ev_begin = 0, ev_end = 0;
   int mv_mode = USX_MV_EXACT;
   int precision = USX_BF_FAST;
-  int* d_mv_stats = nullptr;   // [0] FP64 re-solves, [1] factorisation failures
+  int* d_mv_stats = nullptr;   // [0] FP64 re-solves, [1] factorisation failures, [2] learned-MV gate rejections
+  // Learned minimum variance: the network (not owned) and the gate on |1^H w - 1|.
+  usx_mlp* mlp = nullptr;
+  float lmv_gate = 0.05f;
+  int64_t lmv_pixels = 0;      // pixels beamformed by the learned path since the last stats read
+  // Training export (minimum variance plans): features, weights, valid flags.
+  float* exp_feat = nullptr;
+  float* exp_w = nullptr;
+  uint8_t* exp_valid = nullptr;
 };
 
 namespace {
@@ -667,7 +676,7 @@ BfArgs make_args(const usx_bf_plan* p) {
   a.compounding = p->cfg.compounding;
   a.tx_weighting = p->cfg.transmit_weighting;
   a.cf = p->cfg.coherence_factor;
-  a.is_mv = p->cfg.combiner == USX_COMB_MV;
+  a.is_mv = p->cfg.combiner == USX_COMB_MV || p->cfg.combiner == USX_COMB_LEARNED_MV;
   a.mv_subarray = p->cfg.mv_subarray;
   a.mv_range_average = a.is_mv ? p->cfg.mv_range_average : 0;
   a.mv_loading = p->cfg.mv_diagonal_loading;
@@ -701,8 +710,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     return USX_OK;
   }
   const bool fast = plan->precision == USX_BF_FAST;
-  const dim3 grid_das(fast ? ceil_div(plan->n0, kTileLines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
-                      n_frames);
+  dim3 grid_das(fast ? ceil_div(plan->n0, kTileLines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
+                n_frames);
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
     prof_begin(ctx, name);
     if (fast) {
@@ -721,6 +730,93 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     return USX_OK;
   };
   if (!a.is_mv) return launch_das(a, fast ? "das_fast_kernel" : "das_kernel");
+  if (a.combiner == USX_COMB_LEARNED_MV) {
+    // Frames go through in chunks of at most 2^21 pixels: export the
+    // compounded channel samples, features, network, gated apply, and the
+    // exact tensor-core solve of the gated pixels.
+    if (!plan->mlp)
+      return fail(USX_ERR_INVALID, "learned minimum variance: no network attached (usx_cu_bf_plan_set_learned)");
+    if (a.compounding == USX_COMP_INCOHERENT)
+      return fail(USX_ERR_UNSUPPORTED, "learned minimum variance supports coherent and select compounding only");
+    const int chunk = static_cast<int>(std::max<long>(1, std::min<long>(n_frames, (1L << 21) / n_pix)));
+    const long rows = chunk * n_pix, padded = (rows + 127) / 128 * 128;
+    const int widest = mlp_widest(plan->mlp);
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t sz[9] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
+                          up(sizeof(float2) * rows * 64),       up(sizeof(float4) * rows),
+                          up(2 * padded * widest),              up(2 * padded * widest),
+                          up(sizeof(float) * padded * kLmvOutputs), up(sizeof(int2) * rows),
+                          up(sizeof(int2) * rows)};
+    size_t total = 256;
+    for (size_t b : sz) total += b;
+    void* ws = nullptr;
+    if (int rc = scratch(ctx, total, &ws)) return rc;
+    char* q = static_cast<char*>(ws);
+    void* bufs[9];
+    for (int i = 0; i < 9; ++i) {
+      bufs[i] = q;
+      q += sz[i];
+    }
+    int* counters = reinterpret_cast<int*>(q);  // [0] gated, [1] FP64 re-solves
+    float2* y = static_cast<float2*>(bufs[0]);
+    char* feat16 = static_cast<char*>(bufs[1]);
+    float2* avg = static_cast<float2*>(bufs[2]);
+    float4* meta = static_cast<float4*>(bufs[3]);
+    float* net = static_cast<float*>(bufs[6]);
+    int2* gated = static_cast<int2*>(bufs[7]);
+    int2* fb = static_cast<int2*>(bufs[8]);
+    for (int f0 = 0; f0 < n_frames; f0 += chunk) {
+      const int nf = std::min(chunk, n_frames - f0);
+      const long nrows = nf * n_pix, npad = (nrows + 127) / 128 * 128;
+      BfArgs b = a;
+      b.y_out = y;
+      if (b.iq) b.iq += f0 * data_stride;
+      if (b.rf) b.rf += f0 * data_stride;
+      b.out = a.out + f0 * frame_stride;
+      if (seq_epf > 0) b.ev_begin += f0 * seq_epf;
+      grid_das.y = nf;
+      if (int rc = launch_das(b, fast ? "das_fast_kernel(mv export)" : "das_kernel(mv export)")) return rc;
+      LmvLaunch l;
+      l.y = y;
+      l.points = b.points;
+      l.n_ch = b.n_ch;
+      l.n_pix = b.n_pix;
+      l.n1 = b.n1;
+      l.n_frames = nf;
+      l.mv_subarray = b.mv_subarray;
+      l.range_avg = b.mv_range_average;
+      l.f_number = b.f_number;
+      l.tukey_alpha = b.tukey_alpha;
+      l.half_nm1 = b.half_nm1;
+      l.pitch = b.pitch;
+      l.rx_window = b.rx_window;
+      l.cf = b.cf;
+      l.feat16 = feat16;
+      l.avg = avg;
+      l.meta = meta;
+      l.out = b.out;
+      l.out_stride = b.out_stride;
+      if (npad > nrows)
+        USX_CUDA(cudaMemsetAsync(feat16 + 2 * nrows * kLmvFeatures, 0, 2 * (npad - nrows) * kLmvFeatures, ctx->stream));
+      if (int rc = launch_lmv_features(ctx, l)) return rc;
+      if (int rc = mlp_infer(plan->mlp, ctx, feat16, npad, bufs[4], bufs[5], net)) return rc;
+      USX_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), ctx->stream));
+      if (int rc = launch_lmv_apply(ctx, net, avg, meta, b.out, b.out_stride, b.n_pix, nf, plan->lmv_gate,
+                                    counters, gated, static_cast<int>(nrows), plan->d_mv_stats + 2))
+        return rc;
+      MvTcExtra ex;
+      ex.list = gated;
+      ex.list_count = counters;
+      ex.list_cap = static_cast<int>(nrows);
+      if (int rc = launch_mv_tc(ctx, y, b.points, b.out, b.out_stride, nullptr, b.n_ch, b.n_pix, b.n1, nf,
+                                b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number, b.tukey_alpha,
+                                b.rx_window, b.half_nm1, b.pitch, b.cf, 0, plan->d_mv_stats, counters + 1, fb,
+                                static_cast<int>(nrows), ex))
+        return rc;
+    }
+    plan->lmv_pixels += static_cast<int64_t>(n_frames) * n_pix;
+    return USX_OK;
+  }
   // Minimum variance: per pass, export compounded channel samples, then solve.
   const size_t y_bytes = static_cast<size_t>(n_frames) * n_pix * a.n_ch * sizeof(float2);
   const size_t acc_bytes = static_cast<size_t>(n_frames) * n_pix * sizeof(float);
@@ -747,11 +843,34 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     b.pass = incoherent ? pass : -1;
     if (int rc = launch_das(b, fast ? "das_fast_kernel(mv export)" : "das_kernel(mv export)")) return rc;
     if (tensor) {
+      MvTcExtra ex;
+      if (plan->exp_feat) {
+        // Training pairs: features of every pixel and its Capon weights.
+        LmvLaunch l;
+        l.y = b.y_out;
+        l.points = b.points;
+        l.n_ch = b.n_ch;
+        l.n_pix = b.n_pix;
+        l.n1 = b.n1;
+        l.n_frames = n_frames;
+        l.mv_subarray = b.mv_subarray;
+        l.range_avg = b.mv_range_average;
+        l.f_number = b.f_number;
+        l.tukey_alpha = b.tukey_alpha;
+        l.half_nm1 = b.half_nm1;
+        l.pitch = b.pitch;
+        l.rx_window = b.rx_window;
+        l.cf = b.cf;
+        l.feat32 = plan->exp_feat;
+        if (int rc = launch_lmv_features(ctx, l)) return rc;
+        ex.w_export = plan->exp_w;
+        ex.w_valid = plan->exp_valid;
+      }
       USX_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(int), ctx->stream));
       if (int rc = launch_mv_tc(ctx, b.y_out, b.points, b.out, b.out_stride, b.acc_out, b.n_ch, b.n_pix, b.n1,
                                 n_frames, b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number,
                                 b.tukey_alpha, b.rx_window, b.half_nm1, b.pitch, b.cf, incoherent ? 1 : 0,
-                                plan->d_mv_stats, fb_count, fb_list, static_cast<int>(n_frames * n_pix)))
+                                plan->d_mv_stats, fb_count, fb_list, static_cast<int>(n_frames * n_pix), ex))
         return rc;
     } else {
       prof_begin(ctx, "mv_kernel");
@@ -782,9 +901,14 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
   if (int rc = validate_bf_config(*cfg)) return rc;
   if (grid->n_axis0 <= 0 || grid->n_axis1 <= 0)
     return fail(USX_ERR_INVALID, "ScanGrid dimensions must be > 0");
-  if (cfg->combiner != USX_COMB_DAS && cfg->combiner != USX_COMB_DMAS && cfg->combiner != USX_COMB_MV)
+  if (cfg->combiner != USX_COMB_DAS && cfg->combiner != USX_COMB_DMAS && cfg->combiner != USX_COMB_MV &&
+      cfg->combiner != USX_COMB_LEARNED_MV)
     return fail(USX_ERR_UNSUPPORTED, "usx_cu_bf_plan_create: unknown combiner");
-  if (cfg->combiner == USX_COMB_MV) {
+  if (cfg->combiner == USX_COMB_LEARNED_MV &&
+      !mv_tc_supported(cd->probe.n_elements, cfg->mv_subarray, cfg->mv_range_average))
+    return fail(USX_ERR_UNSUPPORTED,
+                "learned minimum variance supports <= 128 channels, subarrays <= 64 and range averaging <= +/-4");
+  if (cfg->combiner == USX_COMB_MV || cfg->combiner == USX_COMB_LEARNED_MV) {
     if (cd->probe.n_elements > kMaxCh)
       return fail(USX_ERR_UNSUPPORTED, "minimum variance supports at most 256 channels");
     if (std::min(cfg->mv_subarray, std::max(2, cd->probe.n_elements / 2)) > kMaxL)
@@ -801,6 +925,7 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
 
   usx_bf_plan* p = new usx_bf_plan();
   p->ctx = ctx;
+  p->device = ctx->device;
   p->cd = *cd;
   p->cd.transmits = nullptr;
   p->cfg = *cfg;
@@ -829,7 +954,9 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
 
 int usx_cu_bf_plan_destroy(usx_bf_plan* plan) {
   if (!plan) return USX_OK;
-  cudaStreamSynchronize(plan->ctx->stream);
+  // The context may already be gone: synchronise the device, not its stream.
+  cudaSetDevice(plan->device);
+  cudaDeviceSynchronize();
   cudaFree(plan->d_points);
   cudaFree(plan->d_tx);
   cudaFree(plan->d_mv_stats);
@@ -841,7 +968,7 @@ int usx_cu_bf_plan_workspace(const usx_bf_plan* plan, size_t* bytes) {
   if (!plan || !bytes) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_workspace: null argument");
   const size_t n_pix = static_cast<size_t>(plan->n0) * plan->n1;
   *bytes = 0;
-  if (plan->cfg.combiner == USX_COMB_MV)
+  if (plan->cfg.combiner == USX_COMB_MV || plan->cfg.combiner == USX_COMB_LEARNED_MV)
     *bytes = n_pix * plan->cd.probe.n_elements * sizeof(float2) + n_pix * sizeof(float);
   return USX_OK;
 }
@@ -888,6 +1015,45 @@ int usx_cu_bf_plan_mv_stats(usx_bf_plan* plan, int64_t* fp64_resolves, int64_t* 
   USX_CUDA(cudaMemsetAsync(plan->d_mv_stats, 0, sizeof(h), plan->ctx->stream));
   if (fp64_resolves) *fp64_resolves = h[0];
   if (factorization_failures) *factorization_failures = h[1];
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned: null plan");
+  if (plan->cfg.combiner != USX_COMB_LEARNED_MV)
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned: the plan's combiner is not LEARNED_MV");
+  if (mlp && !mlp_is_lmv(mlp))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned: the network must map 256 features to 128 outputs");
+  if (!(gate >= 0.0f)) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned: gate must be >= 0");
+  plan->mlp = mlp;
+  plan->lmv_gate = gate;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_training_export(usx_bf_plan* plan, float* features, float* weights, uint8_t* valid) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_training_export: null plan");
+  const bool any = features || weights || valid;
+  if (any && !(features && weights && valid))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_training_export: give all three buffers or none");
+  if (any && (plan->cfg.combiner != USX_COMB_MV || plan->mv_mode != USX_MV_TENSOR ||
+              plan->cfg.compounding == USX_COMP_INCOHERENT))
+    return fail(USX_ERR_INVALID,
+                "usx_cu_bf_plan_set_training_export: needs a coherent minimum-variance plan in USX_MV_TENSOR mode");
+  plan->exp_feat = features;
+  plan->exp_w = weights;
+  plan->exp_valid = valid;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_learned_stats: null plan");
+  int h = 0;
+  USX_CUDA(cudaMemcpyAsync(&h, plan->d_mv_stats + 2, sizeof(int), cudaMemcpyDeviceToHost, plan->ctx->stream));
+  USX_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  USX_CUDA(cudaMemsetAsync(plan->d_mv_stats + 2, 0, sizeof(int), plan->ctx->stream));
+  if (gated) *gated = h;
+  if (pixels) *pixels = plan->lmv_pixels;
+  plan->lmv_pixels = 0;
   return USX_OK;
 }
 

@@ -111,7 +111,41 @@ struct MvTcArgs {
   int* fallback_count;    // pixels whose refined residual failed
   int2* fallback;         // (pixel, frame) of each, up to fallback_cap
   int fallback_cap;
+  const int2* list;       // optional (pixel, frame) work list instead of all pixels
+  const int* list_count;
+  int list_cap;
+  float* w_export;        // optional [frame * n_pix + pix][2 * kTcMaxL]: L w / sum(w)
+  uint8_t* w_valid;       // [frame * n_pix + pix]: 1 where w_export holds a solve
 };
+
+// Training export of a solved pixel: L * w_i / sum(w) for i < L, zero beyond;
+// lane-parallel over i = lane, lane + 32.
+__device__ __forceinline__ void export_weights(const MvTcArgs& a, long row, int lane, int L, const float2 (&w)[2],
+                                               float dre, float dim) {
+  if (!a.w_export) return;
+  const float den = dre * dre + dim * dim;
+  float2* dst = reinterpret_cast<float2*>(a.w_export) + row * kTcMaxL;
+#pragma unroll
+  for (int s2 = 0; s2 < 2; ++s2) {
+    const int i = lane + 32 * s2;
+    float2 v = make_float2(0.f, 0.f);
+    if (i < L && den > 0.f) {
+      // w / d = w conj(d) / |d|^2
+      v.x = (w[s2].x * dre + w[s2].y * dim) / den * static_cast<float>(L);
+      v.y = (w[s2].y * dre - w[s2].x * dim) / den * static_cast<float>(L);
+    }
+    dst[i] = v;
+  }
+  if (lane == 0) a.w_valid[row] = den > 0.f ? 1 : 0;
+}
+
+// Marks a pixel with no Capon solve in the training export.
+__device__ __forceinline__ void export_invalid(const MvTcArgs& a, long row, int tid) {
+  if (!a.w_export) return;
+  float2* dst = reinterpret_cast<float2*>(a.w_export) + row * kTcMaxL;
+  for (int i = tid; i < kTcMaxL; i += 32) dst[i] = make_float2(0.f, 0.f);
+  if (tid == 0) a.w_valid[row] = 0;
+}
 
 // One CTA (kTcWarps warps) per pixel; a grid-stride loop over pixels keeps
 // the shared layout resident.
@@ -129,11 +163,19 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
   __shared__ int s_misc[8];
   __shared__ float s_red[kTcWarps][4];
 
-  const long total = static_cast<long>(a.n_pix) * gridDim.y;
-  for (long item = blockIdx.x; item < static_cast<long>(a.n_pix); item += gridDim.x) {
-    const int pix = static_cast<int>(item);
-    const long frame = blockIdx.y;
-    (void)total;
+  const long n_items = a.list ? static_cast<long>(min(*a.list_count, a.list_cap)) : static_cast<long>(a.n_pix);
+  for (long item = blockIdx.x; item < n_items; item += gridDim.x) {
+    int pix;
+    long frame;
+    if (a.list) {
+      const int2 pf = a.list[item];
+      pix = pf.x;
+      frame = pf.y;
+    } else {
+      pix = static_cast<int>(item);
+      frame = blockIdx.y;
+    }
+    const long row = frame * a.n_pix + pix;
     const int j = pix % a.n1;
     const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
     const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
@@ -182,12 +224,13 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
       }
       return acc;
     };
-    if (n_act == 0) {
-      if (tid == 0 && !a.incoherent) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
-      continue;
-    }
     if (n_act < 4) {
-      if (tid == 0) finish(center_das());
+      if (warp == 0) export_invalid(a, row, tid);
+      if (n_act == 0) {
+        if (tid == 0 && !a.incoherent) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
+      } else if (tid == 0) {
+        finish(center_das());
+      }
       continue;
     }
     int L = a.mv_subarray;
@@ -214,6 +257,7 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
     __syncthreads();
     amax = fmaxf(fmaxf(s_red[0][0], s_red[1][0]), fmaxf(s_red[2][0], s_red[3][0]));
     if (!(amax > 0.0f)) {
+      if (warp == 0) export_invalid(a, row, tid);
       if (tid == 0) finish(mk(0.f, 0.f));
       continue;
     }
@@ -345,6 +389,7 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
       __syncthreads();
     }
     if (!ok) {
+      if (warp == 0) export_invalid(a, row, tid);
       if (tid == 0) {
         if (a.stats) atomicAdd(a.stats + 1, 1);
         finish(center_das());
@@ -506,6 +551,10 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
           ore += __shfl_xor_sync(0xffffffffu, ore, o);
           oim += __shfl_xor_sync(0xffffffffu, oim, o);
         }
+        if (hypotf(dre, dim) < 1e-30f)
+          export_invalid(a, row, lane);
+        else
+          export_weights(a, row, lane, L, w, dre, dim);
         if (lane == 0) {
           cplx out;
           if (hypotf(dre, dim) < 1e-30f)
@@ -613,6 +662,12 @@ __global__ void __launch_bounds__(32) mv_fp64_kernel(const MvTcArgs a) {
     }
     cplx out;
     if (!ok) {
+      if (a.w_export) {
+        const long row = frame * a.n_pix + pix;
+        float2* dst = reinterpret_cast<float2*>(a.w_export) + row * kTcMaxL;
+        for (int i = lane; i < kTcMaxL; i += 32) dst[i] = make_float2(0.f, 0.f);
+        if (lane == 0) a.w_valid[row] = 0;
+      }
       if (a.stats && lane == 0) atomicAdd(a.stats + 1, 1);
       out = mk(0.f, 0.f);
       for (int q = 0; q < n_act; ++q) out = cadd(out, mk(yc[act[q]].x, yc[act[q]].y));
@@ -677,6 +732,21 @@ __global__ void __launch_bounds__(32) mv_fp64_kernel(const MvTcArgs a) {
         oim += __shfl_xor_sync(0xffffffffu, oim, o);
       }
       const double den = dre * dre + dim * dim;
+      if (a.w_export) {
+        const long row = frame * a.n_pix + pix;
+        float2* dst = reinterpret_cast<float2*>(a.w_export) + row * kTcMaxL;
+        const bool solved = !(sqrt(den) < 1e-30);
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          float2 val = make_float2(0.f, 0.f);
+          if (i < L && solved) {
+            val.x = static_cast<float>((v[s2].x * dre + v[s2].y * dim) / den * L);
+            val.y = static_cast<float>((v[s2].y * dre - v[s2].x * dim) / den * L);
+          }
+          dst[i] = val;
+        }
+        if (lane == 0) a.w_valid[row] = solved ? 1 : 0;
+      }
       if (sqrt(den) < 1e-30) {
         out = mk(0.f, 0.f);
         for (int q = 0; q < n_act; ++q) out = cadd(out, mk(yc[act[q]].x, yc[act[q]].y));
@@ -716,7 +786,8 @@ int mv_tc_supported(int n_ch, int mv_subarray, int range_avg) {
 int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,
                  float* acc_out, int n_ch, int n_pix, int n1, int n_frames, int mv_subarray, int range_avg,
                  float loading, float f_number, float tukey_alpha, int rx_window, float half_nm1, float pitch,
-                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap) {
+                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap,
+                 const MvTcExtra& extra) {
   MvTcArgs a;
   a.y = y;
   a.points = points;
@@ -742,13 +813,22 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
   a.fallback_count = fallback_count;
   a.fallback = fallback;
   a.fallback_cap = fallback_cap;
+  a.list = extra.list;
+  a.list_count = extra.list_count;
+  a.list_cap = extra.list_cap;
+  a.w_export = extra.w_export;
+  a.w_valid = extra.w_valid;
   const MvTcLayout l = mv_tc_layout(n_ch, a.n_dmax, a.lmax);
   const size_t smem = l.bytes;
   USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_tc_kernel, 32 * kTcWarps, smem));
-  const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 4 / std::max(1, n_frames);
-  const dim3 grid(static_cast<unsigned>(std::max(1L, std::min<long>(n_pix, want))), n_frames);
+  // Full frames: a grid-stride loop over pixels, frames on y. Work list: its
+  // length is only known on the device, so one resident wave loops over it.
+  const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
+  const long want = resident * 4 / std::max(1, n_frames);
+  const dim3 grid = extra.list ? dim3(static_cast<unsigned>(resident), 1)
+                               : dim3(static_cast<unsigned>(std::max(1L, std::min<long>(n_pix, want))), n_frames);
   prof_begin(ctx, "mv_tc_kernel");
   mv_tc_kernel<<<grid, 32 * kTcWarps, smem, ctx->stream>>>(a);
   prof_end(ctx);

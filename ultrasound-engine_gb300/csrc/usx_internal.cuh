@@ -215,11 +215,51 @@ TxDev make_txdev(const usx_probe& probe, const usx_transmit& tx);
 
 inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); }
 
-// Tensor-core minimum variance (mv_tc.cu).
+// Tensor-core minimum variance (mv_tc.cu). Optional extras: a device work
+// list of (pixel, frame) pairs in place of every pixel of every frame, and a
+// training export of the normalised Capon weights L w / sum(w)
+// ([frame * n_pix + pix][2 * 64] floats, zero past L) with a per-pixel valid flag.
+struct MvTcExtra {
+  const int2* list = nullptr;
+  const int* list_count = nullptr;
+  int list_cap = 0;
+  float* w_export = nullptr;
+  uint8_t* w_valid = nullptr;
+};
 int mv_tc_supported(int n_ch, int mv_subarray, int range_avg);
 int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,
                  float* acc_out, int n_ch, int n_pix, int n1, int n_frames, int mv_subarray, int range_avg,
                  float loading, float f_number, float tukey_alpha, int rx_window, float half_nm1, float pitch,
-                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap);
+                 int cf, int incoherent, int* stats, int* fallback_count, int2* fallback, int fallback_cap,
+                 const MvTcExtra& extra = MvTcExtra());
+
+// Learned minimum variance (learned.cu): per-pixel features of the compounded
+// channel samples, and the gated apply of the network's weights.
+constexpr int kLmvFeatures = 256;  // network inputs per pixel
+constexpr int kLmvOutputs = 128;   // network outputs per pixel: 64 complex weights
+struct LmvLaunch {
+  const float2* y = nullptr;       // [frame][pix][n_ch]
+  const float* points = nullptr;
+  int n_ch = 0, n_pix = 0, n1 = 0, n_frames = 0, mv_subarray = 0, range_avg = 0;
+  float f_number = 0, tukey_alpha = 0, half_nm1 = 0, pitch = 0;
+  int rx_window = 0, cf = 0;
+  void* feat16 = nullptr;          // BF16 [row][256] (inference)
+  float* feat32 = nullptr;         // FP32 [row][256] (training export)
+  float2* avg = nullptr;           // [row][64]
+  float4* meta = nullptr;          // [row] (L, n_act, coherence factor, 0)
+  float2* out = nullptr;           // frames (DAS for n_act < 4)
+  long out_stride = 0;
+};
+int launch_lmv_features(usx_ctx* ctx, const LmvLaunch& l);
+int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const float4* meta, float2* out,
+                     long out_stride, int n_pix, int n_frames, float gate, int* gated_count, int2* gated,
+                     int gated_cap, int* stats);
+
+// The network (mlp.cu). mlp_infer runs `rows` (a multiple of 128) BF16 input
+// rows through every layer with caller scratch t0, t1 (rows x widest BF16
+// each) and writes the FP32 outputs.
+int mlp_widest(const usx_mlp* n);
+bool mlp_is_lmv(const usx_mlp* n);
+int mlp_infer(usx_mlp* n, usx_ctx* ctx, const void* x16, long rows, void* t0, void* t1, float* out32);
 
 }  // namespace usxcu

@@ -320,6 +320,26 @@ class Plan:
         check(lib().usx_cu_bf_plan_mv_stats(self._h, C.byref(a), C.byref(b)), "bf_plan_mv_stats")
         return a.value, b.value
 
+    def set_learned(self, mlp: "Mlp | None", gate: float = 0.05) -> None:
+        """Attach the network of a LEARNED_MV plan (kept alive by the plan)."""
+        check(lib().usx_cu_bf_plan_set_learned(self._h, mlp.handle if mlp else None, C.c_float(gate)),
+              "bf_plan_set_learned")
+        self._mlp = mlp
+
+    def learned_stats(self):
+        """(pixels gated to the exact solver, pixels beamformed) since the last call."""
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().usx_cu_bf_plan_learned_stats(self._h, C.byref(a), C.byref(b)), "bf_plan_learned_stats")
+        return a.value, b.value
+
+    def set_training_export(self, features_ptr: int | None, weights_ptr: int | None, valid_ptr: int | None):
+        """Per-pixel features [rows][256], Capon weights [rows][128] and valid
+        flags [rows] (device pointers) written by every execution; None turns it off."""
+        check(lib().usx_cu_bf_plan_set_training_export(self._h, vp(features_ptr) if features_ptr else None,
+                                                       vp(weights_ptr) if weights_ptr else None,
+                                                       vp(valid_ptr) if valid_ptr else None),
+              "bf_plan_set_training_export")
+
     def workspace_bytes(self) -> int:
         n = C.c_size_t()
         check(lib().usx_cu_bf_plan_workspace(self._h, C.byref(n)), "bf_plan_workspace")
@@ -328,6 +348,77 @@ class Plan:
     def close(self):
         if self._h:
             lib().usx_cu_bf_plan_destroy(self._h)
+            self._h = vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Mlp:
+    """usx_mlp: fully connected ReLU network trained and run on the device
+    (BF16 GEMMs with FP32 accumulation, FP32 master weights, Adam)."""
+
+    def __init__(self, ctx: Context, dims, seed: int = 0):
+        self.ctx = ctx
+        self.dims = [int(d) for d in dims]
+        self._h = vp()
+        arr = (C.c_int * len(self.dims))(*self.dims)
+        check(lib().usx_cu_mlp_create(ctx.handle, len(self.dims) - 1, arr, C.c_uint64(seed), C.byref(self._h)),
+              "mlp_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n_params(self) -> int:
+        n = C.c_int64()
+        check(lib().usx_cu_mlp_num_params(self._h, C.byref(n)), "mlp_num_params")
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.n_params, np.float32)
+        check(lib().usx_cu_mlp_get_params(self._h, out.ctypes.data_as(f32p)), "mlp_get_params")
+        return out
+
+    def set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters, got {p.size}")
+        check(lib().usx_cu_mlp_set_params(self._h, p.ctypes.data_as(f32p)), "mlp_set_params")
+
+    def layers(self, params=None):
+        """[(W [din, dout], b [dout]), ...] views of a parameter vector."""
+        p = self.get_params() if params is None else params
+        out, o = [], 0
+        for din, dout in zip(self.dims[:-1], self.dims[1:]):
+            w = p[o:o + din * dout].reshape(din, dout)
+            o += din * dout
+            b = p[o:o + dout]
+            o += dout
+            out.append((w, b))
+        return out
+
+    def forward(self, x_ptr: int, rows: int, y_ptr: int) -> None:
+        check(lib().usx_cu_mlp_forward(self._h, vp(x_ptr), C.c_int64(rows), vp(y_ptr)), "mlp_forward")
+
+    def train_step(self, x_ptr: int, t_ptr: int, mask_ptr: int | None, rows: int, lr: float,
+                   want_loss: bool = False, want_grad: bool = False):
+        """One step; returns (loss or None, gradient vector or None)."""
+        loss = C.c_float()
+        grad = np.empty(self.n_params, np.float32) if want_grad else None
+        check(lib().usx_cu_mlp_train_step(self._h, vp(x_ptr), vp(t_ptr), vp(mask_ptr) if mask_ptr else None,
+                                          C.c_int64(rows), C.c_float(lr),
+                                          C.byref(loss) if want_loss else None,
+                                          grad.ctypes.data_as(f32p) if want_grad else None), "mlp_train_step")
+        return (loss.value if want_loss else None), grad
+
+    def close(self):
+        if self._h:
+            lib().usx_cu_mlp_destroy(self._h)
             self._h = vp()
 
     def __del__(self):

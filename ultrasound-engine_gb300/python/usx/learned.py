@@ -1,0 +1,420 @@
+"""Learned minimum variance: training pairs, on-device training, evaluation.
+
+The surrogate is a 4-layer fully connected network (256 -> 256 -> 256 -> 256
+-> 128, ReLU, BF16 weights and activations with FP32 accumulation) that maps a
+pixel's 256 minimum-variance features (normalised diagonal sums of the
+spatially smoothed covariance and the subarray-averaged snapshot, computed by
+the library's feature kernel) to its Capon weights L w / sum(w). Training
+pairs come from the plain tensor-core minimum variance run on simulated
+phantoms (the plan's training export); training runs on the device through
+usx_cu_mlp_train_step (hand-written forward/backward GEMMs and Adam). At
+inference the plan gates each pixel on |1^H w - 1| and solves the rejected
+ones exactly, so plain minimum variance is both the fallback and the judge.
+
+    python -m usx.learned train --phantoms 200 --out weights.bin
+    python -m usx.learned evaluate --weights weights.bin --phantoms 16
+
+No counterpart in the reference; its minimum variance is
+core/src/beamformer.cpp:137-214.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import capi
+
+DIMS = (256, 256, 256, 256, 128)
+FEATURES, OUTPUTS = DIMS[0], DIMS[-1]
+DEFAULT_GATE = 0.05
+COMB_MV, COMB_LEARNED_MV = 2, 3
+MAGIC = b"USXMLP1\0"
+DEFAULT_WEIGHTS = Path(__file__).resolve().parents[2] / "weights" / "learned_mv_128ch_l64.bin"
+
+
+# ------------------------------------------------------------------ weights file
+
+def save_weights(path, dims, params) -> None:
+    """Raw little-endian file: magic, int32 n_layers, int32 dims[n+1], float32 params."""
+    dims = np.asarray(dims, np.int32)
+    with open(path, "wb") as f:
+        f.write(MAGIC)
+        f.write(np.int32(len(dims) - 1).tobytes())
+        f.write(dims.astype("<i4").tobytes())
+        f.write(np.ascontiguousarray(params, dtype="<f4").tobytes())
+
+
+def load_weights(path):
+    """(dims, params) from a file written by save_weights."""
+    raw = Path(path).read_bytes()
+    if raw[:8] != MAGIC:
+        raise ValueError(f"{path}: not a usx network file")
+    n = int(np.frombuffer(raw, "<i4", 1, 8)[0])
+    dims = tuple(int(d) for d in np.frombuffer(raw, "<i4", n + 1, 12))
+    params = np.frombuffer(raw, "<f4", offset=12 + 4 * (n + 1)).copy()
+    expect = sum(a * b + b for a, b in zip(dims[:-1], dims[1:]))
+    if params.size != expect:
+        raise ValueError(f"{path}: {params.size} parameters, expected {expect}")
+    return dims, params
+
+
+# ------------------------------------------------------------------ geometry
+
+@dataclass
+class Setup:
+    """Probe, acquisition and grid of the 128-channel 75-plane-wave 512 x 1024
+    configuration (the shapes the surrogate is trained for)."""
+    n_el: int = 128
+    pitch: float = 300e-6
+    width: float = 270e-6
+    f0: float = 5e6
+    fs: float = 20e6
+    c: float = 1540.0
+    n_tx: int = 75
+    max_angle_deg: float = 16.0
+    depth: float = 0.060
+    z0: float = 0.005
+    n0: int = 512
+    n1: int = 1024
+    f_number: float = 1.5
+    subarray: int = 64
+    loading: float = 0.01
+    range_avg: int = 2
+
+    def build(self):
+        """(ch_rf, ch_iq, grid, n_samples, transmits) capi descriptors; transmit
+        delays from the host library."""
+        import usx
+        probe = usx.Probe()
+        probe.n_elements, probe.pitch, probe.element_width = self.n_el, self.pitch, self.width
+        probe.center_frequency, probe.bandwidth = self.f0, 0.6
+        medium = usx.Medium()
+        acq = usx.presets.acquisition(probe, depth=self.depth, medium=medium, samples_per_wavelength=self.fs / self.f0)
+        sim = usx.Simulator(probe, medium, acq, usx.SimulatorConfig())
+        txs = sim.make_plane_waves(usx.angles_deg(-self.max_angle_deg, self.max_angle_deg, self.n_tx))
+        tx = [dict(type=1, angle=t.angle, delays=t.delays, apodization=t.apodization) for t in txs]
+        cp = capi.Probe(self.n_el, probe.pitch, probe.element_width, probe.elevation_height, self.f0, probe.bandwidth)
+        cm = capi.Medium(medium.speed_of_sound, medium.attenuation, medium.density)
+        ca = capi.Acquisition(acq.sampling_frequency, acq.n_samples, acq.t0, acq.prf)
+        ch_rf = capi.Channel(cp, cm, ca, tx)
+        ch_iq = capi.Channel(cp, cm, ca, tx, is_iq=True, fdem=self.f0)
+        grid = usx.grid_for(probe, self.z0, self.depth, self.n0, self.n1)
+        cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), np.asarray(grid.points).reshape(-1, 3))
+        return ch_rf, ch_iq, cgrid, acq.n_samples, tx
+
+    def bf(self, combiner: int) -> capi.BeamformerConfig:
+        return capi.bf_config(f_number=self.f_number, combiner=combiner, mv_subarray=self.subarray,
+                              mv_diagonal_loading=self.loading, mv_range_average=self.range_avg)
+
+    @property
+    def half_width(self) -> float:
+        return 0.5 * (self.n_el - 1) * self.pitch
+
+
+# ------------------------------------------------------------------ phantoms
+
+@dataclass
+class PhantomSpec:
+    scatterers: np.ndarray      # [n, 8] float32 (x, y, z, amplitude, vx, vy, vz, pad)
+    cysts: list                 # [(x, z, r)]
+    wires: list                 # [(x, z, amplitude)]
+
+
+def phantom(seed: int, setup: Setup = Setup()) -> PhantomSpec:
+    """Seeded speckle phantom: 50k-150k N(0,1) scatterers over the imaged
+    region, 1-3 anechoic cysts of radius 1-5 mm and 2-6 wires of amplitude
+    5-50 (numpy PCG64 stream `seed`). Cysts and wires keep 3 mm apart."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(50_000, 150_001))
+    xh = 1.1 * setup.half_width
+    pos = np.stack([rng.uniform(-xh, xh, n), np.zeros(n), rng.uniform(setup.z0 - 1e-3, setup.depth + 2e-3, n)], 1)
+    amp = rng.standard_normal(n)
+    cysts, wires = [], []
+    for _ in range(int(rng.integers(1, 4))):
+        for _try in range(50):
+            r = rng.uniform(1e-3, 5e-3)
+            x, z = rng.uniform(-0.8 * xh, 0.8 * xh), rng.uniform(setup.z0 + 2 * r + 2e-3, setup.depth - 2 * r - 2e-3)
+            if all(math.hypot(x - cx, z - cz) > r + cr + 3e-3 for cx, cz, cr in cysts):
+                cysts.append((x, z, r))
+                break
+    keep = np.ones(n, bool)
+    for x, z, r in cysts:
+        keep &= np.hypot(pos[:, 0] - x, pos[:, 2] - z) > r
+    pos, amp = pos[keep], amp[keep]
+    for _ in range(int(rng.integers(2, 7))):
+        for _try in range(50):
+            x, z = rng.uniform(-0.85 * setup.half_width, 0.85 * setup.half_width), rng.uniform(setup.z0 + 3e-3,
+                                                                                                setup.depth - 3e-3)
+            if all(math.hypot(x - cx, z - cz) > cr + 3e-3 for cx, cz, cr in cysts) and \
+                    all(math.hypot(x - wx, z - wz) > 3e-3 for wx, wz, _ in wires):
+                wires.append((x, z, float(rng.uniform(5.0, 50.0))))
+                break
+    if wires:
+        pos = np.concatenate([pos, np.array([[x, 0.0, z] for x, z, _ in wires])])
+        amp = np.concatenate([amp, np.array([a for _, _, a in wires])])
+    s = np.zeros((len(amp), 8), np.float32)
+    s[:, 0:3] = pos
+    s[:, 3] = amp
+    return PhantomSpec(s, cysts, wires)
+
+
+# ------------------------------------------------------------------ acquisition
+
+class Imager:
+    """GPU simulation, demodulation and beamforming of phantoms in one context
+    (the legacy default stream, so torch and the library share ordering)."""
+
+    def __init__(self, setup: Setup = Setup(), device: int = 0, noise_db: float = -60.0):
+        import torch
+        self.torch = torch
+        self.setup = setup
+        self.ctx = capi.Context(device, stream=0)
+        self.ch_rf, self.ch_iq, self.grid, self.n_smp, self.transmits = setup.build()
+        self.sim_cfg = capi.sim_config(noise_db=noise_db)
+        self.n_pix = setup.n0 * setup.n1
+        self.rf = torch.empty((setup.n_tx, setup.n_el, self.n_smp), dtype=torch.float32, device="cuda")
+        self.iq = torch.empty((setup.n_tx, setup.n_el, self.n_smp), dtype=torch.complex64, device="cuda")
+        self.plans = {}
+
+    def plan(self, combiner: int) -> capi.Plan:
+        if combiner not in self.plans:
+            p = self.ctx.plan(self.ch_iq, self.grid, self.setup.bf(combiner))
+            if combiner == COMB_MV:
+                p.set_mv_mode(1)
+            self.plans[combiner] = p
+        return self.plans[combiner]
+
+    def acquire(self, spec: PhantomSpec, noise_seed: int = 0):
+        """Simulate (with receive noise from seeded device normals) and demodulate into self.iq."""
+        torch = self.torch
+        scat = torch.from_numpy(spec.scatterers).cuda()
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(int(noise_seed) + 77)
+        z = torch.randn(self.rf.shape, generator=gen, device="cuda", dtype=torch.float32)
+        self.ctx.simulate(self.ch_rf, self.sim_cfg, scat.data_ptr(), scat.shape[0], z.data_ptr(),
+                          self.rf.data_ptr())
+        self.ctx.demodulate(self.ch_rf, capi.demod_config(), self.rf.data_ptr(), self.iq.data_ptr())
+        self.ctx.synchronize()
+        del scat, z
+
+    def beamform(self, combiner: int):
+        frame = self.torch.empty((self.setup.n0, self.setup.n1), dtype=self.torch.complex64, device="cuda")
+        self.plan(combiner).execute(self.iq.data_ptr(), frame.data_ptr())
+        return frame
+
+    def export_pairs(self):
+        """Plain tensor-core MV frame with every pixel's (features, weights, valid)."""
+        torch = self.torch
+        feat = torch.empty((self.n_pix, FEATURES), dtype=torch.float32, device="cuda")
+        w = torch.empty((self.n_pix, OUTPUTS), dtype=torch.float32, device="cuda")
+        valid = torch.empty(self.n_pix, dtype=torch.uint8, device="cuda")
+        p = self.plan(COMB_MV)
+        p.set_training_export(feat.data_ptr(), w.data_ptr(), valid.data_ptr())
+        try:
+            frame = self.beamform(COMB_MV)
+        finally:
+            p.set_training_export(None, None, None)
+        return frame, feat, w, valid
+
+    def close(self):
+        for p in self.plans.values():
+            p.close()
+        self.plans = {}
+        self.ctx.close()
+
+
+def output_mask(feat):
+    """1 for the outputs of weights i < L (L = 64 f[0]), 0 beyond."""
+    torch = __import__("torch")
+    L = torch.round(feat[:, 0] * 64.0)
+    k = torch.arange(OUTPUTS, device=feat.device)
+    return ((k[None, :] // 2) < L[:, None]).float()
+
+
+def sample_rows(frame, valid, n: int, gen, bright_frac: float = 0.25):
+    """n valid pixel rows: (1 - bright_frac) uniform, bright_frac from the 2%
+    brightest (point targets and their side lobes are where weights matter most)."""
+    torch = __import__("torch")
+    idx = torch.nonzero(valid.bool(), as_tuple=False).squeeze(1)
+    n_b = int(n * bright_frac)
+    u = idx[torch.randint(idx.numel(), (n - n_b,), generator=gen, device=idx.device)]
+    mag = frame.reshape(-1).abs()[idx]
+    k = max(1, int(0.02 * idx.numel()))
+    top = idx[torch.topk(mag, k).indices]
+    b = top[torch.randint(top.numel(), (n_b,), generator=gen, device=idx.device)]
+    return torch.cat([u, b])
+
+
+def make_pairs(imager: Imager, seeds, per_phantom: int = 16384, log=print):
+    """Training pairs from the plain MV on the phantoms `seeds` (device tensors)."""
+    torch = imager.torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(12345)
+    X, T = [], []
+    t0 = time.time()
+    for i, s in enumerate(seeds):
+        imager.acquire(phantom(int(s), imager.setup))
+        frame, feat, w, valid = imager.export_pairs()
+        rows = sample_rows(frame, valid, per_phantom, gen)
+        X.append(feat[rows].clone())
+        T.append(w[rows].clone())
+        del feat, w, valid, frame
+        if log and (i + 1) % 20 == 0:
+            log(f"pairs: {i + 1}/{len(seeds)} phantoms, {time.time() - t0:.1f} s")
+    X = torch.cat(X)
+    T = torch.cat(T)
+    return X, T, output_mask(X)
+
+
+def train(ctx: capi.Context, X, T, M, steps: int = 6000, batch: int = 4096, lr: float = 1e-3, seed: int = 0,
+          log=print, log_every: int = 500) -> tuple[capi.Mlp, list]:
+    """Adam on minibatches drawn on the device, cosine learning-rate decay."""
+    torch = __import__("torch")
+    mlp = capi.Mlp(ctx, DIMS, seed)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed + 1)
+    n = X.shape[0]
+    losses = []
+    for step in range(steps):
+        idx = torch.randint(n, (batch,), generator=gen, device=X.device)
+        xb, tb, mb = X[idx].contiguous(), T[idx].contiguous(), M[idx].contiguous()
+        lr_t = lr * 0.5 * (1.0 + math.cos(math.pi * step / steps))
+        want = step % log_every == 0 or step == steps - 1
+        loss, _ = mlp.train_step(xb.data_ptr(), tb.data_ptr(), mb.data_ptr(), batch, lr_t, want_loss=want)
+        if want:
+            losses.append((step, loss))
+            if log:
+                log(f"step {step}: loss {loss:.5f} lr {lr_t:.2e}")
+    return mlp, losses
+
+
+def validation_loss(mlp: capi.Mlp, X, T, M) -> float:
+    """Masked mean squared error of the network on (X, T)."""
+    torch = __import__("torch")
+    n = X.shape[0] // 128 * 128
+    Y = torch.empty((n, OUTPUTS), dtype=torch.float32, device=X.device)
+    mlp.forward(X[:n].contiguous().data_ptr(), n, Y.data_ptr())
+    torch.cuda.synchronize()
+    d = (Y - T[:n]) * M[:n]
+    return float((d * d).sum() / (n * OUTPUTS))
+
+
+def image_metrics(frame, imager: Imager, spec: PhantomSpec) -> dict:
+    """gCNR/CNR per cyst and lateral/axial FWHM per wire (envelope of the frame)."""
+    from . import metrics
+    env = frame.abs().cpu().numpy()
+    g = imager.grid
+    out = {"gcnr": [], "cnr": [], "lateral_fwhm_mm": [], "axial_fwhm_mm": []}
+    for x, z, r in spec.cysts:
+        out["gcnr"].append(metrics.gcnr(env, g, (x, z), r))
+        out["cnr"].append(metrics.cnr(env, g, (x, z), r))
+    for x, z, _ in spec.wires:
+        psf = metrics.measure_psf(env, g, (x, z), 1e-3)
+        out["lateral_fwhm_mm"].append(psf.lateral_fwhm * 1e3)
+        out["axial_fwhm_mm"].append(psf.axial_fwhm * 1e3)
+    return out
+
+
+def evaluate(imager: Imager, mlp: capi.Mlp | None, seeds, gate: float = DEFAULT_GATE, baseline: int = COMB_MV,
+             log=print) -> dict:
+    """Per-phantom metrics of plain MV and the learned MV (or, with mlp=None
+    and baseline given, of any other combiner) on held-out phantoms."""
+    learned = imager.plan(COMB_LEARNED_MV)
+    learned.set_learned(mlp, gate)
+    rows = []
+    for s in seeds:
+        spec = phantom(int(s), imager.setup)
+        imager.acquire(spec)
+        ref = imager.beamform(baseline)
+        learned.learned_stats()
+        lf = imager.beamform(COMB_LEARNED_MV)
+        gated, pixels = learned.learned_stats()
+        a, b = image_metrics(ref, imager, spec), image_metrics(lf, imager, spec)
+        d = {k: [y - x for x, y in zip(a[k], b[k])] for k in a}
+        rows.append({"seed": int(s), "plain": a, "learned": b, "delta": d,
+                     "fallback_rate": gated / max(1, pixels),
+                     "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt() / ref.abs().pow(2).sum().sqrt())})
+        if log:
+            log(f"phantom {s}: fallback {rows[-1]['fallback_rate']:.4f} rel_l2 {rows[-1]['rel_l2']:.4f} "
+                f"dgcnr {d['gcnr']} dfwhm {d['lateral_fwhm_mm']}")
+    return summarize(rows)
+
+
+def summarize(rows) -> dict:
+    def flat(key, part):
+        return [v for r in rows for v in r[part][key]]
+    out = {"phantoms": len(rows), "fallback_rate": float(np.mean([r["fallback_rate"] for r in rows])),
+           "rel_l2_mean": float(np.mean([r["rel_l2"] for r in rows]))}
+    for k in ("gcnr", "cnr", "lateral_fwhm_mm", "axial_fwhm_mm"):
+        p, l_ = np.array(flat(k, "plain")), np.array(flat(k, "learned"))
+        if p.size:
+            out[k] = {"plain_mean": float(p.mean()), "learned_mean": float(l_.mean()),
+                      "max_abs_delta": float(np.max(np.abs(l_ - p))), "mean_delta": float(np.mean(l_ - p)),
+                      "max_rel_delta": float(np.max(np.abs(l_ - p) / np.maximum(np.abs(p), 1e-12)))}
+    out["rows"] = rows
+    return out
+
+
+def load_mlp(ctx: capi.Context, path=DEFAULT_WEIGHTS) -> capi.Mlp:
+    dims, params = load_weights(path)
+    mlp = capi.Mlp(ctx, dims)
+    mlp.set_params(params)
+    return mlp
+
+
+def main(argv=None) -> None:
+    ap = argparse.ArgumentParser(prog="python -m usx.learned")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("--phantoms", type=int, default=200)
+    t.add_argument("--per-phantom", type=int, default=16384)
+    t.add_argument("--steps", type=int, default=6000)
+    t.add_argument("--batch", type=int, default=4096)
+    t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
+    t.add_argument("--eval-phantoms", type=int, default=16)
+    t.add_argument("--report", default=None)
+    e = sub.add_parser("evaluate")
+    e.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
+    e.add_argument("--phantoms", type=int, default=16)
+    e.add_argument("--gate", type=float, default=DEFAULT_GATE)
+    e.add_argument("--report", default=None)
+    a = ap.parse_args(argv)
+    imager = Imager()
+    report = {}
+    if a.cmd == "train":
+        train_seeds = np.arange(1000, 1000 + a.phantoms)
+        t0 = time.time()
+        X, T, M = make_pairs(imager, train_seeds, a.per_phantom)
+        report["pairs"] = int(X.shape[0])
+        report["pair_seconds"] = time.time() - t0
+        t0 = time.time()
+        mlp, losses = train(imager.ctx, X, T, M, a.steps, a.batch, a.lr, a.seed)
+        imager.ctx.synchronize()
+        report["train_seconds"] = time.time() - t0
+        report["losses"] = losses
+        Path(a.out).parent.mkdir(parents=True, exist_ok=True)
+        save_weights(a.out, DIMS, mlp.get_params())
+        if a.eval_phantoms:
+            report["eval"] = evaluate(imager, mlp, np.arange(900_000, 900_000 + a.eval_phantoms))
+    else:
+        mlp = load_mlp(imager.ctx, a.weights)
+        report["eval"] = evaluate(imager, mlp, np.arange(900_000, 900_000 + a.phantoms), a.gate)
+    s = json.dumps(report, indent=1, default=float)
+    if a.report:
+        Path(a.report).write_text(s)
+    ev = report.get("eval", {})
+    print(json.dumps({k: v for k, v in ev.items() if k != "rows"}, default=float))
+    imager.close()
+
+
+if __name__ == "__main__":
+    main()
