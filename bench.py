@@ -43,7 +43,9 @@ N_EL, N_TX, N_SMP = 128, 75, 2073
 N0, N1 = 512, 1024
 FS, F0, C0 = 20e6, 5e6, 1540.0
 MV_KW = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01, mv_range_average=2)
+LEARNED_KW = dict(MV_KW, combiner=3)
 WORKLOADS = {
+    "learned": LEARNED_KW,   # learned MV with plain-MV fallback (the headline), plain MV timed beside it
     "mv": MV_KW,             # tensor-core covariance (the fast plain MV)
     "mv_exact": MV_KW,       # FP32 in the reference's operation order
     "das": dict(f_number=1.5),
@@ -125,6 +127,36 @@ class ClockSampler:
         reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
+
+
+def das_active_ops(grid_pts: np.ndarray, txs, probe, f_number: float) -> float:
+    """Active (pixel, channel, transmit) triples of the delay-and-sum: receive
+    aperture |x_e - x_p| < z / (2 F#) times transmits whose illuminated band
+    (firing aperture shifted by z tan(angle), widened by the diffraction
+    width, Tukey 0.4) covers the pixel (reference beamformer.cpp:238-288)."""
+    x, z = grid_pts[:, 0].astype(np.float64), grid_pts[:, 2].astype(np.float64)
+    ex = (np.arange(N_EL) - 0.5 * (N_EL - 1)) * probe.pitch
+    half = 0.5 * z / f_number
+    lo = np.maximum(0, np.ceil(0.5 * (N_EL - 1) + (x - half) / probe.pitch))
+    hi = np.minimum(N_EL - 1, np.floor(0.5 * (N_EL - 1) + (x + half) / probe.pitch))
+    n_act = np.maximum(0, hi - lo + 1)
+    lam = C0 / F0
+    n_tx = np.zeros_like(x)
+    for t in txs:
+        ap = np.asarray(t.apodization)
+        on = np.nonzero(ap > 0)[0]
+        if on.size == 0:
+            continue
+        x_lo, x_hi = ex[on[0]], ex[on[-1]]
+        shift = z * np.tan(t.angle)
+        aperture = max(x_hi - x_lo, probe.pitch)
+        diff = np.clip(z / aperture, 0.5, 20.0) * lam
+        a, b = x_lo + shift - diff, x_hi + shift + diff
+        n_tx += np.abs(x - 0.5 * (a + b)) < 0.5 * (b - a)
+    return float(np.sum(n_act * n_tx))
 
 
 def mv_flops_per_frame(grid_pts: np.ndarray, cfg: dict) -> float:

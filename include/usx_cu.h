@@ -207,6 +207,17 @@ int usx_cu_mlp_forward(usx_mlp* mlp, const float* x, int64_t rows, float* y);
  * make the call synchronise. */
 int usx_cu_mlp_train_step(usx_mlp* mlp, const float* x, const float* target, const float* mask,
                           int64_t rows, float lr, float* loss_host, float* grad_host);
+/* Training loss of usx_cu_mlp_train_step:
+ *   USX_MLP_LOSS_MSE         the masked mean squared error above (default);
+ *   USX_MLP_LOSS_LMV_OUTPUT  for the learned minimum variance (256 -> 128):
+ *     per row, with w the 64 predicted complex weights, t the target weights,
+ *     a the normalised subarray-averaged snapshot (input features 128..255)
+ *     and the mask selecting i < L, the squared error of the combiner output
+ *     sum conj(w) a / conj(sum w) against the same with t, plus the squared
+ *     distortionless residual |sum w / L - 1|^2, plus beta * sum mask
+ *     |w - t|^2; the sum over rows divided by rows. */
+enum { USX_MLP_LOSS_MSE = 0, USX_MLP_LOSS_LMV_OUTPUT = 1 };
+int usx_cu_mlp_set_loss(usx_mlp* mlp, int kind, float beta);
 
 /* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one
  * launch: frame f uses the plan's events [first + f*events_per_frame,

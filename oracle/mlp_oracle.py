@@ -84,6 +84,56 @@ def backward(params, dims, x, t, mask=None, quantize=True):
     return lval, flat
 
 
+def lmv_output_loss(y, t, mask, x, beta):
+    """Learned-MV output loss and its gradient with respect to y (float64).
+
+    y, t, mask: [rows, 128] (64 complex weights interleaved); x: [rows, 256]
+    features whose entries 128..255 are the normalised averaged snapshot a.
+    Per row: o = sum conj(w) a / conj(sum w) over the masked weights, o_ref the
+    same with t, loss = |o - o_ref|^2 + |sum w / L - 1|^2 + beta * sum mask
+    |w - t|^2, averaged over rows (L = the number of masked weights)."""
+    y = np.asarray(y, np.float64)
+    t = np.asarray(t, np.float64)
+    m = np.asarray(mask, np.float64)[:, 0::2]
+    a = np.asarray(x, np.float64)[:, 128::2] + 1j * np.asarray(x, np.float64)[:, 129::2]
+    w = y[:, 0::2] + 1j * y[:, 1::2]
+    tw = t[:, 0::2] + 1j * t[:, 1::2]
+    rows = y.shape[0]
+    D = np.conj((m * w).sum(1))
+    small = np.abs(D) ** 2 < 1e-6
+    D = np.where(small, 1e-3, D)
+    o = (m * np.conj(w) * a).sum(1) / D
+    o_ref = (m * np.conj(tw) * a).sum(1) / np.conj((m * tw).sum(1))
+    e = o - o_ref
+    Lr = np.maximum(m.sum(1), 1.0)
+    sd = (m * w).sum(1) / Lr - 1.0
+    loss = float((np.abs(e) ** 2 + np.abs(sd) ** 2 + beta * (m * np.abs(w - tw) ** 2).sum(1)).sum() / rows)
+    g = ((2 * np.conj(e) / D)[:, None] * (a - o[:, None]) + (2 * sd / Lr)[:, None]) * m + 2 * beta * m * (w - tw)
+    g /= rows
+    out = np.empty_like(y)
+    out[:, 0::2] = g.real
+    out[:, 1::2] = g.imag
+    return loss, out
+
+
+def backward_from(params, dims, x, g_out, quantize=True):
+    """Gradient vector for a given output gradient g_out = dLoss/dy."""
+    q = bf16 if quantize else (lambda v: np.asarray(v, np.float64))
+    _, acts = forward(params, dims, x, quantize)
+    g = q(g_out).astype(np.float64)
+    ls = layers(np.asarray(params, np.float32 if quantize else np.float64), dims)
+    grads = []
+    for l in range(len(ls) - 1, -1, -1):
+        w, _ = ls[l]
+        a = acts[l]
+        grads.append((a.T @ g, g.sum(0)))
+        if l > 0:
+            da = g @ q(w).astype(np.float64).T
+            g = q(np.where(a > 0, da, 0.0)).astype(np.float64)
+    grads.reverse()
+    return np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
+
+
 def adam_step(params, grad, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
     """One Adam update (bias-corrected); returns (params, m, v)."""
     m = b1 * m + (1 - b1) * grad

@@ -114,7 +114,7 @@ def build_host(jobs: int) -> Path:
         list(ex.map(_run, cmds))
     libhost = LIB / "libusx.so"
     if cmds or _stale(libhost, objs):
-        _run(["g++", "-shared", "-o", str(libhost), *map(str, objs), "-L", str(LIB), "-lusx_cu",
+        _run(["g++", "-shared", "-o", str(libhost), *map(str, objs), "-L", str(LIB), "-lusx_cu", "-ldl",
               "-Wl,-rpath,$ORIGIN"])
     for old in PYPKG.glob("_usx*.so"):
         if old.name != "_usx" + ext:

@@ -22,6 +22,7 @@
 // range-averaged covariance, diagonal loading, Cholesky solve of R w = 1 and
 // the weighted subarray average, in the reference's operation order.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -635,6 +636,11 @@ struct usx_bf_plan {
   float* exp_feat = nullptr;
   float* exp_w = nullptr;
   uint8_t* exp_valid = nullptr;
+  // Tensor-core minimum variance: pixels in classes of similar subarray
+  // length (built on first use), device pixel lists per class.
+  std::vector<MvClass> mv_classes;
+  int* d_class_pixels = nullptr;
+  bool classes_built = false;
 };
 
 namespace {
@@ -646,6 +652,52 @@ int validate_bf_config(const usx_beamformer_config& c) {
     return fail(USX_ERR_INVALID, "BeamformerConfig.mv_diagonal_loading must be >= 0");
   if (c.mv_range_average < 0)
     return fail(USX_ERR_INVALID, "BeamformerConfig.mv_range_average must be >= 0");
+  return USX_OK;
+}
+
+// Pixels are sorted into classes of similar subarray length from the
+// aperture interval |x_e - x_p| <= z / (2 F#) (the support of every receive
+// window). The count may differ by one from the kernel's window test at the
+// interval's ends; a class keeps a margin of one L and two channels, and the
+// kernel sends anything beyond it to the general kernel.
+int build_mv_classes(usx_bf_plan* p, const float* points_host) {
+  const int n_ch = p->cd.probe.n_elements;
+  const long n_pix = static_cast<long>(p->n0) * p->n1;
+  const float half_nm1 = 0.5f * static_cast<float>(n_ch - 1), pitch = p->cd.probe.pitch;
+  const int plan_lmax = std::min(std::max(p->cfg.mv_subarray, 2), std::max(2, n_ch / 2));
+  constexpr int kClasses = 4;
+  std::vector<int> bucket[kClasses];
+  int nmax[kClasses] = {0, 0, 0, 0};
+  for (long i = 0; i < n_pix; ++i) {
+    const float px = points_host[3 * i], pz = points_host[3 * i + 2];
+    int n_act = 0;
+    if (pz > 0.0f) {
+      const double half = 0.5 * pz / std::max(p->cfg.f_number, 1e-3f);
+      const double lo = std::max(0.0, std::ceil(half_nm1 + (px - half) / pitch));
+      const double hi = std::min(static_cast<double>(n_ch - 1), std::floor(half_nm1 + (px + half) / pitch));
+      n_act = hi >= lo ? static_cast<int>(hi - lo) + 1 : 0;
+    }
+    int L = std::min(std::max(p->cfg.mv_subarray, 2), std::max(2, n_act / 2));
+    const int b = std::min(kClasses - 1, L / 16);
+    bucket[b].push_back(static_cast<int>(i));
+    nmax[b] = std::max(nmax[b], n_act);
+  }
+  USX_CUDA(cudaMalloc(&p->d_class_pixels, sizeof(int) * std::max<long>(1, n_pix)));
+  long off = 0;
+  p->mv_classes.clear();
+  for (int b = 0; b < kClasses; ++b) {
+    if (bucket[b].empty()) continue;
+    USX_CUDA(cudaMemcpy(p->d_class_pixels + off, bucket[b].data(), sizeof(int) * bucket[b].size(),
+                        cudaMemcpyHostToDevice));
+    MvClass c;
+    c.pixels = p->d_class_pixels + off;
+    c.count = static_cast<int>(bucket[b].size());
+    c.lmax = std::min(16 * (b + 1), plan_lmax);
+    c.nmax = std::min(n_ch, nmax[b] + 2);
+    p->mv_classes.push_back(c);
+    off += static_cast<long>(bucket[b].size());
+  }
+  p->classes_built = true;
   return USX_OK;
 }
 
@@ -823,12 +875,13 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
   const size_t fb_bytes = static_cast<size_t>(n_frames) * n_pix * sizeof(int2);
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   void* ws = nullptr;
-  if (int rc = scratch(ctx, up(y_bytes) + up(acc_bytes) + up(fb_bytes) + 256, &ws)) return rc;
+  if (int rc = scratch(ctx, up(y_bytes) + up(acc_bytes) + 2 * up(fb_bytes) + 256, &ws)) return rc;
   char* wsb = static_cast<char*>(ws);
   a.y_out = reinterpret_cast<float2*>(wsb);
   a.acc_out = reinterpret_cast<float*>(wsb + up(y_bytes));
   int2* fb_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes));
-  int* fb_count = reinterpret_cast<int*>(wsb + up(y_bytes) + up(acc_bytes) + up(fb_bytes));
+  int2* ov_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes) + up(fb_bytes));
+  int* fb_count = reinterpret_cast<int*>(wsb + up(y_bytes) + up(acc_bytes) + 2 * up(fb_bytes));  // [0] FP64, [1] overflow
   const bool tensor = plan->mv_mode == USX_MV_TENSOR &&
                       mv_tc_supported(a.n_ch, a.mv_subarray, a.mv_range_average);
   const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
@@ -866,6 +919,11 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
         ex.w_export = plan->exp_w;
         ex.w_valid = plan->exp_valid;
       }
+      ex.classes = plan->mv_classes.data();
+      ex.n_classes = static_cast<int>(plan->mv_classes.size());
+      ex.overflow_count = fb_count + 1;
+      ex.overflow = ov_list;
+      ex.overflow_cap = static_cast<int>(n_frames * n_pix);
       USX_CUDA(cudaMemsetAsync(fb_count, 0, sizeof(int), ctx->stream));
       if (int rc = launch_mv_tc(ctx, b.y_out, b.points, b.out, b.out_stride, b.acc_out, b.n_ch, b.n_pix, b.n1,
                                 n_frames, b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number,
@@ -947,6 +1005,12 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
   }
   cudaMemset(p->d_mv_stats, 0, sizeof(int) * 4);
   cudaMemcpy(p->d_points, points_host, sizeof(float) * 3 * n_pix, cudaMemcpyHostToDevice);
+  if (cfg->combiner == USX_COMB_MV && mv_tc_supported(cd->probe.n_elements, cfg->mv_subarray, cfg->mv_range_average)) {
+    if (int rc = build_mv_classes(p, points_host)) {
+      usx_cu_bf_plan_destroy(p);
+      return rc;
+    }
+  }
   cudaMemcpy(p->d_tx, txs.data(), sizeof(TxDev) * n_ev, cudaMemcpyHostToDevice);
   *out = p;
   return USX_OK;
@@ -960,6 +1024,7 @@ int usx_cu_bf_plan_destroy(usx_bf_plan* plan) {
   cudaFree(plan->d_points);
   cudaFree(plan->d_tx);
   cudaFree(plan->d_mv_stats);
+  cudaFree(plan->d_class_pixels);
   delete plan;
   return USX_OK;
 }

@@ -255,6 +255,89 @@ __global__ void mse_grad_kernel(const float* y, const float* t, const float* mas
   if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, l * inv_count);
 }
 
+// Learned-MV output loss, one warp per row. The network's 128 outputs are 64
+// complex weights w (interleaved); the row's input features hold the
+// normalised subarray-averaged snapshot a at 128 + 2i; the mask selects
+// i < L. With num = sum conj(w) a and D = conj(sum w) the combiner outputs
+// o = num / D; the loss is |o - o_ref|^2 (o_ref from the target weights) plus
+// |sum w / L - 1|^2 (the distortionless residual the plan gates on; it also
+// keeps D away from zero) plus beta * |w - t|^2 over the masked outputs, all
+// divided by `rows`. Gradients with respect to (Re w_i, Im w_i) are the real
+// and imaginary parts of 2 conj(e) (a_i - o) / D + 2 (sum w / L - 1) / L +
+// 2 beta (w_i - t_i).
+__global__ void lmv_output_loss_kernel(const float* y, const float* t, const float* mask, const float* x,
+                                       long rows, float beta, float inv_rows, __nv_bfloat16* dy16, float* loss) {
+  const int lane = threadIdx.x & 31;
+  const long r = (blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x) >> 5;
+  if (r >= rows) return;
+  const float4 w4 = reinterpret_cast<const float4*>(y + r * 128)[lane];
+  const float4 t4 = reinterpret_cast<const float4*>(t + r * 128)[lane];
+  const float4 m4 = mask ? reinterpret_cast<const float4*>(mask + r * 128)[lane] : make_float4(1.f, 1.f, 1.f, 1.f);
+  const float4 a4 = reinterpret_cast<const float4*>(x + r * 256 + 128)[lane];
+  // Two complex weights per lane: (w4.x, w4.y), (w4.z, w4.w).
+  float nre = 0.f, nim = 0.f, dre = 0.f, dim = 0.f, rre = 0.f, rim = 0.f, tre = 0.f, tim = 0.f, wse = 0.f;
+  float cnt = 0.f;
+  auto acc = [&](float wr, float wi, float tr, float ti, float m, float ar, float ai) {
+    if (m <= 0.f) return;
+    cnt += 1.f;
+    nre += wr * ar + wi * ai;   // conj(w) a
+    nim += wr * ai - wi * ar;
+    dre += wr;
+    dim += wi;
+    rre += tr * ar + ti * ai;
+    rim += tr * ai - ti * ar;
+    tre += tr;
+    tim += ti;
+    wse += (wr - tr) * (wr - tr) + (wi - ti) * (wi - ti);
+  };
+  acc(w4.x, w4.y, t4.x, t4.y, m4.x, a4.x, a4.y);
+  acc(w4.z, w4.w, t4.z, t4.w, m4.z, a4.z, a4.w);
+  for (int o = 16; o > 0; o >>= 1) {
+    nre += __shfl_xor_sync(0xffffffffu, nre, o);
+    nim += __shfl_xor_sync(0xffffffffu, nim, o);
+    dre += __shfl_xor_sync(0xffffffffu, dre, o);
+    dim += __shfl_xor_sync(0xffffffffu, dim, o);
+    rre += __shfl_xor_sync(0xffffffffu, rre, o);
+    rim += __shfl_xor_sync(0xffffffffu, rim, o);
+    tre += __shfl_xor_sync(0xffffffffu, tre, o);
+    tim += __shfl_xor_sync(0xffffffffu, tim, o);
+    wse += __shfl_xor_sync(0xffffffffu, wse, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  const float inv_l = cnt > 0.f ? 1.0f / cnt : 0.f;
+  const float sre = dre * inv_l - 1.0f, sim = dim * inv_l;   // sum w / L - 1
+  // D = conj(sum w), guarded away from zero.
+  float Dr = dre, Di = -dim;
+  float dn = Dr * Dr + Di * Di;
+  if (dn < 1e-6f) {
+    Dr = 1e-3f;
+    Di = 0.f;
+    dn = 1e-6f;
+  }
+  // o = num / D; o_ref = (sum conj(t) a) / conj(sum t).
+  const float ore = (nre * Dr + nim * Di) / dn, oim = (nim * Dr - nre * Di) / dn;
+  const float Tr = tre, Ti = -tim, tn = fmaxf(Tr * Tr + Ti * Ti, 1e-12f);
+  const float fre = (rre * Tr + rim * Ti) / tn, fim = (rim * Tr - rre * Ti) / tn;
+  const float ere = ore - fre, eim = oim - fim;
+  // c = 2 conj(e) / D
+  const float cre0 = 2.f * ere, cim0 = -2.f * eim;
+  const float cre = (cre0 * Dr + cim0 * Di) / dn, cim = (cim0 * Dr - cre0 * Di) / dn;
+  auto grad = [&](float wr, float wi, float tr, float ti, float m, float ar, float ai, float& gr, float& gi) {
+    gr = gi = 0.f;
+    if (m <= 0.f) return;
+    const float ur = ar - ore, ui = ai - oim;        // a_i - o
+    gr = (cre * ur - cim * ui + 2.f * sre * inv_l + 2.f * beta * (wr - tr)) * inv_rows;
+    gi = (cre * ui + cim * ur + 2.f * sim * inv_l + 2.f * beta * (wi - ti)) * inv_rows;
+  };
+  float g0, g1, g2, g3;
+  grad(w4.x, w4.y, t4.x, t4.y, m4.x, a4.x, a4.y, g0, g1);
+  grad(w4.z, w4.w, t4.z, t4.w, m4.z, a4.z, a4.w, g2, g3);
+  __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dy16 + r * 128) + 2 * lane;
+  d2[0] = __floats2bfloat162_rn(g0, g1);
+  d2[1] = __floats2bfloat162_rn(g2, g3);
+  if (lane == 0 && loss) atomicAdd(loss, (ere * ere + eim * eim + sre * sre + sim * sim + beta * wse) * inv_rows);
+}
+
 // db[n] += sum_m dY[m][n] (FP32 gradient rows as BF16 tiles were used in GEMMs).
 __global__ void bias_grad_kernel(const __nv_bfloat16* dy, long rows, int n, int ld, float* db) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -337,6 +420,8 @@ struct usx_mlp {
   __nv_bfloat16* g16a = nullptr;    // gradient buffers
   __nv_bfloat16* g16b = nullptr;
   float* loss = nullptr;
+  int loss_kind = USX_MLP_LOSS_MSE;
+  float loss_beta = 0.0f;
 };
 
 namespace {
@@ -501,6 +586,18 @@ int usx_cu_mlp_set_params(usx_mlp* n, const float* host) {
   return USX_OK;
 }
 
+int usx_cu_mlp_set_loss(usx_mlp* n, int kind, float beta) {
+  if (!n) return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: null network");
+  if (kind != USX_MLP_LOSS_MSE && kind != USX_MLP_LOSS_LMV_OUTPUT)
+    return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: unknown loss");
+  if (kind == USX_MLP_LOSS_LMV_OUTPUT && !(n->dims.front() == 256 && n->dims.back() == 128))
+    return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: the output loss needs a 256 -> 128 network");
+  if (!(beta >= 0.0f)) return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: beta must be >= 0");
+  n->loss_kind = kind;
+  n->loss_beta = beta;
+  return USX_OK;
+}
+
 // y[rows x dims.back()] (FP32) = net(x[rows x dims[0]] FP32), device pointers.
 int usx_cu_mlp_forward(usx_mlp* n, const float* x, int64_t rows, float* y) {
   if (!n || !x || !y) return fail(USX_ERR_INVALID, "usx_cu_mlp_forward: null argument");
@@ -535,11 +632,17 @@ int usx_cu_mlp_train_step(usx_mlp* n, const float* x, const float* target, const
   USX_CUDA(cudaMemsetAsync(n->grad, 0, sizeof(float) * n->n_params, st));
   USX_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), st));
   const int n_out = n->dims.back();
-  // Count of valid outputs (mask sum) is taken as rows * n_out when no mask.
-  const float inv_count = 1.0f / static_cast<float>(rows * n_out);
-  mse_grad_kernel<<<ceil_div(static_cast<long>(rows) * n_out, 256), 256, 0, st>>>(
-      n->out32, target, mask, rows, n_out, n_out, inv_count, nullptr, n->g16a, n->loss);
-  USX_CHECK_LAUNCH("mse_grad_kernel");
+  if (n->loss_kind == USX_MLP_LOSS_LMV_OUTPUT) {
+    lmv_output_loss_kernel<<<ceil_div(static_cast<long>(rows) * 32, 256), 256, 0, st>>>(
+        n->out32, target, mask, x, rows, n->loss_beta, 1.0f / static_cast<float>(rows), n->g16a, n->loss);
+    USX_CHECK_LAUNCH("lmv_output_loss_kernel");
+  } else {
+    // Count of valid outputs (mask sum) is taken as rows * n_out when no mask.
+    const float inv_count = 1.0f / static_cast<float>(rows * n_out);
+    mse_grad_kernel<<<ceil_div(static_cast<long>(rows) * n_out, 256), 256, 0, st>>>(
+        n->out32, target, mask, rows, n_out, n_out, inv_count, nullptr, n->g16a, n->loss);
+    USX_CHECK_LAUNCH("mse_grad_kernel");
+  }
   __nv_bfloat16* dcur = n->g16a;   // gradient w.r.t. layer l output
   __nv_bfloat16* dnext = n->g16b;
   for (int l = L - 1; l >= 0; --l) {

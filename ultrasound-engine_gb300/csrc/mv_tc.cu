@@ -568,6 +568,487 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-per-pixel minimum variance: every warp of the CTA solves its own
+// pixels end to end (no CTA barriers), with shared memory sized for a class of
+// pixels (largest L and active aperture of the class), so that short
+// subarrays, the common case, pack many warps per SM.
+//
+// Per pixel: the active channels of the range rows in the smoothing window
+// are staged once in FP32 (yf) and as BF16 pairs (yb, scaled by a power of
+// two); G = A A^T on the tensor cores gives R~; the exact trace comes from
+// the FP32 rows with each channel's subarray multiplicity; the Cholesky runs
+// right-looking with the pivot column held in registers (one row of the
+// trailing update per step, lanes over columns); the solves, the refinement
+// step and the refined-residual gate are those of mv_tc_kernel.
+
+constexpr int kWarpMvWarps = 4;
+
+struct MvWarpLayout {
+  int words;
+  size_t off_act, off_yf, off_yb, off_r, off_w, bytes;  // per warp
+};
+
+__host__ __device__ inline MvWarpLayout mv_warp_layout(int nmax, int n_dmax, int lmax) {
+  MvWarpLayout l;
+  l.words = nmax / 2 + 10;
+  size_t o = 0;
+  l.off_act = o; o = align16(o + sizeof(int) * nmax);
+  l.off_yf = o;  o = align16(o + sizeof(float2) * n_dmax * nmax);
+  l.off_yb = o;  o = align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);  // also t_k after the covariance
+  l.off_r = o;   o = align16(o + sizeof(float2) * (lmax * (lmax + 1) / 2));
+  l.off_w = o;   o = align16(o + sizeof(float2) * 2 * lmax);
+  l.bytes = o;
+  return l;
+}
+
+struct MvWarpArgs {
+  MvTcArgs base;          // geometry, outputs, FP64 list, export
+  int lmax, nmax;         // class limits (shared-memory sizing)
+  const int* pix_list;    // class mode: pixels of the class, every frame
+  int n_list, n_frames;
+  const int2* pair_list;  // pair mode: (pixel, frame) with a device count
+  const int* pair_count;
+  int pair_cap;
+  int* overflow_count;    // pixels beyond the class limits (solved by mv_tc_kernel)
+  int2* overflow;
+  int overflow_cap;
+};
+
+__global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarpArgs wa) {
+  extern __shared__ float4 mvw_smem_raw[];
+  const MvTcArgs& a = wa.base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const MvWarpLayout lay = mv_warp_layout(wa.nmax, a.n_dmax, wa.lmax);
+  char* base = reinterpret_cast<char*>(mvw_smem_raw) + warp * lay.bytes;
+  int* act = reinterpret_cast<int*>(base + lay.off_act);
+  float2* yf = reinterpret_cast<float2*>(base + lay.off_yf);
+  uint32_t* yb = reinterpret_cast<uint32_t*>(base + lay.off_yb);
+  float2* tk = reinterpret_cast<float2*>(base + lay.off_yb);
+  float2* Rl = reinterpret_cast<float2*>(base + lay.off_r);
+  float2* wv = reinterpret_cast<float2*>(base + lay.off_w);
+  const int nmax = wa.nmax;
+
+  const long n_items = wa.pair_list ? static_cast<long>(min(*wa.pair_count, wa.pair_cap))
+                                    : static_cast<long>(wa.n_list) * wa.n_frames;
+  for (long item = static_cast<long>(blockIdx.x) * kWarpMvWarps + warp; item < n_items;
+       item += static_cast<long>(gridDim.x) * kWarpMvWarps) {
+    int pix;
+    long frame;
+    if (wa.pair_list) {
+      const int2 pf = wa.pair_list[item];
+      pix = pf.x;
+      frame = pf.y;
+    } else {
+      frame = item / wa.n_list;
+      pix = wa.pix_list[item - frame * wa.n_list];
+    }
+    const long row = frame * a.n_pix + pix;
+    const int j = pix % a.n1;
+    const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+    __syncwarp();
+    int n_act = 0;
+    for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+      const int ch = c0 + lane;
+      bool on = false;
+      if (ch < a.n_ch)
+        on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                             a.tukey_alpha) > 0.0f;
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (on && n_act + __popc(m & ((1u << lane) - 1u)) < nmax) act[n_act + __popc(m & ((1u << lane) - 1u))] = ch;
+      n_act += __popc(m);
+    }
+    __syncwarp();
+    auto finish = [&](cplx out, float cre, float cim, float inc) {  // lane 0
+      if (a.cf && n_act > 0) {
+        const float coh = cre * cre + cim * cim;
+        out = cscale(out, (inc > 0.0f) ? coh / (static_cast<float>(n_act) * inc) : 0.0f);
+      }
+      if (a.incoherent)
+        a.acc_out[frame * a.n_pix + pix] += cnorm(out);
+      else
+        a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+    };
+    int L = a.mv_subarray;
+    const int hi = max(2, n_act / 2);
+    if (L < 2) L = 2;
+    if (L > hi) L = hi;
+    if (n_act > nmax || L > wa.lmax) {
+      if (lane == 0 && wa.overflow_count) {
+        const int slot = atomicAdd(wa.overflow_count, 1);
+        if (slot < wa.overflow_cap) wa.overflow[slot] = make_int2(pix, static_cast<int>(frame));
+      }
+      continue;
+    }
+    const float2* yc = Y + static_cast<long>(pix) * a.n_ch;
+    if (n_act < 4) {
+      export_invalid(a, row, lane);
+      if (lane == 0) {
+        // The reference's rule: the DAS sum, channels in ascending order.
+        cplx acc = mk(0.f, 0.f);
+        float inc = 0.0f;
+        for (int q = 0; q < n_act; ++q) {
+          const float2 v = yc[act[q]];
+          acc = cadd(acc, mk(v.x, v.y));
+          inc += cnorm(mk(v.x, v.y));
+        }
+        if (n_act == 0) {
+          if (!a.incoherent) a.out[frame * a.out_stride + pix] = make_float2(0.f, 0.f);
+        } else {
+          finish(acc, acc.re, acc.im, inc);
+        }
+      }
+      continue;
+    }
+    const int n_sub = n_act - L + 1;
+    int dlo = -a.range_avg, dhi = a.range_avg;
+    while (j + dlo < 0) ++dlo;
+    while (j + dhi >= a.n1) --dhi;
+    const int n_d = dhi - dlo + 1, dc = -dlo;
+    const int K = n_d * n_sub;
+
+    // FP32 rows of the active channels, largest magnitude.
+    float amax = 0.0f;
+    for (int k = lane; k < n_d * n_act; k += 32) {
+      const int d = k / n_act, q = k - d * n_act;
+      const float2 v = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[q]];
+      yf[d * nmax + q] = v;
+      amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    __syncwarp();
+    // Coherence-factor terms and the DAS sum of the centre row (ascending in
+    // lanes, then a fixed tree).
+    float cre = 0.f, cim = 0.f, inc = 0.f;
+    if (a.cf) {
+      for (int q = lane; q < n_act; q += 32) {
+        const float2 v = yf[dc * nmax + q];
+        cre += v.x;
+        cim += v.y;
+        inc += v.x * v.x + v.y * v.y;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        cre += __shfl_xor_sync(0xffffffffu, cre, o);
+        cim += __shfl_xor_sync(0xffffffffu, cim, o);
+        inc += __shfl_xor_sync(0xffffffffu, inc, o);
+      }
+    }
+    if (!(amax > 0.0f)) {
+      export_invalid(a, row, lane);
+      if (lane == 0) finish(mk(0.f, 0.f), cre, cim, inc);
+      continue;
+    }
+    int e2;
+    frexpf(amax, &e2);
+    const float sc = ldexpf(1.0f, -e2), sc2 = ldexpf(1.0f, -2 * e2);
+    // BF16 pairs: word (p, par, d, w) = (v[2w+par], v[2w+par+1]) of part p, scaled.
+    const int words = lay.words;
+    for (int k = lane; k < 4 * n_d * words; k += 32) {
+      const int w = k % words;
+      const int rest = k / words;
+      const int d = rest % n_d, pp = rest / n_d;
+      const int p = pp >> 1, par = pp & 1;
+      const int q0 = 2 * w + par, q1 = q0 + 1;
+      const float2 v0 = q0 < n_act ? yf[d * nmax + q0] : make_float2(0.f, 0.f);
+      const float2 v1 = q1 < n_act ? yf[d * nmax + q1] : make_float2(0.f, 0.f);
+      yb[(pp * a.n_dmax + d) * words + w] = pack_bf16((p ? v0.y : v0.x) * sc, (p ? v1.y : v1.x) * sc);
+    }
+    __syncwarp();
+
+    // ---- R~ = A A^T / K on the tensor cores (upper block-triangle) --------
+    const int g = lane >> 2, t4 = lane & 3;
+    const int two_l = 2 * L;
+    const int MT = (two_l + 15) / 16, NT = (two_l + 7) / 8;
+    const int n_kstep = (n_sub + 15) / 16;
+    const float inv_k = 1.0f / static_cast<float>(K);
+    for (int mt = 0; mt < MT; ++mt) {
+      for (int nt0 = 2 * mt; nt0 < NT; nt0 += 8) {
+        float acc[8][4];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) acc[x][0] = acc[x][1] = acc[x][2] = acc[x][3] = 0.f;
+        const int r0 = mt * 16 + g, r1 = r0 + 8;
+        for (int d = 0; d < n_d; ++d) {
+          for (int ks = 0; ks < n_kstep; ++ks) {
+            const int s_lo = ks * 16 + 2 * t4, s_hi = s_lo + 8;
+            uint32_t af[4];
+            af[0] = r0 < two_l ? mask_pair(pair_at(yb, words, a.n_dmax, r0 & 1, d, s_lo + (r0 >> 1)), s_lo, n_sub) : 0u;
+            af[1] = r1 < two_l ? mask_pair(pair_at(yb, words, a.n_dmax, r1 & 1, d, s_lo + (r1 >> 1)), s_lo, n_sub) : 0u;
+            af[2] = r0 < two_l ? mask_pair(pair_at(yb, words, a.n_dmax, r0 & 1, d, s_hi + (r0 >> 1)), s_hi, n_sub) : 0u;
+            af[3] = r1 < two_l ? mask_pair(pair_at(yb, words, a.n_dmax, r1 & 1, d, s_hi + (r1 >> 1)), s_hi, n_sub) : 0u;
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+              const int nt = nt0 + x;
+              if (nt < NT) {
+                const int c = nt * 8 + g;
+                uint32_t b0 = 0u, b1 = 0u;
+                if (c < two_l) {
+                  b0 = mask_pair(pair_at(yb, words, a.n_dmax, c & 1, d, s_lo + (c >> 1)), s_lo, n_sub);
+                  b1 = mask_pair(pair_at(yb, words, a.n_dmax, c & 1, d, s_hi + (c >> 1)), s_hi, n_sub);
+                }
+                mma16816(acc[x], af, b0, b1);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+          const int nt = nt0 + x;
+          if (nt >= NT) continue;
+          const float o0 = __shfl_xor_sync(0xffffffffu, acc[x][0], 4);
+          const float o1 = __shfl_xor_sync(0xffffffffu, acc[x][1], 4);
+          const float o2 = __shfl_xor_sync(0xffffffffu, acc[x][2], 4);
+          const float o3 = __shfl_xor_sync(0xffffffffu, acc[x][3], 4);
+          if ((g & 1) == 0) {
+            const int bcol = (nt * 8 + 2 * t4) >> 1;
+            const int ar0 = r0 >> 1, ar1 = r1 >> 1;
+            if (bcol < L && ar0 < L && bcol >= ar0)
+              Rl[tri(bcol, ar0)] = make_float2((acc[x][0] + o1) * inv_k, -(o0 - acc[x][1]) * inv_k);
+            if (bcol < L && ar1 < L && bcol >= ar1)
+              Rl[tri(bcol, ar1)] = make_float2((acc[x][2] + o3) * inv_k, -(o2 - acc[x][3]) * inv_k);
+          }
+        }
+      }
+    }
+    __syncwarp();
+
+    // ---- exact trace: channel t of a row appears in c(t) subarrays -------
+    float tr = 0.0f;
+    for (int k = lane; k < n_d * n_act; k += 32) {
+      const int d = k / n_act, t = k - d * n_act;
+      const int c = min(t, n_sub - 1) - max(0, t - L + 1) + 1;
+      const float2 v = yf[d * nmax + t];
+      tr = fmaf(static_cast<float>(c), fmaf(v.x, v.x, v.y * v.y), tr);
+    }
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    tr *= sc2 * inv_k;
+    const float eps = fmaxf(a.loading * tr / static_cast<float>(L), 1e-20f);
+    for (int i = lane; i < L; i += 32) Rl[tri(i, i)].x += eps;
+    __syncwarp();
+
+    // ---- Cholesky, right-looking; pivot column in registers ---------------
+    bool ok = true;
+    for (int c = 0; c < L; ++c) {
+      const float dgl = Rl[tri(c, c)].x;
+      if (!(dgl > 0.0f)) {
+        ok = false;
+        break;
+      }
+      const float ljj = sqrtf(dgl), inv = 1.0f / ljj;
+      float2 lc[2];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = c + 1 + lane + 32 * s2;
+        lc[s2] = make_float2(0.f, 0.f);
+        if (i < L) {
+          const float2 v = Rl[tri(i, c)];
+          lc[s2] = make_float2(v.x * inv, v.y * inv);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = c + 1 + lane + 32 * s2;
+        if (i < L) Rl[tri(i, c)] = lc[s2];
+      }
+      // Row i of the trailing matrix: R[i][k] -= l_ic conj(l_kc), k = c+1..i.
+      for (int i = c + 1; i < L; ++i) {
+        const int ii = i - c - 1, src = ii & 31;
+        const float lix = __shfl_sync(0xffffffffu, ii >> 5 ? lc[1].x : lc[0].x, src);
+        const float liy = __shfl_sync(0xffffffffu, ii >> 5 ? lc[1].y : lc[0].y, src);
+        float2* rowp = Rl + i * (i + 1) / 2;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int k = c + 1 + lane + 32 * s2;
+          if (k <= i) {
+            const float2 lk = lc[s2];
+            float2 v = rowp[k];
+            v.x -= fmaf(lix, lk.x, liy * lk.y);
+            v.y -= fmaf(liy, lk.x, -lix * lk.y);
+            rowp[k] = v;
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (!ok) {
+      export_invalid(a, row, lane);
+      if (lane == 0) {
+        if (a.stats) atomicAdd(a.stats + 1, 1);
+        cplx acc = mk(0.f, 0.f);
+        for (int q = 0; q < n_act; ++q) acc = cadd(acc, mk(yc[act[q]].x, yc[act[q]].y));
+        finish(acc, cre, cim, inc);
+      }
+      continue;
+    }
+
+    auto solve = [&](float2 (&v)[2]) {
+      for (int c = 0; c < L; ++c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const float ljj = Rl[tri(c, c)].x;
+          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+        }
+        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i > c && i < L) {
+            const float2 l = Rl[tri(i, c)];
+            v[s2].x -= fmaf(l.x, vx, -l.y * vy);
+            v[s2].y -= fmaf(l.x, vy, l.y * vx);
+          }
+        }
+      }
+      for (int c = L - 1; c >= 0; --c) {
+        const int own = c & 31, sl = c >> 5;
+        if (lane == own) {
+          const float ljj = Rl[tri(c, c)].x;
+          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+        }
+        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        const int rowc = c * (c + 1) / 2;
+#pragma unroll
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const int i = lane + 32 * s2;
+          if (i < c) {
+            const float2 l = Rl[rowc + i];
+            v[s2].x -= fmaf(l.x, vx, l.y * vy);
+            v[s2].y -= fmaf(l.x, vy, -l.y * vx);
+          }
+        }
+      }
+    };
+    // r = 1 - (R + eps I) w (scaled domain) for w in wv[0, L); into wv[L, 2L).
+    auto residual = [&]() {
+      for (int k = lane; k < K; k += 32) {  // t_k = x_k^H w
+        const int d = k / n_sub, s = k - d * n_sub;
+        const float2* x = yf + d * nmax + s;
+        float tre = 0.f, tim = 0.f;
+        for (int i = 0; i < L; ++i) {
+          const float2 xi = x[i], wi = wv[i];
+          tre = fmaf(xi.x, wi.x, fmaf(xi.y, wi.y, tre));
+          tim = fmaf(xi.x, wi.y, fmaf(-xi.y, wi.x, tim));
+        }
+        tk[k] = make_float2(tre, tim);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        if (i < L) {
+          float are = 0.f, aim = 0.f;
+          for (int d = 0; d < n_d; ++d) {
+            const float2* xr = yf + d * nmax + i;
+            const float2* tr_ = tk + d * n_sub;
+            for (int s = 0; s < n_sub; ++s) {
+              const float2 x = xr[s], t = tr_[s];
+              are = fmaf(x.x, t.x, fmaf(-x.y, t.y, are));
+              aim = fmaf(x.x, t.y, fmaf(x.y, t.x, aim));
+            }
+          }
+          const float2 wi = wv[i];
+          const float f = sc2 * inv_k;
+          wv[L + i] = make_float2(1.0f - fmaf(are, f, eps * wi.x), -fmaf(aim, f, eps * wi.y));
+        }
+      }
+      __syncwarp();
+    };
+
+    float2 w[2];
+    w[0] = lane < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+    w[1] = lane + 32 < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+    solve(w);
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2)
+      if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
+    __syncwarp();
+    residual();
+    {
+      float2 r[2];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int i = lane + 32 * s2;
+        r[s2] = i < L ? wv[L + i] : make_float2(0.f, 0.f);
+      }
+      solve(r);
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        w[s2].x += r[s2].x;
+        w[s2].y += r[s2].y;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2)
+        if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
+      __syncwarp();
+    }
+    residual();
+    float rn = 0.f;
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      if (i < L) {
+        const float2 r = wv[L + i];
+        rn = fmaf(r.x, r.x, fmaf(r.y, r.y, rn));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) rn += __shfl_xor_sync(0xffffffffu, rn, o);
+    if (!(sqrtf(rn / static_cast<float>(L)) <= kRefineGate)) {
+      if (lane == 0) {
+        const int slot = atomicAdd(a.fallback_count, 1);
+        if (slot < a.fallback_cap) a.fallback[slot] = make_int2(pix, static_cast<int>(frame));
+        if (a.stats) atomicAdd(a.stats, 1);
+      }
+      continue;
+    }
+    // out = n_act * sum conj(w_i) avg_i / sum w, avg from the centre row.
+    float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
+    const float inv_nsub = 1.0f / static_cast<float>(n_sub);
+#pragma unroll
+    for (int s2 = 0; s2 < 2; ++s2) {
+      const int i = lane + 32 * s2;
+      if (i < L) {
+        dre += w[s2].x;
+        dim += w[s2].y;
+        float are = 0.f, aim = 0.f;
+        const float2* yr = yf + dc * nmax + i;
+        for (int s = 0; s < n_sub; ++s) {
+          are += yr[s].x;
+          aim += yr[s].y;
+        }
+        are *= inv_nsub;
+        aim *= inv_nsub;
+        ore += w[s2].x * are + w[s2].y * aim;
+        oim += w[s2].x * aim - w[s2].y * are;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dre += __shfl_xor_sync(0xffffffffu, dre, o);
+      dim += __shfl_xor_sync(0xffffffffu, dim, o);
+      ore += __shfl_xor_sync(0xffffffffu, ore, o);
+      oim += __shfl_xor_sync(0xffffffffu, oim, o);
+    }
+    if (hypotf(dre, dim) < 1e-30f)
+      export_invalid(a, row, lane);
+    else
+      export_weights(a, row, lane, L, w, dre, dim);
+    if (lane == 0) {
+      cplx out;
+      if (hypotf(dre, dim) < 1e-30f) {
+        out = mk(0.f, 0.f);
+        for (int q = 0; q < n_act; ++q) out = cadd(out, mk(yc[act[q]].x, yc[act[q]].y));
+      } else {
+        out = cscale(cdiv_wide(mk(ore, oim), mk(dre, dim)), static_cast<float>(n_act));
+      }
+      finish(out, cre, cim, inc);
+    }
+  }
+}
+
 // FP64 re-solve of the pixels whose refined FP32 residual failed: covariance
 // from the snapshots, Cholesky and solves in double, one warp per pixel.
 
@@ -818,21 +1299,81 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
   a.list_cap = extra.list_cap;
   a.w_export = extra.w_export;
   a.w_valid = extra.w_valid;
-  const MvTcLayout l = mv_tc_layout(n_ch, a.n_dmax, a.lmax);
-  const size_t smem = l.bytes;
-  USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-  int per_sm = 0;
-  USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_tc_kernel, 32 * kTcWarps, smem));
-  // Full frames: a grid-stride loop over pixels, frames on y. Work list: its
-  // length is only known on the device, so one resident wave loops over it.
-  const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
-  const long want = resident * 4 / std::max(1, n_frames);
-  const dim3 grid = extra.list ? dim3(static_cast<unsigned>(resident), 1)
-                               : dim3(static_cast<unsigned>(std::max(1L, std::min<long>(n_pix, want))), n_frames);
-  prof_begin(ctx, "mv_tc_kernel");
-  mv_tc_kernel<<<grid, 32 * kTcWarps, smem, ctx->stream>>>(a);
-  prof_end(ctx);
-  USX_CHECK_LAUNCH("mv_tc_kernel");
+  auto launch_cta = [&](const MvTcArgs& b, bool list_mode) -> int {
+    const MvTcLayout l = mv_tc_layout(n_ch, b.n_dmax, b.lmax);
+    const size_t smem = l.bytes;
+    USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_tc_kernel, 32 * kTcWarps, smem));
+    // Full frames: a grid-stride loop over pixels, frames on y. Work list: its
+    // length is only known on the device, so one resident wave loops over it.
+    const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
+    const long want = resident * 4 / std::max(1, n_frames);
+    const dim3 grid = list_mode ? dim3(static_cast<unsigned>(resident), 1)
+                                : dim3(static_cast<unsigned>(std::max(1L, std::min<long>(n_pix, want))), n_frames);
+    prof_begin(ctx, "mv_tc_kernel");
+    mv_tc_kernel<<<grid, 32 * kTcWarps, smem, ctx->stream>>>(b);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("mv_tc_kernel");
+    return USX_OK;
+  };
+  auto launch_warp = [&](MvWarpArgs& w, long items, const char* name) -> int {
+    const MvWarpLayout l = mv_warp_layout(w.nmax, a.n_dmax, w.lmax);
+    const size_t smem = l.bytes * kWarpMvWarps;
+    if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "minimum variance: class too large for shared memory");
+    USX_CUDA(cudaFuncSetAttribute(mv_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int per_sm = 0;
+    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_warp_kernel, 32 * kWarpMvWarps, smem));
+    const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
+    const long need = (items + kWarpMvWarps - 1) / kWarpMvWarps;
+    const long blocks = items < 0 ? resident : std::max(1L, std::min(need, resident * 8));
+    prof_begin(ctx, name);
+    mv_warp_kernel<<<static_cast<unsigned>(blocks), 32 * kWarpMvWarps, smem, ctx->stream>>>(w);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH(name);
+    return USX_OK;
+  };
+  if (extra.list) {
+    // Work list of (pixel, frame): one warp per pixel, sized for the plan's
+    // largest subarray and the whole array.
+    MvWarpArgs w{};
+    w.base = a;
+    w.lmax = a.lmax;
+    w.nmax = n_ch;
+    w.pair_list = extra.list;
+    w.pair_count = extra.list_count;
+    w.pair_cap = extra.list_cap;
+    w.overflow_count = extra.overflow_count;
+    w.overflow = extra.overflow;
+    w.overflow_cap = 0;
+    if (int rc = launch_warp(w, -1, "mv_warp_kernel(list)")) return rc;
+  } else if (extra.n_classes > 0 && extra.overflow_count) {
+    // Pixel classes of similar subarray length, one launch each; pixels past
+    // a class's limits go to the CTA kernel through the overflow list.
+    USX_CUDA(cudaMemsetAsync(extra.overflow_count, 0, sizeof(int), ctx->stream));
+    for (int c = 0; c < extra.n_classes; ++c) {
+      const MvClass& k = extra.classes[c];
+      if (k.count <= 0) continue;
+      MvWarpArgs w{};
+      w.base = a;
+      w.lmax = k.lmax;
+      w.nmax = k.nmax;
+      w.pix_list = k.pixels;
+      w.n_list = k.count;
+      w.n_frames = n_frames;
+      w.overflow_count = extra.overflow_count;
+      w.overflow = extra.overflow;
+      w.overflow_cap = extra.overflow_cap;
+      if (int rc = launch_warp(w, static_cast<long>(k.count) * n_frames, "mv_warp_kernel")) return rc;
+    }
+    MvTcArgs b = a;
+    b.list = extra.overflow;
+    b.list_count = extra.overflow_count;
+    b.list_cap = extra.overflow_cap;
+    if (int rc = launch_cta(b, true)) return rc;
+  } else {
+    if (int rc = launch_cta(a, false)) return rc;
+  }
   // FP64 re-solve of the pixels whose refined residual failed (usually none).
   const size_t smem64 = sizeof(double2) * (a.lmax * (a.lmax + 1) / 2) + sizeof(int) * n_ch;
   USX_CUDA(cudaFuncSetAttribute(mv_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem64)));

@@ -219,12 +219,24 @@ inline int ceil_div(long a, long b) { return static_cast<int>((a + b - 1) / b); 
 // list of (pixel, frame) pairs in place of every pixel of every frame, and a
 // training export of the normalised Capon weights L w / sum(w)
 // ([frame * n_pix + pix][2 * 64] floats, zero past L) with a per-pixel valid flag.
+// Pixels of similar subarray length: the warp-per-pixel kernel sizes its
+// shared memory for the class's largest L and active aperture.
+struct MvClass {
+  const int* pixels = nullptr;   // device list of pixel indices
+  int count = 0;
+  int lmax = 0, nmax = 0;
+};
 struct MvTcExtra {
   const int2* list = nullptr;
   const int* list_count = nullptr;
   int list_cap = 0;
   float* w_export = nullptr;
   uint8_t* w_valid = nullptr;
+  const MvClass* classes = nullptr;  // full frames by class (else the CTA-per-pixel kernel)
+  int n_classes = 0;
+  int* overflow_count = nullptr;     // device scratch: pixels past their class's limits
+  int2* overflow = nullptr;
+  int overflow_cap = 0;
 };
 int mv_tc_supported(int n_ch, int mv_subarray, int range_avg);
 int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out, long out_stride,

@@ -5,11 +5,17 @@
 // their samples and the kernels.
 #include "usx/beamformer.hpp"
 
+#include <dlfcn.h>
+
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <list>
+#include <map>
 #include <mutex>
+#include <stdexcept>
 
 #include "desc.hpp"
 #include "usx/geometry.hpp"
@@ -25,6 +31,69 @@ void BeamformerConfig::validate() const {
   if (mv_range_average < 0)
     throw std::invalid_argument("BeamformerConfig.mv_range_average must be >= 0");
 }
+
+namespace {
+
+// The learned minimum-variance network of a context: read once from
+// USX_LEARNED_MV_WEIGHTS, else the weights shipped beside the library
+// (<package>/weights/learned_mv_128ch_l64.bin); its gate from
+// USX_LEARNED_MV_GATE, else the ".gate" file written with the weights, else
+// 0.05. The file is the trainer's raw format: "USXMLP1\0", int32 n_layers,
+// int32 dims[n_layers + 1], float32 parameters.
+struct LearnedNet {
+  usx_mlp* mlp = nullptr;
+  float gate = 0.05f;
+};
+
+std::string library_dir() {
+  Dl_info info{};
+  if (dladdr(reinterpret_cast<void*>(&library_dir), &info) && info.dli_fname) {
+    std::string p(info.dli_fname);
+    const auto k = p.find_last_of('/');
+    if (k != std::string::npos) return p.substr(0, k);
+  }
+  return ".";
+}
+
+LearnedNet learned_net(usx_ctx* ctx) {
+  static std::mutex mu;
+  static std::map<usx_ctx*, LearnedNet> nets;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = nets.find(ctx);
+  if (it != nets.end()) return it->second;
+  const char* env = std::getenv("USX_LEARNED_MV_WEIGHTS");
+  const std::string path = env ? std::string(env) : library_dir() + "/../weights/learned_mv_128ch_l64.bin";
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("learned minimum variance: cannot open the network weights " + path);
+  char magic[8];
+  std::int32_t n_layers = 0;
+  f.read(magic, 8);
+  f.read(reinterpret_cast<char*>(&n_layers), 4);
+  if (!f || std::memcmp(magic, "USXMLP1\0", 8) != 0 || n_layers < 1 || n_layers > 64)
+    throw std::runtime_error("learned minimum variance: " + path + " is not a network file");
+  std::vector<int> dims(static_cast<std::size_t>(n_layers) + 1);
+  f.read(reinterpret_cast<char*>(dims.data()), 4 * static_cast<std::streamsize>(dims.size()));
+  std::size_t n_params = 0;
+  for (int l = 0; l < n_layers; ++l)
+    n_params += static_cast<std::size_t>(dims[l]) * dims[l + 1] + static_cast<std::size_t>(dims[l + 1]);
+  std::vector<float> params(n_params);
+  f.read(reinterpret_cast<char*>(params.data()), static_cast<std::streamsize>(4 * n_params));
+  if (!f) throw std::runtime_error("learned minimum variance: " + path + " is truncated");
+  LearnedNet net;
+  rt::check(usx_cu_mlp_create(ctx, n_layers, dims.data(), 0, &net.mlp), "learned network");
+  rt::check(usx_cu_mlp_set_params(net.mlp, params.data()), "learned network weights");
+  if (const char* g = std::getenv("USX_LEARNED_MV_GATE")) {
+    net.gate = std::strtof(g, nullptr);
+  } else {
+    std::ifstream gf(path.substr(0, path.size() - 4) + ".gate");
+    float gv = 0.0f;
+    if (gf >> gv) net.gate = gv;
+  }
+  nets.emplace(ctx, net);
+  return net;
+}
+
+}  // namespace
 
 // The key of a plan is everything that is frozen into it.
 struct PlanKey {
@@ -59,6 +128,9 @@ class PlanCache {
     put(&b, sizeof b);
     const int iq = data.is_iq ? 1 : 0;
     put(&iq, sizeof iq);
+    const char* solver = std::getenv("USX_MV_SOLVER");
+    const int exact_mv = solver && std::string(solver) == "exact" ? 1 : 0;
+    put(&exact_mv, sizeof exact_mv);  // the solver is frozen into the plan
     put(&data.demodulation_frequency, sizeof(real));
     put(&ev_begin, sizeof ev_begin);
     put(&ev_end, sizeof ev_end);
@@ -97,6 +169,15 @@ class PlanCache {
       const char* solver = std::getenv("USX_MV_SOLVER");
       const bool exact = solver && std::string(solver) == "exact";
       if (!exact) usx_cu_bf_plan_set_mv_mode(plan, USX_MV_TENSOR);  // unsupported shapes stay exact
+    }
+    if (cfg.combiner == Combiner::LearnedMV) {
+      try {
+        const LearnedNet net = learned_net(key.ctx);
+        rt::check(usx_cu_bf_plan_set_learned(plan, net.mlp, net.gate), "learned minimum variance");
+      } catch (...) {
+        usx_cu_bf_plan_destroy(plan);
+        throw;
+      }
     }
     entries_.emplace_front(std::move(key), plan);
     while (entries_.size() > kMaxPlans) {

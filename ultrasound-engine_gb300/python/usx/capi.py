@@ -402,6 +402,13 @@ class Mlp:
             out.append((w, b))
         return out
 
+    LOSS_MSE, LOSS_LMV_OUTPUT = 0, 1
+
+    def set_loss(self, kind: int, beta: float = 0.0) -> None:
+        """Training loss: LOSS_MSE (masked MSE) or LOSS_LMV_OUTPUT (learned-MV
+        combiner output error + beta * weight MSE)."""
+        check(lib().usx_cu_mlp_set_loss(self._h, int(kind), C.c_float(beta)), "mlp_set_loss")
+
     def forward(self, x_ptr: int, rows: int, y_ptr: int) -> None:
         check(lib().usx_cu_mlp_forward(self._h, vp(x_ptr), C.c_int64(rows), vp(y_ptr)), "mlp_forward")
 

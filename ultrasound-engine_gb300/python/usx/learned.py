@@ -238,18 +238,41 @@ def output_mask(feat):
     return ((k[None, :] // 2) < L[:, None]).float()
 
 
-def sample_rows(frame, valid, n: int, gen, bright_frac: float = 0.25):
-    """n valid pixel rows: (1 - bright_frac) uniform, bright_frac from the 2%
-    brightest (point targets and their side lobes are where weights matter most)."""
+def sample_rows(frame, valid, n: int, gen, points=None, spec: PhantomSpec | None = None):
+    """n valid pixel rows: 50% uniform, 20% within 1.5 mm of a wire, 20% inside
+    or within 1 mm of a cyst, 10% from the 2% brightest pixels. Point targets,
+    their side lobes and the cyst interiors are where the Capon weights move
+    the image metrics; uniform rows cover the speckle."""
     torch = __import__("torch")
-    idx = torch.nonzero(valid.bool(), as_tuple=False).squeeze(1)
-    n_b = int(n * bright_frac)
-    u = idx[torch.randint(idx.numel(), (n - n_b,), generator=gen, device=idx.device)]
+    dev = frame.device
+    ok = valid.bool()
+    pools = [(torch.nonzero(ok, as_tuple=False).squeeze(1), 0.5)]
+    if spec is not None and points is not None:
+        pts = torch.as_tensor(points, device=dev).reshape(-1, 3)
+        near_w = torch.zeros_like(ok)
+        for x, z, _ in spec.wires:
+            near_w |= torch.hypot(pts[:, 0] - x, pts[:, 2] - z) < 1.5e-3
+        near_c = torch.zeros_like(ok)
+        for x, z, r in spec.cysts:
+            near_c |= torch.hypot(pts[:, 0] - x, pts[:, 2] - z) < r + 1e-3
+        pools += [(torch.nonzero(ok & near_w, as_tuple=False).squeeze(1), 0.2),
+                  (torch.nonzero(ok & near_c, as_tuple=False).squeeze(1), 0.2)]
+    idx = pools[0][0]
     mag = frame.reshape(-1).abs()[idx]
     k = max(1, int(0.02 * idx.numel()))
-    top = idx[torch.topk(mag, k).indices]
-    b = top[torch.randint(top.numel(), (n_b,), generator=gen, device=idx.device)]
-    return torch.cat([u, b])
+    pools.append((idx[torch.topk(mag, k).indices], 0.1))
+    total = sum(f for p, f in pools if p.numel())
+    out = []
+    for p, f in pools:
+        if p.numel() == 0:
+            continue
+        m = int(round(n * f / total))
+        out.append(p[torch.randint(p.numel(), (m,), generator=gen, device=dev)])
+    rows = torch.cat(out)
+    if rows.numel() < n:
+        rows = torch.cat([rows, pools[0][0][torch.randint(pools[0][0].numel(), (n - rows.numel(),), generator=gen,
+                                                          device=dev)]])
+    return rows[:n]
 
 
 def make_pairs(imager: Imager, seeds, per_phantom: int = 16384, log=print):
@@ -260,9 +283,10 @@ def make_pairs(imager: Imager, seeds, per_phantom: int = 16384, log=print):
     X, T = [], []
     t0 = time.time()
     for i, s in enumerate(seeds):
-        imager.acquire(phantom(int(s), imager.setup))
+        spec = phantom(int(s), imager.setup)
+        imager.acquire(spec, noise_seed=int(s))
         frame, feat, w, valid = imager.export_pairs()
-        rows = sample_rows(frame, valid, per_phantom, gen)
+        rows = sample_rows(frame, valid, per_phantom, gen, imager.grid.points, spec)
         X.append(feat[rows].clone())
         T.append(w[rows].clone())
         del feat, w, valid, frame
@@ -274,10 +298,13 @@ def make_pairs(imager: Imager, seeds, per_phantom: int = 16384, log=print):
 
 
 def train(ctx: capi.Context, X, T, M, steps: int = 6000, batch: int = 4096, lr: float = 1e-3, seed: int = 0,
-          log=print, log_every: int = 500) -> tuple[capi.Mlp, list]:
-    """Adam on minibatches drawn on the device, cosine learning-rate decay."""
+          log=print, log_every: int = 500, loss: str = "output", beta: float = 0.02) -> tuple[capi.Mlp, list]:
+    """Adam on minibatches drawn on the device, cosine learning-rate decay.
+    loss="output": the combiner-output error against plain MV's (plus beta x
+    the weight MSE); loss="mse": the weight MSE alone."""
     torch = __import__("torch")
     mlp = capi.Mlp(ctx, DIMS, seed)
+    mlp.set_loss(capi.Mlp.LOSS_LMV_OUTPUT if loss == "output" else capi.Mlp.LOSS_MSE, beta)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed + 1)
     n = X.shape[0]
@@ -322,29 +349,37 @@ def image_metrics(frame, imager: Imager, spec: PhantomSpec) -> dict:
     return out
 
 
-def evaluate(imager: Imager, mlp: capi.Mlp | None, seeds, gate: float = DEFAULT_GATE, baseline: int = COMB_MV,
-             log=print) -> dict:
-    """Per-phantom metrics of plain MV and the learned MV (or, with mlp=None
-    and baseline given, of any other combiner) on held-out phantoms."""
+def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=print) -> dict:
+    """Image metrics of plain MV and of the learned MV at each gate on the
+    held-out phantoms `seeds`: {gate: summary}."""
     learned = imager.plan(COMB_LEARNED_MV)
-    learned.set_learned(mlp, gate)
-    rows = []
+    rows = {g: [] for g in gates}
     for s in seeds:
         spec = phantom(int(s), imager.setup)
-        imager.acquire(spec)
-        ref = imager.beamform(baseline)
-        learned.learned_stats()
-        lf = imager.beamform(COMB_LEARNED_MV)
-        gated, pixels = learned.learned_stats()
-        a, b = image_metrics(ref, imager, spec), image_metrics(lf, imager, spec)
-        d = {k: [y - x for x, y in zip(a[k], b[k])] for k in a}
-        rows.append({"seed": int(s), "plain": a, "learned": b, "delta": d,
-                     "fallback_rate": gated / max(1, pixels),
-                     "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt() / ref.abs().pow(2).sum().sqrt())})
+        imager.acquire(spec, noise_seed=int(s))
+        ref = imager.beamform(COMB_MV)
+        a = image_metrics(ref, imager, spec)
+        for g in gates:
+            learned.set_learned(mlp, g)
+            learned.learned_stats()
+            lf = imager.beamform(COMB_LEARNED_MV)
+            gated, pixels = learned.learned_stats()
+            b = image_metrics(lf, imager, spec)
+            d = {k: [y - x for x, y in zip(a[k], b[k])] for k in a}
+            rows[g].append({"seed": int(s), "plain": a, "learned": b, "delta": d,
+                            "fallback_rate": gated / max(1, pixels),
+                            "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt() / ref.abs().pow(2).sum().sqrt())})
         if log:
-            log(f"phantom {s}: fallback {rows[-1]['fallback_rate']:.4f} rel_l2 {rows[-1]['rel_l2']:.4f} "
-                f"dgcnr {d['gcnr']} dfwhm {d['lateral_fwhm_mm']}")
-    return summarize(rows)
+            log(f"phantom {s}: " + ", ".join(
+                f"gate {g}: fallback {rows[g][-1]['fallback_rate']:.3f} dgcnr "
+                f"{max([abs(v) for v in rows[g][-1]['delta']['gcnr']] or [0]):.4f}" for g in gates))
+    return {g: summarize(r) for g, r in rows.items()}
+
+
+def choose_gate(results: dict, max_dgcnr: float = 0.01) -> float | None:
+    """The largest gate whose held-out max |delta gCNR| stays within max_dgcnr."""
+    ok = [g for g, r in results.items() if r.get("gcnr", {}).get("max_abs_delta", 1.0) <= max_dgcnr]
+    return max(ok) if ok else None
 
 
 def summarize(rows) -> dict:
@@ -375,45 +410,64 @@ def main(argv=None) -> None:
     t = sub.add_parser("train")
     t.add_argument("--phantoms", type=int, default=200)
     t.add_argument("--per-phantom", type=int, default=16384)
-    t.add_argument("--steps", type=int, default=6000)
+    t.add_argument("--steps", type=int, default=50000)
     t.add_argument("--batch", type=int, default=4096)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
+    t.add_argument("--loss", default="output", choices=["output", "mse"])
+    t.add_argument("--beta", type=float, default=0.02)
     t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     t.add_argument("--eval-phantoms", type=int, default=16)
-    t.add_argument("--report", default=None)
     e = sub.add_parser("evaluate")
     e.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
     e.add_argument("--phantoms", type=int, default=16)
-    e.add_argument("--gate", type=float, default=DEFAULT_GATE)
-    e.add_argument("--report", default=None)
+    for p in (t, e):
+        p.add_argument("--gates", default="0.005,0.01,0.02,0.03,0.05,0.1")
+        p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
     a = ap.parse_args(argv)
+    gates = tuple(float(g) for g in a.gates.split(","))
     imager = Imager()
-    report = {}
+    report = {"dims": list(DIMS), "setup": imager.setup.__dict__}
+    eval_seeds = np.arange(900_000, 900_000 + (a.eval_phantoms if a.cmd == "train" else a.phantoms))
     if a.cmd == "train":
         train_seeds = np.arange(1000, 1000 + a.phantoms)
         t0 = time.time()
         X, T, M = make_pairs(imager, train_seeds, a.per_phantom)
-        report["pairs"] = int(X.shape[0])
-        report["pair_seconds"] = time.time() - t0
+        report.update(phantoms=a.phantoms, pairs=int(X.shape[0]), pair_seconds=time.time() - t0)
+        Xv, Tv, Mv = make_pairs(imager, np.arange(5000, 5008), a.per_phantom, log=None)
         t0 = time.time()
-        mlp, losses = train(imager.ctx, X, T, M, a.steps, a.batch, a.lr, a.seed)
+        mlp, losses = train(imager.ctx, X, T, M, a.steps, a.batch, a.lr, a.seed, loss=a.loss, beta=a.beta)
         imager.ctx.synchronize()
-        report["train_seconds"] = time.time() - t0
-        report["losses"] = losses
-        Path(a.out).parent.mkdir(parents=True, exist_ok=True)
-        save_weights(a.out, DIMS, mlp.get_params())
-        if a.eval_phantoms:
-            report["eval"] = evaluate(imager, mlp, np.arange(900_000, 900_000 + a.eval_phantoms))
+        report.update(steps=a.steps, batch=a.batch, lr=a.lr, loss=a.loss, beta=a.beta,
+                      train_seconds=time.time() - t0, losses=losses,
+                      validation_loss=validation_loss(mlp, Xv, Tv, Mv))
+        del X, T, M, Xv, Tv, Mv
+        out = Path(a.out)
+        out.parent.mkdir(parents=True, exist_ok=True)
+        save_weights(out, DIMS, mlp.get_params())
     else:
-        mlp = load_mlp(imager.ctx, a.weights)
-        report["eval"] = evaluate(imager, mlp, np.arange(900_000, 900_000 + a.phantoms), a.gate)
-    s = json.dumps(report, indent=1, default=float)
-    if a.report:
-        Path(a.report).write_text(s)
-    ev = report.get("eval", {})
-    print(json.dumps({k: v for k, v in ev.items() if k != "rows"}, default=float))
+        out = Path(a.weights)
+        mlp = load_mlp(imager.ctx, out)
+    results = evaluate(imager, mlp, eval_seeds, gates)
+    report["eval"] = {str(g): {k: v for k, v in r.items() if k != "rows"} for g, r in results.items()}
+    report["eval_rows"] = {str(g): r["rows"] for g, r in results.items()}
+    report["gate"] = choose_gate(results)
+    path = Path(a.report) if a.report else out.with_suffix(".json")
+    path.write_text(json.dumps(report, indent=1, default=float))
+    if report["gate"] is not None:
+        out.with_suffix(".gate").write_text(f"{report['gate']}\n")
+    print(json.dumps({"gate": report["gate"], "eval": report["eval"]}, default=float))
     imager.close()
+
+
+def trained_gate(weights=DEFAULT_WEIGHTS) -> float:
+    """The gate chosen when the weights were trained (their JSON report)."""
+    p = Path(weights).with_suffix(".json")
+    if p.exists():
+        g = json.loads(p.read_text()).get("gate")
+        if g is not None:
+            return float(g)
+    return DEFAULT_GATE
 
 
 if __name__ == "__main__":
