@@ -64,7 +64,7 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
-def workload_setup():
+def workload_setup(n_scat: int = 100_000):
     """Probe, acquisition, transmits, grid and phantom of the headline workload (host objects)."""
     import usx
     probe = usx.Probe()
@@ -77,7 +77,7 @@ def workload_setup():
     sim = usx.Simulator(probe, medium, acq, cfg)
     txs = sim.make_plane_waves(usx.angles_deg(-16, 16, N_TX))
     half = 0.5 * probe.aperture_width()
-    ph = usx.Phantom.speckle_box(-half * 1.1, half * 1.1, 0.004, 0.062, 0.0, 100_000, 2026)
+    ph = usx.Phantom.speckle_box(-half * 1.1, half * 1.1, 0.004, 0.062, 0.0, n_scat, 2026)
     for x, z, r in CYSTS:
         ph.scale_amplitude_in_circle(usx.Vec3(x, 0.0, z), r, 0.0)
     grid = usx.grid_for(probe, 0.005, 0.060, N0, N1)
@@ -233,6 +233,72 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+WEIGHTS = PKG / "weights" / "learned_mv_128ch_l64.bin"
+# DRAM bytes per launch of the dominant kernels from one ncu capture of the
+# same workload (profiles/ holds the summaries these come from), scaled to a
+# full 512-line frame where the capture was a subset of lines.
+TRAFFIC_PER_FRAME = {}
+
+
+def timed(stream, fn, steps: int):
+    """Device time (ms) of `steps` calls of fn on `stream`, CUDA events around."""
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(steps):
+        fn()
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks: dict) -> dict:
+    """Roofline of the dominant kernel of the timed region: algorithmic work
+    per frame over that kernel's device time per frame (CUDA events on the
+    launching stream)."""
+    if not prof:
+        return {"kernel": None, "bound": None, "achieved": None, "peak": None, "unit": None, "frac": None,
+                "traffic": None}
+    per_frame = {k: v[0] / frames for k, v in prof.items()}
+    kname = max(per_frame, key=per_frame.get)
+    kms = per_frame[kname]
+    out = {"kernel": kname, "kernel_ms_per_frame": kms,
+           "kernels_ms_per_frame": per_frame,
+           "launches_per_frame": {k: v[1] / frames for k, v in prof.items()}}
+    base = kname.split("(")[0]
+    if base.startswith("mv"):
+        flops = mv_flops_per_frame(pts, MV_KW)
+        achieved = flops / (kms / 1e3) / 1e12
+        out.update(bound="tensor", achieved=achieved, peak=peaks["bf16_tflops_sustained"], unit="TFLOP/s",
+                   algorithmic_gflop_per_frame=flops / 1e9,
+                   note="covariance 4 L^2 n_snap + Cholesky 4/3 L^3 + solves 16 L^2 per pixel; "
+                        "peak = cuBLAS bf16 sustained (measured)")
+    elif base.startswith("das"):
+        ops = das_active_ops(pts, txs, probe, 1.5)
+        flops = 20.0 * ops
+        achieved = flops / (kms / 1e3) / 1e12
+        hbm = (8.0 * N_TX * N_EL * N_SMP + 8.0 * len(pts)) / (kms / 1e3) / 1e9
+        out.update(bound="fp32", achieved=achieved, peak=FP32_NOMINAL_TFLOPS, unit="TFLOP/s",
+                   algorithmic_gflop_per_frame=flops / 1e9, compulsory_hbm_gbs=hbm,
+                   hbm_frac=hbm / peaks["hbm_gbs"],
+                   note="20 FP32 flops per active (pixel, channel, transmit); peak = nominal FP32 "
+                        "(152 SMs x 128 lanes x FMA x 2.07 GHz); compulsory HBM bytes = IQ + frame")
+    elif base.startswith("mlp"):
+        flops = 2.0 * len(pts) * sum(a * b for a, b in zip((256, 256, 256, 256), (256, 256, 256, 128)))
+        achieved = flops / (kms / 1e3) / 1e12
+        out.update(bound="tensor", achieved=achieved, peak=peaks["bf16_tflops"], unit="TFLOP/s",
+                   algorithmic_gflop_per_frame=flops / 1e9)
+    else:
+        out.update(bound=None, achieved=None, peak=None, unit=None)
+    out["frac"] = (out["achieved"] / out["peak"]) if out.get("achieved") and out.get("peak") else None
+    tr = TRAFFIC_PER_FRAME.get(base)
+    out["traffic"] = (tr / max(1.0, out["launches_per_frame"][kname])) if tr else None
+    out["peak_source"] = peaks["source"]
+    return out
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -266,29 +332,50 @@ def run_ours(args) -> None:
     pts = np.asarray(grid.points).reshape(N0, N1, 3)[:n0].reshape(-1, 3)
     cgrid = capi.Grid(0, np.asarray(grid.axis0)[:n0], np.asarray(grid.axis1), pts)
     bkw = WORKLOADS[args.workload]
-    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
-    if args.workload == "mv":
-        plan.set_mv_mode(1)
     frame = torch.empty((n0, N1), dtype=torch.complex64, device="cuda")
-
     stream = torch.cuda.ExternalStream(ctx.stream())
+
+    extra = {}
+    mlp = None
+    if args.workload == "learned":
+        from usx import learned
+        if not WEIGHTS.exists():
+            raise SystemExit(f"bench: the learned workload needs the trained network {WEIGHTS}")
+        mlp = learned.load_mlp(ctx, WEIGHTS)
+        gate = learned.trained_gate(WEIGHTS)
+        refine = learned.trained_refine(WEIGHTS)
+        # Plain minimum variance (tensor-core solver) on the same frame, timed first.
+        plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
+        plain.set_mv_mode(1)
+        for _ in range(args.warmup):
+            plain.execute(d_iq.data_ptr(), frame.data_ptr())
+        ctx.synchronize()
+        plain_ms = timed(stream, lambda: plain.execute(d_iq.data_ptr(), frame.data_ptr()), args.steps)
+        ref_frame = frame.clone()
+        plain.close()
+        plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
+        plan.set_learned(mlp, gate)
+        plan.set_learned_refine(refine)
+        extra["plain_mv"] = {"value": world * args.steps / (plain_ms / 1e3) * N0 / n0, "unit": "frames/s",
+                             "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": "tensor"}
+        extra["gate"] = gate
+        extra["refine_beams"] = refine
+    else:
+        plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
+        if args.workload == "mv":
+            plan.set_mv_mode(1)
+
     for _ in range(args.warmup):
         plan.execute(d_iq.data_ptr(), frame.data_ptr())
     ctx.synchronize()
+    if args.workload == "learned":
+        plan.learned_stats()
     if world > 1:
         torch.distributed.barrier()
     capi.profile(ctx, True)
     capi.profile_reset(ctx)
     with ClockSampler(local) as clocks:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            plan.execute(d_iq.data_ptr(), frame.data_ptr())
-        ev1.record(stream)
-        ev1.synchronize()
-    ms = ev0.elapsed_time(ev1)
+        ms = timed(stream, lambda: plan.execute(d_iq.data_ptr(), frame.data_ptr()), args.steps)
     prof = capi.profile_read(ctx)
     capi.profile(ctx, False)
     if world > 1:
@@ -297,26 +384,28 @@ def run_ours(args) -> None:
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1e3)
+    if args.workload == "learned":
+        gated, pixels = plan.learned_stats()
+        extra["fallback_rate"] = gated / max(1, pixels)
+        extra["speedup_vs_plain_mv"] = (extra["plain_mv"]["ms_per_step"] / (ms_per_step * N0 / n0))
+        extra["rel_l2_vs_plain_mv"] = float((frame - ref_frame).abs().pow(2).sum().sqrt()
+                                            / ref_frame.abs().pow(2).sum().sqrt())
+        rep = WEIGHTS.with_suffix(".json")
+        if rep.exists():
+            r = json.loads(rep.read_text())
+            ev = r.get("eval", {}).get(str(gate)) or r.get("eval", {}).get(repr(gate))
+            if ev:
+                extra["held_out_quality"] = {
+                    "phantoms": ev.get("phantoms"), "fallback_rate": ev.get("fallback_rate"),
+                    "max_abs_delta_gcnr": ev.get("gcnr", {}).get("max_abs_delta"),
+                    "max_rel_delta_lateral_fwhm": ev.get("lateral_fwhm_mm", {}).get("max_rel_delta"),
+                    "source": str(rep.relative_to(ROOT))}
 
-    # Dominant kernel and its roofline (algorithmic FLOPs over live device time).
     peaks = load_peaks()
-    top = max(prof.items(), key=lambda kv: kv[1][0]) if prof else ("none", (0.0, 0))
     launches_in_region = sum(n for _, n in prof.values())
-    mv_flops = mv_flops_per_frame(pts, MV_KW)
-    kname, (kms, kn) = top
-    achieved_tflops = mv_flops / (kms / kn / 1e3) / 1e12 if kn and kname.startswith("mv") else None
-    roofline = {"kernel": kname, "bound": "tensor", "achieved": achieved_tflops,
-                "peak": peaks["bf16_tflops_sustained"], "unit": "TFLOP/s",
-                "frac": (achieved_tflops / peaks["bf16_tflops_sustained"]) if achieved_tflops else None,
-                "traffic": None, "peak_source": peaks["source"],
-                "kernels_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in prof.items()},
-                "algorithmic_gflop_per_frame": mv_flops / 1e9}
+    roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks)
 
-    e2e = None
-    if args.no_e2e:
-        pass
-    else:
-        e2e = run_e2e(usx, grid, raw, rf_host, args, world)
+    e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world)
     if bkw.get("combiner") == 2:
         fp64, failed = plan.mv_stats()
         roofline["mv_fp64_resolves_per_frame"] = fp64 / max(1, args.steps + args.warmup)
@@ -330,7 +419,8 @@ def run_ours(args) -> None:
             lines = max(2, min(threads, 16))
             dt, kind = cpu_baseline_mv(iq_host, np.asarray(grid.points), txs, probe, acq, lines, threads)
             cpu = {"value": 1.0 / (dt * N0 / lines), "unit": "frames/s", "cores": threads, "kind": kind,
-                   "sample": f"{lines} of {N0} lateral lines (one per core), scaled to a frame"}
+                   "sample": f"minimum variance on {lines} of {N0} lateral lines (one per core), "
+                             f"scaled to a frame"}
         frames_per_s = value * N0 / n0
         line = {"metric": METRIC, "value": frames_per_s, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step * N0 / n0, "higher_is_better": True,
@@ -341,8 +431,90 @@ def run_ours(args) -> None:
                            "l2": "inputs larger than L2 (159 MB IQ), no flush"},
                 "gpu_launches": launches_in_region, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary()}
+        line.update(extra)
         print(json.dumps(line))
     plan.close()
+    if mlp is not None:
+        mlp.close()
+    ctx.close()
+
+
+def run_stage(args) -> None:
+    """Single-stage workloads on the headline acquisition: the forward
+    simulator (`simulate`, args.scatterers scatterers x 128 elements x 75 plane
+    waves, receive noise on) and the demodulator (`demod`, RF (75, 128, 2073)
+    float32 -> IQ complex64, 33 taps, decimation 1)."""
+    import torch
+    from usx import capi
+    torch.cuda.set_device(0)
+    usx, probe, medium, acq, sim, txs, ph, grid = workload_setup(args.scatterers)
+    ctx = capi.Context(0)
+    tx = [dict(type=1, angle=t.angle, delays=t.delays, apodization=t.apodization) for t in txs]
+    ch_rf = capi.Channel(capi.Probe(N_EL, probe.pitch, probe.element_width, probe.elevation_height, F0,
+                                    probe.bandwidth),
+                         capi.Medium(medium.speed_of_sound, medium.attenuation, medium.density),
+                         capi.Acquisition(acq.sampling_frequency, acq.n_samples, acq.t0, acq.prf), tx)
+    pos, amp = np.asarray(ph.positions), np.asarray(ph.amplitudes)
+    sc = np.zeros((len(amp), 8), np.float32)
+    sc[:, :3], sc[:, 3] = pos, amp
+    d_sc = torch.from_numpy(sc).cuda()
+    d_rf = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.float32, device="cuda")
+    d_iq = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    z = torch.randn((N_TX, N_EL, N_SMP), device="cuda")
+    torch.cuda.synchronize()
+    scfg = capi.sim_config()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    stats = ctx.simulate(ch_rf, scfg, d_sc.data_ptr(), len(sc), z.data_ptr(), d_rf.data_ptr(), want_stats=True)
+    if args.workload == "simulate":
+        step = lambda: ctx.simulate(ch_rf, scfg, d_sc.data_ptr(), len(sc), z.data_ptr(), d_rf.data_ptr())
+    else:
+        step = lambda: ctx.demodulate(ch_rf, capi.demod_config(), d_rf.data_ptr(), d_iq.data_ptr())
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    capi.profile(ctx, True)
+    capi.profile_reset(ctx)
+    with ClockSampler(0) as clocks:
+        ms = timed(stream, step, args.steps)
+    prof = capi.profile_read(ctx)
+    capi.profile(ctx, False)
+    peaks = load_peaks()
+    per = {k: v[0] / args.steps for k, v in prof.items()}
+    top = max(per, key=per.get)
+    line = {"metric": f"{args.workload}: acquisitions/s", "value": args.steps / (ms / 1e3), "unit": "acquisitions/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "gpu_launches": sum(n for _, n in prof.values()), "clocks": clocks.summary()}
+    if args.workload == "simulate":
+        samples = stats[0]
+        # Stage 1: a two-tap lerp-add (4 flops) per pulse tap per firing element
+        # per (scatterer, transmit); stage 2: 4 flops per echo sample.
+        import ctypes as C
+        n_taps, half = C.c_int(), C.c_float()
+        capi.lib().usx_cu_pulse(C.byref(ch_rf.desc.probe), C.byref(ch_rf.desc.acq), C.byref(scfg), None, 0,
+                                C.byref(n_taps), C.byref(half))
+        pulse_taps = n_taps.value
+        n_fire = sum(int(np.count_nonzero(np.asarray(t.apodization))) for t in txs)
+        flops = 4.0 * len(sc) * n_fire * pulse_taps + 4.0 * samples
+        kms = per[top]
+        line["config"] = {"workload": f"simulate_{len(sc)}scat_128el_75pw", "scatterers": len(sc),
+                          "elements": N_EL, "transmits": N_TX, "samples": N_SMP}
+        line["scatterer_element_samples_per_s"] = samples / (ms / args.steps / 1e3)
+        line["roofline"] = {"kernel": top, "bound": "fp32", "achieved": flops / (kms / 1e3) / 1e12,
+                            "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                            "frac": flops / (kms / 1e3) / 1e12 / FP32_NOMINAL_TFLOPS, "traffic": None,
+                            "gflop_per_step": flops / 1e9, "echo_samples_per_step": samples,
+                            "kernels_ms_per_step": per,
+                            "note": "peak = nominal FP32 (152 SMs x 128 lanes x FMA x 2.07 GHz)"}
+    else:
+        nbytes = 4.0 * N_TX * N_EL * N_SMP + 8.0 * N_TX * N_EL * N_SMP
+        kms = per[top]
+        line["config"] = {"workload": "demod_75x128x2073_33taps_dec1"}
+        line["roofline"] = {"kernel": top, "bound": "hbm", "achieved": nbytes / (kms / 1e3) / 1e9,
+                            "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                            "frac": nbytes / (kms / 1e3) / 1e9 / peaks["hbm_gbs"], "traffic": None,
+                            "algorithmic_bytes": nbytes, "kernels_ms_per_step": per}
+    print(json.dumps(line))
     ctx.close()
 
 
@@ -378,13 +550,16 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="mv", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="learned", choices=sorted(WORKLOADS) + ["simulate", "demod"])
+    ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("simulate", "demod"):
+        run_stage(args)
     else:
         run_ours(args)
     return 0

@@ -141,6 +141,21 @@ int usx_cu_bf_execute_batch(usx_bf_plan* plan, int n_frames, const void* data,
 enum { USX_BF_FAST = 0, USX_BF_EXACT = 1 };
 int usx_cu_bf_plan_set_precision(usx_bf_plan* plan, int precision);
 
+/* Launch shapes of the fast delay-and-sum (no counterpart in the reference):
+ * variant i has a channel group (channels whose transmit geometry is shared
+ * per event), a tile of tile_lines lateral lines x 32 depths per CTA and a
+ * register cap for min_blocks resident CTAs per SM. All variants produce
+ * bit-identical frames. usx_cu_bf_plan_autotune beamforms `data` once per
+ * variant (plus a warm-up) `repeats` times, keeps the fastest in the plan,
+ * writes every variant's mean milliseconds to ms_out[variant] (host, may be
+ * NULL; usx_cu_bf_variant_count() entries), leaves the frame of the chosen
+ * variant in `frame` and synchronises. Variant 0 is the default. */
+int usx_cu_bf_variant_count(void);
+int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks);
+int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
+int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);
+int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, int repeats, float* ms_out);
+
 /* Minimum-variance solver of a plan (no counterpart in the reference, whose
  * one solver is combine_mv_windowed, beamformer.cpp:137-214):
  *   USX_MV_EXACT   FP32, the reference's operation order (default);
@@ -174,6 +189,17 @@ int usx_cu_bf_plan_mv_stats(usx_bf_plan* plan, int64_t* fp64_resolves,
  * the DAS sum, as in the reference. Coherent and select compounding only.
  * The network is not owned and must outlive the plan's executions. */
 int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate);
+/* How the learned path uses the network's weights w~ of a pixel that passes
+ * the gate (no counterpart in the reference):
+ *   n_beams < 0      as predicted (the default), the output above;
+ *   n_beams = 0,2,4  the Capon problem of the reference's minimum variance,
+ *                    min w^H (R + eps I) w subject to 1^H w = 1, solved
+ *                    exactly within span{1, w~, e^{+-j 2 pi b i / L} for
+ *                    b = 1..n_beams/2} through the pixel's snapshots (the
+ *                    covariance is never formed). Equal to the exact minimum
+ *                    variance when w~ is the Capon direction; always
+ *                    distortionless. */
+int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams);
 /* Pixels gated to the exact solver and pixels beamformed by the learned path
  * since the last call (synchronises). */
 int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels);

@@ -254,6 +254,20 @@ class Lib:
             raise ValueError("mv_training_pairs needs a coherent minimum-variance config")
         return out[..., 0] + 1j * out[..., 1], feat, w, valid
 
+    def set_lmv_subspace(self, net_out128, n_beams: int, prec="f32"):
+        """Make the MV combiner solve within span{n_beams + 1 DFT beams, the
+        network output vector net_out128 / L} (None restores the exact solve)."""
+        f = self._fn("orc_set_lmv_subspace", prec)
+        f.argtypes = [f32p, C.c_int]
+        f.restype = None
+        if net_out128 is None:
+            f(None, -1)
+        else:
+            v = np.ascontiguousarray(net_out128, dtype=np.float32)
+            assert v.size == 128
+            self._sub_keep = v
+            f(_ptr(v, f32p), int(n_beams))
+
     def _cplx(self, a, prec):
         dt = self._dt(prec)
         return np.ascontiguousarray(np.stack([np.real(a), np.imag(a)], -1), dtype=dt)

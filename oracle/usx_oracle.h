@@ -50,6 +50,8 @@ extern "C" {
                        R* frame);                                                        \
   /* learned minimum variance (no reference counterpart): MV beamform plus per-pixel */ \
   /* features [n_pix][256], Capon weights L w / sum(w) [n_pix][128] and valid flags */     \
+  /* Learned-subspace refinement in the MV combiner (NULL disables). */    \
+  void orc_set_lmv_subspace_##S(const float* net_out128, int n_beams);     \
   int orc_mv_training_pairs_##S(const usx_channel_desc* cd, const R* data, int n_pix_axis0, \
                                 int n_pix_axis1, const float* points,                     \
                                 const usx_beamformer_config* cfg, R* frame, R* feat,      \

@@ -237,6 +237,38 @@ def test_beamform_geometries_match_reference(capi, ctx, torch, golden):
                       g["div_iq"]), g["bf_div_mv"]) < TOL_MV
 
 
+@pytest.mark.parametrize("cfg_kw", [dict(f_number=1.5), dict(f_number=1.5, combiner=1),
+                                    dict(f_number=1.5, coherence_factor=1), dict(f_number=1.5, compounding=2)])
+def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_kw):
+    """Every delay-and-sum launch shape gives the same frame bit for bit; the
+    autotuner keeps one of them and leaves its frame in the output."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    plan = ctx.plan(ch, grid, capi.bf_config(**cfg_kw))
+    d = dev(torch, g["iq"])
+    out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
+    frames = []
+    variants = capi.das_variants()
+    assert len(variants) >= 2 and variants[0] == (16, 4, 1)
+    for v in range(len(variants)):
+        plan.set_variant(v)
+        plan.execute(d.data_ptr(), out.data_ptr())
+        frames.append(host(torch, out))
+    for f in frames[1:]:
+        assert np.array_equal(f, frames[0])
+    out.zero_()
+    best, ms = plan.autotune(d.data_ptr(), out.data_ptr(), repeats=1)
+    assert 0 <= best < len(variants) and plan.variant() == best
+    assert len(ms) == len(variants) and all(m > 0 for m in ms) and ms[best] == min(ms)
+    assert np.array_equal(host(torch, out), frames[0])
+    with pytest.raises(ValueError):
+        plan.set_variant(len(variants))
+    plan.close()
+
+
 def test_batch_and_sequence_equal_single_frames(capi, ctx, torch, golden):
     g = golden("bf")
     s = golden("sim")

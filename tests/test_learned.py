@@ -109,6 +109,28 @@ def test_oracle_training_pairs_reproduce_the_reference_frame(oracle, golden):
     assert np.all(feat[~ok & (L == 0)] == 0)
 
 
+def test_oracle_subspace_with_full_span_is_exact_mv(oracle, golden):
+    """With L <= the number of DFT beams the subspace is all of C^L, so the
+    learned-subspace solve must reproduce the exact minimum variance."""
+    g, s, pr, med, acq = _golden_mv_case(golden)
+    cd = O.channel_desc(pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    n0, n1 = len(g["ax0"]), len(g["ax1"])
+    cfg = O.bf_config(**dict(BF_CASES["mv"], mv_subarray=4))
+    exact = oracle.beamform(cd, g["iq"], g["pts"], n0, n1, cfg, prec="f64")
+    v = np.zeros(128, np.float32)
+    v[0::2] = 1.0 + 0.5 * np.cos(np.arange(64) * 0.7)
+    v[1::2] = 0.3 * np.sin(np.arange(64) * 1.3)
+    try:
+        oracle.set_lmv_subspace(v, 4, prec="f64")
+        sub = oracle.beamform(cd, g["iq"], g["pts"], n0, n1, cfg, prec="f64")
+        oracle.set_lmv_subspace(v, 0, prec="f64")
+        narrow = oracle.beamform(cd, g["iq"], g["pts"], n0, n1, cfg, prec="f64")
+    finally:
+        oracle.set_lmv_subspace(None, -1, prec="f64")
+    assert rel_l2(sub, exact) < 1e-9
+    assert rel_l2(narrow, exact) > 1e-4   # two directions do not span C^4
+
+
 # ------------------------------------------------------------------ GPU
 
 @pytest.fixture(scope="module")
@@ -311,6 +333,68 @@ def test_gate_zero_falls_back_to_plain_mv_everywhere(capi, torch):
         im.beamform(learned.COMB_LEARNED_MV)
         gated, pixels = plan.learned_stats()
         assert gated == 0 and pixels == setup.n0 * setup.n1
+    finally:
+        im.close()
+
+
+def _constant_net(capi, ctx, v):
+    """A network whose output is the vector v for every pixel (zero weights,
+    last bias v)."""
+    mlp = capi.Mlp(ctx, DIMS, seed=0)
+    p = np.zeros(mlp.n_params, np.float32)
+    _, b = mlp.layers(p)[-1]
+    b[:] = v
+    mlp.set_params(p)
+    return mlp
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("beams", [0, 2, 4])
+def test_subspace_refinement_matches_oracle(capi, torch, oracle, beams):
+    """The learned-subspace refinement (Capon solve within span{DFT beams,
+    network direction}, through the snapshots) against the oracle's
+    restatement, which forms the covariance and projects it."""
+    learned, setup = _learned_setup()
+    im = learned.Imager(setup)
+    try:
+        im.acquire(learned.phantom(31, setup))
+        v = np.zeros(128, np.float32)
+        i = np.arange(64)
+        v[0::2] = 1.0 + 0.4 * np.cos(2 * np.pi * 3.3 * i / 40.0)
+        v[1::2] = 0.25 * np.sin(2 * np.pi * 1.7 * i / 40.0)
+        mlp = _constant_net(capi, im.ctx, v)
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        plan.set_learned(mlp, float("inf"))
+        plan.set_learned_refine(beams)
+        plan.learned_stats()
+        out = im.beamform(learned.COMB_LEARNED_MV).cpu().numpy()
+        gated, pixels = plan.learned_stats()
+        assert gated == 0
+        iq = im.iq.cpu().numpy()
+        lines = np.arange(40, 46)
+        pts = im.grid.points.reshape(setup.n0, setup.n1, 3)[lines].reshape(-1, 3)
+        pr = O.probe(n_elements=setup.n_el, pitch=setup.pitch, element_width=setup.width,
+                     center_frequency=setup.f0, bandwidth=0.6)
+        a = im.ch_iq.desc.acq
+        acq = O.acquisition(fs=a.sampling_frequency, n_samples=a.n_samples, t0=a.t0, prf=a.prf)
+        tx = im.transmits
+        n = len(tx)
+        txs = O.TxSet(np.array([t["type"] for t in tx]), np.array([t["angle"] for t in tx], np.float32),
+                      np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32),
+                      np.stack([np.asarray(t["delays"], np.float32) for t in tx]),
+                      np.stack([np.asarray(t["apodization"], np.float32) for t in tx]))
+        cd = O.channel_desc(pr, O.medium(), acq, txs, is_iq=True, fdem=setup.f0)
+        try:
+            oracle.set_lmv_subspace(v, beams, prec="f64")
+            want = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)),
+                                   prec="f64")
+        finally:
+            oracle.set_lmv_subspace(None, -1, prec="f64")
+        got = out[lines]
+        assert rel_l2(got, want) < 2e-4
+        # The refinement is a proper approximation of plain MV here, not MV itself.
+        mv = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)), prec="f64")
+        assert rel_l2(want, mv) > 1e-3
     finally:
         im.close()
 

@@ -249,11 +249,13 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
 //   * a block is a 4-line x 32-depth tile, so the four warps read
 //     overlapping windows of every trace and share them in L1.
 // The result differs from the reference's rounding by ~1e-7 relative L2.
-constexpr int kFastGroup = 16;
-constexpr int kTileLines = 4;
-
-template <bool IQ>
-__global__ void __launch_bounds__(kBfThreads) das_fast_kernel(const BfArgs a) {
+//
+// The group size G, the tile's line count TL (a CTA is TL warps) and the
+// register cap (MINB resident CTAs per SM) are template parameters; every
+// variant computes the same sums in the same order (bit-identical frames),
+// and the plan's autotuner picks the fastest for its geometry.
+template <bool IQ, int kFastGroup, int kTileLines, int MINB>
+__global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
   const int tile = blockIdx.x;
@@ -415,6 +417,25 @@ __global__ void __launch_bounds__(kBfThreads) das_fast_kernel(const BfArgs a) {
   if (incoherent) result = mk(sqrtf(inc_acc), 0.0f);
   a.out[frame * a.out_stride + pix] = make_float2(result.re, result.im);
 }
+
+// The delay-and-sum variants the autotuner chooses from (index 0 is the
+// default): (channel group, tile lines, minimum resident CTAs per SM).
+struct DasVariant {
+  int group, tile_lines, min_blocks;
+  void (*iq)(BfArgs);
+  void (*rf)(BfArgs);
+};
+// RF input (the reference's interp_rf path) keeps the default shape in
+// every variant.
+template <int G, int TL, int MB>
+constexpr DasVariant das_variant() {
+  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB>, das_fast_kernel<false, 16, 4, 1>};
+}
+const DasVariant kDasVariants[] = {
+    das_variant<16, 4, 1>(), das_variant<8, 4, 8>(), das_variant<16, 8, 2>(),
+    das_variant<32, 4, 1>(), das_variant<8, 8, 4>(), das_variant<16, 2, 8>(),
+};
+constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
 // ------------------------------------------------------------------------
 // Minimum variance (reference beamformer.cpp:137-214, Cholesky :47-79).
@@ -627,10 +648,12 @@ struct usx_bf_plan {
   int ev_begin = 0, ev_end = 0;
   int mv_mode = USX_MV_EXACT;
   int precision = USX_BF_FAST;
+  int das_variant = 0;         // index into kDasVariants (the autotuner's choice)
   int* d_mv_stats = nullptr;   // [0] FP64 re-solves, [1] factorisation failures, [2] learned-MV gate rejections
   // Learned minimum variance: the network (not owned) and the gate on |1^H w - 1|.
   usx_mlp* mlp = nullptr;
   float lmv_gate = 0.05f;
+  int lmv_beams = -1;   // < 0: the network's weights as predicted; >= 0: subspace refinement
   int64_t lmv_pixels = 0;      // pixels beamformed by the learned path since the last stats read
   // Training export (minimum variance plans): features, weights, valid flags.
   float* exp_feat = nullptr;
@@ -762,15 +785,16 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     return USX_OK;
   }
   const bool fast = plan->precision == USX_BF_FAST;
-  dim3 grid_das(fast ? ceil_div(plan->n0, kTileLines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
+  const DasVariant& dv = kDasVariants[plan->das_variant];
+  dim3 grid_das(fast ? ceil_div(plan->n0, dv.tile_lines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
                 n_frames);
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
     prof_begin(ctx, name);
     if (fast) {
       if (plan->cd.is_iq)
-        das_fast_kernel<true><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
+        dv.iq<<<grid_das, 32 * dv.tile_lines, 0, ctx->stream>>>(b);
       else
-        das_fast_kernel<false><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
+        dv.rf<<<grid_das, 32 * dv.tile_lines, 0, ctx->stream>>>(b);
     } else {
       if (plan->cd.is_iq)
         das_kernel<true><<<grid_das, kBfThreads, 0, ctx->stream>>>(b);
@@ -853,9 +877,14 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       if (int rc = launch_lmv_features(ctx, l)) return rc;
       if (int rc = mlp_infer(plan->mlp, ctx, feat16, npad, bufs[4], bufs[5], net)) return rc;
       USX_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), ctx->stream));
-      if (int rc = launch_lmv_apply(ctx, net, avg, meta, b.out, b.out_stride, b.n_pix, nf, plan->lmv_gate,
-                                    counters, gated, static_cast<int>(nrows), plan->d_mv_stats + 2))
+      if (plan->lmv_beams >= 0) {
+        if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate, counters,
+                                         gated, static_cast<int>(nrows), plan->d_mv_stats + 2))
+          return rc;
+      } else if (int rc = launch_lmv_apply(ctx, net, avg, meta, b.out, b.out_stride, b.n_pix, nf, plan->lmv_gate,
+                                           counters, gated, static_cast<int>(nrows), plan->d_mv_stats + 2)) {
         return rc;
+      }
       MvTcExtra ex;
       ex.list = gated;
       ex.list_count = counters;
@@ -1064,6 +1093,72 @@ int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode) {
   return USX_OK;
 }
 
+int usx_cu_bf_variant_count(void) { return kNumDasVariants; }
+
+int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks) {
+  if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_info: no such variant");
+  if (channel_group) *channel_group = kDasVariants[index].group;
+  if (tile_lines) *tile_lines = kDasVariants[index].tile_lines;
+  if (min_blocks) *min_blocks = kDasVariants[index].min_blocks;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_variant: null plan");
+  if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_variant: no such variant");
+  plan->das_variant = index;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index) {
+  if (!plan || !index) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_get_variant: null argument");
+  *index = plan->das_variant;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, int repeats, float* ms_out) {
+  if (!plan || !data || !frame) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_autotune: null argument");
+  if (plan->precision != USX_BF_FAST) return USX_OK;  // the exact kernel has one shape
+  usx_ctx* ctx = plan->ctx;
+  const int reps = std::max(1, repeats);
+  cudaEvent_t e0, e1;
+  USX_CUDA(cudaEventCreate(&e0));
+  USX_CUDA(cudaEventCreate(&e1));
+  int best = plan->das_variant;
+  float best_ms = 0.0f;
+  int rc = USX_OK;
+  const bool saved_prof = ctx->profiling;
+  ctx->profiling = false;
+  for (int v = 0; v < kNumDasVariants && rc == USX_OK; ++v) {
+    plan->das_variant = v;
+    rc = bf_execute(plan, 1, data, 0, frame, 0, 0);  // warm-up (first-use set-up, caches)
+    if (rc != USX_OK) break;
+    if (cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(USX_ERR_CUDA, "autotune: event record");
+    for (int r = 0; r < reps && rc == USX_OK; ++r) rc = bf_execute(plan, 1, data, 0, frame, 0, 0);
+    if (rc != USX_OK) break;
+    float ms = 0.0f;
+    if (cudaEventRecord(e1, ctx->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = fail(USX_ERR_CUDA, "autotune: event timing");
+      break;
+    }
+    ms /= static_cast<float>(reps);
+    if (ms_out) ms_out[v] = ms;
+    if (v == 0 || ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  ctx->profiling = saved_prof;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  plan->das_variant = best;
+  if (rc != USX_OK) return rc;
+  // Leave the caller's frame holding the chosen variant's result (all
+  // variants agree bit for bit, so this is the same frame).
+  return bf_execute(plan, 1, data, 0, frame, 0, 0);
+}
+
 int usx_cu_bf_plan_set_precision(usx_bf_plan* plan, int precision) {
   if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_precision: null plan");
   if (precision != USX_BF_FAST && precision != USX_BF_EXACT)
@@ -1092,6 +1187,14 @@ int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate) {
   if (!(gate >= 0.0f)) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned: gate must be >= 0");
   plan->mlp = mlp;
   plan->lmv_gate = gate;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: null plan");
+  if (n_beams > 4 || (n_beams >= 0 && n_beams % 2 != 0))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: n_beams must be negative, 0, 2 or 4");
+  plan->lmv_beams = n_beams < 0 ? -1 : n_beams;
   return USX_OK;
 }
 

@@ -281,6 +281,402 @@ __global__ void __launch_bounds__(256) lmv_apply_kernel(const ApplyArgs a) {
   }
 }
 
+// Learned-subspace refinement (an alternative to lmv_apply_kernel).
+//
+// The network's weights w~ are a guess of the Capon direction R^-1 1. Instead
+// of using them as they are, the pixel solves the Capon problem exactly
+// within the subspace spanned by the DFT beams u_b[i] = e^{j 2 pi b i / L} / sqrt(L),
+// b = 0, +1, -1, ... (n_beams + 1 of them; b = 0 is the look direction) and w~
+// (its part orthogonal to the beams, dropped when negligible):
+//   minimise w^H R~ w subject to 1^H w = 1, w = Q c,
+//   (Q^H R Q + eps I) c = Q^H 1,   eps = max(delta tr(R) / L, 1e-20),
+// with R the spatially smoothed, range-averaged covariance of the reference's
+// minimum variance (beamformer.cpp:158-187) applied through its snapshots
+// y_s = y_d[s0 .. s0 + L), never formed. The beams are orthonormal, so their
+// snapshot projections are window sums of e^{-j w t} y_d[t], i.e. differences
+// of one prefix sum per beam and range row (O(1) per snapshot); only w~
+// costs L multiply-adds per snapshot. If w~ is the Capon direction the result
+// is the exact minimum variance; in every case it is distortionless, and its
+// output power is at most that of DAS (w = 1/L) and of w~. The gate on the
+// network's distortionless residual |1^H w~ / L - 1| comes first; gated
+// pixels go to the exact solver.
+constexpr int kSubMaxBeams = 5;            // b = 0, +1, -1, +2, -2
+constexpr int kSubMaxK = kSubMaxBeams + 1; // plus the network's direction
+constexpr int kSubWarps = 4;
+constexpr int kSubMaxN = 128;              // active channels
+
+struct SubArgs {
+  const float2* y;        // [frame][pix][n_ch]
+  const float* points;
+  const float* net;       // [row][128]
+  const float2* avg;      // [row][64] subarray-averaged snapshot of the centre row
+  const float4* meta;     // [row] (L, n_act, cf, 0)
+  float2* out;
+  long out_stride;
+  int n_ch, n_pix, n1, n_dmax;
+  long n_rows;
+  int range_avg, n_beams;
+  float f_number, tukey_alpha, half_nm1, pitch, loading, gate;
+  int rx_window;
+  int* gated_count;
+  int2* gated;
+  int gated_cap;
+  int* stats;
+};
+
+// Per-warp shared memory; the range rows follow it (n_dmax x kSubMaxN).
+struct SubWarpSmem {
+  float2 pre[kSubMaxBeams][kSubMaxN + 1];   // prefix sums of one row, per beam
+  float2 tw[kSubMaxBeams][kSubMaxN];        // e^{-j 2 pi b t / L}
+  float2 wq[kLmvMaxL];                      // the network's direction, orthogonalised
+  int act[kSubMaxN];
+  float2 rows[1][kSubMaxN];                 // [n_dmax][kSubMaxN] range rows, active channels
+};
+__host__ __device__ constexpr size_t sub_warp_bytes(int n_dmax) {
+  return (sizeof(SubWarpSmem) + sizeof(float2) * kSubMaxN * (n_dmax - 1) + 15) / 16 * 16;
+}
+
+__device__ __forceinline__ float2 warp_sum2(float2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+__device__ __forceinline__ int beam_index(int k) { return (k + 1) / 2 * ((k & 1) ? 1 : -1); }  // 0,1,-1,2,-2
+
+__global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubArgs a) {
+  extern __shared__ float4 sub_smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  SubWarpSmem& sm = *reinterpret_cast<SubWarpSmem*>(reinterpret_cast<char*>(sub_smem_raw) +
+                                                   warp * sub_warp_bytes(a.n_dmax));
+  float2* srow = &sm.rows[0][0];  // [n_dmax][kSubMaxN]
+  const int nb_all = min(kSubMaxBeams, 1 + a.n_beams);
+
+  for (long row = static_cast<long>(blockIdx.x) * kSubWarps + warp; row < a.n_rows;
+       row += static_cast<long>(gridDim.x) * kSubWarps) {
+    const float4 meta = a.meta[row];
+    const int L = static_cast<int>(meta.x);
+    if (L == 0) continue;  // n_act < 4: written by the feature pass
+    const long frame = row / a.n_pix;
+    const int pix = static_cast<int>(row - frame * a.n_pix);
+    // The first nb of b = 0, 1, -1, 2, -2 are distinct modulo L when nb <= L;
+    // with nb = L they span every length-L vector (the exact solve).
+    const int nb = min(nb_all, L);
+    // The network's weights (lane holds i = 2 lane, 2 lane + 1) and the gate.
+    const float4 o = reinterpret_cast<const float4*>(a.net + row * kLmvOut)[lane];
+    const float inv_l = 1.0f / static_cast<float>(L);
+    float2 w0 = make_float2(0.f, 0.f), w1 = make_float2(0.f, 0.f);
+    if (2 * lane < L) w0 = make_float2(o.x * inv_l, o.y * inv_l);
+    if (2 * lane + 1 < L) w1 = make_float2(o.z * inv_l, o.w * inv_l);
+    const float2 sw = warp_sum2(make_float2(w0.x + w1.x, w0.y + w1.y));
+    const float res = sqrtf((sw.x - 1.f) * (sw.x - 1.f) + sw.y * sw.y);
+    if (!(res <= a.gate)) {
+      if (lane == 0) {
+        const int slot = atomicAdd(a.gated_count, 1);
+        if (slot < a.gated_cap) a.gated[slot] = make_int2(pix, static_cast<int>(frame));
+        if (a.stats) atomicAdd(a.stats, 1);
+      }
+      continue;
+    }
+    __syncwarp();
+    // Twiddles e^{-j 2 pi b t / L}, t < 128, argument reduced to one turn.
+    for (int e = lane; e < nb * kSubMaxN; e += 32) {
+      const int k = e / kSubMaxN, t = e - k * kSubMaxN;
+      const int b = beam_index(k);
+      const int r = ((b * t) % L + L) % L;
+      float sn, cs;
+      sincospif(2.0f * static_cast<float>(r) * inv_l, &sn, &cs);
+      sm.tw[k][t] = make_float2(cs, -sn);
+    }
+    // w~ minus its projections on the beams: c_b = u_b^H w~ (u_b = conj(tw_b) / sqrt(L)).
+    const float rs = rsqrtf(static_cast<float>(L));
+    __syncwarp();
+    float2 wv[2];
+    {
+      const int i0 = 2 * lane;
+      wv[0] = w0;
+      wv[1] = w1;
+      float2 cb[kSubMaxBeams];
+#pragma unroll
+      for (int k = 0; k < kSubMaxBeams; ++k) {
+        float2 d = make_float2(0.f, 0.f);
+        if (k < nb) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int i = i0 + h;
+            if (i < L) {  // conj(u_b[i]) w~_i = tw_b[i] w~_i / sqrt(L)
+              const float2 t = sm.tw[k][i];
+              d.x += (t.x * wv[h].x - t.y * wv[h].y) * rs;
+              d.y += (t.x * wv[h].y + t.y * wv[h].x) * rs;
+            }
+          }
+        }
+        cb[k] = warp_sum2(d);
+      }
+      float n0 = w0.x * w0.x + w0.y * w0.y + w1.x * w1.x + w1.y * w1.y;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = i0 + h;
+        if (i >= L) continue;
+#pragma unroll
+        for (int k = 0; k < kSubMaxBeams; ++k) {
+          if (k >= nb) continue;
+          const float2 t = sm.tw[k][i];  // u_b[i] = conj(t) / sqrt(L)
+          const float ux = t.x * rs, uy = -t.y * rs;
+          wv[h].x -= cb[k].x * ux - cb[k].y * uy;
+          wv[h].y -= cb[k].x * uy + cb[k].y * ux;
+        }
+      }
+      for (int o2 = 16; o2 > 0; o2 >>= 1) n0 += __shfl_xor_sync(0xffffffffu, n0, o2);
+      float n1 = wv[0].x * wv[0].x + wv[0].y * wv[0].y + wv[1].x * wv[1].x + wv[1].y * wv[1].y;
+      for (int o2 = 16; o2 > 0; o2 >>= 1) n1 += __shfl_xor_sync(0xffffffffu, n1, o2);
+      const float sc = (n0 > 0.f && n1 > 1e-4f * n0) ? rsqrtf(n1) : 0.f;
+      if (i0 < kLmvMaxL) sm.wq[i0] = make_float2(wv[0].x * sc, wv[0].y * sc);
+      if (i0 + 1 < kLmvMaxL) sm.wq[i0 + 1] = make_float2(wv[1].x * sc, wv[1].y * sc);
+      wv[0] = make_float2(wv[0].x * sc, wv[0].y * sc);
+      wv[1] = make_float2(wv[1].x * sc, wv[1].y * sc);
+    }
+    const bool has_w =
+        __any_sync(0xffffffffu, wv[0].x != 0.f || wv[0].y != 0.f || wv[1].x != 0.f || wv[1].y != 0.f);
+
+    // Active aperture and the range rows of the smoothing window.
+    const int j = pix % a.n1;
+    const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+    int n_act = 0;
+    for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+      const int ch = c0 + lane;
+      bool on = false;
+      if (ch < a.n_ch)
+        on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                             a.tukey_alpha) > 0.0f;
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      const int slot = n_act + __popc(m & ((1u << lane) - 1u));
+      if (on && slot < kSubMaxN) sm.act[slot] = ch;
+      n_act += __popc(m);
+    }
+    n_act = min(n_act, kSubMaxN);
+    __syncwarp();
+    const int n_sub = n_act - L + 1;
+    int dlo = -a.range_avg, dhi = a.range_avg;
+    while (j + dlo < 0) ++dlo;
+    while (j + dhi >= a.n1) --dhi;
+    const int n_d = dhi - dlo + 1;
+    for (int k = lane; k < n_d * n_act; k += 32) {
+      const int d = k / n_act, q = k - d * n_act;
+      srow[d * kSubMaxN + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + sm.act[q]];
+    }
+    __syncwarp();
+
+    // Trace of the covariance (times K): every sample weighted by the number
+    // of subarrays that contain it.
+    float tr = 0.f;
+    for (int k = lane; k < n_d * n_act; k += 32) {
+      const int d = k / n_act, t = k - d * n_act;
+      const float2 yv = srow[d * kSubMaxN + t];
+      const int c = min(t, n_sub - 1) - max(0, t - L + 1) + 1;
+      tr = fmaf(static_cast<float>(c), fmaf(yv.x, yv.x, yv.y * yv.y), tr);
+    }
+    for (int o2 = 16; o2 > 0; o2 >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o2);
+    const float K = static_cast<float>(n_d * n_sub);
+
+    // G = sum_s z_s z_s^H over the snapshots, z = (beams..., w_q)^H y_s.
+    constexpr int kG = kSubMaxK * (kSubMaxK + 1);  // upper triangle, (re, im)
+    float g[kG];
+#pragma unroll
+    for (int e = 0; e < kG; ++e) g[e] = 0.f;
+    for (int d = 0; d < n_d; ++d) {
+      // Prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y_d[t'] (warp scans, 32 at a time).
+      float2 carry[kSubMaxBeams];
+#pragma unroll
+      for (int k = 0; k < kSubMaxBeams; ++k) carry[k] = make_float2(0.f, 0.f);
+      if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < kSubMaxBeams; ++k)
+          if (k < nb) sm.pre[k][0] = make_float2(0.f, 0.f);
+      for (int t0 = 0; t0 < n_act; t0 += 32) {
+        const int t = t0 + lane;
+        const float2 yv = t < n_act ? srow[d * kSubMaxN + t] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kSubMaxBeams; ++k) {
+          if (k >= nb) continue;
+          const float2 tw = t < n_act ? sm.tw[k][t] : make_float2(1.f, 0.f);
+          float2 v = make_float2(tw.x * yv.x - tw.y * yv.y, tw.x * yv.y + tw.y * yv.x);
+          for (int o2 = 1; o2 < 32; o2 <<= 1) {
+            const float px2 = __shfl_up_sync(0xffffffffu, v.x, o2), py2 = __shfl_up_sync(0xffffffffu, v.y, o2);
+            if (lane >= o2) {
+              v.x += px2;
+              v.y += py2;
+            }
+          }
+          v.x += carry[k].x;
+          v.y += carry[k].y;
+          if (t < n_act) sm.pre[k][t + 1] = v;
+          carry[k] = make_float2(__shfl_sync(0xffffffffu, v.x, 31), __shfl_sync(0xffffffffu, v.y, 31));
+        }
+      }
+      __syncwarp();
+      const float2* yr = srow + d * kSubMaxN;
+      for (int s0 = lane; s0 < n_sub; s0 += 32) {
+        float2 z[kSubMaxK];
+        // Beams: u_b^H y_s = conj(tw_b[s0]) (P_b[s0 + L] - P_b[s0]) / sqrt(L).
+#pragma unroll
+        for (int k = 0; k < kSubMaxBeams; ++k) {
+          z[k] = make_float2(0.f, 0.f);
+          if (k >= nb) continue;
+          const float2 hi = sm.pre[k][s0 + L], lo = sm.pre[k][s0];
+          const float2 df = make_float2((hi.x - lo.x) * rs, (hi.y - lo.y) * rs);
+          const float2 t = sm.tw[k][s0];
+          z[k] = make_float2(t.x * df.x + t.y * df.y, t.x * df.y - t.y * df.x);
+        }
+        // The network's direction: w_q^H y_s.
+        float2 zw = make_float2(0.f, 0.f);
+        if (has_w)
+          for (int i = 0; i < L; ++i) {
+            const float2 q = sm.wq[i], yv = yr[s0 + i];
+            zw.x = fmaf(q.x, yv.x, fmaf(q.y, yv.y, zw.x));
+            zw.y = fmaf(q.x, yv.y, fmaf(-q.y, yv.x, zw.y));
+          }
+        z[kSubMaxBeams] = zw;
+        int e = 0;
+#pragma unroll
+        for (int r = 0; r < kSubMaxK; ++r)
+#pragma unroll
+          for (int c = r; c < kSubMaxK; ++c, e += 2) {
+            g[e] = fmaf(z[r].x, z[c].x, fmaf(z[r].y, z[c].y, g[e]));      // z_r conj(z_c)
+            g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
+          }
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int e = 0; e < kG; ++e)
+      for (int o2 = 16; o2 > 0; o2 >>= 1) g[e] += __shfl_xor_sync(0xffffffffu, g[e], o2);
+
+    // Basis in use: beams k < nb, and w_q if it survived.
+    bool keep[kSubMaxK];
+#pragma unroll
+    for (int k = 0; k < kSubMaxBeams; ++k) keep[k] = k < nb;
+    keep[kSubMaxBeams] = has_w;
+    // Right-hand side Q^H 1: sqrt(L) for the look direction, 0 for the other
+    // beams; w_q^H 1 for the network's direction.
+    float2 bq[kSubMaxK];
+#pragma unroll
+    for (int k = 0; k < kSubMaxK; ++k) bq[k] = make_float2(0.f, 0.f);
+    bq[0] = make_float2(sqrtf(static_cast<float>(L)), 0.f);
+    {
+      float2 sq = make_float2(0.f, 0.f);
+      if (2 * lane < L) sq = make_float2(wv[0].x, -wv[0].y);
+      if (2 * lane + 1 < L) sq = make_float2(sq.x + wv[1].x, sq.y - wv[1].y);
+      bq[kSubMaxBeams] = warp_sum2(sq);
+    }
+
+    // Solve (G / K + eps I) c = b in every lane (complex Cholesky, k <= 6).
+    const float eps = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);
+    float2 A[kSubMaxK][kSubMaxK];
+    {
+      int e = 0;
+#pragma unroll
+      for (int r = 0; r < kSubMaxK; ++r)
+#pragma unroll
+        for (int c = r; c < kSubMaxK; ++c, e += 2) {
+          float2 x = make_float2(g[e] / K, g[e + 1] / K);
+          if (r == c) x = make_float2(x.x + eps, 0.f);
+          if (!(keep[r] && keep[c])) x = (r == c) ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+          A[r][c] = x;
+          A[c][r] = make_float2(x.x, -x.y);
+        }
+    }
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < kSubMaxK; ++c) {
+      float dsum = A[c][c].x;
+#pragma unroll
+      for (int k = 0; k < kSubMaxK; ++k)
+        if (k < c) dsum -= A[c][k].x * A[c][k].x + A[c][k].y * A[c][k].y;
+      ok = ok && dsum > 0.f;
+      const float lc = sqrtf(fmaxf(dsum, 1e-30f));
+      A[c][c] = make_float2(lc, 0.f);
+      const float il = 1.0f / lc;
+#pragma unroll
+      for (int r = 0; r < kSubMaxK; ++r) {
+        if (r <= c) continue;
+        float2 s = A[r][c];
+#pragma unroll
+        for (int k = 0; k < kSubMaxK; ++k)
+          if (k < c) {  // s -= L[r][k] conj(L[c][k])
+            s.x -= A[r][k].x * A[c][k].x + A[r][k].y * A[c][k].y;
+            s.y -= A[r][k].y * A[c][k].x - A[r][k].x * A[c][k].y;
+          }
+        A[r][c] = make_float2(s.x * il, s.y * il);
+      }
+    }
+    float2 cv[kSubMaxK];
+#pragma unroll
+    for (int r = 0; r < kSubMaxK; ++r) {  // forward: L u = b
+      float2 s = keep[r] ? bq[r] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < kSubMaxK; ++k)
+        if (k < r) {
+          s.x -= A[r][k].x * cv[k].x - A[r][k].y * cv[k].y;
+          s.y -= A[r][k].x * cv[k].y + A[r][k].y * cv[k].x;
+        }
+      cv[r] = make_float2(s.x / A[r][r].x, s.y / A[r][r].x);
+    }
+#pragma unroll
+    for (int r = kSubMaxK - 1; r >= 0; --r) {  // backward: L^H c = u
+      float2 s = cv[r];
+#pragma unroll
+      for (int k = 0; k < kSubMaxK; ++k)
+        if (k > r) {  // s -= conj(L[k][r]) c_k
+          s.x -= A[k][r].x * cv[k].x + A[k][r].y * cv[k].y;
+          s.y -= A[k][r].x * cv[k].y - A[k][r].y * cv[k].x;
+        }
+      cv[r] = make_float2(s.x / A[r][r].x, s.y / A[r][r].x);
+    }
+    // w = Q c; output n_act * (w^H abar) / (1^H w) with the coherence factor.
+    const float4 av4 = reinterpret_cast<const float4*>(a.avg + row * kLmvMaxL)[lane];
+    float2 num = make_float2(0.f, 0.f), den = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = 2 * lane + h;   // the element this lane holds in wv[h] and av4
+      if (i >= L) continue;
+      float2 w = make_float2(wv[h].x * cv[kSubMaxBeams].x - wv[h].y * cv[kSubMaxBeams].y,
+                             wv[h].x * cv[kSubMaxBeams].y + wv[h].y * cv[kSubMaxBeams].x);
+#pragma unroll
+      for (int k = 0; k < kSubMaxBeams; ++k) {
+        if (k >= nb) continue;
+        const float2 t = sm.tw[k][i];  // u_b[i] = conj(t) / sqrt(L)
+        const float ux = t.x * rs, uy = -t.y * rs;
+        w.x += ux * cv[k].x - uy * cv[k].y;
+        w.y += ux * cv[k].y + uy * cv[k].x;
+      }
+      const float ax = h ? av4.z : av4.x, ay = h ? av4.w : av4.y;
+      num.x = fmaf(w.x, ax, fmaf(w.y, ay, num.x));   // conj(w) abar
+      num.y = fmaf(w.x, ay, fmaf(-w.y, ax, num.y));
+      den.x += w.x;
+      den.y += w.y;
+    }
+    num = warp_sum2(num);
+    den = warp_sum2(den);
+    if (lane == 0) {
+      const float dn = den.x * den.x + den.y * den.y;
+      if (!ok || !(dn > 1e-30f)) {
+        const int slot = atomicAdd(a.gated_count, 1);
+        if (slot < a.gated_cap) a.gated[slot] = make_int2(pix, static_cast<int>(frame));
+        if (a.stats) atomicAdd(a.stats, 1);
+      } else {
+        const float scale = meta.y * meta.z / dn;   // n_act * cf * num / den
+        a.out[frame * a.out_stride + pix] =
+            make_float2((num.x * den.x + num.y * den.y) * scale, (num.y * den.x - num.x * den.y) * scale);
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace
 
 int lmv_features_smem(int n_ch, int range_avg) {
@@ -347,6 +743,51 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
   lmv_apply_kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 256, 0, ctx->stream>>>(a);
   prof_end(ctx);
   USX_CHECK_LAUNCH("lmv_apply_kernel");
+  return USX_OK;
+}
+
+
+int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
+                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats) {
+  SubArgs a;
+  a.y = l.y;
+  a.points = l.points;
+  a.net = net;
+  a.avg = l.avg;
+  a.meta = l.meta;
+  a.out = l.out;
+  a.out_stride = l.out_stride;
+  a.n_ch = l.n_ch;
+  a.n_pix = l.n_pix;
+  a.n1 = l.n1;
+  a.n_dmax = 2 * l.range_avg + 1;
+  a.n_rows = static_cast<long>(l.n_frames) * l.n_pix;
+  a.range_avg = l.range_avg;
+  a.n_beams = n_beams;
+  a.f_number = l.f_number;
+  a.tukey_alpha = l.tukey_alpha;
+  a.half_nm1 = l.half_nm1;
+  a.pitch = l.pitch;
+  a.loading = loading;
+  a.gate = gate;
+  a.rx_window = l.rx_window;
+  a.gated_count = gated_count;
+  a.gated = gated;
+  a.gated_cap = gated_cap;
+  a.stats = stats;
+  if (l.n_ch > kSubMaxN || a.n_dmax > 9)
+    return fail(USX_ERR_UNSUPPORTED, "learned-subspace refinement supports <= 128 channels, range average <= 4");
+  const int smem = static_cast<int>(sub_warp_bytes(a.n_dmax) * kSubWarps);
+  USX_CUDA(cudaFuncSetAttribute(lmv_subspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int per_sm = 0;
+  USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lmv_subspace_kernel, 32 * kSubWarps, smem));
+  const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
+  const long need = (a.n_rows + kSubWarps - 1) / kSubWarps;
+  prof_begin(ctx, "lmv_subspace_kernel");
+  lmv_subspace_kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem,
+                        ctx->stream>>>(a);
+  prof_end(ctx);
+  USX_CHECK_LAUNCH("lmv_subspace_kernel");
   return USX_OK;
 }
 

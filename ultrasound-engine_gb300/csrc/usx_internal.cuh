@@ -266,6 +266,11 @@ int launch_lmv_features(usx_ctx* ctx, const LmvLaunch& l);
 int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const float4* meta, float2* out,
                      long out_stride, int n_pix, int n_frames, float gate, int* gated_count, int2* gated,
                      int gated_cap, int* stats);
+// Learned-subspace refinement: gate on the network's distortionless residual,
+// then the exact Capon solve within span{1, network weights, n_beams DFT
+// beams} through the pixel's snapshots (learned.cu).
+int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
+                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats);
 
 // The network (mlp.cu). mlp_infer runs `rows` (a multiple of 128) BF16 input
 // rows through every layer with caller scratch t0, t1 (rows x widest BF16

@@ -36,13 +36,16 @@ namespace {
 
 // The learned minimum-variance network of a context: read once from
 // USX_LEARNED_MV_WEIGHTS, else the weights shipped beside the library
-// (<package>/weights/learned_mv_128ch_l64.bin); its gate from
-// USX_LEARNED_MV_GATE, else the ".gate" file written with the weights, else
-// 0.05. The file is the trainer's raw format: "USXMLP1\0", int32 n_layers,
-// int32 dims[n_layers + 1], float32 parameters.
+// (<package>/weights/learned_mv_128ch_l64.bin); its gate and subspace
+// refinement from the ".gate" file written with the weights ("<gate>
+// [<beams>]"), overridden by USX_LEARNED_MV_GATE / USX_LEARNED_MV_REFINE;
+// without either, gate 0.05 and no refinement. The weights file is the
+// trainer's raw format: "USXMLP1\0", int32 n_layers, int32 dims[n_layers + 1],
+// float32 parameters.
 struct LearnedNet {
   usx_mlp* mlp = nullptr;
   float gate = 0.05f;
+  int refine = -1;   // DFT beams of the subspace refinement (< 0: none)
 };
 
 std::string library_dir() {
@@ -82,13 +85,16 @@ LearnedNet learned_net(usx_ctx* ctx) {
   LearnedNet net;
   rt::check(usx_cu_mlp_create(ctx, n_layers, dims.data(), 0, &net.mlp), "learned network");
   rt::check(usx_cu_mlp_set_params(net.mlp, params.data()), "learned network weights");
-  if (const char* g = std::getenv("USX_LEARNED_MV_GATE")) {
-    net.gate = std::strtof(g, nullptr);
-  } else {
+  {
+    // "<gate> [<refine beams>]", as written by the trainer's evaluation.
     std::ifstream gf(path.substr(0, path.size() - 4) + ".gate");
-    float gv = 0.0f;
-    if (gf >> gv) net.gate = gv;
+    std::string gs;
+    if (gf >> gs) net.gate = std::strtof(gs.c_str(), nullptr);
+    int rv = 0;
+    if (gf >> rv) net.refine = rv;
   }
+  if (const char* g = std::getenv("USX_LEARNED_MV_GATE")) net.gate = std::strtof(g, nullptr);
+  if (const char* r = std::getenv("USX_LEARNED_MV_REFINE")) net.refine = std::atoi(r);
   nets.emplace(ctx, net);
   return net;
 }
@@ -174,6 +180,7 @@ class PlanCache {
       try {
         const LearnedNet net = learned_net(key.ctx);
         rt::check(usx_cu_bf_plan_set_learned(plan, net.mlp, net.gate), "learned minimum variance");
+        rt::check(usx_cu_bf_plan_set_learned_refine(plan, net.refine), "learned minimum variance refinement");
       } catch (...) {
         usx_cu_bf_plan_destroy(plan);
         throw;

@@ -326,6 +326,28 @@ class Plan:
               "bf_plan_set_learned")
         self._mlp = mlp
 
+    def autotune(self, data_ptr: int, frame_ptr: int, repeats: int = 2):
+        """Time every delay-and-sum variant on this acquisition, keep the
+        fastest; returns (chosen index, [ms per variant])."""
+        n = lib().usx_cu_bf_variant_count()
+        ms = (C.c_float * n)()
+        check(lib().usx_cu_bf_plan_autotune(self._h, vp(data_ptr), vp(frame_ptr), int(repeats), ms),
+              "bf_plan_autotune")
+        return self.variant(), list(ms)
+
+    def variant(self) -> int:
+        v = C.c_int()
+        check(lib().usx_cu_bf_plan_get_variant(self._h, C.byref(v)), "bf_plan_get_variant")
+        return v.value
+
+    def set_variant(self, index: int) -> None:
+        check(lib().usx_cu_bf_plan_set_variant(self._h, int(index)), "bf_plan_set_variant")
+
+    def set_learned_refine(self, n_beams: int) -> None:
+        """Negative: the network's weights as predicted; 0, 2, 4: exact Capon
+        solve within span{1, network weights, n_beams DFT beams}."""
+        check(lib().usx_cu_bf_plan_set_learned_refine(self._h, int(n_beams)), "bf_plan_set_learned_refine")
+
     def learned_stats(self):
         """(pixels gated to the exact solver, pixels beamformed) since the last call."""
         a, b = C.c_int64(), C.c_int64()
@@ -433,6 +455,16 @@ class Mlp:
             self.close()
         except Exception:
             pass
+
+
+def das_variants() -> list:
+    """(channel group, tile lines, min resident CTAs) of each delay-and-sum variant."""
+    out = []
+    for i in range(lib().usx_cu_bf_variant_count()):
+        g, t, m = C.c_int(), C.c_int(), C.c_int()
+        check(lib().usx_cu_bf_variant_info(i, C.byref(g), C.byref(t), C.byref(m)), "bf_variant_info")
+        out.append((g.value, t.value, m.value))
+    return out
 
 
 def profile(ctx: Context, on: bool = True) -> None:

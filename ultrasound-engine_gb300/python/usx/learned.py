@@ -34,6 +34,9 @@ from . import capi
 DIMS = (256, 256, 256, 256, 128)
 FEATURES, OUTPUTS = DIMS[0], DIMS[-1]
 DEFAULT_GATE = 0.05
+# Subspace refinement: the exact Capon solve within span{network weights,
+# look direction, DFT beams +-1, +-2} (usx_cu_bf_plan_set_learned_refine).
+DEFAULT_REFINE = 4
 COMB_MV, COMB_LEARNED_MV = 2, 3
 MAGIC = b"USXMLP1\0"
 DEFAULT_WEIGHTS = Path(__file__).resolve().parents[2] / "weights" / "learned_mv_128ch_l64.bin"
@@ -349,10 +352,12 @@ def image_metrics(frame, imager: Imager, spec: PhantomSpec) -> dict:
     return out
 
 
-def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=print) -> dict:
+def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=print,
+             refine: int = DEFAULT_REFINE) -> dict:
     """Image metrics of plain MV and of the learned MV at each gate on the
     held-out phantoms `seeds`: {gate: summary}."""
     learned = imager.plan(COMB_LEARNED_MV)
+    learned.set_learned_refine(refine)
     rows = {g: [] for g in gates}
     for s in seeds:
         spec = phantom(int(s), imager.setup)
@@ -376,9 +381,22 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=pr
     return {g: summarize(r) for g, r in rows.items()}
 
 
+def meets_bar(r: dict, max_dgcnr: float = 0.01, max_fwhm: float = 0.01) -> bool:
+    """Held-out summary within the quality bar: every cyst's |delta gCNR| <=
+    max_dgcnr and the mean lateral and axial FWHM within max_fwhm (relative)
+    of plain minimum variance."""
+    if r.get("gcnr", {}).get("max_abs_delta", 1.0) > max_dgcnr:
+        return False
+    for k in ("lateral_fwhm_mm", "axial_fwhm_mm"):
+        m = r.get(k)
+        if m and abs(m["learned_mean"] - m["plain_mean"]) > max_fwhm * abs(m["plain_mean"]):
+            return False
+    return True
+
+
 def choose_gate(results: dict, max_dgcnr: float = 0.01) -> float | None:
-    """The largest gate whose held-out max |delta gCNR| stays within max_dgcnr."""
-    ok = [g for g, r in results.items() if r.get("gcnr", {}).get("max_abs_delta", 1.0) <= max_dgcnr]
+    """The largest gate whose held-out summary meets the quality bar."""
+    ok = [g for g, r in results.items() if meets_bar(r, max_dgcnr)]
     return max(ok) if ok else None
 
 
@@ -422,7 +440,9 @@ def main(argv=None) -> None:
     e.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
     e.add_argument("--phantoms", type=int, default=16)
     for p in (t, e):
-        p.add_argument("--gates", default="0.005,0.01,0.02,0.03,0.05,0.1")
+        p.add_argument("--gates", default="0.01,0.03,0.1,0.3,1,inf")
+        p.add_argument("--refine", type=int, default=DEFAULT_REFINE,
+                       help="DFT beams beside the network's direction (-1: no refinement)")
         p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
     a = ap.parse_args(argv)
     gates = tuple(float(g) for g in a.gates.split(","))
@@ -448,26 +468,39 @@ def main(argv=None) -> None:
     else:
         out = Path(a.weights)
         mlp = load_mlp(imager.ctx, out)
-    results = evaluate(imager, mlp, eval_seeds, gates)
+        prev = Path(a.report) if a.report else out.with_suffix(".json")
+        if prev.exists():  # keep the training record, replace the evaluation
+            report = {**json.loads(prev.read_text()), **report}
+    results = evaluate(imager, mlp, eval_seeds, gates, refine=a.refine)
+    report["refine"] = a.refine
     report["eval"] = {str(g): {k: v for k, v in r.items() if k != "rows"} for g, r in results.items()}
-    report["eval_rows"] = {str(g): r["rows"] for g, r in results.items()}
     report["gate"] = choose_gate(results)
     path = Path(a.report) if a.report else out.with_suffix(".json")
     path.write_text(json.dumps(report, indent=1, default=float))
     if report["gate"] is not None:
-        out.with_suffix(".gate").write_text(f"{report['gate']}\n")
+        out.with_suffix(".gate").write_text(f"{report['gate']} {a.refine}\n")
     print(json.dumps({"gate": report["gate"], "eval": report["eval"]}, default=float))
     imager.close()
 
 
 def trained_gate(weights=DEFAULT_WEIGHTS) -> float:
-    """The gate chosen when the weights were trained (their JSON report)."""
+    """The gate chosen when the weights were evaluated (their JSON report)."""
     p = Path(weights).with_suffix(".json")
     if p.exists():
         g = json.loads(p.read_text()).get("gate")
         if g is not None:
             return float(g)
     return DEFAULT_GATE
+
+
+def trained_refine(weights=DEFAULT_WEIGHTS) -> int:
+    """The refinement the weights were evaluated with (their JSON report)."""
+    p = Path(weights).with_suffix(".json")
+    if p.exists():
+        r = json.loads(p.read_text()).get("refine")
+        if r is not None:
+            return int(r)
+    return -1
 
 
 if __name__ == "__main__":
