@@ -342,11 +342,12 @@ def run_ours(args) -> None:
         if not WEIGHTS.exists():
             raise SystemExit(f"bench: the learned workload needs the trained network {WEIGHTS}")
         mlp = learned.load_mlp(ctx, WEIGHTS)
-        gate = learned.trained_gate(WEIGHTS)
-        refine = learned.trained_refine(WEIGHTS)
+        gate = learned.trained_gate(WEIGHTS) if args.gate is None else args.gate
+        refine = learned.trained_refine(WEIGHTS) if args.refine is None else args.refine
         # Plain minimum variance (tensor-core solver) on the same frame, timed first.
         plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
         plain.set_mv_mode(1)
+        plain.autotune(d_iq.data_ptr(), frame.data_ptr(), repeats=1)
         for _ in range(args.warmup):
             plain.execute(d_iq.data_ptr(), frame.data_ptr())
         ctx.synchronize()
@@ -365,6 +366,10 @@ def run_ours(args) -> None:
         if args.workload == "mv":
             plan.set_mv_mode(1)
 
+    # The plan's autotuner picks the delay-and-sum launch shape on this acquisition.
+    best, tune_ms = plan.autotune(d_iq.data_ptr(), frame.data_ptr(), repeats=2)
+    extra["das_variant"] = {"chosen": capi.das_variants()[best], "ms_per_variant": tune_ms,
+                            "variants": capi.das_variants()}
     for _ in range(args.warmup):
         plan.execute(d_iq.data_ptr(), frame.data_ptr())
     ctx.synchronize()
@@ -552,6 +557,8 @@ def main() -> int:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="learned", choices=sorted(WORKLOADS) + ["simulate", "demod"])
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
+    ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
+    ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -241,8 +241,14 @@ int usx_cu_mlp_train_step(usx_mlp* mlp, const float* x, const float* target, con
  *     and the mask selecting i < L, the squared error of the combiner output
  *     sum conj(w) a / conj(sum w) against the same with t, plus the squared
  *     distortionless residual |sum w / L - 1|^2, plus beta * sum mask
- *     |w - t|^2; the sum over rows divided by rows. */
-enum { USX_MLP_LOSS_MSE = 0, USX_MLP_LOSS_LMV_OUTPUT = 1 };
+ *     |w - t|^2; the sum over rows divided by rows;
+ *   USX_MLP_LOSS_LMV_SUBSPACE  for the learned-subspace refinement (256 -> 128):
+ *     per row, with P the projector onto the complement of the DFT beams
+ *     b = 0, +1, -1, +2, -2 of length L (the first min(5, L)), u = P w,
+ *     v = P t: 1 - |u^H v|^2 / (|u|^2 |v|^2) (skipped where the target lies in
+ *     the beams' span) plus beta * sum mask |w - t|^2 / L; summed over rows
+ *     and divided by rows. */
+enum { USX_MLP_LOSS_MSE = 0, USX_MLP_LOSS_LMV_OUTPUT = 1, USX_MLP_LOSS_LMV_SUBSPACE = 2 };
 int usx_cu_mlp_set_loss(usx_mlp* mlp, int kind, float beta);
 
 /* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one

@@ -116,6 +116,50 @@ def lmv_output_loss(y, t, mask, x, beta):
     return loss, out
 
 
+def _beam_basis(L):
+    """Columns u_b[i] = e^{j 2 pi b i / L} / sqrt(L), b = 0, 1, -1, 2, -2 (first min(5, L))."""
+    i = np.arange(L)
+    bs = [0, 1, -1, 2, -2][:min(5, L)]
+    return np.stack([np.exp(2j * np.pi * b * i / L) / np.sqrt(L) for b in bs], 1)
+
+
+def lmv_subspace_loss(y, t, mask, beta):
+    """Learned-subspace loss and its gradient with respect to y (float64).
+
+    Per row, with L the masked count, w / tt the predicted / target complex
+    weights i < L and P the projector onto the complement of the first
+    min(5, L) DFT beams: u = P w, v = P tt,
+    loss = 1 - |u^H v|^2 / (|u|^2 |v|^2) (0 where |v|^2 <= 1e-8 |tt|^2)
+           + beta * sum |w - tt|^2 / L, averaged over rows."""
+    y = np.asarray(y, np.float64)
+    t = np.asarray(t, np.float64)
+    m = np.asarray(mask, np.float64)[:, 0::2]
+    rows = y.shape[0]
+    total = 0.0
+    out = np.zeros_like(y)
+    for r in range(rows):
+        L = int(round(m[r].sum()))
+        if L == 0:
+            continue
+        w = y[r, 0:2 * L:2] + 1j * y[r, 1:2 * L:2]
+        tt = t[r, 0:2 * L:2] + 1j * t[r, 1:2 * L:2]
+        U = _beam_basis(L)
+        P = np.eye(L) - U @ U.conj().T
+        u, v = P @ w, P @ tt
+        a, b = np.vdot(u, u).real, np.vdot(v, v).real
+        c = np.vdot(u, v)
+        g = np.zeros(L, complex)
+        lr = beta * np.sum(np.abs(w - tt) ** 2) / L
+        if b > 1e-8 * np.vdot(tt, tt).real and a > 1e-30:
+            lr += 1.0 - abs(c) ** 2 / (a * b)
+            g = P @ (-2.0 * (v * np.conj(c) / (a * b) - abs(c) ** 2 * u / (a * a * b)))
+        g = g + 2.0 * beta * (w - tt) / L
+        total += lr
+        out[r, 0:2 * L:2] = g.real / rows
+        out[r, 1:2 * L:2] = g.imag / rows
+    return total / rows, out
+
+
 def backward_from(params, dims, x, g_out, quantize=True):
     """Gradient vector for a given output gradient g_out = dLoss/dy."""
     q = bf16 if quantize else (lambda v: np.asarray(v, np.float64))

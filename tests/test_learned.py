@@ -70,6 +70,32 @@ def test_lmv_output_loss_gradient_matches_finite_differences():
     assert np.all(g[mask == 0] == 0)
 
 
+def test_lmv_subspace_loss_gradient_matches_finite_differences():
+    rng = np.random.default_rng(9)
+    rows = 3
+    y = rng.standard_normal((rows, 128))
+    t = rng.standard_normal((rows, 128))
+    L = np.array([3, 17, 64])
+    mask = (np.arange(128)[None, :] // 2 < L[:, None]).astype(np.float64)
+    loss, g = MO.lmv_subspace_loss(y, t, mask, 0.1)
+    assert loss > 0
+    h = 1e-6
+    for r in range(rows):
+        for k in (0, 1, 4, 5, 2 * L[r] - 1, 2 * L[r] - 2):
+            e = np.zeros_like(y)
+            e[r, k] = h
+            fd = (MO.lmv_subspace_loss(y + e, t, mask, 0.1)[0] - MO.lmv_subspace_loss(y - e, t, mask, 0.1)[0]) / (2 * h)
+            assert abs(fd - g[r, k]) < 1e-6 * max(1.0, abs(fd))
+    assert np.all(g[mask == 0] == 0)
+    # Scale and phase of the complement direction do not matter: a target
+    # equal to (1 + 2j) times the prediction has zero direction loss.
+    w = y[:, 0::2] + 1j * y[:, 1::2]
+    t2 = np.zeros_like(y)
+    t2[:, 0::2], t2[:, 1::2] = ((1 + 2j) * w).real, ((1 + 2j) * w).imag
+    l2, _ = MO.lmv_subspace_loss(y, t2, mask, 0.0)
+    assert l2 < 1e-12
+
+
 def test_weights_file_roundtrip(tmp_path):
     from usx import learned
     rng = np.random.default_rng(0)
@@ -210,6 +236,22 @@ def test_output_loss_gradients_match_oracle(capi, ctx, torch):
     loss, grad = mlp.train_step(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), x.shape[0], 0.0, True, True)
     y, _ = MO.forward(p, DIMS, x, quantize=True)
     want_loss, g_out = MO.lmv_output_loss(y, t, m, x, 0.05)
+    want = MO.backward_from(p, DIMS, x, g_out, quantize=True)
+    assert abs(loss - want_loss) < 2e-3 * want_loss
+    assert rel_l2(grad, want) < 5e-3
+
+
+@pytest.mark.gpu
+def test_subspace_loss_gradients_match_oracle(capi, ctx, torch):
+    """The learned-subspace direction loss kernel and the backward through it."""
+    mlp, p, x, t, m = _net_case(capi, ctx, torch)
+    L = np.random.default_rng(6).integers(2, 65, x.shape[0])
+    m = (np.arange(128)[None, :] // 2 < L[:, None]).astype(np.float32)
+    mlp.set_loss(capi.Mlp.LOSS_LMV_SUBSPACE, 0.05)
+    dx, dt, dm = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (x, t, m))
+    loss, grad = mlp.train_step(dx.data_ptr(), dt.data_ptr(), dm.data_ptr(), x.shape[0], 0.0, True, True)
+    y, _ = MO.forward(p, DIMS, x, quantize=True)
+    want_loss, g_out = MO.lmv_subspace_loss(y, t, m, 0.05)
     want = MO.backward_from(p, DIMS, x, g_out, quantize=True)
     assert abs(loss - want_loss) < 2e-3 * want_loss
     assert rel_l2(grad, want) < 5e-3
@@ -384,17 +426,20 @@ def test_subspace_refinement_matches_oracle(capi, torch, oracle, beams):
                       np.stack([np.asarray(t["delays"], np.float32) for t in tx]),
                       np.stack([np.asarray(t["apodization"], np.float32) for t in tx]))
         cd = O.channel_desc(pr, O.medium(), acq, txs, is_iq=True, fdem=setup.f0)
+        # The oracle in float (its channel samples are the reference's to the
+        # bit); the minimum-variance family amplifies FP32 rounding to ~1e-3
+        # against an FP64 evaluation, so the FP32 oracle is the like-for-like check.
         try:
-            oracle.set_lmv_subspace(v, beams, prec="f64")
-            want = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)),
-                                   prec="f64")
+            oracle.set_lmv_subspace(v, beams, prec="f32")
+            want = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)))
         finally:
-            oracle.set_lmv_subspace(None, -1, prec="f64")
+            oracle.set_lmv_subspace(None, -1, prec="f32")
         got = out[lines]
-        assert rel_l2(got, want) < 2e-4
+        mv = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)))
+        err, err_mv = rel_l2(got, want), rel_l2(got, mv)
+        assert err < 1e-3
         # The refinement is a proper approximation of plain MV here, not MV itself.
-        mv = oracle.beamform(cd, iq, pts, len(lines), setup.n1, O.bf_config(**setup_bf_kw(setup)), prec="f64")
-        assert rel_l2(want, mv) > 1e-3
+        assert rel_l2(want, mv) > 3e-3 and err < 0.2 * err_mv
     finally:
         im.close()
 

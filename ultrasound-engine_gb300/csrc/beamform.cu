@@ -432,8 +432,8 @@ constexpr DasVariant das_variant() {
   return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB>, das_fast_kernel<false, 16, 4, 1>};
 }
 const DasVariant kDasVariants[] = {
-    das_variant<16, 4, 1>(), das_variant<8, 4, 8>(), das_variant<16, 8, 2>(),
-    das_variant<32, 4, 1>(), das_variant<8, 8, 4>(), das_variant<16, 2, 8>(),
+    das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
+    das_variant<8, 8, 4>(),  das_variant<16, 2, 8>(), das_variant<4, 4, 12>(), das_variant<8, 2, 16>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 

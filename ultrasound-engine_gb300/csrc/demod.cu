@@ -9,9 +9,11 @@
 // sample is read from HBM once per block; blocks overlap by taps-1 samples,
 // which is the only re-read (3% at 33 taps, dec 1).
 //
-// Arithmetic follows the reference term by term (mix, then tap product, then
-// accumulate in ascending tap order, then x2), with no FMA contraction; the
-// mixing phase -2*pi*f*t(n) is evaluated on the device with sincosf.
+// Arithmetic follows the reference term by term (mix, then tap product and
+// accumulation in ascending tap order, then x2); the tap product and the
+// accumulation are one FMA (~1e-7 relative from the reference's separate
+// multiply and add); the mixing phase -2*pi*f*t(n) is evaluated on the device
+// with sincosf once per block for all of its traces.
 #include <algorithm>
 #include <vector>
 
@@ -21,7 +23,7 @@ namespace usxcu {
 namespace {
 
 constexpr int kMaxTaps = 255;
-constexpr int kTraces = 4;
+constexpr int kTraces = 8;
 constexpr int kOut = 128;
 
 struct DemodParams {
@@ -85,8 +87,8 @@ __global__ void __launch_bounds__(kOut) demod_kernel(const DemodParams p) {
     for (int j = j_lo; j <= j_hi; ++j) {
       const float2 v = m[off - j];
       const float hj = p.h[j];
-      ar = ar + v.x * hj;
-      ai = ai + v.y * hj;
+      ar = fmaf(v.x, hj, ar);
+      ai = fmaf(v.y, hj, ai);
     }
     p.iq[tr * p.n_out + k] = make_float2(ar * 2.0f, ai * 2.0f);
   }

@@ -137,19 +137,22 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
       const int m = lane + 32 * s2;
       if (m >= L) continue;
       const int lm1 = L - m - 1;
-      for (int d = 0; d < n_d; ++d) {
-        const float2* yr = rows + d * a.n_ch;
-        float are = 0.f, aim = 0.f;
-        for (int t = 0; t < n_act - m; ++t) {
-          const int c = min(t, n_sub - 1) - max(0, t - lm1) + 1;
-          const float2 p = yr[t + m], q = yr[t];
-          const float w = static_cast<float>(c);
-          are = fmaf(w, fmaf(p.x, q.x, p.y * q.y), are);
-          aim = fmaf(w, fmaf(p.y, q.x, -p.x * q.y), aim);
+      // The trapezoid weight depends on t only: sum the range rows first.
+      float are = 0.f, aim = 0.f;
+      for (int t = 0; t < n_act - m; ++t) {
+        const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
+        float sre = 0.f, sim = 0.f;
+#pragma unroll 5
+        for (int d = 0; d < n_d; ++d) {
+          const float2 p = rows[d * a.n_ch + t + m], q = rows[d * a.n_ch + t];
+          sre = fmaf(p.x, q.x, fmaf(p.y, q.y, sre));
+          sim = fmaf(p.y, q.x, fmaf(-p.x, q.y, sim));
         }
-        rre[s2] += are;
-        rim[s2] += aim;
+        are = fmaf(w, sre, are);
+        aim = fmaf(w, sim, aim);
       }
+      rre[s2] += are;
+      rim[s2] += aim;
       rre[s2] /= static_cast<float>(L - m);
       rim[s2] /= static_cast<float>(L - m);
     }
@@ -327,11 +330,18 @@ struct SubArgs {
 // Per-warp shared memory; the range rows follow it (n_dmax x kSubMaxN).
 struct SubWarpSmem {
   float2 pre[kSubMaxBeams][kSubMaxN + 1];   // prefix sums of one row, per beam
-  float2 tw[kSubMaxBeams][kSubMaxN];        // e^{-j 2 pi b t / L}
+  float2 tw1[kSubMaxN];                     // e^{-j 2 pi t / L}; beam b's twiddle is its b-th power
   float2 wq[kLmvMaxL];                      // the network's direction, orthogonalised
-  int act[kSubMaxN];
   float2 rows[1][kSubMaxN];                 // [n_dmax][kSubMaxN] range rows, active channels
 };
+
+// e^{-j 2 pi b t / L} for b = 0, 1, -1, 2, -2 (k = 0..4) from t1 = e^{-j 2 pi t / L}.
+__device__ __forceinline__ float2 beam_twiddle(float2 t1, int k) {
+  if (k == 0) return make_float2(1.f, 0.f);
+  float2 t = t1;
+  if (k >= 3) t = make_float2(t1.x * t1.x - t1.y * t1.y, 2.f * t1.x * t1.y);
+  return (k & 1) ? t : make_float2(t.x, -t.y);
+}
 __host__ __device__ constexpr size_t sub_warp_bytes(int n_dmax) {
   return (sizeof(SubWarpSmem) + sizeof(float2) * kSubMaxN * (n_dmax - 1) + 15) / 16 * 16;
 }
@@ -343,8 +353,6 @@ __device__ __forceinline__ float2 warp_sum2(float2 v) {
   }
   return v;
 }
-
-__device__ __forceinline__ int beam_index(int k) { return (k + 1) / 2 * ((k & 1) ? 1 : -1); }  // 0,1,-1,2,-2
 
 __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubArgs a) {
   extern __shared__ float4 sub_smem_raw[];
@@ -381,14 +389,11 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       continue;
     }
     __syncwarp();
-    // Twiddles e^{-j 2 pi b t / L}, t < 128, argument reduced to one turn.
-    for (int e = lane; e < nb * kSubMaxN; e += 32) {
-      const int k = e / kSubMaxN, t = e - k * kSubMaxN;
-      const int b = beam_index(k);
-      const int r = ((b * t) % L + L) % L;
+    // Twiddles e^{-j 2 pi t / L}, t < 128, argument reduced to one turn.
+    for (int t = lane; t < kSubMaxN; t += 32) {
       float sn, cs;
-      sincospif(2.0f * static_cast<float>(r) * inv_l, &sn, &cs);
-      sm.tw[k][t] = make_float2(cs, -sn);
+      sincospif(2.0f * static_cast<float>(t % L) * inv_l, &sn, &cs);
+      sm.tw1[t] = make_float2(cs, -sn);
     }
     // w~ minus its projections on the beams: c_b = u_b^H w~ (u_b = conj(tw_b) / sqrt(L)).
     const float rs = rsqrtf(static_cast<float>(L));
@@ -407,7 +412,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
           for (int h = 0; h < 2; ++h) {
             const int i = i0 + h;
             if (i < L) {  // conj(u_b[i]) w~_i = tw_b[i] w~_i / sqrt(L)
-              const float2 t = sm.tw[k][i];
+              const float2 t = beam_twiddle(sm.tw1[i], k);
               d.x += (t.x * wv[h].x - t.y * wv[h].y) * rs;
               d.y += (t.x * wv[h].y + t.y * wv[h].x) * rs;
             }
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
 #pragma unroll
         for (int k = 0; k < kSubMaxBeams; ++k) {
           if (k >= nb) continue;
-          const float2 t = sm.tw[k][i];  // u_b[i] = conj(t) / sqrt(L)
+          const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
           const float ux = t.x * rs, uy = -t.y * rs;
           wv[h].x -= cb[k].x * ux - cb[k].y * uy;
           wv[h].y -= cb[k].x * uy + cb[k].y * ux;
@@ -445,7 +450,8 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     const int j = pix % a.n1;
     const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
     const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
-    int n_act = 0;
+    // The active channels |x_e - x_p| < z / (2 F#) are one contiguous run.
+    int n_act = 0, first = -1;
     for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
       const int ch = c0 + lane;
       bool on = false;
@@ -453,12 +459,10 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
         on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
                              a.tukey_alpha) > 0.0f;
       const unsigned m = __ballot_sync(0xffffffffu, on);
-      const int slot = n_act + __popc(m & ((1u << lane) - 1u));
-      if (on && slot < kSubMaxN) sm.act[slot] = ch;
+      if (first < 0 && m) first = c0 + __ffs(m) - 1;
       n_act += __popc(m);
     }
     n_act = min(n_act, kSubMaxN);
-    __syncwarp();
     const int n_sub = n_act - L + 1;
     int dlo = -a.range_avg, dhi = a.range_avg;
     while (j + dlo < 0) ++dlo;
@@ -466,7 +470,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     const int n_d = dhi - dlo + 1;
     for (int k = lane; k < n_d * n_act; k += 32) {
       const int d = k / n_act, q = k - d * n_act;
-      srow[d * kSubMaxN + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + sm.act[q]];
+      srow[d * kSubMaxN + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + first + q];
     }
     __syncwarp();
 
@@ -502,7 +506,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
 #pragma unroll
         for (int k = 0; k < kSubMaxBeams; ++k) {
           if (k >= nb) continue;
-          const float2 tw = t < n_act ? sm.tw[k][t] : make_float2(1.f, 0.f);
+          const float2 tw = t < n_act ? beam_twiddle(sm.tw1[t], k) : make_float2(1.f, 0.f);
           float2 v = make_float2(tw.x * yv.x - tw.y * yv.y, tw.x * yv.y + tw.y * yv.x);
           for (int o2 = 1; o2 < 32; o2 <<= 1) {
             const float px2 = __shfl_up_sync(0xffffffffu, v.x, o2), py2 = __shfl_up_sync(0xffffffffu, v.y, o2);
@@ -528,7 +532,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
           if (k >= nb) continue;
           const float2 hi = sm.pre[k][s0 + L], lo = sm.pre[k][s0];
           const float2 df = make_float2((hi.x - lo.x) * rs, (hi.y - lo.y) * rs);
-          const float2 t = sm.tw[k][s0];
+          const float2 t = beam_twiddle(sm.tw1[s0], k);
           z[k] = make_float2(t.x * df.x + t.y * df.y, t.x * df.y - t.y * df.x);
         }
         // The network's direction: w_q^H y_s.
@@ -648,7 +652,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
 #pragma unroll
       for (int k = 0; k < kSubMaxBeams; ++k) {
         if (k >= nb) continue;
-        const float2 t = sm.tw[k][i];  // u_b[i] = conj(t) / sqrt(L)
+        const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
         const float ux = t.x * rs, uy = -t.y * rs;
         w.x += ux * cv[k].x - uy * cv[k].y;
         w.y += ux * cv[k].y + uy * cv[k].x;

@@ -338,6 +338,150 @@ __global__ void lmv_output_loss_kernel(const float* y, const float* t, const flo
   if (lane == 0 && loss) atomicAdd(loss, (ere * ere + eim * eim + sre * sre + sim * sim + beta * wse) * inv_rows);
 }
 
+// Learned-subspace loss, one warp per row. The refinement solves the Capon
+// problem within span{DFT beams b = 0, +1, -1, +2, -2 (the first min(5, L)),
+// network weights}, so what the network must supply is the direction of the
+// Capon weights outside the beams. With P the projector onto the complement
+// of the beams (length L = the masked count), u = P w, v = P t (w, t the
+// predicted and target complex weights, i < L):
+//   loss = 1 - |u^H v|^2 / (|u|^2 |v|^2)  +  beta * sum_i |w_i - t_i|^2 / L,
+// scale- and phase-free in u; rows whose target lies in the beams' span
+// (|v|^2 <= 1e-8 |t|^2) keep only the second term. d loss / d(Re w_i, Im w_i)
+// is P applied to -2 (v conj(c) / (a b) - |c|^2 u / (a^2 b)) (c = u^H v,
+// a = |u|^2, b = |v|^2) plus 2 beta (w_i - t_i) / L; all divided by `rows`.
+__device__ __forceinline__ float2 wsum2(float2 v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+__global__ void lmv_subspace_loss_kernel(const float* y, const float* t, const float* mask, long rows,
+                                         float beta, float inv_rows, __nv_bfloat16* dy16, float* loss) {
+  const int lane = threadIdx.x & 31;
+  const long r = (blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x) >> 5;
+  if (r >= rows) return;
+  const float4 w4 = reinterpret_cast<const float4*>(y + r * 128)[lane];
+  const float4 t4 = reinterpret_cast<const float4*>(t + r * 128)[lane];
+  const float4 m4 = mask ? reinterpret_cast<const float4*>(mask + r * 128)[lane] : make_float4(1.f, 1.f, 1.f, 1.f);
+  float cnt = (m4.x > 0.f ? 1.f : 0.f) + (m4.z > 0.f ? 1.f : 0.f);
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  const int L = static_cast<int>(cnt);
+  float2 w[2] = {make_float2(w4.x, w4.y), make_float2(w4.z, w4.w)};
+  float2 tv[2] = {make_float2(t4.x, t4.y), make_float2(t4.z, t4.w)};
+  const bool in[2] = {2 * lane < L, 2 * lane + 1 < L};
+  float2 tw1[2];   // e^{-j 2 pi i / L}
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float sn = 0.f, cs = 1.f;
+    if (in[h]) sincospif(2.0f * static_cast<float>((2 * lane + h) % max(L, 1)) / static_cast<float>(max(L, 1)), &sn, &cs);
+    tw1[h] = make_float2(cs, -sn);
+    if (!in[h]) w[h] = tv[h] = make_float2(0.f, 0.f);
+  }
+  const int nb = min(5, L);
+  const float rs = L > 0 ? rsqrtf(static_cast<float>(L)) : 0.f;
+  auto twk = [&](int h, int k) -> float2 {  // e^{-j 2 pi b i / L}, b = 0, 1, -1, 2, -2
+    const float2 t1 = tw1[h];
+    if (k == 0) return make_float2(1.f, 0.f);
+    float2 q = t1;
+    if (k >= 3) q = make_float2(t1.x * t1.x - t1.y * t1.y, 2.f * t1.x * t1.y);
+    return (k & 1) ? q : make_float2(q.x, -q.y);
+  };
+  // u = P w, v = P t: subtract sum_b u_b (u_b^H x), u_b[i] = conj(twk) / sqrt(L).
+  float2 u[2] = {w[0], w[1]}, v[2] = {tv[0], tv[1]};
+  float tn = 0.f;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) tn += tv[h].x * tv[h].x + tv[h].y * tv[h].y;
+  for (int o = 16; o > 0; o >>= 1) tn += __shfl_xor_sync(0xffffffffu, tn, o);
+  for (int k = 0; k < 5; ++k) {
+    if (k >= nb) break;
+    float2 cw = make_float2(0.f, 0.f), ct = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float2 q = twk(h, k);  // conj(u_b) sqrt(L)
+      cw.x += q.x * w[h].x - q.y * w[h].y;
+      cw.y += q.x * w[h].y + q.y * w[h].x;
+      ct.x += q.x * tv[h].x - q.y * tv[h].y;
+      ct.y += q.x * tv[h].y + q.y * tv[h].x;
+    }
+    cw = wsum2(cw);
+    ct = wsum2(ct);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!in[h]) continue;
+      const float2 q = twk(h, k);
+      const float ubx = q.x * rs * rs, uby = -q.y * rs * rs;  // u_b / sqrt(L) (the coefficient carries sqrt(L))
+      u[h].x -= cw.x * ubx - cw.y * uby;
+      u[h].y -= cw.x * uby + cw.y * ubx;
+      v[h].x -= ct.x * ubx - ct.y * uby;
+      v[h].y -= ct.x * uby + ct.y * ubx;
+    }
+  }
+  float2 c = make_float2(0.f, 0.f);
+  float a = 0.f, b = 0.f, se = 0.f;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    c.x += u[h].x * v[h].x + u[h].y * v[h].y;   // conj(u) v
+    c.y += u[h].x * v[h].y - u[h].y * v[h].x;
+    a += u[h].x * u[h].x + u[h].y * u[h].y;
+    b += v[h].x * v[h].x + v[h].y * v[h].y;
+    se += (w[h].x - tv[h].x) * (w[h].x - tv[h].x) + (w[h].y - tv[h].y) * (w[h].y - tv[h].y);
+  }
+  c = wsum2(c);
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    se += __shfl_xor_sync(0xffffffffu, se, o);
+  }
+  const float inv_l = L > 0 ? 1.0f / static_cast<float>(L) : 0.f;
+  const bool dir = b > 1e-8f * tn && a > 1e-30f;
+  const float c2 = c.x * c.x + c.y * c.y;
+  const float f = dir ? c2 / (a * b) : 1.0f;
+  // g = -2 (v conj(c) / (a b) - |c|^2 u / (a^2 b)) on the complement, then P.
+  float2 g[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    g[h] = make_float2(0.f, 0.f);
+    if (dir && in[h]) {
+      const float2 vc = make_float2(v[h].x * c.x + v[h].y * c.y, v[h].y * c.x - v[h].x * c.y);  // v conj(c)
+      const float s1 = 1.0f / (a * b), s2 = c2 / (a * a * b);
+      g[h] = make_float2(-2.f * (vc.x * s1 - u[h].x * s2), -2.f * (vc.y * s1 - u[h].y * s2));
+    }
+  }
+  for (int k = 0; k < 5; ++k) {   // P g (P is self-adjoint)
+    if (k >= nb) break;
+    float2 cg = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const float2 q = twk(h, k);
+      cg.x += q.x * g[h].x - q.y * g[h].y;
+      cg.y += q.x * g[h].y + q.y * g[h].x;
+    }
+    cg = wsum2(cg);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (!in[h]) continue;
+      const float2 q = twk(h, k);
+      const float ubx = q.x * rs * rs, uby = -q.y * rs * rs;
+      g[h].x -= cg.x * ubx - cg.y * uby;
+      g[h].y -= cg.x * uby + cg.y * ubx;
+    }
+  }
+  float gg[4];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const float ex = in[h] ? 2.f * beta * (w[h].x - tv[h].x) * inv_l : 0.f;
+    const float ey = in[h] ? 2.f * beta * (w[h].y - tv[h].y) * inv_l : 0.f;
+    gg[2 * h] = (g[h].x + ex) * inv_rows;
+    gg[2 * h + 1] = (g[h].y + ey) * inv_rows;
+  }
+  __nv_bfloat162* d2 = reinterpret_cast<__nv_bfloat162*>(dy16 + r * 128) + 2 * lane;
+  d2[0] = __floats2bfloat162_rn(gg[0], gg[1]);
+  d2[1] = __floats2bfloat162_rn(gg[2], gg[3]);
+  if (lane == 0 && loss) atomicAdd(loss, ((dir ? 1.0f - f : 0.0f) + beta * se * inv_l) * inv_rows);
+}
+
 // db[n] += sum_m dY[m][n] (FP32 gradient rows as BF16 tiles were used in GEMMs).
 __global__ void bias_grad_kernel(const __nv_bfloat16* dy, long rows, int n, int ld, float* db) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
@@ -588,9 +732,9 @@ int usx_cu_mlp_set_params(usx_mlp* n, const float* host) {
 
 int usx_cu_mlp_set_loss(usx_mlp* n, int kind, float beta) {
   if (!n) return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: null network");
-  if (kind != USX_MLP_LOSS_MSE && kind != USX_MLP_LOSS_LMV_OUTPUT)
+  if (kind != USX_MLP_LOSS_MSE && kind != USX_MLP_LOSS_LMV_OUTPUT && kind != USX_MLP_LOSS_LMV_SUBSPACE)
     return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: unknown loss");
-  if (kind == USX_MLP_LOSS_LMV_OUTPUT && !(n->dims.front() == 256 && n->dims.back() == 128))
+  if (kind != USX_MLP_LOSS_MSE && !(n->dims.front() == 256 && n->dims.back() == 128))
     return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: the output loss needs a 256 -> 128 network");
   if (!(beta >= 0.0f)) return fail(USX_ERR_INVALID, "usx_cu_mlp_set_loss: beta must be >= 0");
   n->loss_kind = kind;
@@ -632,7 +776,11 @@ int usx_cu_mlp_train_step(usx_mlp* n, const float* x, const float* target, const
   USX_CUDA(cudaMemsetAsync(n->grad, 0, sizeof(float) * n->n_params, st));
   USX_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), st));
   const int n_out = n->dims.back();
-  if (n->loss_kind == USX_MLP_LOSS_LMV_OUTPUT) {
+  if (n->loss_kind == USX_MLP_LOSS_LMV_SUBSPACE) {
+    lmv_subspace_loss_kernel<<<ceil_div(static_cast<long>(rows) * 32, 256), 256, 0, st>>>(
+        n->out32, target, mask, rows, n->loss_beta, 1.0f / static_cast<float>(rows), n->g16a, n->loss);
+    USX_CHECK_LAUNCH("lmv_subspace_loss_kernel");
+  } else if (n->loss_kind == USX_MLP_LOSS_LMV_OUTPUT) {
     lmv_output_loss_kernel<<<ceil_div(static_cast<long>(rows) * 32, 256), 256, 0, st>>>(
         n->out32, target, mask, x, rows, n->loss_beta, 1.0f / static_cast<float>(rows), n->g16a, n->loss);
     USX_CHECK_LAUNCH("lmv_output_loss_kernel");

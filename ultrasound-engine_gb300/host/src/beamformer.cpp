@@ -15,6 +15,7 @@
 #include <list>
 #include <map>
 #include <mutex>
+#include <set>
 #include <stdexcept>
 
 #include "desc.hpp"
@@ -188,17 +189,28 @@ class PlanCache {
     }
     entries_.emplace_front(std::move(key), plan);
     while (entries_.size() > kMaxPlans) {
+      used_.erase(entries_.back().second);
       usx_cu_bf_plan_destroy(entries_.back().second);
       entries_.pop_back();
     }
     return plan;
   }
 
+  // True the first time it is asked about `plan` (the plan was just created).
+  bool first_use(usx_bf_plan* plan) {
+    std::lock_guard<std::mutex> lock(mu_);
+    return used_.insert(plan).second;
+  }
+
  private:
   static constexpr std::size_t kMaxPlans = 4;
   std::mutex mu_;
   std::list<std::pair<PlanKey, usx_bf_plan*>> entries_;
+  std::set<usx_bf_plan*> used_;
 };
+
+// (pixels x events x channels) above which a new plan autotunes on its first frame.
+constexpr double kAutotuneWork = 1e9;
 
 Beamformer::Beamformer(BeamformerConfig config) : config_(config), plans_(std::make_shared<PlanCache>()) {
   config_.validate();
@@ -249,7 +261,13 @@ Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, con
   frame.allocate();
   usx_bf_plan* plan = plans_->get(data, grid, config_, event_begin, event_end);
   void* d_out = rt::slot(4, frame.data.size() * sizeof(cplx));
-  rt::check(usx_cu_bf_execute(plan, d_in, static_cast<float*>(d_out)), "beamform");
+  // A plan's first frame of a large acquisition picks the delay-and-sum launch
+  // shape by timing each variant on it (the frame is the chosen variant's).
+  const double work = static_cast<double>(grid.n_pixels()) * (event_end - event_begin) * data.n_channels();
+  if (work >= kAutotuneWork && plans_->first_use(plan))
+    rt::check(usx_cu_bf_plan_autotune(plan, d_in, static_cast<float*>(d_out), 1, nullptr), "beamform autotune");
+  else
+    rt::check(usx_cu_bf_execute(plan, d_in, static_cast<float*>(d_out)), "beamform");
   rt::d2h(frame.data.data(), d_out, frame.data.size() * sizeof(cplx));
   return frame;
 }

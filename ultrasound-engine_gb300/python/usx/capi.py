@@ -424,7 +424,7 @@ class Mlp:
             out.append((w, b))
         return out
 
-    LOSS_MSE, LOSS_LMV_OUTPUT = 0, 1
+    LOSS_MSE, LOSS_LMV_OUTPUT, LOSS_LMV_SUBSPACE = 0, 1, 2
 
     def set_loss(self, kind: int, beta: float = 0.0) -> None:
         """Training loss: LOSS_MSE (masked MSE) or LOSS_LMV_OUTPUT (learned-MV

