@@ -192,7 +192,7 @@ int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate);
 /* How the learned path uses the network's weights w~ of a pixel that passes
  * the gate (no counterpart in the reference):
  *   n_beams < 0      as predicted (the default), the output above;
- *   n_beams = 0,2,4  the Capon problem of the reference's minimum variance,
+ *   n_beams = 0,2,4,6  the Capon problem of the reference's minimum variance,
  *                    min w^H (R + eps I) w subject to 1^H w = 1, solved
  *                    exactly within span{1, w~, e^{+-j 2 pi b i / L} for
  *                    b = 1..n_beams/2} through the pixel's snapshots (the

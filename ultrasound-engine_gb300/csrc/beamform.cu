@@ -1192,8 +1192,8 @@ int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate) {
 
 int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams) {
   if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: null plan");
-  if (n_beams > 4 || (n_beams >= 0 && n_beams % 2 != 0))
-    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: n_beams must be negative, 0, 2 or 4");
+  if (n_beams > 6 || (n_beams >= 0 && n_beams % 2 != 0))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: n_beams must be negative, 0, 2, 4 or 6");
   plan->lmv_beams = n_beams < 0 ? -1 : n_beams;
   return USX_OK;
 }

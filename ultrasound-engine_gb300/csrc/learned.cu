@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(256) lmv_apply_kernel(const ApplyArgs a) {
 // The network's weights w~ are a guess of the Capon direction R^-1 1. Instead
 // of using them as they are, the pixel solves the Capon problem exactly
 // within the subspace spanned by the DFT beams u_b[i] = e^{j 2 pi b i / L} / sqrt(L),
-// b = 0, +1, -1, ... (n_beams + 1 of them; b = 0 is the look direction) and w~
+// b = 0, +1, -1, ..., +3, -3 (n_beams + 1 of them; b = 0 is the look direction) and w~
 // (its part orthogonal to the beams, dropped when negligible):
 //   minimise w^H R~ w subject to 1^H w = 1, w = Q c,
 //   (Q^H R Q + eps I) c = Q^H 1,   eps = max(delta tr(R) / L, 1e-20),
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256) lmv_apply_kernel(const ApplyArgs a) {
 // output power is at most that of DAS (w = 1/L) and of w~. The gate on the
 // network's distortionless residual |1^H w~ / L - 1| comes first; gated
 // pixels go to the exact solver.
-constexpr int kSubMaxBeams = 5;            // b = 0, +1, -1, +2, -2
+constexpr int kSubMaxBeams = 7;            // b = 0, +1, -1, +2, -2, +3, -3
 constexpr int kSubMaxK = kSubMaxBeams + 1; // plus the network's direction
 constexpr int kSubWarps = 4;
 constexpr int kSubMaxN = 128;              // active channels
@@ -335,11 +335,13 @@ struct SubWarpSmem {
   float2 rows[1][kSubMaxN];                 // [n_dmax][kSubMaxN] range rows, active channels
 };
 
-// e^{-j 2 pi b t / L} for b = 0, 1, -1, 2, -2 (k = 0..4) from t1 = e^{-j 2 pi t / L}.
+// e^{-j 2 pi b t / L} for b = 0, 1, -1, 2, -2, 3, -3 (k = 0..6) from
+// t1 = e^{-j 2 pi t / L}: the |b|-th power, conjugated for negative b.
 __device__ __forceinline__ float2 beam_twiddle(float2 t1, int k) {
   if (k == 0) return make_float2(1.f, 0.f);
   float2 t = t1;
   if (k >= 3) t = make_float2(t1.x * t1.x - t1.y * t1.y, 2.f * t1.x * t1.y);
+  if (k >= 5) t = make_float2(t.x * t1.x - t.y * t1.y, t.x * t1.y + t.y * t1.x);
   return (k & 1) ? t : make_float2(t.x, -t.y);
 }
 __host__ __device__ constexpr size_t sub_warp_bytes(int n_dmax) {

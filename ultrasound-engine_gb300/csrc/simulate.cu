@@ -31,6 +31,7 @@ namespace {
 constexpr int kSimWarps = 4;
 constexpr int kMaxElem = 256;
 constexpr int kMaxPulse = 1024;
+constexpr int kMaxTimeTable = 8192;
 
 struct SimArgs {
   const usx_scatterer* scat;
@@ -46,6 +47,7 @@ struct SimArgs {
   float c, fs, t0, fs_os, lambda, width, prf, half_nm1, pitch;
   float pulse_half, max_window_s, trim_amp, atten_db_per_m;
   int spreading, directivity_on, motion, full;
+  int t_table;             // the block holds the sample-time table (n_smp <= kMaxTimeTable)
 };
 
 __device__ __forceinline__ float elem_amp(const SimArgs& a, float base_amp, float px, float ex, float r) {
@@ -71,6 +73,11 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
   float* e_ctr = e_amp + kMaxElem;              // stage-1 centre index (active order)
   int* e_base = reinterpret_cast<int*>(e_ctr + kMaxElem);
   for (int k = threadIdx.x; k < a.pulse_n; k += blockDim.x) pulse[k] = a.pulse[k];
+  // Sample times t0 + n / fs of the RF axis, each computed as the reference
+  // does (float division), once per block instead of once per echo sample.
+  float* t_axis = pulse + kMaxPulse + kSimWarps * (a.inc_cap + 4 * kMaxElem);
+  if (a.t_table)
+    for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
   __syncthreads();
 
   const int ev = blockIdx.y;
@@ -188,24 +195,44 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
     const float* tr = inc + lo;
 
     // ---- stage 2: echo on every receive element ---------------------------------
-    for (int e = 0; e < a.n_el; ++e) {
+    // Per receive element, one lane each: amplitude, delay and the echo's
+    // sample window (the stage-1 tables are free again; e_r[e] is read by
+    // the lane that then overwrites it with the window's last sample).
+    const float span_t = static_cast<float>(trim_n - 1) / a.fs_os;
+    for (int e = lane; e < a.n_el; e += 32) {
       const float r = e_r[e];
-      if (r < 1e-6f) continue;
-      const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
-      const float amp = elem_amp(a, sc.amplitude, px, ex, r);
-      if (amp == 0.0f) continue;
-      const float delay = r / a.c;
-      const float t_start = trim_t0 + delay;
-      const float t_end = t_start + static_cast<float>(trim_n - 1) / a.fs_os;
-      int n0 = static_cast<int>(ceilf((t_start - a.t0) * a.fs));
-      int n1 = static_cast<int>(floorf((t_end - a.t0) * a.fs));
-      n0 = max(n0, 0);
-      n1 = min(n1, a.n_smp - 1);
+      float amp = 0.0f, delay = 0.0f;
+      int n0 = 1, n1 = 0;
+      if (!(r < 1e-6f)) {
+        const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
+        amp = elem_amp(a, sc.amplitude, px, ex, r);
+        if (amp != 0.0f) {
+          delay = r / a.c;
+          const float t_start = trim_t0 + delay;
+          const float t_end = t_start + span_t;
+          n0 = max(static_cast<int>(ceilf((t_start - a.t0) * a.fs)), 0);
+          n1 = min(static_cast<int>(floorf((t_end - a.t0) * a.fs)), a.n_smp - 1);
+        }
+      }
+      if (n0 > n1) {
+        n0 = 1;
+        n1 = 0;
+      } else {
+        samples += static_cast<unsigned long long>(n1 - n0 + 1);
+      }
+      e_amp[e] = amp;
+      e_ctr[e] = delay;
+      e_base[e] = n0;
+      e_r[e] = __int_as_float(n1);
+    }
+    __syncwarp();
+    for (int e = 0; e < a.n_el; ++e) {
+      const int n0 = e_base[e], n1 = __float_as_int(e_r[e]);
       if (n0 > n1) continue;
-      if (lane == 0) samples += static_cast<unsigned long long>(n1 - n0 + 1);
+      const float amp = e_amp[e], delay = e_ctr[e];
       float* dst = rf_ev + static_cast<long>(e) * a.n_smp;
       for (int n = n0 + lane; n <= n1; n += 32) {
-        const float t = (a.t0 + static_cast<float>(n) / a.fs) - delay;
+        const float t = (a.t_table ? t_axis[n] : (a.t0 + static_cast<float>(n) / a.fs)) - delay;
         const float u = (t - trim_t0) * a.fs_os;
         const int k = static_cast<int>(u);
         if (k < 0 || k + 1 >= trim_n) continue;
@@ -216,6 +243,7 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
     }
     __syncwarp();
   }
+  for (int o = 16; o > 0; o >>= 1) samples += __shfl_xor_sync(0xffffffffu, samples, o);
   if (lane == 0 && samples) atomicAdd(a.counter, samples);
 }
 
@@ -358,7 +386,9 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.scat_per_block = static_cast<int>(std::max<long>(kSimWarps, (n_scat + target_blocks - 1) / target_blocks));
   a.scat_per_block = std::min(a.scat_per_block, 256);
   const long gx = std::max<long>(1, (n_scat + a.scat_per_block - 1) / a.scat_per_block);
-  const size_t smem = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem));
+  a.t_table = n_smp <= kMaxTimeTable ? 1 : 0;
+  const size_t smem = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem) +
+                                       (a.t_table ? static_cast<size_t>(n_smp) : 0));
   if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
   USX_CUDA(cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 static_cast<int>(smem)));

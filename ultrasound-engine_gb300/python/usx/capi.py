@@ -344,7 +344,7 @@ class Plan:
         check(lib().usx_cu_bf_plan_set_variant(self._h, int(index)), "bf_plan_set_variant")
 
     def set_learned_refine(self, n_beams: int) -> None:
-        """Negative: the network's weights as predicted; 0, 2, 4: exact Capon
+        """Negative: the network's weights as predicted; 0, 2, 4, 6: exact Capon
         solve within span{1, network weights, n_beams DFT beams}."""
         check(lib().usx_cu_bf_plan_set_learned_refine(self._h, int(n_beams)), "bf_plan_set_learned_refine")
 
