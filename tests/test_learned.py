@@ -391,7 +391,7 @@ def _constant_net(capi, ctx, v):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("beams", [0, 2, 4])
+@pytest.mark.parametrize("beams", [0, 2, 4, 6])
 def test_subspace_refinement_matches_oracle(capi, torch, oracle, beams):
     """The learned-subspace refinement (Capon solve within span{DFT beams,
     network direction}, through the snapshots) against the oracle's

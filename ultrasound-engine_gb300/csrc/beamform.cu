@@ -818,29 +818,31 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     const long rows = chunk * n_pix, padded = (rows + 127) / 128 * 128;
     const int widest = mlp_widest(plan->mlp);
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t sz[9] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
+    const size_t sz[10] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
                           up(sizeof(float2) * rows * 64),       up(sizeof(float4) * rows),
                           up(2 * padded * widest),              up(2 * padded * widest),
-                          up(sizeof(float) * padded * kLmvOutputs), up(sizeof(int2) * rows),
-                          up(sizeof(int2) * rows)};
+                          up(sizeof(float) * padded * kLmvOutputs), up(sizeof(int2) * rows * kLmvGateClasses),
+                          up(sizeof(int2) * rows), up(sizeof(int2) * rows)};
     size_t total = 256;
     for (size_t b : sz) total += b;
     void* ws = nullptr;
     if (int rc = scratch(ctx, total, &ws)) return rc;
     char* q = static_cast<char*>(ws);
-    void* bufs[9];
-    for (int i = 0; i < 9; ++i) {
+    void* bufs[10];
+    for (int i = 0; i < 10; ++i) {
       bufs[i] = q;
       q += sz[i];
     }
-    int* counters = reinterpret_cast<int*>(q);  // [0] gated, [1] FP64 re-solves
+    // [0, kLmvGateClasses) gated pixels per subarray class, then FP64 re-solves, then overflow.
+    int* counters = reinterpret_cast<int*>(q);
     float2* y = static_cast<float2*>(bufs[0]);
     char* feat16 = static_cast<char*>(bufs[1]);
     float2* avg = static_cast<float2*>(bufs[2]);
     float4* meta = static_cast<float4*>(bufs[3]);
     float* net = static_cast<float*>(bufs[6]);
     int2* gated = static_cast<int2*>(bufs[7]);
-    int2* fb = static_cast<int2*>(bufs[8]);
+    int2* fb = static_cast<int2*>(bufs[8]);      // FP64 re-solves
+    int2* ovf = static_cast<int2*>(bufs[9]);     // pixels past their class's aperture limit
     for (int f0 = 0; f0 < n_frames; f0 += chunk) {
       const int nf = std::min(chunk, n_frames - f0);
       const long nrows = nf * n_pix, npad = (nrows + 127) / 128 * 128;
@@ -876,7 +878,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
         USX_CUDA(cudaMemsetAsync(feat16 + 2 * nrows * kLmvFeatures, 0, 2 * (npad - nrows) * kLmvFeatures, ctx->stream));
       if (int rc = launch_lmv_features(ctx, l)) return rc;
       if (int rc = mlp_infer(plan->mlp, ctx, feat16, npad, bufs[4], bufs[5], net)) return rc;
-      USX_CUDA(cudaMemsetAsync(counters, 0, 2 * sizeof(int), ctx->stream));
+      USX_CUDA(cudaMemsetAsync(counters, 0, (kLmvGateClasses + 2) * sizeof(int), ctx->stream));
       if (plan->lmv_beams >= 0) {
         if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate, counters,
                                          gated, static_cast<int>(nrows), plan->d_mv_stats + 2))
@@ -885,15 +887,30 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
                                            counters, gated, static_cast<int>(nrows), plan->d_mv_stats + 2)) {
         return rc;
       }
-      MvTcExtra ex;
-      ex.list = gated;
-      ex.list_count = counters;
-      ex.list_cap = static_cast<int>(nrows);
-      if (int rc = launch_mv_tc(ctx, y, b.points, b.out, b.out_stride, nullptr, b.n_ch, b.n_pix, b.n1, nf,
-                                b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number, b.tukey_alpha,
-                                b.rx_window, b.half_nm1, b.pitch, b.cf, 0, plan->d_mv_stats, counters + 1, fb,
-                                static_cast<int>(nrows), ex))
-        return rc;
+      // The exact solve of the gated pixels, one launch per subarray class so
+      // that shared memory is sized for the class; pixels past a class's
+      // aperture limit go to the CTA kernel.
+      const int plan_lmax = std::min(std::max(b.mv_subarray, 2), std::max(2, b.n_ch / 2));
+      for (int c = 0; c < kLmvGateClasses; ++c) {
+        const int lmax = std::min(kLmvClassWidth * (c + 1), plan_lmax);
+        if (c > 0 && kLmvClassWidth * c >= plan_lmax) break;
+        MvTcExtra ex;
+        ex.list = gated + static_cast<long>(c) * nrows;
+        ex.list_count = counters + c;
+        ex.list_cap = static_cast<int>(nrows);
+        ex.list_lmax = lmax;
+        // Below the plan's clamp L = n_act / 2, so n_act <= 2 L + 1; the clamped
+        // class can hold every aperture.
+        ex.list_nmax = lmax >= plan_lmax ? b.n_ch : std::min(b.n_ch, 2 * lmax + 2);
+        ex.overflow_count = counters + kLmvGateClasses + 1;
+        ex.overflow = ovf;
+        ex.overflow_cap = static_cast<int>(nrows);
+        if (int rc = launch_mv_tc(ctx, y, b.points, b.out, b.out_stride, nullptr, b.n_ch, b.n_pix, b.n1, nf,
+                                  b.mv_subarray, b.mv_range_average, b.mv_loading, b.f_number, b.tukey_alpha,
+                                  b.rx_window, b.half_nm1, b.pitch, b.cf, 0, plan->d_mv_stats,
+                                  counters + kLmvGateClasses, fb, static_cast<int>(nrows), ex))
+          return rc;
+      }
     }
     plan->lmv_pixels += static_cast<int64_t>(n_frames) * n_pix;
     return USX_OK;

@@ -217,6 +217,13 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
   }
 }
 
+// A gated pixel joins the exact solver's work list of its subarray class.
+__device__ __forceinline__ void push_gated(int* counts, int2* lists, int cap, int L, int pix, long frame) {
+  const int c = min(kLmvGateClasses - 1, max(0, (L - 1) / kLmvClassWidth));
+  const int slot = atomicAdd(counts + c, 1);
+  if (slot < cap) lists[static_cast<long>(c) * cap + slot] = make_int2(pix, static_cast<int>(frame));
+}
+
 struct ApplyArgs {
   const float* net;       // [row][128] network outputs (FP32)
   const float2* avg;      // [row][64]
@@ -226,8 +233,8 @@ struct ApplyArgs {
   int n_pix;
   long n_rows;
   float gate;
-  int* gated_count;       // pixels sent to the exact solver
-  int2* gated;            // their (pixel, frame)
+  int* gated_count;       // pixels sent to the exact solver, per subarray class
+  int2* gated;            // their (pixel, frame): kLmvGateClasses lists of gated_cap
   int gated_cap;
   int* stats;             // running count of gated pixels (plan statistics)
 };
@@ -271,8 +278,7 @@ __global__ void __launch_bounds__(256) lmv_apply_kernel(const ApplyArgs a) {
     const int pix = static_cast<int>(row - frame * a.n_pix);
     const float res = sqrtf((dre - 1.f) * (dre - 1.f) + dim * dim);
     if (!(res <= a.gate)) {
-      const int slot = atomicAdd(a.gated_count, 1);
-      if (slot < a.gated_cap) a.gated[slot] = make_int2(pix, static_cast<int>(frame));
+      push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
       if (a.stats) atomicAdd(a.stats, 1);
       continue;
     }
@@ -328,8 +334,9 @@ struct SubArgs {
 };
 
 // Per-warp shared memory; the range rows follow it (n_dmax x kSubMaxN).
+template <int NB>
 struct SubWarpSmem {
-  float2 pre[kSubMaxBeams][kSubMaxN + 1];   // prefix sums of one row, per beam
+  float2 pre[NB][kSubMaxN + 1];             // prefix sums of one row, per beam
   float2 tw1[kSubMaxN];                     // e^{-j 2 pi t / L}; beam b's twiddle is its b-th power
   float2 wq[kLmvMaxL];                      // the network's direction, orthogonalised
   float2 rows[1][kSubMaxN];                 // [n_dmax][kSubMaxN] range rows, active channels
@@ -344,8 +351,9 @@ __device__ __forceinline__ float2 beam_twiddle(float2 t1, int k) {
   if (k >= 5) t = make_float2(t.x * t1.x - t.y * t1.y, t.x * t1.y + t.y * t1.x);
   return (k & 1) ? t : make_float2(t.x, -t.y);
 }
+template <int NB>
 __host__ __device__ constexpr size_t sub_warp_bytes(int n_dmax) {
-  return (sizeof(SubWarpSmem) + sizeof(float2) * kSubMaxN * (n_dmax - 1) + 15) / 16 * 16;
+  return (sizeof(SubWarpSmem<NB>) + sizeof(float2) * kSubMaxN * (n_dmax - 1) + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ float2 warp_sum2(float2 v) {
@@ -356,13 +364,16 @@ __device__ __forceinline__ float2 warp_sum2(float2 v) {
   return v;
 }
 
+// NB, the number of beams (1, 3, 5 or 7), is a template parameter so that
+// every loop over the basis is unrolled to its size.
+template <int NB>
 __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubArgs a) {
   extern __shared__ float4 sub_smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  SubWarpSmem& sm = *reinterpret_cast<SubWarpSmem*>(reinterpret_cast<char*>(sub_smem_raw) +
-                                                   warp * sub_warp_bytes(a.n_dmax));
+  SubWarpSmem<NB>& sm = *reinterpret_cast<SubWarpSmem<NB>*>(reinterpret_cast<char*>(sub_smem_raw) +
+                                                           warp * sub_warp_bytes<NB>(a.n_dmax));
   float2* srow = &sm.rows[0][0];  // [n_dmax][kSubMaxN]
-  const int nb_all = min(kSubMaxBeams, 1 + a.n_beams);
+  const int nb_all = NB;
 
   for (long row = static_cast<long>(blockIdx.x) * kSubWarps + warp; row < a.n_rows;
        row += static_cast<long>(gridDim.x) * kSubWarps) {
@@ -384,8 +395,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     const float res = sqrtf((sw.x - 1.f) * (sw.x - 1.f) + sw.y * sw.y);
     if (!(res <= a.gate)) {
       if (lane == 0) {
-        const int slot = atomicAdd(a.gated_count, 1);
-        if (slot < a.gated_cap) a.gated[slot] = make_int2(pix, static_cast<int>(frame));
+        push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
         if (a.stats) atomicAdd(a.stats, 1);
       }
       continue;
@@ -405,9 +415,9 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       const int i0 = 2 * lane;
       wv[0] = w0;
       wv[1] = w1;
-      float2 cb[kSubMaxBeams];
+      float2 cb[NB];
 #pragma unroll
-      for (int k = 0; k < kSubMaxBeams; ++k) {
+      for (int k = 0; k < NB; ++k) {
         float2 d = make_float2(0.f, 0.f);
         if (k < nb) {
 #pragma unroll
@@ -428,7 +438,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
         const int i = i0 + h;
         if (i >= L) continue;
 #pragma unroll
-        for (int k = 0; k < kSubMaxBeams; ++k) {
+        for (int k = 0; k < NB; ++k) {
           if (k >= nb) continue;
           const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
           const float ux = t.x * rs, uy = -t.y * rs;
@@ -489,24 +499,24 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     const float K = static_cast<float>(n_d * n_sub);
 
     // G = sum_s z_s z_s^H over the snapshots, z = (beams..., w_q)^H y_s.
-    constexpr int kG = kSubMaxK * (kSubMaxK + 1);  // upper triangle, (re, im)
+    constexpr int kG = (NB + 1) * (NB + 2);  // upper triangle, (re, im)
     float g[kG];
 #pragma unroll
     for (int e = 0; e < kG; ++e) g[e] = 0.f;
     for (int d = 0; d < n_d; ++d) {
       // Prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y_d[t'] (warp scans, 32 at a time).
-      float2 carry[kSubMaxBeams];
+      float2 carry[NB];
 #pragma unroll
-      for (int k = 0; k < kSubMaxBeams; ++k) carry[k] = make_float2(0.f, 0.f);
+      for (int k = 0; k < NB; ++k) carry[k] = make_float2(0.f, 0.f);
       if (lane == 0)
 #pragma unroll
-        for (int k = 0; k < kSubMaxBeams; ++k)
+        for (int k = 0; k < NB; ++k)
           if (k < nb) sm.pre[k][0] = make_float2(0.f, 0.f);
       for (int t0 = 0; t0 < n_act; t0 += 32) {
         const int t = t0 + lane;
         const float2 yv = t < n_act ? srow[d * kSubMaxN + t] : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < kSubMaxBeams; ++k) {
+        for (int k = 0; k < NB; ++k) {
           if (k >= nb) continue;
           const float2 tw = t < n_act ? beam_twiddle(sm.tw1[t], k) : make_float2(1.f, 0.f);
           float2 v = make_float2(tw.x * yv.x - tw.y * yv.y, tw.x * yv.y + tw.y * yv.x);
@@ -526,10 +536,10 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       __syncwarp();
       const float2* yr = srow + d * kSubMaxN;
       for (int s0 = lane; s0 < n_sub; s0 += 32) {
-        float2 z[kSubMaxK];
+        float2 z[(NB + 1)];
         // Beams: u_b^H y_s = conj(tw_b[s0]) (P_b[s0 + L] - P_b[s0]) / sqrt(L).
 #pragma unroll
-        for (int k = 0; k < kSubMaxBeams; ++k) {
+        for (int k = 0; k < NB; ++k) {
           z[k] = make_float2(0.f, 0.f);
           if (k >= nb) continue;
           const float2 hi = sm.pre[k][s0 + L], lo = sm.pre[k][s0];
@@ -545,12 +555,12 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
             zw.x = fmaf(q.x, yv.x, fmaf(q.y, yv.y, zw.x));
             zw.y = fmaf(q.x, yv.y, fmaf(-q.y, yv.x, zw.y));
           }
-        z[kSubMaxBeams] = zw;
+        z[NB] = zw;
         int e = 0;
 #pragma unroll
-        for (int r = 0; r < kSubMaxK; ++r)
+        for (int r = 0; r < (NB + 1); ++r)
 #pragma unroll
-          for (int c = r; c < kSubMaxK; ++c, e += 2) {
+          for (int c = r; c < (NB + 1); ++c, e += 2) {
             g[e] = fmaf(z[r].x, z[c].x, fmaf(z[r].y, z[c].y, g[e]));      // z_r conj(z_c)
             g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
           }
@@ -562,32 +572,32 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       for (int o2 = 16; o2 > 0; o2 >>= 1) g[e] += __shfl_xor_sync(0xffffffffu, g[e], o2);
 
     // Basis in use: beams k < nb, and w_q if it survived.
-    bool keep[kSubMaxK];
+    bool keep[(NB + 1)];
 #pragma unroll
-    for (int k = 0; k < kSubMaxBeams; ++k) keep[k] = k < nb;
-    keep[kSubMaxBeams] = has_w;
+    for (int k = 0; k < NB; ++k) keep[k] = k < nb;
+    keep[NB] = has_w;
     // Right-hand side Q^H 1: sqrt(L) for the look direction, 0 for the other
     // beams; w_q^H 1 for the network's direction.
-    float2 bq[kSubMaxK];
+    float2 bq[(NB + 1)];
 #pragma unroll
-    for (int k = 0; k < kSubMaxK; ++k) bq[k] = make_float2(0.f, 0.f);
+    for (int k = 0; k < (NB + 1); ++k) bq[k] = make_float2(0.f, 0.f);
     bq[0] = make_float2(sqrtf(static_cast<float>(L)), 0.f);
     {
       float2 sq = make_float2(0.f, 0.f);
       if (2 * lane < L) sq = make_float2(wv[0].x, -wv[0].y);
       if (2 * lane + 1 < L) sq = make_float2(sq.x + wv[1].x, sq.y - wv[1].y);
-      bq[kSubMaxBeams] = warp_sum2(sq);
+      bq[NB] = warp_sum2(sq);
     }
 
     // Solve (G / K + eps I) c = b in every lane (complex Cholesky, k <= 6).
     const float eps = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);
-    float2 A[kSubMaxK][kSubMaxK];
+    float2 A[(NB + 1)][(NB + 1)];
     {
       int e = 0;
 #pragma unroll
-      for (int r = 0; r < kSubMaxK; ++r)
+      for (int r = 0; r < (NB + 1); ++r)
 #pragma unroll
-        for (int c = r; c < kSubMaxK; ++c, e += 2) {
+        for (int c = r; c < (NB + 1); ++c, e += 2) {
           float2 x = make_float2(g[e] / K, g[e + 1] / K);
           if (r == c) x = make_float2(x.x + eps, 0.f);
           if (!(keep[r] && keep[c])) x = (r == c) ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
@@ -597,21 +607,21 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     }
     bool ok = true;
 #pragma unroll
-    for (int c = 0; c < kSubMaxK; ++c) {
+    for (int c = 0; c < (NB + 1); ++c) {
       float dsum = A[c][c].x;
 #pragma unroll
-      for (int k = 0; k < kSubMaxK; ++k)
+      for (int k = 0; k < (NB + 1); ++k)
         if (k < c) dsum -= A[c][k].x * A[c][k].x + A[c][k].y * A[c][k].y;
       ok = ok && dsum > 0.f;
       const float lc = sqrtf(fmaxf(dsum, 1e-30f));
       A[c][c] = make_float2(lc, 0.f);
       const float il = 1.0f / lc;
 #pragma unroll
-      for (int r = 0; r < kSubMaxK; ++r) {
+      for (int r = 0; r < (NB + 1); ++r) {
         if (r <= c) continue;
         float2 s = A[r][c];
 #pragma unroll
-        for (int k = 0; k < kSubMaxK; ++k)
+        for (int k = 0; k < (NB + 1); ++k)
           if (k < c) {  // s -= L[r][k] conj(L[c][k])
             s.x -= A[r][k].x * A[c][k].x + A[r][k].y * A[c][k].y;
             s.y -= A[r][k].y * A[c][k].x - A[r][k].x * A[c][k].y;
@@ -619,12 +629,12 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
         A[r][c] = make_float2(s.x * il, s.y * il);
       }
     }
-    float2 cv[kSubMaxK];
+    float2 cv[(NB + 1)];
 #pragma unroll
-    for (int r = 0; r < kSubMaxK; ++r) {  // forward: L u = b
+    for (int r = 0; r < (NB + 1); ++r) {  // forward: L u = b
       float2 s = keep[r] ? bq[r] : make_float2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < kSubMaxK; ++k)
+      for (int k = 0; k < (NB + 1); ++k)
         if (k < r) {
           s.x -= A[r][k].x * cv[k].x - A[r][k].y * cv[k].y;
           s.y -= A[r][k].x * cv[k].y + A[r][k].y * cv[k].x;
@@ -632,10 +642,10 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       cv[r] = make_float2(s.x / A[r][r].x, s.y / A[r][r].x);
     }
 #pragma unroll
-    for (int r = kSubMaxK - 1; r >= 0; --r) {  // backward: L^H c = u
+    for (int r = (NB + 1) - 1; r >= 0; --r) {  // backward: L^H c = u
       float2 s = cv[r];
 #pragma unroll
-      for (int k = 0; k < kSubMaxK; ++k)
+      for (int k = 0; k < (NB + 1); ++k)
         if (k > r) {  // s -= conj(L[k][r]) c_k
           s.x -= A[k][r].x * cv[k].x + A[k][r].y * cv[k].y;
           s.y -= A[k][r].x * cv[k].y - A[k][r].y * cv[k].x;
@@ -649,10 +659,10 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     for (int h = 0; h < 2; ++h) {
       const int i = 2 * lane + h;   // the element this lane holds in wv[h] and av4
       if (i >= L) continue;
-      float2 w = make_float2(wv[h].x * cv[kSubMaxBeams].x - wv[h].y * cv[kSubMaxBeams].y,
-                             wv[h].x * cv[kSubMaxBeams].y + wv[h].y * cv[kSubMaxBeams].x);
+      float2 w = make_float2(wv[h].x * cv[NB].x - wv[h].y * cv[NB].y,
+                             wv[h].x * cv[NB].y + wv[h].y * cv[NB].x);
 #pragma unroll
-      for (int k = 0; k < kSubMaxBeams; ++k) {
+      for (int k = 0; k < NB; ++k) {
         if (k >= nb) continue;
         const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
         const float ux = t.x * rs, uy = -t.y * rs;
@@ -670,8 +680,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
     if (lane == 0) {
       const float dn = den.x * den.x + den.y * den.y;
       if (!ok || !(dn > 1e-30f)) {
-        const int slot = atomicAdd(a.gated_count, 1);
-        if (slot < a.gated_cap) a.gated[slot] = make_int2(pix, static_cast<int>(frame));
+        push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
         if (a.stats) atomicAdd(a.stats, 1);
       } else {
         const float scale = meta.y * meta.z / dn;   // n_act * cf * num / den
@@ -783,18 +792,25 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.stats = stats;
   if (l.n_ch > kSubMaxN || a.n_dmax > 9)
     return fail(USX_ERR_UNSUPPORTED, "learned-subspace refinement supports <= 128 channels, range average <= 4");
-  const int smem = static_cast<int>(sub_warp_bytes(a.n_dmax) * kSubWarps);
-  USX_CUDA(cudaFuncSetAttribute(lmv_subspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  int per_sm = 0;
-  USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lmv_subspace_kernel, 32 * kSubWarps, smem));
-  const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
-  const long need = (a.n_rows + kSubWarps - 1) / kSubWarps;
-  prof_begin(ctx, "lmv_subspace_kernel");
-  lmv_subspace_kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem,
-                        ctx->stream>>>(a);
-  prof_end(ctx);
-  USX_CHECK_LAUNCH("lmv_subspace_kernel");
-  return USX_OK;
+  auto go = [&](auto kernel, size_t per_warp) -> int {
+    const int smem = static_cast<int>(per_warp * kSubWarps);
+    USX_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int per_sm = 0;
+    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * kSubWarps, smem));
+    const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
+    const long need = (a.n_rows + kSubWarps - 1) / kSubWarps;
+    prof_begin(ctx, "lmv_subspace_kernel");
+    kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem, ctx->stream>>>(a);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("lmv_subspace_kernel");
+    return USX_OK;
+  };
+  switch (std::min(kSubMaxBeams, 1 + n_beams)) {
+    case 1: return go(lmv_subspace_kernel<1>, sub_warp_bytes<1>(a.n_dmax));
+    case 3: return go(lmv_subspace_kernel<3>, sub_warp_bytes<3>(a.n_dmax));
+    case 5: return go(lmv_subspace_kernel<5>, sub_warp_bytes<5>(a.n_dmax));
+    default: return go(lmv_subspace_kernel<7>, sub_warp_bytes<7>(a.n_dmax));
+  }
 }
 
 }  // namespace usxcu

@@ -1338,15 +1338,26 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
     // largest subarray and the whole array.
     MvWarpArgs w{};
     w.base = a;
-    w.lmax = a.lmax;
-    w.nmax = n_ch;
+    w.lmax = extra.list_lmax > 0 ? std::min(extra.list_lmax, a.lmax) : a.lmax;
+    w.nmax = extra.list_nmax > 0 ? std::min(extra.list_nmax, n_ch) : n_ch;
     w.pair_list = extra.list;
     w.pair_count = extra.list_count;
     w.pair_cap = extra.list_cap;
-    w.overflow_count = extra.overflow_count;
+    const bool limited = w.lmax < a.lmax || w.nmax < n_ch;
+    if (limited && !extra.overflow_count)
+      return fail(USX_ERR_INVALID, "minimum variance: a limited work list needs an overflow list");
+    w.overflow_count = limited ? extra.overflow_count : nullptr;
     w.overflow = extra.overflow;
-    w.overflow_cap = 0;
+    w.overflow_cap = limited ? extra.overflow_cap : 0;
+    if (limited) USX_CUDA(cudaMemsetAsync(extra.overflow_count, 0, sizeof(int), ctx->stream));
     if (int rc = launch_warp(w, -1, "mv_warp_kernel(list)")) return rc;
+    if (limited) {
+      MvTcArgs b = a;
+      b.list = extra.overflow;
+      b.list_count = extra.overflow_count;
+      b.list_cap = extra.overflow_cap;
+      if (int rc = launch_cta(b, true)) return rc;
+    }
   } else if (extra.n_classes > 0 && extra.overflow_count) {
     // Pixel classes of similar subarray length, one launch each; pixels past
     // a class's limits go to the CTA kernel through the overflow list.

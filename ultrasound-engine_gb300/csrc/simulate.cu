@@ -4,10 +4,11 @@
 //   stage 1  the incident field at the scatterer, a sum over firing elements of
 //            the delayed, weighted two-way pulse linearly interpolated onto an
 //            oversampled time axis, built in the warp's shared-memory buffer.
-//            Per element the lanes split the pulse taps; the "next sample"
-//            terms of all taps are added before the "this sample" terms, which
-//            is exactly the order in which the reference's serial tap loop
-//            updates each buffer position, so the buffer is bit-identical;
+//            Per element the lanes split the buffer slots the pulse covers;
+//            each slot adds the "next sample" term of the previous tap and
+//            then the "this sample" term of its own tap, which is exactly the
+//            order in which the reference's serial tap loop updates each
+//            buffer position, so the buffer is bit-identical;
 //   trim     the buffer's -40 dB tails are cut (warp max + ballots);
 //   stage 2  for every receive element the lanes produce the delayed,
 //            weighted echo samples and add them into RF[event][element][n]
@@ -155,19 +156,18 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
       const int base = e_base[q];
       const float frac = centre - floorf(centre);
       const float omf = 1.0f - frac;
-      // "next sample" terms first, then "this sample" terms (see header).
-      for (int k = lane; k < a.pulse_n; k += 32) {
-        const int idx = base + k;
-        if (idx < 0 || idx + 1 >= inc_n) continue;
-        const float v = amp * pulse[k];
-        inc[idx + 1] += v * frac;
-      }
-      __syncwarp();
-      for (int k = lane; k < a.pulse_n; k += 32) {
-        const int idx = base + k;
-        if (idx < 0 || idx + 1 >= inc_n) continue;
-        const float v = amp * pulse[k];
-        inc[idx] += v * omf;
+      // One lane per buffer slot s = base + j: first the "next sample" term of
+      // tap j - 1, then the "this sample" term of tap j, which is the order in
+      // which the reference's serial tap loop updates slot s (see header).
+      for (int j = lane; j <= a.pulse_n; j += 32) {
+        const int s = base + j;
+        const bool nx = j >= 1 && s >= 1 && s < inc_n;          // tap j - 1 at index s - 1
+        const bool th = j < a.pulse_n && s >= 0 && s + 1 < inc_n; // tap j at index s
+        if (!nx && !th) continue;
+        float t = inc[s];
+        if (nx) t += (amp * pulse[j - 1]) * frac;
+        if (th) t += (amp * pulse[j]) * omf;
+        inc[s] = t;
       }
       __syncwarp();
       if (!a.full) break;

@@ -230,6 +230,7 @@ struct MvTcExtra {
   const int2* list = nullptr;
   const int* list_count = nullptr;
   int list_cap = 0;
+  int list_lmax = 0, list_nmax = 0;  // limits of the listed pixels (0: the plan's L and all channels)
   float* w_export = nullptr;
   uint8_t* w_valid = nullptr;
   const MvClass* classes = nullptr;  // full frames by class (else the CTA-per-pixel kernel)
@@ -248,6 +249,9 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
 // Learned minimum variance (learned.cu): per-pixel features of the compounded
 // channel samples, and the gated apply of the network's weights.
 constexpr int kLmvFeatures = 256;  // network inputs per pixel
+// Gated pixels are listed per subarray class c (L in (16 c, 16 (c + 1)]).
+constexpr int kLmvGateClasses = 4;
+constexpr int kLmvClassWidth = 16;
 constexpr int kLmvOutputs = 128;   // network outputs per pixel: 64 complex weights
 struct LmvLaunch {
   const float2* y = nullptr;       // [frame][pix][n_ch]

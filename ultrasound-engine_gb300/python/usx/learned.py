@@ -475,7 +475,7 @@ def main(argv=None) -> None:
     else:
         out = Path(a.weights)
         mlp = load_mlp(imager.ctx, out)
-        prev = Path(a.report) if a.report else out.with_suffix(".json")
+        prev = out.with_suffix(".json")
         if prev.exists():  # keep the training record, replace the evaluation
             report = {**json.loads(prev.read_text()), **report}
     results = evaluate(imager, mlp, eval_seeds, gates, refine=a.refine)
