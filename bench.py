@@ -237,7 +237,11 @@ WEIGHTS = PKG / "weights" / "learned_mv_128ch_l64.bin"
 # DRAM bytes per launch of the dominant kernels from one ncu capture of the
 # same workload (profiles/ holds the summaries these come from), scaled to a
 # full 512-line frame where the capture was a subset of lines.
-TRAFFIC_PER_FRAME = {}
+TRAFFIC_PER_FRAME = {
+    # profiles/lmv_subspace_kernel_7beams_64x1024.md: 96.15 MB read + 2.83 MB written for the
+    # first 64 of 512 lines, scaled by 8 (deeper lines read wider apertures: a lower bound).
+    "lmv_subspace_kernel": 8 * (96.148e6 + 2.830e6),
+}
 
 
 def timed(stream, fn, steps: int):
@@ -254,7 +258,21 @@ def timed(stream, fn, steps: int):
     return ev0.elapsed_time(ev1)
 
 
-def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks: dict) -> dict:
+def subspace_flops_per_frame(grid_pts: np.ndarray, nb: int) -> float:
+    """Algorithmic FLOPs of the learned-subspace refinement over the grid."""
+    z, x = grid_pts[:, 2], grid_pts[:, 0]
+    ex = (np.arange(N_EL) - 0.5 * (N_EL - 1)) * 300e-6
+    n_act = (np.abs(ex[None, :] - x[:, None]) < 0.5 * z[:, None] / MV_KW["f_number"]).sum(1).astype(np.float64)
+    L = np.clip(np.minimum(MV_KW["mv_subarray"], np.maximum(2, n_act // 2)), 2, None)
+    n_d = 2 * MV_KW["mv_range_average"] + 1
+    K = n_d * (n_act - L + 1)
+    k = np.minimum(nb, L) + 1
+    f = 8 * K * (L + k * (k + 1) / 2) + 8 * n_d * n_act * np.minimum(nb, L)
+    return float(np.sum(f[n_act >= 4]))
+
+
+def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks: dict,
+                    refine_beams: int = -1) -> dict:
     """Roofline of the dominant kernel of the timed region: algorithmic work
     per frame over that kernel's device time per frame (CUDA events on the
     launching stream)."""
@@ -285,6 +303,15 @@ def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks:
                    hbm_frac=hbm / peaks["hbm_gbs"],
                    note="20 FP32 flops per active (pixel, channel, transmit); peak = nominal FP32 "
                         "(152 SMs x 128 lanes x FMA x 2.07 GHz); compulsory HBM bytes = IQ + frame")
+    elif base.startswith("lmv_subspace"):
+        nb = min(7, 1 + max(0, refine_beams))
+        flops = subspace_flops_per_frame(pts, nb)
+        achieved = flops / (kms / 1e3) / 1e12
+        out.update(bound="fp32", achieved=achieved, peak=FP32_NOMINAL_TFLOPS, unit="TFLOP/s",
+                   algorithmic_gflop_per_frame=flops / 1e9,
+                   note="per pixel: 8 (L + k(k+1)/2) flops per snapshot (network-direction projection, "
+                        "k = beams + 1 Gram entries) + 8 flops per beam and range-row sample (prefix "
+                        "sums); peak = nominal FP32")
     elif base.startswith("mlp"):
         flops = 2.0 * len(pts) * sum(a * b for a, b in zip((256, 256, 256, 256), (256, 256, 256, 128)))
         achieved = flops / (kms / 1e3) / 1e12
@@ -408,7 +435,7 @@ def run_ours(args) -> None:
 
     peaks = load_peaks()
     launches_in_region = sum(n for _, n in prof.values())
-    roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks)
+    roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks, extra.get("refine_beams", -1))
 
     e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world)
     if bkw.get("combiner") == 2:

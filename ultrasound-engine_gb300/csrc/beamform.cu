@@ -932,8 +932,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
                       mv_tc_supported(a.n_ch, a.mv_subarray, a.mv_range_average);
   const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
   const size_t smem = sizeof(MvShared) * kMvWarps;
-  USX_CUDA(cudaFuncSetAttribute(mv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(smem)));
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   const dim3 grid_mv(ceil_div(n_pix, kMvWarps), n_frames);
   if (incoherent) USX_CUDA(cudaMemsetAsync(a.acc_out, 0, acc_bytes, ctx->stream));
   const int n_pass = incoherent ? ev_per_frame : 1;

@@ -7,6 +7,10 @@
 #include <string>
 #include <vector>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "usx_internal.cuh"
 
 namespace usxcu {
@@ -108,6 +112,38 @@ void prof_begin(usx_ctx* ctx, const char* name) {
 void prof_end(usx_ctx* ctx) {
   if (!ctx->profiling || ctx->prof.empty()) return;
   cudaEventRecord(ctx->prof.back().stop, ctx->stream);
+}
+
+namespace {
+std::mutex g_launch_mu;
+std::map<std::pair<int, const void*>, size_t> g_smem_set;
+std::map<std::tuple<int, const void*, int, size_t>, int> g_occupancy;
+}  // namespace
+
+int smem_limit(const void* func, size_t bytes) {
+  int dev = 0;
+  USX_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_launch_mu);
+  size_t& have = g_smem_set[{dev, func}];
+  if (bytes <= have) return USX_OK;
+  USX_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)));
+  have = bytes;
+  return USX_OK;
+}
+
+int occupancy(const void* func, int threads, size_t smem, int* blocks_per_sm) {
+  int dev = 0;
+  USX_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_launch_mu);
+  const auto key = std::make_tuple(dev, func, threads, smem);
+  auto it = g_occupancy.find(key);
+  if (it == g_occupancy.end()) {
+    int n = 0;
+    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, func, threads, smem));
+    it = g_occupancy.emplace(key, n).first;
+  }
+  *blocks_per_sm = it->second;
+  return USX_OK;
 }
 
 int validate_channel(const usx_channel_desc& cd) {

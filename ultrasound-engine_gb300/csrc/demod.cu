@@ -130,8 +130,7 @@ extern "C" int usx_cu_demodulate(usx_ctx* ctx, const usx_channel_desc* cd,
   const int span = kOut * dec + n_taps - 1;
   const size_t smem = sizeof(float2) * static_cast<size_t>(span) * (1 + kTraces);
   if (smem > 48 * 1024)
-    USX_CUDA(cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(demod_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   const long gx = (p.n_traces + kTraces - 1) / kTraces;
   const int gy = ceil_div(p.n_out, kOut);
   if (gx > 0x7fffffffL || gy > 65535) return fail(USX_ERR_UNSUPPORTED, "usx_cu_demodulate: acquisition too large");

@@ -286,8 +286,7 @@ int launch_wall(usx_ctx* ctx, const float* ens, int n, long n_pix, int type, int
   const int threads = 128;
   const size_t smem = sizeof(float2) * n * threads;
   if (smem > 48 * 1024)
-    USX_CUDA(cudaFuncSetAttribute(wall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(wall_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   wall_kernel<<<ceil_div(n_pix, threads), threads, smem, ctx->stream>>>(a);
   USX_CHECK_LAUNCH("wall_kernel");
   return USX_OK;
@@ -470,7 +469,7 @@ int usx_cu_color_flow_noalloc(void* stream, const float* ens, int n_frames, int 
   const int threads = 128;
   const size_t smem = sizeof(float2) * n_frames * threads;
   if (smem > 48 * 1024)
-    USX_CUDA(cudaFuncSetAttribute(wall_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(wall_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   wall_kernel<<<ceil_div(n_pix, threads), threads, smem, st>>>(w);
   USX_CHECK_LAUNCH("wall_kernel");
 

@@ -723,9 +723,9 @@ int launch_lmv_features(usx_ctx* ctx, const LmvLaunch& l) {
   a.out = l.out;
   a.out_stride = l.out_stride;
   const int smem = lmv_features_smem(l.n_ch, l.range_avg);
-  USX_CUDA(cudaFuncSetAttribute(lmv_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(lmv_features_kernel), static_cast<size_t>(smem))) return rc_;
   int per_sm = 0;
-  USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lmv_features_kernel, 32 * kLmvWarps, smem));
+  if (int rc_ = occupancy(reinterpret_cast<const void*>(lmv_features_kernel), 32 * kLmvWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
   const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
   const long need = (a.n_rows + kLmvWarps - 1) / kLmvWarps;
   prof_begin(ctx, "lmv_features_kernel");
@@ -794,9 +794,9 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
     return fail(USX_ERR_UNSUPPORTED, "learned-subspace refinement supports <= 128 channels, range average <= 4");
   auto go = [&](auto kernel, size_t per_warp) -> int {
     const int smem = static_cast<int>(per_warp * kSubWarps);
-    USX_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(kernel), static_cast<size_t>(smem))) return rc_;
     int per_sm = 0;
-    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * kSubWarps, smem));
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(kernel), 32 * kSubWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
     const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
     const long need = (a.n_rows + kSubWarps - 1) / kSubWarps;
     prof_begin(ctx, "lmv_subspace_kernel");

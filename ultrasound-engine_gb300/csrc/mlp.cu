@@ -532,8 +532,7 @@ int launch_gemm(cudaStream_t st, const __nv_bfloat16* A, int lda, bool a_kmajor,
   g.atomic = split_k > 1;
   g.k_per_split = ((K / split_k + BK - 1) / BK) * BK;
   const int nz = (K + g.k_per_split - 1) / g.k_per_split;
-  USX_CUDA(cudaFuncSetAttribute(gemm_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(kGemmSmem)));
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(gemm_bf16_kernel), static_cast<size_t>(static_cast<int>(kGemmSmem)))) return rc_;
   gemm_bf16_kernel<<<dim3(N / BN, M / BM, nz), kGemmThreads, kGemmSmem, st>>>(g);
   USX_CHECK_LAUNCH("gemm_bf16_kernel");
   return USX_OK;

@@ -1302,9 +1302,9 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
   auto launch_cta = [&](const MvTcArgs& b, bool list_mode) -> int {
     const MvTcLayout l = mv_tc_layout(n_ch, b.n_dmax, b.lmax);
     const size_t smem = l.bytes;
-    USX_CUDA(cudaFuncSetAttribute(mv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_tc_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
     int per_sm = 0;
-    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_tc_kernel, 32 * kTcWarps, smem));
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(mv_tc_kernel), 32 * kTcWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
     // Full frames: a grid-stride loop over pixels, frames on y. Work list: its
     // length is only known on the device, so one resident wave loops over it.
     const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
@@ -1321,9 +1321,9 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
     const MvWarpLayout l = mv_warp_layout(w.nmax, a.n_dmax, w.lmax);
     const size_t smem = l.bytes * kWarpMvWarps;
     if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "minimum variance: class too large for shared memory");
-    USX_CUDA(cudaFuncSetAttribute(mv_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_warp_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
     int per_sm = 0;
-    USX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mv_warp_kernel, 32 * kWarpMvWarps, smem));
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(mv_warp_kernel), 32 * kWarpMvWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
     const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
     const long need = (items + kWarpMvWarps - 1) / kWarpMvWarps;
     const long blocks = items < 0 ? resident : std::max(1L, std::min(need, resident * 8));
@@ -1387,7 +1387,7 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
   }
   // FP64 re-solve of the pixels whose refined residual failed (usually none).
   const size_t smem64 = sizeof(double2) * (a.lmax * (a.lmax + 1) / 2) + sizeof(int) * n_ch;
-  USX_CUDA(cudaFuncSetAttribute(mv_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem64)));
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_fp64_kernel), static_cast<size_t>(static_cast<int>(smem64)))) return rc_;
   prof_begin(ctx, "mv_fp64_kernel");
   mv_fp64_kernel<<<ctx->sm_count * 4, 32, smem64, ctx->stream>>>(a);
   prof_end(ctx);

@@ -218,8 +218,7 @@ int usx_cu_envelope(usx_ctx* ctx, const float* frame, int n0, int n1, float fdem
   USX_CUDA(cudaMemcpyAsync(ws, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, ctx->stream));
   const size_t smem = sizeof(float2) * n_fft;
   if (smem > 48 * 1024)
-    USX_CUDA(cudaFuncSetAttribute(hilbert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)));
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(hilbert_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   hilbert_kernel<<<n0, 256, smem, ctx->stream>>>(reinterpret_cast<const float2*>(frame), n1, n_fft,
                                                  log2n, static_cast<const float2*>(ws), env);
   USX_CHECK_LAUNCH("hilbert_kernel");

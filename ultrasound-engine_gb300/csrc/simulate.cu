@@ -390,8 +390,7 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   const size_t smem = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem) +
                                        (a.t_table ? static_cast<size_t>(n_smp) : 0));
   if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
-  USX_CUDA(cudaFuncSetAttribute(simulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(smem)));
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(simulate_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
   if (n_scat > 0) {
     prof_begin(ctx, "simulate_kernel");
     simulate_kernel<<<dim3(static_cast<unsigned>(gx), n_ev), 32 * kSimWarps, smem, ctx->stream>>>(a);

@@ -71,6 +71,14 @@ int scratch(usx_ctx* ctx, size_t bytes, void** out);
 void prof_begin(usx_ctx* ctx, const char* name);
 void prof_end(usx_ctx* ctx);
 
+// Launch-configuration queries, cached per device and kernel so that a plan
+// that has run once makes no attribute or occupancy call again (its launches
+// can then be captured into a CUDA graph): smem_limit raises a kernel's
+// dynamic shared-memory limit only when `bytes` exceeds what was set before;
+// occupancy returns cudaOccupancyMaxActiveBlocksPerMultiprocessor.
+int smem_limit(const void* func, size_t bytes);
+int occupancy(const void* func, int threads, size_t smem, int* blocks_per_sm);
+
 // ------------------------------------------------------------- device side
 
 constexpr float kPi = 3.14159265358979323846f;

@@ -414,10 +414,13 @@ def summarize(rows) -> dict:
         p, l_ = np.array(flat(k, "plain")), np.array(flat(k, "learned"))
         if p.size:
             rel = np.abs(l_ - p) / np.maximum(np.abs(p), 1e-12)
+            where = [(r["seed"], i) for r in rows for i in range(len(r["plain"][k]))]
+            worst = [{"seed": int(where[j][0]), "target": int(where[j][1]), "plain": float(p[j]),
+                      "learned": float(l_[j])} for j in np.argsort(-rel)[:3]]
             out[k] = {"plain_mean": float(p.mean()), "learned_mean": float(l_.mean()),
                       "max_abs_delta": float(np.max(np.abs(l_ - p))), "mean_delta": float(np.mean(l_ - p)),
                       "max_rel_delta": float(np.max(rel)), "median_rel_delta": float(np.median(rel)),
-                      "n": int(p.size)}
+                      "n": int(p.size), "worst": worst}
     out["rows"] = rows
     return out
 
