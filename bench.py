@@ -238,9 +238,9 @@ WEIGHTS = PKG / "weights" / "learned_mv_128ch_l64.bin"
 # same workload (profiles/ holds the summaries these come from), scaled to a
 # full 512-line frame where the capture was a subset of lines.
 TRAFFIC_PER_FRAME = {
-    # profiles/lmv_subspace_kernel_7beams_64x1024.md: 96.15 MB read + 2.83 MB written for the
-    # first 64 of 512 lines, scaled by 8 (deeper lines read wider apertures: a lower bound).
-    "lmv_subspace_kernel": 8 * (96.148e6 + 2.830e6),
+    # profiles/lmv_subspace_gram_kernel_7beams_64x1024.md: 96.11 MB read + 10.08 MB written for
+    # the first 64 of 512 lines, scaled by 8 (deeper lines read wider apertures: a lower bound).
+    "lmv_subspace_gram_kernel": 8 * (96.113e6 + 10.075e6),
 }
 
 
@@ -303,7 +303,7 @@ def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks:
                    hbm_frac=hbm / peaks["hbm_gbs"],
                    note="20 FP32 flops per active (pixel, channel, transmit); peak = nominal FP32 "
                         "(152 SMs x 128 lanes x FMA x 2.07 GHz); compulsory HBM bytes = IQ + frame")
-    elif base.startswith("lmv_subspace"):
+    elif base.startswith("lmv_subspace"):  # the Gram stage dominates; the per-pixel solve is ~0.2 ms
         nb = min(7, 1 + max(0, refine_beams))
         flops = subspace_flops_per_frame(pts, nb)
         achieved = flops / (kms / 1e3) / 1e12
@@ -550,6 +550,306 @@ def run_stage(args) -> None:
     ctx.close()
 
 
+def _capi_channel(capi, probe, medium, acq, txs, is_iq=False, fdem=0.0):
+    tx = [dict(type=int(t.type.value) if hasattr(t.type, "value") else 1, angle=t.angle,
+               focus=(t.focus.x, t.focus.y, t.focus.z), origin=(t.origin.x, t.origin.y, t.origin.z),
+               delays=t.delays, apodization=t.apodization) for t in txs]
+    return capi.Channel(capi.Probe(probe.n_elements, probe.pitch, probe.element_width, probe.elevation_height,
+                                   probe.center_frequency, probe.bandwidth),
+                        capi.Medium(medium.speed_of_sound, medium.attenuation, medium.density),
+                        capi.Acquisition(acq.sampling_frequency, acq.n_samples, acq.t0, acq.prf), tx, is_iq, fdem)
+
+
+def _scatterers(ph) -> np.ndarray:
+    pos, amp, vel = np.asarray(ph.positions), np.asarray(ph.amplitudes), np.asarray(ph.velocities)
+    sc = np.zeros((len(amp), 8), np.float32)
+    sc[:, :3], sc[:, 3], sc[:, 4:7] = pos, amp, vel
+    return sc
+
+
+def _stage_line(metric, unit, value, args, ms, prof, clocks, config, roofline, extra=None) -> dict:
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-simulated phantom)",
+            "config": config, "gpu_launches": sum(n for _, n in prof.values()), "roofline": roofline,
+            "kernels_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+            "clocks": clocks.summary()}
+    line.update(extra or {})
+    return line
+
+
+def run_doppler(args) -> None:
+    """Colour flow of uneven ensembles packed into one launch sequence: a
+    3 mm vessel at 25 degrees (parabolic flow, 0.4 m/s peak, blood at 0.1 x the
+    tissue amplitude, tissue moving at 5 mm/s), ensembles of 8, 12, 16 and 32
+    pulses at 5 kHz, 3 plane waves per pulse, 32 ensembles; one step = the
+    delay-and-sum of all 544 frames (one launch) + order-2 polynomial wall
+    filter and Loupas velocity for all 32 ensembles (one launch sequence)."""
+    import torch
+    import usx
+    from usx import capi
+    torch.cuda.set_device(0)
+    probe = usx.Probe()
+    probe.n_elements, probe.pitch, probe.element_width = N_EL, 300e-6, 270e-6
+    probe.center_frequency, probe.bandwidth = F0, 0.6
+    medium = usx.Medium()
+    acq = usx.presets.acquisition(probe, depth=0.04, medium=medium, samples_per_wavelength=FS / F0)
+    acq.prf = 5000.0
+    sim = usx.Simulator(probe, medium, acq, usx.SimulatorConfig())
+    angles = usx.angles_deg(-5, 5, 3)
+    lens = [8, 12, 16, 32] * 8
+    n_max = max(lens)
+    txs = sim.make_plane_waves(angles * n_max)
+    ph = usx.phantoms.flow_phantom(probe, medium, vessel_depth=0.022, vessel_radius=0.003, angle_deg=25.0,
+                                  peak_velocity=0.4, z_min=0.005, z_max=0.04)
+    sc = _scatterers(ph)
+    blood = np.linalg.norm(sc[:, 4:7], axis=1) > 0
+    sc[blood, 3] *= 0.1 / max(1e-12, np.abs(sc[blood, 3]).mean() / max(1e-12, np.abs(sc[~blood, 3]).mean()))
+    sc[~blood, 6] = 0.005                       # tissue drifting axially at 5 mm/s
+    ctx = capi.Context(0)
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    n_ev, n_smp = len(txs), acq.n_samples
+    d_sc = torch.from_numpy(sc).cuda()
+    d_rf = torch.empty((n_ev, N_EL, n_smp), dtype=torch.float32, device="cuda")
+    d_iq1 = torch.empty((n_ev, N_EL, n_smp), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.simulate(ch_rf, capi.sim_config(noise_db=-200.0), d_sc.data_ptr(), len(sc), None, d_rf.data_ptr())
+    ctx.demodulate(ch_rf, capi.demod_config(), d_rf.data_ptr(), d_iq1.data_ptr())
+    ctx.synchronize()
+    # Pack the 32 ensembles (each the first n_e pulses) into one acquisition.
+    n_frames_total = sum(lens)
+    iq = torch.empty((3 * n_frames_total, N_EL, n_smp), dtype=torch.complex64, device="cuda")
+    off, offsets = 0, []
+    for n in lens:
+        iq[3 * off:3 * (off + n)] = d_iq1[:3 * n]
+        offsets.append(off)
+        off += n
+    del d_rf
+    all_tx = [t for n in lens for t in txs[:3 * n]]
+    ch_iq = _capi_channel(capi, probe, medium, acq, all_tx, is_iq=True, fdem=F0)
+    n0, n1 = 256, 512
+    grid = usx.grid_for(probe, 0.01, 0.035, n0, n1)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), np.asarray(grid.points).reshape(-1, 3))
+    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(f_number=1.5))
+    frames = torch.empty((n_frames_total, n0 * n1), dtype=torch.complex64, device="cuda")
+    n_ens = len(lens)
+    vel = torch.empty((n_ens, n0 * n1), device="cuda")
+    pw, var = torch.empty_like(vel), torch.empty_like(vel)
+    valid = torch.empty((n_ens, n0 * n1), dtype=torch.uint8, device="cuda")
+    dcfg = capi.doppler_config(wall_filter=1, polynomial_order=2, loupas=1)
+    axis1 = np.asarray(grid.axis1)
+
+    def step():
+        plan.execute_sequence(3, n_frames_total, iq.data_ptr(), frames.data_ptr(), n0 * n1)
+        ctx.color_flow_batch(frames.data_ptr(), lens, offsets, n0, n1, axis1, F0, acq.prf / 3.0,
+                             medium.speed_of_sound, dcfg, vel.data_ptr(), pw.data_ptr(), var.data_ptr(),
+                             valid.data_ptr())
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    capi.profile(ctx, True)
+    capi.profile_reset(ctx)
+    with ClockSampler(0) as clocks:
+        ms = timed(stream, step, args.steps)
+    prof = capi.profile_read(ctx)
+    capi.profile(ctx, False)
+    peaks = load_peaks()
+    per = {k: v[0] / args.steps for k, v in prof.items()}
+    flow = [k for k in per if k.startswith("flow") or k.startswith("wall")]
+    flow_ms = sum(per[k] for k in flow)
+    # Colour flow reads every packed frame once and writes four maps per ensemble.
+    flow_bytes = 8.0 * n_frames_total * n0 * n1 + n_ens * n0 * n1 * (3 * 4 + 1)
+    v = vel.cpu().numpy()
+    inside = valid.cpu().numpy().astype(bool)
+    roof = {"kernel": max(per, key=per.get), "bound": "hbm",
+            "achieved": flow_bytes / (flow_ms / 1e3) / 1e9 if flow_ms else None, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": (flow_bytes / (flow_ms / 1e3) / 1e9 / peaks["hbm_gbs"]) if flow_ms else None,
+            "traffic": None, "note": "achieved = colour-flow kernels' algorithmic bytes over their time"}
+    line = _stage_line("colour-flow ensembles/s (32 uneven ensembles of 8-32 pulses x 3 PW, 256x512)",
+                       "ensembles/s", n_ens * args.steps / (ms / 1e3), args, ms, prof, clocks,
+                       {"workload": "doppler_32ens_8-32pulses_3pw_256x512", "frames_per_step": n_frames_total,
+                        "events_per_step": 3 * n_frames_total},
+                       roof, {"valid_fraction": float(inside.mean()),
+                              "peak_velocity_valid_m_s": float(np.abs(v[inside]).max()) if inside.any() else None})
+    print(json.dumps(line))
+    plan.close()
+    ctx.close()
+
+
+def run_strain(args) -> None:
+    """Elastography: a 4x-stiff 5 mm inclusion at 30 mm under 1% compression,
+    one plane wave before and after; one step = two 256 x 1024 delay-and-sum
+    frames, axial displacement tracking and least-squares strain (2 mm fit)."""
+    import torch
+    import usx
+    from usx import capi
+    torch.cuda.set_device(0)
+    probe = usx.Probe()
+    probe.n_elements, probe.pitch, probe.element_width = N_EL, 300e-6, 270e-6
+    probe.center_frequency, probe.bandwidth = F0, 0.6
+    medium = usx.Medium()
+    acq = usx.presets.acquisition(probe, depth=0.05, medium=medium, samples_per_wavelength=FS / F0)
+    sim = usx.Simulator(probe, medium, acq, usx.SimulatorConfig())
+    txs = sim.make_plane_waves(usx.angles_deg(0, 0, 1))
+    ctx = capi.Context(0)
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    ch_iq = _capi_channel(capi, probe, medium, acq, txs, is_iq=True, fdem=F0)
+    n_smp = acq.n_samples
+    iqs = []
+    for strain in (0.0, 0.01):
+        sc = _scatterers(usx.phantoms.elastography_phantom(probe, medium, strain=strain))
+        d_sc = torch.from_numpy(sc).cuda()
+        rf = torch.empty((1, N_EL, n_smp), device="cuda")
+        iq = torch.empty((1, N_EL, n_smp), dtype=torch.complex64, device="cuda")
+        torch.cuda.synchronize()
+        ctx.simulate(ch_rf, capi.sim_config(noise_db=-200.0, enable_motion=0), d_sc.data_ptr(), len(sc), None,
+                     rf.data_ptr())
+        ctx.demodulate(ch_rf, capi.demod_config(), rf.data_ptr(), iq.data_ptr())
+        ctx.synchronize()
+        iqs.append(iq)
+    n0, n1 = 256, 1024
+    grid = usx.grid_for(probe, 0.012, 0.048, n0, n1)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), np.asarray(grid.points).reshape(-1, 3))
+    plan = ctx.plan(ch_iq, cgrid, capi.bf_config(f_number=1.5))
+    fa = torch.empty((n0, n1), dtype=torch.complex64, device="cuda")
+    fb = torch.empty_like(fa)
+    axial = torch.empty((n0, n1), device="cuda")
+    corr, strain_map = torch.empty_like(axial), torch.empty_like(axial)
+    axis1 = np.asarray(grid.axis1)
+    dz = float(axis1[1] - axis1[0])
+    fit = max(3, int(round(0.002 / dz)) | 1)
+
+    def step():
+        plan.execute(iqs[0].data_ptr(), fa.data_ptr())
+        plan.execute(iqs[1].data_ptr(), fb.data_ptr())
+        ctx.axial_displacement(fa.data_ptr(), fb.data_ptr(), n0, n1, axis1, F0, medium.speed_of_sound, 8, 2, 8,
+                               axial.data_ptr(), corr.data_ptr())
+        ctx.axial_strain(axial.data_ptr(), n0, n1, axis1, fit, strain_map.data_ptr())
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    capi.profile(ctx, True)
+    capi.profile_reset(ctx)
+    with ClockSampler(0) as clocks:
+        ms = timed(stream, step, args.steps)
+    prof = capi.profile_read(ctx)
+    capi.profile(ctx, False)
+    peaks = load_peaks()
+    per = {k: v[0] / args.steps for k, v in prof.items()}
+    track = sum(v for k, v in per.items() if k.startswith("displacement") or k.startswith("strain"))
+    tbytes = 2 * 8.0 * n0 * n1 + 3 * 4.0 * n0 * n1
+    s = strain_map.cpu().numpy()
+    roof = {"kernel": max(per, key=per.get), "bound": "hbm",
+            "achieved": tbytes / (track / 1e3) / 1e9 if track else None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": (tbytes / (track / 1e3) / 1e9 / peaks["hbm_gbs"]) if track else None, "traffic": None,
+            "note": "tracking kernels: two frames in, displacement, correlation and strain out"}
+    mid = s[:, n1 // 4:3 * n1 // 4]
+    line = _stage_line("strain maps/s (1% compression, 256x1024, 2 mm fit)", "maps/s", args.steps / (ms / 1e3),
+                       args, ms, prof, clocks, {"workload": "strain_1pw_256x1024", "fit_samples": fit}, roof,
+                       {"median_strain_background": float(np.median(mid))})
+    print(json.dumps(line))
+    plan.close()
+    ctx.close()
+
+
+def run_sector(args) -> None:
+    """Phased-array sector imaging: 64 elements, 2.5 MHz, pitch 0.2 mm, 31
+    diverging waves over +/-45 degrees (virtual source 10 mm behind the
+    array), a 100,000-scatterer phantom with two cysts to 80 mm; one step =
+    delay-and-sum onto 256 beams x 1024 samples, envelope, 60 dB log
+    compression and scan conversion to 800 x 800. The tensor-core minimum
+    variance of the same frame is timed beside it."""
+    import torch
+    import usx
+    from usx import capi
+    torch.cuda.set_device(0)
+    probe = usx.Probe()
+    probe.n_elements, probe.pitch, probe.element_width = 64, 200e-6, 180e-6
+    probe.center_frequency, probe.bandwidth = 2.5e6, 0.6
+    medium = usx.Medium()
+    acq = usx.presets.acquisition(probe, depth=0.082, medium=medium, samples_per_wavelength=4.0)
+    sim = usx.Simulator(probe, medium, acq, usx.SimulatorConfig())
+    txs = sim.make_diverging_waves(usx.angles_deg(-45, 45, 31), 0.01)
+    ph = usx.Phantom.speckle_box(-0.06, 0.06, 0.004, 0.084, 0.0, 100_000, 2027)
+    for x, z, r in ((-0.015, 0.04, 0.004), (0.02, 0.06, 0.005)):
+        ph.scale_amplitude_in_circle(usx.Vec3(x, 0.0, z), r, 0.0)
+    sc = _scatterers(ph)
+    ctx = capi.Context(0)
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    ch_iq = _capi_channel(capi, probe, medium, acq, txs, is_iq=True, fdem=probe.center_frequency)
+    n_ev, n_smp = len(txs), acq.n_samples
+    d_sc = torch.from_numpy(sc).cuda()
+    rf = torch.empty((n_ev, 64, n_smp), device="cuda")
+    iq = torch.empty((n_ev, 64, n_smp), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.simulate(ch_rf, capi.sim_config(noise_db=-60.0), d_sc.data_ptr(), len(sc), None, rf.data_ptr())
+    ctx.demodulate(ch_rf, capi.demod_config(), rf.data_ptr(), iq.data_ptr())
+    ctx.synchronize()
+    n0, n1 = 256, 1024
+    grid = usx.ScanGrid.sector(float(np.deg2rad(-45.0)), float(np.deg2rad(45.0)), n0, 0.005, 0.08, n1,
+                               usx.Vec3(0.0, 0.0, 0.0))
+    pts = np.asarray(grid.points).reshape(-1, 3)
+    cgrid = capi.Grid(1, np.asarray(grid.axis0), np.asarray(grid.axis1), pts)
+    d_pts = torch.from_numpy(pts).cuda()
+    frame = torch.empty((n0, n1), dtype=torch.complex64, device="cuda")
+    env, logi = torch.empty((n0, n1), device="cuda"), torch.empty((n0, n1), device="cuda")
+    W = H = 800
+    img = torch.empty((H, W), device="cuda")
+    fdem = probe.center_frequency
+
+    def make(kw, mv=False):
+        plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**kw))
+        if mv:
+            plan.set_mv_mode(1)
+        plan.autotune(iq.data_ptr(), frame.data_ptr(), repeats=1)
+        return plan
+
+    def step_with(plan):
+        def step():
+            plan.execute(iq.data_ptr(), frame.data_ptr())
+            ctx.envelope(frame.data_ptr(), n0, n1, fdem, env.data_ptr())
+            ctx.log_compress(env.data_ptr(), n0 * n1, 60.0, 0.0, -1.0, logi.data_ptr())
+            ctx.scan_convert(logi.data_ptr(), cgrid, W, H, 0.0, img.data_ptr())
+        return step
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    das = make(dict(f_number=1.5))
+    mvp = make(dict(f_number=1.5, combiner=2, mv_subarray=32, mv_diagonal_loading=0.01, mv_range_average=2),
+               mv=True)
+    results = {}
+    for name, plan in (("mv", mvp), ("das", das)):
+        step = step_with(plan)
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        capi.profile(ctx, True)
+        capi.profile_reset(ctx)
+        with ClockSampler(0) as clocks:
+            ms = timed(stream, step, args.steps)
+        results[name] = (ms, capi.profile_read(ctx), clocks)
+        capi.profile(ctx, False)
+    ms, prof, clocks = results["das"]
+    per = {k: v[0] / args.steps for k, v in prof.items()}
+    ops = 0.0  # active (pixel, channel, transmit) triples are not counted for diverging waves
+    roof = {"kernel": max(per, key=per.get), "bound": None, "achieved": None, "peak": None, "unit": None,
+            "frac": None, "traffic": None}
+    mv_ms = results["mv"][0] / args.steps
+    line = _stage_line("sector frames/s (64-el 2.5 MHz phased array, 31 diverging waves, 256x1024 -> 800x800)",
+                       "frames/s", args.steps / (ms / 1e3), args, ms, prof, clocks,
+                       {"workload": "sector_64el_31dw_256x1024_800x800", "beamformer": "das f#1.5"}, roof,
+                       {"mv_tensor": {"value": 1e3 / mv_ms, "unit": "frames/s", "ms_per_step": mv_ms,
+                                      "kernels_ms_per_step": {k: v[0] / args.steps
+                                                              for k, v in results["mv"][1].items()}}})
+    print(json.dumps(line))
+    das.close()
+    mvp.close()
+    ctx.close()
+
+
 def run_e2e(usx, grid, raw, rf_host, args, world):
     """The same frame through the public API with host buffers: RF up, frame back."""
     import torch
@@ -582,7 +882,8 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="learned", choices=sorted(WORKLOADS) + ["simulate", "demod"])
+    ap.add_argument("--workload", default="learned",
+                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "sector"])
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
     ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
@@ -594,6 +895,12 @@ def main() -> int:
         run_reference(args)
     elif args.workload in ("simulate", "demod"):
         run_stage(args)
+    elif args.workload == "doppler":
+        run_doppler(args)
+    elif args.workload == "strain":
+        run_strain(args)
+    elif args.workload == "sector":
+        run_sector(args)
     else:
         run_ours(args)
     return 0

@@ -818,18 +818,20 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     const long rows = chunk * n_pix, padded = (rows + 127) / 128 * 128;
     const int widest = mlp_widest(plan->mlp);
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t sz[10] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
+    const size_t sz[11] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
                           up(sizeof(float2) * rows * 64),       up(sizeof(float4) * rows),
                           up(2 * padded * widest),              up(2 * padded * widest),
                           up(sizeof(float) * padded * kLmvOutputs), up(sizeof(int2) * rows * kLmvGateClasses),
-                          up(sizeof(int2) * rows), up(sizeof(int2) * rows)};
+                          up(sizeof(int2) * rows), up(sizeof(int2) * rows),
+                          plan->lmv_beams >= 0 ? up(static_cast<size_t>(lmv_subspace_record_bytes(plan->lmv_beams)) * rows)
+                                               : 0};
     size_t total = 256;
     for (size_t b : sz) total += b;
     void* ws = nullptr;
     if (int rc = scratch(ctx, total, &ws)) return rc;
     char* q = static_cast<char*>(ws);
-    void* bufs[10];
-    for (int i = 0; i < 10; ++i) {
+    void* bufs[11];
+    for (int i = 0; i < 11; ++i) {
       bufs[i] = q;
       q += sz[i];
     }
@@ -881,7 +883,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       USX_CUDA(cudaMemsetAsync(counters, 0, (kLmvGateClasses + 2) * sizeof(int), ctx->stream));
       if (plan->lmv_beams >= 0) {
         if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate, counters,
-                                         gated, static_cast<int>(nrows), plan->d_mv_stats + 2))
+                                         gated, static_cast<int>(nrows), plan->d_mv_stats + 2,
+                                         static_cast<float*>(bufs[10])))
           return rc;
       } else if (int rc = launch_lmv_apply(ctx, net, avg, meta, b.out, b.out_stride, b.n_pix, nf, plan->lmv_gate,
                                            counters, gated, static_cast<int>(nrows), plan->d_mv_stats + 2)) {

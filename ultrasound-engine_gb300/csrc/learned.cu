@@ -331,7 +331,15 @@ struct SubArgs {
   int2* gated;
   int gated_cap;
   int* stats;
+  float* rec;             // [row][lmv_rec_floats(NB)] stage-1 records
 };
+
+// Floats per pixel record between the two stages: the Gram matrix (upper
+// triangle, re/im), the projections of the subarray average, w_q^H 1, eps,
+// the snapshot count, the basis size, flags, L, valid.
+__host__ __device__ constexpr int lmv_rec_floats(int nb) {
+  return ((nb + 1) * (nb + 2) + 2 * (nb + 1) + 8 + 3) / 4 * 4;
+}
 
 // Per-warp shared memory; the range rows follow it (n_dmax x kSubMaxN).
 template <int NB>
@@ -364,10 +372,14 @@ __device__ __forceinline__ float2 warp_sum2(float2 v) {
   return v;
 }
 
+// Stage 1 of the refinement, one warp per pixel: the gate, the basis, the
+// snapshot projections and the Gram matrix G = sum_s z_s z_s^H (z = Q^H y_s),
+// written with the projections of the subarray average and of 1 onto the
+// basis as one record per pixel (stage 2 solves it, one thread per pixel).
 // NB, the number of beams (1, 3, 5 or 7), is a template parameter so that
 // every loop over the basis is unrolled to its size.
 template <int NB>
-__global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubArgs a) {
+__global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_gram_kernel(const SubArgs a) {
   extern __shared__ float4 sub_smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   SubWarpSmem<NB>& sm = *reinterpret_cast<SubWarpSmem<NB>*>(reinterpret_cast<char*>(sub_smem_raw) +
@@ -379,7 +391,10 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
        row += static_cast<long>(gridDim.x) * kSubWarps) {
     const float4 meta = a.meta[row];
     const int L = static_cast<int>(meta.x);
-    if (L == 0) continue;  // n_act < 4: written by the feature pass
+    if (L == 0) {  // n_act < 4: written by the feature pass
+      if (lane == 0) a.rec[row * lmv_rec_floats(NB) + (NB + 1) * (NB + 2) + 2 * (NB + 1) + 7] = 0.f;
+      continue;
+    }
     const long frame = row / a.n_pix;
     const int pix = static_cast<int>(row - frame * a.n_pix);
     // The first nb of b = 0, 1, -1, 2, -2 are distinct modulo L when nb <= L;
@@ -397,6 +412,7 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       if (lane == 0) {
         push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
         if (a.stats) atomicAdd(a.stats, 1);
+        a.rec[row * lmv_rec_floats(NB) + (NB + 1) * (NB + 2) + 2 * (NB + 1) + 7] = 0.f;
       }
       continue;
     }
@@ -504,33 +520,41 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
 #pragma unroll
     for (int e = 0; e < kG; ++e) g[e] = 0.f;
     for (int d = 0; d < n_d; ++d) {
-      // Prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y_d[t'] (warp scans, 32 at a time).
-      float2 carry[NB];
-#pragma unroll
-      for (int k = 0; k < NB; ++k) carry[k] = make_float2(0.f, 0.f);
+      // Prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y_d[t']: each lane sums
+      // its run of C consecutive samples, then one warp scan of the run totals.
+      const int C = (n_act + 31) >> 5;
+      const int t_beg = lane * C;
       if (lane == 0)
 #pragma unroll
         for (int k = 0; k < NB; ++k)
           if (k < nb) sm.pre[k][0] = make_float2(0.f, 0.f);
-      for (int t0 = 0; t0 < n_act; t0 += 32) {
-        const int t = t0 + lane;
-        const float2 yv = t < n_act ? srow[d * kSubMaxN + t] : make_float2(0.f, 0.f);
 #pragma unroll
-        for (int k = 0; k < NB; ++k) {
-          if (k >= nb) continue;
-          const float2 tw = t < n_act ? beam_twiddle(sm.tw1[t], k) : make_float2(1.f, 0.f);
-          float2 v = make_float2(tw.x * yv.x - tw.y * yv.y, tw.x * yv.y + tw.y * yv.x);
-          for (int o2 = 1; o2 < 32; o2 <<= 1) {
-            const float px2 = __shfl_up_sync(0xffffffffu, v.x, o2), py2 = __shfl_up_sync(0xffffffffu, v.y, o2);
-            if (lane >= o2) {
-              v.x += px2;
-              v.y += py2;
-            }
+      for (int k = 0; k < NB; ++k) {
+        if (k >= nb) continue;
+        float2 run = make_float2(0.f, 0.f), loc[kSubMaxN / 32];
+#pragma unroll
+        for (int c = 0; c < kSubMaxN / 32; ++c) {
+          const int t = t_beg + c;
+          if (c < C && t < n_act) {
+            const float2 yv = srow[d * kSubMaxN + t], tw = beam_twiddle(sm.tw1[t], k);
+            run.x += tw.x * yv.x - tw.y * yv.y;
+            run.y += tw.x * yv.y + tw.y * yv.x;
           }
-          v.x += carry[k].x;
-          v.y += carry[k].y;
-          if (t < n_act) sm.pre[k][t + 1] = v;
-          carry[k] = make_float2(__shfl_sync(0xffffffffu, v.x, 31), __shfl_sync(0xffffffffu, v.y, 31));
+          loc[c] = run;
+        }
+        float2 inc = run;
+        for (int o2 = 1; o2 < 32; o2 <<= 1) {
+          const float ux = __shfl_up_sync(0xffffffffu, inc.x, o2), uy = __shfl_up_sync(0xffffffffu, inc.y, o2);
+          if (lane >= o2) {
+            inc.x += ux;
+            inc.y += uy;
+          }
+        }
+        const float2 ex = make_float2(inc.x - run.x, inc.y - run.y);
+#pragma unroll
+        for (int c = 0; c < kSubMaxN / 32; ++c) {
+          const int t = t_beg + c;
+          if (c < C && t < n_act) sm.pre[k][t + 1] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
         }
       }
       __syncwarp();
@@ -567,129 +591,187 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_kernel(const SubA
       }
       __syncwarp();
     }
-#pragma unroll
-    for (int e = 0; e < kG; ++e)
-      for (int o2 = 16; o2 > 0; o2 >>= 1) g[e] += __shfl_xor_sync(0xffffffffu, g[e], o2);
 
-    // Basis in use: beams k < nb, and w_q if it survived.
-    bool keep[(NB + 1)];
+    // G, reduced across the warp by a reduce-scatter: after five halvings each
+    // lane holds kPad / 32 finished entries, written straight to the record.
+    constexpr int kPad = (kG + 31) / 32 * 32;
+    float v[kPad];
 #pragma unroll
-    for (int k = 0; k < NB; ++k) keep[k] = k < nb;
-    keep[NB] = has_w;
-    // Right-hand side Q^H 1: sqrt(L) for the look direction, 0 for the other
-    // beams; w_q^H 1 for the network's direction.
-    float2 bq[(NB + 1)];
+    for (int e = 0; e < kPad; ++e) v[e] = e < kG ? g[e] : 0.f;
+    int base = 0;
 #pragma unroll
-    for (int k = 0; k < (NB + 1); ++k) bq[k] = make_float2(0.f, 0.f);
-    bq[0] = make_float2(sqrtf(static_cast<float>(L)), 0.f);
-    {
-      float2 sq = make_float2(0.f, 0.f);
-      if (2 * lane < L) sq = make_float2(wv[0].x, -wv[0].y);
-      if (2 * lane + 1 < L) sq = make_float2(sq.x + wv[1].x, sq.y - wv[1].y);
-      bq[NB] = warp_sum2(sq);
-    }
-
-    // Solve (G / K + eps I) c = b in every lane (complex Cholesky, k <= 6).
-    const float eps = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);
-    float2 A[(NB + 1)][(NB + 1)];
-    {
-      int e = 0;
+    for (int lvl = 0; lvl < 5; ++lvl) {
+      const int m = 16 >> lvl;
+      const int half = kPad >> (lvl + 1);
+      const bool up = (lane & m) != 0;
 #pragma unroll
-      for (int r = 0; r < (NB + 1); ++r)
-#pragma unroll
-        for (int c = r; c < (NB + 1); ++c, e += 2) {
-          float2 x = make_float2(g[e] / K, g[e + 1] / K);
-          if (r == c) x = make_float2(x.x + eps, 0.f);
-          if (!(keep[r] && keep[c])) x = (r == c) ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
-          A[r][c] = x;
-          A[c][r] = make_float2(x.x, -x.y);
-        }
-    }
-    bool ok = true;
-#pragma unroll
-    for (int c = 0; c < (NB + 1); ++c) {
-      float dsum = A[c][c].x;
-#pragma unroll
-      for (int k = 0; k < (NB + 1); ++k)
-        if (k < c) dsum -= A[c][k].x * A[c][k].x + A[c][k].y * A[c][k].y;
-      ok = ok && dsum > 0.f;
-      const float lc = sqrtf(fmaxf(dsum, 1e-30f));
-      A[c][c] = make_float2(lc, 0.f);
-      const float il = 1.0f / lc;
-#pragma unroll
-      for (int r = 0; r < (NB + 1); ++r) {
-        if (r <= c) continue;
-        float2 s = A[r][c];
-#pragma unroll
-        for (int k = 0; k < (NB + 1); ++k)
-          if (k < c) {  // s -= L[r][k] conj(L[c][k])
-            s.x -= A[r][k].x * A[c][k].x + A[r][k].y * A[c][k].y;
-            s.y -= A[r][k].y * A[c][k].x - A[r][k].x * A[c][k].y;
-          }
-        A[r][c] = make_float2(s.x * il, s.y * il);
+      for (int i = 0; i < kPad / 2; ++i) {
+        if (i >= half) break;
+        const float send = up ? v[i] : v[i + half];
+        const float keep = up ? v[i + half] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
       }
+      if (up) base += half;
     }
-    float2 cv[(NB + 1)];
+    float* rec = a.rec + row * lmv_rec_floats(NB);
 #pragma unroll
-    for (int r = 0; r < (NB + 1); ++r) {  // forward: L u = b
-      float2 s = keep[r] ? bq[r] : make_float2(0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < (NB + 1); ++k)
-        if (k < r) {
-          s.x -= A[r][k].x * cv[k].x - A[r][k].y * cv[k].y;
-          s.y -= A[r][k].x * cv[k].y + A[r][k].y * cv[k].x;
-        }
-      cv[r] = make_float2(s.x / A[r][r].x, s.y / A[r][r].x);
-    }
-#pragma unroll
-    for (int r = (NB + 1) - 1; r >= 0; --r) {  // backward: L^H c = u
-      float2 s = cv[r];
-#pragma unroll
-      for (int k = 0; k < (NB + 1); ++k)
-        if (k > r) {  // s -= conj(L[k][r]) c_k
-          s.x -= A[k][r].x * cv[k].x + A[k][r].y * cv[k].y;
-          s.y -= A[k][r].x * cv[k].y - A[k][r].y * cv[k].x;
-        }
-      cv[r] = make_float2(s.x / A[r][r].x, s.y / A[r][r].x);
-    }
-    // w = Q c; output n_act * (w^H abar) / (1^H w) with the coherence factor.
+    for (int i = 0; i < kPad / 32; ++i)
+      if (base + i < kG) rec[base + i] = v[i];
+    // Projections of the subarray average and of 1 onto the basis.
     const float4 av4 = reinterpret_cast<const float4*>(a.avg + row * kLmvMaxL)[lane];
-    float2 num = make_float2(0.f, 0.f), den = make_float2(0.f, 0.f);
+    float2 ak[NB + 1];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int i = 2 * lane + h;   // the element this lane holds in wv[h] and av4
-      if (i >= L) continue;
-      float2 w = make_float2(wv[h].x * cv[NB].x - wv[h].y * cv[NB].y,
-                             wv[h].x * cv[NB].y + wv[h].y * cv[NB].x);
+    for (int k = 0; k <= NB; ++k) {
+      float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < NB; ++k) {
-        if (k >= nb) continue;
-        const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
-        const float ux = t.x * rs, uy = -t.y * rs;
-        w.x += ux * cv[k].x - uy * cv[k].y;
-        w.y += ux * cv[k].y + uy * cv[k].x;
+      for (int h = 0; h < 2; ++h) {
+        const int i = 2 * lane + h;
+        if (i >= L) continue;
+        const float ax = h ? av4.z : av4.x, ay = h ? av4.w : av4.y;
+        float2 q;   // basis vector k at i
+        if (k < NB) {
+          const float2 t = beam_twiddle(sm.tw1[i], k);
+          q = make_float2(t.x * rs, -t.y * rs);
+          if (k >= nb) q = make_float2(0.f, 0.f);
+        } else {
+          q = wv[h];
+        }
+        acc.x += q.x * ax + q.y * ay;   // conj(q) abar
+        acc.y += q.x * ay - q.y * ax;
       }
-      const float ax = h ? av4.z : av4.x, ay = h ? av4.w : av4.y;
-      num.x = fmaf(w.x, ax, fmaf(w.y, ay, num.x));   // conj(w) abar
-      num.y = fmaf(w.x, ay, fmaf(-w.y, ax, num.y));
-      den.x += w.x;
-      den.y += w.y;
+      ak[k] = warp_sum2(acc);
     }
-    num = warp_sum2(num);
-    den = warp_sum2(den);
+    float2 bw = make_float2(0.f, 0.f);
+    if (2 * lane < L) bw = make_float2(wv[0].x, -wv[0].y);
+    if (2 * lane + 1 < L) bw = make_float2(bw.x + wv[1].x, bw.y - wv[1].y);
+    bw = warp_sum2(bw);   // w_q^H 1
     if (lane == 0) {
-      const float dn = den.x * den.x + den.y * den.y;
-      if (!ok || !(dn > 1e-30f)) {
-        push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
-        if (a.stats) atomicAdd(a.stats, 1);
-      } else {
-        const float scale = meta.y * meta.z / dn;   // n_act * cf * num / den
-        a.out[frame * a.out_stride + pix] =
-            make_float2((num.x * den.x + num.y * den.y) * scale, (num.y * den.x - num.x * den.y) * scale);
+      float* tail = rec + kG;
+#pragma unroll
+      for (int k = 0; k <= NB; ++k) {
+        tail[2 * k] = ak[k].x;
+        tail[2 * k + 1] = ak[k].y;
       }
+      tail[2 * (NB + 1) + 0] = bw.x;
+      tail[2 * (NB + 1) + 1] = bw.y;
+      tail[2 * (NB + 1) + 2] = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);   // eps
+      tail[2 * (NB + 1) + 3] = K;
+      tail[2 * (NB + 1) + 4] = static_cast<float>(nb);
+      tail[2 * (NB + 1) + 5] = has_w ? 1.f : 0.f;
+      tail[2 * (NB + 1) + 6] = static_cast<float>(L);
+      tail[2 * (NB + 1) + 7] = 1.f;   // record valid
     }
     __syncwarp();
   }
+}
+
+// Stage 2, one thread per pixel: (G / K + eps I) c = Q^H 1, then the output
+// n_act * cf * sum conj(c_k) (q_k^H abar) / sum c_k (1^H q_k). Pixels whose
+// small factorisation fails go to the exact solver.
+template <int NB>
+__global__ void lmv_subspace_solve_kernel(const SubArgs a) {
+  constexpr int K1 = NB + 1;
+  constexpr int kG = K1 * (K1 + 1);
+  const long row = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (row >= a.n_rows) return;
+  const float* rec = a.rec + row * lmv_rec_floats(NB);
+  const float* tail = rec + kG;
+  if (!(tail[2 * K1 + 7] > 0.f)) return;  // gated, or n_act < 4
+  const float eps = tail[2 * K1 + 2], Kf = tail[2 * K1 + 3];
+  const int nb = static_cast<int>(tail[2 * K1 + 4]);
+  const bool has_w = tail[2 * K1 + 5] > 0.f;
+  const int L = static_cast<int>(tail[2 * K1 + 6]);
+  bool keep[K1];
+#pragma unroll
+  for (int k = 0; k < NB; ++k) keep[k] = k < nb;
+  keep[NB] = has_w;
+  float2 A[K1][K1];
+  {
+    int e = 0;
+    const float ik = 1.0f / Kf;
+#pragma unroll
+    for (int r = 0; r < K1; ++r)
+#pragma unroll
+      for (int c = r; c < K1; ++c, e += 2) {
+        float2 x = make_float2(rec[e] * ik, rec[e + 1] * ik);
+        if (r == c) x = make_float2(x.x + eps, 0.f);
+        if (!(keep[r] && keep[c])) x = (r == c) ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+        A[r][c] = x;
+        A[c][r] = make_float2(x.x, -x.y);
+      }
+  }
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < K1; ++c) {
+    float dsum = A[c][c].x;
+#pragma unroll
+    for (int k = 0; k < c; ++k) dsum -= A[c][k].x * A[c][k].x + A[c][k].y * A[c][k].y;
+    ok = ok && dsum > 0.f;
+    const float lc = sqrtf(fmaxf(dsum, 1e-30f));
+    A[c][c] = make_float2(lc, 0.f);
+    const float il = 1.0f / lc;
+#pragma unroll
+    for (int r = c + 1; r < K1; ++r) {
+      float2 sv = A[r][c];
+#pragma unroll
+      for (int k = 0; k < c; ++k) {  // s -= L[r][k] conj(L[c][k])
+        sv.x -= A[r][k].x * A[c][k].x + A[r][k].y * A[c][k].y;
+        sv.y -= A[r][k].y * A[c][k].x - A[r][k].x * A[c][k].y;
+      }
+      A[r][c] = make_float2(sv.x * il, sv.y * il);
+    }
+  }
+  // Right-hand side Q^H 1: sqrt(L) for the look direction, 0 for the other
+  // beams, w_q^H 1 for the network's direction.
+  float2 cv[K1];
+#pragma unroll
+  for (int r = 0; r < K1; ++r) {
+    float2 sv = make_float2(0.f, 0.f);
+    if (r == 0) sv = make_float2(sqrtf(static_cast<float>(L)), 0.f);
+    if (r == NB && has_w) sv = make_float2(tail[2 * K1], tail[2 * K1 + 1]);
+#pragma unroll
+    for (int k = 0; k < r; ++k) {
+      sv.x -= A[r][k].x * cv[k].x - A[r][k].y * cv[k].y;
+      sv.y -= A[r][k].x * cv[k].y + A[r][k].y * cv[k].x;
+    }
+    cv[r] = make_float2(sv.x / A[r][r].x, sv.y / A[r][r].x);
+  }
+#pragma unroll
+  for (int r = K1 - 1; r >= 0; --r) {
+    float2 sv = cv[r];
+#pragma unroll
+    for (int k = r + 1; k < K1; ++k) {  // s -= conj(L[k][r]) c_k
+      sv.x -= A[k][r].x * cv[k].x + A[k][r].y * cv[k].y;
+      sv.y -= A[k][r].x * cv[k].y - A[k][r].y * cv[k].x;
+    }
+    cv[r] = make_float2(sv.x / A[r][r].x, sv.y / A[r][r].x);
+  }
+  // num = sum_k conj(c_k) a_k, den = sum_k c_k conj(b_k) with b = Q^H 1.
+  float2 num = make_float2(0.f, 0.f), den = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < K1; ++k) {
+    if (!keep[k]) continue;
+    const float2 ak = make_float2(tail[2 * k], tail[2 * k + 1]);
+    num.x += cv[k].x * ak.x + cv[k].y * ak.y;
+    num.y += cv[k].x * ak.y - cv[k].y * ak.x;
+    float2 bk = make_float2(0.f, 0.f);
+    if (k == 0) bk = make_float2(sqrtf(static_cast<float>(L)), 0.f);
+    if (k == NB) bk = make_float2(tail[2 * K1], tail[2 * K1 + 1]);
+    den.x += cv[k].x * bk.x + cv[k].y * bk.y;
+    den.y += cv[k].y * bk.x - cv[k].x * bk.y;
+  }
+  const long frame = row / a.n_pix;
+  const int pix = static_cast<int>(row - frame * a.n_pix);
+  const float dn = den.x * den.x + den.y * den.y;
+  if (!ok || !(dn > 1e-30f)) {
+    push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
+    if (a.stats) atomicAdd(a.stats, 1);
+    return;
+  }
+  const float4 meta = a.meta[row];
+  const float scale = meta.y * meta.z / dn;   // n_act * cf * num / den
+  a.out[frame * a.out_stride + pix] =
+      make_float2((num.x * den.x + num.y * den.y) * scale, (num.y * den.x - num.x * den.y) * scale);
 }
 
 }  // namespace
@@ -763,7 +845,7 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 
 
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats) {
+                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats, float* rec) {
   SubArgs a;
   a.y = l.y;
   a.points = l.points;
@@ -790,27 +872,37 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.gated = gated;
   a.gated_cap = gated_cap;
   a.stats = stats;
+  a.rec = rec;
   if (l.n_ch > kSubMaxN || a.n_dmax > 9)
     return fail(USX_ERR_UNSUPPORTED, "learned-subspace refinement supports <= 128 channels, range average <= 4");
-  auto go = [&](auto kernel, size_t per_warp) -> int {
+  auto go = [&](auto gram, auto solve, size_t per_warp) -> int {
     const int smem = static_cast<int>(per_warp * kSubWarps);
-    if (int rc_ = smem_limit(reinterpret_cast<const void*>(kernel), static_cast<size_t>(smem))) return rc_;
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(gram), static_cast<size_t>(smem))) return rc_;
     int per_sm = 0;
-    if (int rc_ = occupancy(reinterpret_cast<const void*>(kernel), 32 * kSubWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(gram), 32 * kSubWarps, static_cast<size_t>(smem), &per_sm))
+      return rc_;
     const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
     const long need = (a.n_rows + kSubWarps - 1) / kSubWarps;
-    prof_begin(ctx, "lmv_subspace_kernel");
-    kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem, ctx->stream>>>(a);
+    prof_begin(ctx, "lmv_subspace_gram_kernel");
+    gram<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem, ctx->stream>>>(a);
     prof_end(ctx);
-    USX_CHECK_LAUNCH("lmv_subspace_kernel");
+    USX_CHECK_LAUNCH("lmv_subspace_gram_kernel");
+    prof_begin(ctx, "lmv_subspace_solve_kernel");
+    solve<<<static_cast<unsigned>(ceil_div(a.n_rows, 128)), 128, 0, ctx->stream>>>(a);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("lmv_subspace_solve_kernel");
     return USX_OK;
   };
   switch (std::min(kSubMaxBeams, 1 + n_beams)) {
-    case 1: return go(lmv_subspace_kernel<1>, sub_warp_bytes<1>(a.n_dmax));
-    case 3: return go(lmv_subspace_kernel<3>, sub_warp_bytes<3>(a.n_dmax));
-    case 5: return go(lmv_subspace_kernel<5>, sub_warp_bytes<5>(a.n_dmax));
-    default: return go(lmv_subspace_kernel<7>, sub_warp_bytes<7>(a.n_dmax));
+    case 1: return go(lmv_subspace_gram_kernel<1>, lmv_subspace_solve_kernel<1>, sub_warp_bytes<1>(a.n_dmax));
+    case 3: return go(lmv_subspace_gram_kernel<3>, lmv_subspace_solve_kernel<3>, sub_warp_bytes<3>(a.n_dmax));
+    case 5: return go(lmv_subspace_gram_kernel<5>, lmv_subspace_solve_kernel<5>, sub_warp_bytes<5>(a.n_dmax));
+    default: return go(lmv_subspace_gram_kernel<7>, lmv_subspace_solve_kernel<7>, sub_warp_bytes<7>(a.n_dmax));
   }
+}
+
+int lmv_subspace_record_bytes(int n_beams) {
+  return static_cast<int>(sizeof(float)) * lmv_rec_floats(std::min(kSubMaxBeams, 1 + std::max(0, n_beams)));
 }
 
 }  // namespace usxcu

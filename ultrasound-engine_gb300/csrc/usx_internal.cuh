@@ -282,7 +282,9 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 // then the exact Capon solve within span{1, network weights, n_beams DFT
 // beams} through the pixel's snapshots (learned.cu).
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats);
+                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats, float* rec);
+// Bytes per pixel of the scratch record launch_lmv_subspace passes between its two stages.
+int lmv_subspace_record_bytes(int n_beams);
 
 // The network (mlp.cu). mlp_infer runs `rows` (a multiple of 128) BF16 input
 // rows through every layer with caller scratch t0, t1 (rows x widest BF16
