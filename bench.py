@@ -632,6 +632,7 @@ def run_doppler(args) -> None:
     cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), np.asarray(grid.points).reshape(-1, 3))
     plan = ctx.plan(ch_iq, cgrid, capi.bf_config(f_number=1.5))
     frames = torch.empty((n_frames_total, n0 * n1), dtype=torch.complex64, device="cuda")
+    plan.autotune(iq.data_ptr(), frames.data_ptr(), repeats=1)
     n_ens = len(lens)
     vel = torch.empty((n_ens, n0 * n1), device="cuda")
     pw, var = torch.empty_like(vel), torch.empty_like(vel)
@@ -657,16 +658,22 @@ def run_doppler(args) -> None:
     capi.profile(ctx, False)
     peaks = load_peaks()
     per = {k: v[0] / args.steps for k, v in prof.items()}
-    flow = [k for k in per if k.startswith("flow") or k.startswith("wall")]
+    flow = [k for k in per if k.startswith("flow") or k.startswith("wall") or k.startswith("power_gate")]
     flow_ms = sum(per[k] for k in flow)
     # Colour flow reads every packed frame once and writes four maps per ensemble.
     flow_bytes = 8.0 * n_frames_total * n0 * n1 + n_ens * n0 * n1 * (3 * 4 + 1)
     v = vel.cpu().numpy()
     inside = valid.cpu().numpy().astype(bool)
-    roof = {"kernel": max(per, key=per.get), "bound": "hbm",
-            "achieved": flow_bytes / (flow_ms / 1e3) / 1e9 if flow_ms else None, "peak": peaks["hbm_gbs"],
-            "unit": "GB/s", "frac": (flow_bytes / (flow_ms / 1e3) / 1e9 / peaks["hbm_gbs"]) if flow_ms else None,
-            "traffic": None, "note": "achieved = colour-flow kernels' algorithmic bytes over their time"}
+    das_ms = sum(v for k, v in per.items() if k.startswith("das"))
+    das_flops = 20.0 * das_active_ops(np.asarray(grid.points).reshape(-1, 3), txs[:3], probe, 1.5) * n_frames_total
+    roof = {"kernel": max(per, key=per.get), "bound": "fp32",
+            "achieved": das_flops / (das_ms / 1e3) / 1e12 if das_ms else None, "peak": FP32_NOMINAL_TFLOPS,
+            "unit": "TFLOP/s", "frac": das_flops / (das_ms / 1e3) / 1e12 / FP32_NOMINAL_TFLOPS if das_ms else None,
+            "traffic": None, "note": "delay-and-sum of all packed frames (20 flops per active pixel-channel-"
+                                     "transmit); peak = nominal FP32",
+            "colour_flow": {"ms": flow_ms, "bytes": flow_bytes,
+                            "achieved_gbs": flow_bytes / (flow_ms / 1e3) / 1e9 if flow_ms else None,
+                            "hbm_frac": flow_bytes / (flow_ms / 1e3) / 1e9 / peaks["hbm_gbs"] if flow_ms else None}}
     line = _stage_line("colour-flow ensembles/s (32 uneven ensembles of 8-32 pulses x 3 PW, 256x512)",
                        "ensembles/s", n_ens * args.steps / (ms / 1e3), args, ms, prof, clocks,
                        {"workload": "doppler_32ens_8-32pulses_3pw_256x512", "frames_per_step": n_frames_total,
@@ -743,7 +750,7 @@ def run_strain(args) -> None:
     track = sum(v for k, v in per.items() if k.startswith("displacement") or k.startswith("strain"))
     tbytes = 2 * 8.0 * n0 * n1 + 3 * 4.0 * n0 * n1
     s = strain_map.cpu().numpy()
-    roof = {"kernel": max(per, key=per.get), "bound": "hbm",
+    roof = {"kernel": "displacement_kernel + strain_kernel", "bound": "hbm",
             "achieved": tbytes / (track / 1e3) / 1e9 if track else None, "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": (tbytes / (track / 1e3) / 1e9 / peaks["hbm_gbs"]) if track else None, "traffic": None,
             "note": "tracking kernels: two frames in, displacement, correlation and strain out"}
@@ -850,6 +857,102 @@ def run_sector(args) -> None:
     ctx.close()
 
 
+def run_mixed(args) -> None:
+    """Mixed-probe streaming: per step one 128-element linear frame (75 plane
+    waves, 512 x 1024, learned MV with plain-MV fallback) and one 64-element
+    phased-array sector frame (31 diverging waves, 256 x 1024, tensor-core MV,
+    envelope, log compression, scan conversion to 800 x 800), both captured
+    once into a single CUDA graph that each step replays (one launch for the
+    whole mixed batch)."""
+    import torch
+    import usx
+    from usx import capi, learned
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    ctx = capi.Context(0, stream=stream.cuda_stream)
+    # Linear: the headline acquisition.
+    usx_, probe, medium, acq, sim, txs, ph, grid = workload_setup()
+    sc = _scatterers(ph)
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    ch_iq = _capi_channel(capi, probe, medium, acq, txs, is_iq=True, fdem=F0)
+    d_sc = torch.from_numpy(sc).cuda()
+    rf = torch.empty((N_TX, N_EL, N_SMP), device="cuda")
+    iq_lin = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.simulate(ch_rf, capi.sim_config(), d_sc.data_ptr(), len(sc), None, rf.data_ptr())
+    ctx.demodulate(ch_rf, capi.demod_config(), rf.data_ptr(), iq_lin.data_ptr())
+    ctx.synchronize()
+    del rf, d_sc
+    pts = np.asarray(grid.points).reshape(-1, 3)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), pts)
+    mlp = learned.load_mlp(ctx, WEIGHTS)
+    lin = ctx.plan(ch_iq, cgrid, capi.bf_config(**LEARNED_KW))
+    lin.set_learned(mlp, learned.trained_gate(WEIGHTS))
+    lin.set_learned_refine(learned.trained_refine(WEIGHTS))
+    f_lin = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
+    lin.autotune(iq_lin.data_ptr(), f_lin.data_ptr(), repeats=1)
+    # Sector: 64-element phased array.
+    sp = usx.Probe()
+    sp.n_elements, sp.pitch, sp.element_width, sp.center_frequency, sp.bandwidth = 64, 200e-6, 180e-6, 2.5e6, 0.6
+    sacq = usx.presets.acquisition(sp, depth=0.082, medium=medium, samples_per_wavelength=4.0)
+    ssim = usx.Simulator(sp, medium, sacq, usx.SimulatorConfig())
+    stx = ssim.make_diverging_waves(usx.angles_deg(-45, 45, 31), 0.01)
+    sph = usx.Phantom.speckle_box(-0.06, 0.06, 0.004, 0.084, 0.0, 100_000, 2027)
+    ssc = _scatterers(sph)
+    sch_rf = _capi_channel(capi, sp, medium, sacq, stx)
+    sch_iq = _capi_channel(capi, sp, medium, sacq, stx, is_iq=True, fdem=sp.center_frequency)
+    d_ssc = torch.from_numpy(ssc).cuda()
+    srf = torch.empty((len(stx), 64, sacq.n_samples), device="cuda")
+    iq_sec = torch.empty((len(stx), 64, sacq.n_samples), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.simulate(sch_rf, capi.sim_config(), d_ssc.data_ptr(), len(ssc), None, srf.data_ptr())
+    ctx.demodulate(sch_rf, capi.demod_config(), srf.data_ptr(), iq_sec.data_ptr())
+    ctx.synchronize()
+    sgrid = usx.ScanGrid.sector(float(np.deg2rad(-45.0)), float(np.deg2rad(45.0)), 256, 0.005, 0.08, 1024,
+                                usx.Vec3(0.0, 0.0, 0.0))
+    scg = capi.Grid(1, np.asarray(sgrid.axis0), np.asarray(sgrid.axis1), np.asarray(sgrid.points).reshape(-1, 3))
+    sec = ctx.plan(sch_iq, scg, capi.bf_config(f_number=1.5, combiner=2, mv_subarray=32,
+                                                mv_diagonal_loading=0.01, mv_range_average=2))
+    sec.set_mv_mode(1)
+    f_sec = torch.empty((256, 1024), dtype=torch.complex64, device="cuda")
+    sec.autotune(iq_sec.data_ptr(), f_sec.data_ptr(), repeats=1)
+    env, logi = torch.empty((256, 1024), device="cuda"), torch.empty((256, 1024), device="cuda")
+    img = torch.empty((800, 800), device="cuda")
+
+    def batch():
+        lin.execute(iq_lin.data_ptr(), f_lin.data_ptr())
+        sec.execute(iq_sec.data_ptr(), f_sec.data_ptr())
+        ctx.envelope(f_sec.data_ptr(), 256, 1024, sp.center_frequency, env.data_ptr())
+        ctx.log_compress(env.data_ptr(), 256 * 1024, 60.0, 0.0, -1.0, logi.data_ptr())
+        ctx.scan_convert(logi.data_ptr(), scg, 800, 800, 0.0, img.data_ptr())
+
+    with torch.cuda.stream(stream):
+        batch()
+        stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            batch()
+    with torch.cuda.stream(stream):   # replays run on the stream the events are recorded on
+        for _ in range(args.warmup):
+            graph.replay()
+        stream.synchronize()
+        with ClockSampler(0) as clocks:
+            ms = timed(stream, graph.replay, args.steps)
+        ms_direct = timed(stream, batch, args.steps)
+    line = {"metric": "mixed-batch frames/s (128-el linear learned-MV 512x1024 + 64-el sector MV 256x1024 -> 800x800)",
+            "value": 2 * args.steps / (ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-simulated phantoms)",
+            "config": {"workload": "mixed_linear_learned_512x1024_sector_mv_256x1024", "frames_per_step": 2,
+                       "launch": "one CUDA graph per step"},
+            "direct_launch_ms_per_step": ms_direct / args.steps, "clocks": clocks.summary()}
+    print(json.dumps(line))
+    lin.close()
+    sec.close()
+    mlp.close()
+    ctx.close()
+
+
 def run_e2e(usx, grid, raw, rf_host, args, world):
     """The same frame through the public API with host buffers: RF up, frame back."""
     import torch
@@ -883,7 +986,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="learned",
-                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "sector"])
+                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "sector", "mixed"])
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
     ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
@@ -901,6 +1004,8 @@ def main() -> int:
         run_strain(args)
     elif args.workload == "sector":
         run_sector(args)
+    elif args.workload == "mixed":
+        run_mixed(args)
     else:
         run_ours(args)
     return 0

@@ -254,8 +254,11 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
 // register cap (MINB resident CTAs per SM) are template parameters; every
 // variant computes the same sums in the same order (bit-identical frames),
 // and the plan's autotuner picks the fastest for its geometry.
-template <bool IQ, int kFastGroup, int kTileLines, int MINB>
+template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false>
 __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
+  // kRtShared: the group's receive delays live in shared memory instead of
+  // registers, so that a larger group fits the register cap.
+  __shared__ float rt_s[kRtShared ? 32 * kTileLines * kFastGroup : 1];
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
   const int tile = blockIdx.x;
@@ -302,7 +305,8 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
     float incs = 0.0f;
     int n_active = 0;
     for (int g = 0; g < a.n_ch; g += kFastGroup) {
-      float rt[kFastGroup];
+      float rt_r[kRtShared ? 1 : kFastGroup];
+      float* rt = kRtShared ? rt_s + threadIdx.x * kFastGroup : rt_r;
       unsigned mask = 0u;
 #pragma unroll
       for (int k = 0; k < kFastGroup; ++k) {
@@ -427,13 +431,14 @@ struct DasVariant {
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
-template <int G, int TL, int MB>
+template <int G, int TL, int MB, bool RTS = false>
 constexpr DasVariant das_variant() {
-  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB>, das_fast_kernel<false, 16, 4, 1>};
+  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB, RTS>, das_fast_kernel<false, 16, 4, 1>};
 }
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
     das_variant<8, 8, 4>(),  das_variant<16, 2, 8>(), das_variant<4, 4, 12>(), das_variant<8, 2, 16>(),
+    das_variant<16, 4, 8, true>(), das_variant<16, 2, 16, true>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 

@@ -287,7 +287,9 @@ int launch_wall(usx_ctx* ctx, const float* ens, int n, long n_pix, int type, int
   const size_t smem = sizeof(float2) * n * threads;
   if (smem > 48 * 1024)
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(wall_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
+  prof_begin(ctx, "wall_kernel");
   wall_kernel<<<ceil_div(n_pix, threads), threads, smem, ctx->stream>>>(a);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("wall_kernel");
   return USX_OK;
 }
@@ -315,10 +317,14 @@ int launch_flow(usx_ctx* ctx, const float* filt, int n, int n0, int n1, float dz
   a.pmax_bits = pmax_bits;
   const long n_pix = static_cast<long>(n0) * n1;
   USX_CUDA(cudaMemsetAsync(pmax_bits, 0, sizeof(unsigned), ctx->stream));
+  prof_begin(ctx, "flow_kernel");
   flow_kernel<<<ceil_div(n_pix, 128), 128, 0, ctx->stream>>>(a);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("flow_kernel");
   const float ratio = std::pow(10.0f, cfg.power_threshold_db / 10.0f);
+  prof_begin(ctx, "power_gate_kernel");
   power_gate_kernel<<<ceil_div(n_pix, 256), 256, 0, ctx->stream>>>(power, valid, n_pix, ratio, pmax_bits);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("power_gate_kernel");
   return USX_OK;
 }
@@ -523,7 +529,9 @@ int usx_cu_axial_displacement(usx_ctx* ctx, const float* before, const float* af
   p.c = speed_of_sound;
   p.axial = axial;
   p.corr = correlation;
+  prof_begin(ctx, "displacement_kernel");
   displacement_kernel<<<ceil_div(n, 128), 128, 0, ctx->stream>>>(p);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("displacement_kernel");
   return USX_OK;
 }
@@ -533,8 +541,10 @@ int usx_cu_axial_strain(usx_ctx* ctx, const float* axial, int n0, int n1,
   if (!ctx || !axial || !strain) return fail(USX_ERR_INVALID, "usx_cu_axial_strain: null argument");
   const long n = static_cast<long>(n0) * n1;
   if (n <= 0) return USX_OK;
+  prof_begin(ctx, "strain_kernel");
   strain_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(axial, n0, n1, axial_step(axis1_host, n1),
                                                            std::max(1, fit_length / 2), strain);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("strain_kernel");
   return USX_OK;
 }
