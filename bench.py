@@ -632,7 +632,6 @@ def run_doppler(args) -> None:
     cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), np.asarray(grid.points).reshape(-1, 3))
     plan = ctx.plan(ch_iq, cgrid, capi.bf_config(f_number=1.5))
     frames = torch.empty((n_frames_total, n0 * n1), dtype=torch.complex64, device="cuda")
-    plan.autotune(iq.data_ptr(), frames.data_ptr(), repeats=1)
     n_ens = len(lens)
     vel = torch.empty((n_ens, n0 * n1), device="cuda")
     pw, var = torch.empty_like(vel), torch.empty_like(vel)
