@@ -57,6 +57,7 @@ struct BfArgs {
   int rx_window, combiner, compounding, tx_weighting, cf, is_mv;
   int mv_subarray, mv_range_average;
   float mv_loading;
+  int* status;           // context status word (set when a bounded wait gives up)
 };
 
 __device__ __forceinline__ float elem_x(const BfArgs& a, int ch) {
@@ -422,23 +423,353 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
   a.out[frame * a.out_stride + pix] = make_float2(result.re, result.im);
 }
 
+// ------------------------------------------------------------------------
+// das_staged_kernel: the fast delay-and-sum with the IQ windows of every
+// (channel group, kE transmits) step staged in shared memory by the tensor
+// memory accelerator (cp.async.bulk, one 1-D bulk copy per channel row,
+// completion on an mbarrier), double-buffered so that step i+1's copies fly
+// while step i is computed. At 128 channels and 75 plane waves it measured
+// 14.7 ms per 512 x 1024 frame with one transmit per step and 21-22 ms with
+// four or five, against 6.0 ms for das_fast_kernel's L1 gathers (the
+// per-step barrier and the single issuing thread serialise the CTA); it stays
+// one of the autotuner's candidates. Plane waves only: the window of a channel over the CTA's tile
+// is bounded from the tile's pixel extent (the transmit delay is linear in x
+// and z; the receive delay is smallest at the tile point nearest the element
+// and largest at the farthest corner). The per-pixel delay index is the
+// reference's, bit for bit, as in das_fast_kernel; a pixel whose samples fall
+// outside the staged window (rounding at the window's edge, an unusually
+// wide tile) reads them from global memory, so the frame is identical to
+// das_fast_kernel's. Coherent and select compounding.
+constexpr int kStageW = 64;   // staged samples per channel row (512 bytes)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <int kG, int kTL, int kE>
+__global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
+  // A step is one channel group and kE consecutive transmits.
+  __shared__ __align__(16) float2 win[2][kE][kG][kStageW];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ int s_lo[2][kE][kG];
+  __shared__ float s_rmin[kG];
+  __shared__ float bnd[4][kTL];   // per warp: x min, x max, z min, z max
+  __shared__ unsigned s_mask;
+  const int n0 = a.n_pix / a.n1;
+  const int tiles_depth = (a.n1 + 31) / 32;
+  const int tile = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int line = (tile / tiles_depth) * kTL + warp;
+  const int depth = (tile % tiles_depth) * 32 + lane;
+  const bool live = line < n0 && depth < a.n1;
+  const int pix = live ? line * a.n1 + depth : 0;
+  const long frame = blockIdx.y;
+  const float px = live ? __ldg(a.points + 3 * pix) : 0.f, py = live ? __ldg(a.points + 3 * pix + 1) : 0.f,
+              pz = live ? __ldg(a.points + 3 * pix + 2) : 0.f;
+  // The tile's extent.
+  {
+    float xl = live ? px : INFINITY, xh = live ? px : -INFINITY, zl = live ? pz : INFINITY,
+          zh = live ? pz : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+      xl = fminf(xl, __shfl_xor_sync(0xffffffffu, xl, o));
+      xh = fmaxf(xh, __shfl_xor_sync(0xffffffffu, xh, o));
+      zl = fminf(zl, __shfl_xor_sync(0xffffffffu, zl, o));
+      zh = fmaxf(zh, __shfl_xor_sync(0xffffffffu, zh, o));
+    }
+    if (lane == 0) {
+      bnd[0][warp] = xl;
+      bnd[1][warp] = xh;
+      bnd[2][warp] = zl;
+      bnd[3][warp] = zh;
+    }
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  float x_min = bnd[0][0], x_max = bnd[1][0], z_min = bnd[2][0], z_max = bnd[3][0];
+#pragma unroll
+  for (int w = 1; w < kTL; ++w) {
+    x_min = fminf(x_min, bnd[0][w]);
+    x_max = fmaxf(x_max, bnd[1][w]);
+    z_min = fminf(z_min, bnd[2][w]);
+    z_max = fmaxf(z_max, bnd[3][w]);
+  }
+  int ev_first = a.ev_begin, ev_last = a.ev_end;
+  if (a.seq_epf > 0) {
+    ev_first = a.ev_begin + static_cast<int>(frame) * a.seq_epf;
+    ev_last = ev_first + a.seq_epf;
+  }
+  if (a.pass >= 0) {
+    ev_first += a.pass;
+    ev_last = ev_first + 1;
+  }
+  const bool select = a.compounding == USX_COMP_SELECT;
+  int best_ev = -1;
+  float best_w = 0.0f;
+  if (select && live) {
+    for (int ev = ev_first; ev < ev_last; ++ev) {
+      const float tw = tx_sensitivity(a.tx[ev], px, pz, a.lambda, a.pitch);
+      if (tw > best_w) {
+        best_w = tw;
+        best_ev = ev;
+      }
+    }
+  }
+  const float2* iq = a.iq + frame * a.data_stride;
+  const unsigned n_last = static_cast<unsigned>(a.n_smp - 1);
+  const int n_ev = max(0, ev_last - ev_first);
+  const int n_groups = (a.n_ch + kG - 1) / kG;
+  const int n_chunks = (n_ev + kE - 1) / kE;   // steps per group
+  const int n_steps = n_groups * n_chunks;
+  unsigned phase[2] = {0u, 0u};
+
+  // Thread 0: channel windows of step i and their bulk copies into stage i & 1.
+  auto issue = [&](int i) {
+    const int st = i & 1;
+    const int g = (i / n_chunks) * kG, e0 = ev_first + (i % n_chunks) * kE;
+    const long row_base = frame * a.data_stride;
+    unsigned bytes = 0;
+    for (int e = 0; e < kE; ++e) {
+      const int ev = e0 + e;
+      float tmin = 0.0f;
+      if (ev < ev_last) {
+        const TxDev& t = a.tx[ev];
+        const float tx0 = ((x_min - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+        const float tx1 = ((x_max - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+        const float tx2 = ((x_min - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+        const float tx3 = ((x_max - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+        tmin = fminf(fminf(tx0, tx1), fminf(tx2, tx3));
+      }
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        int lo = -1;
+        if (ev < ev_last && ch < a.n_ch && ((s_mask >> k) & 1u)) {
+          lo = static_cast<int>(floorf((tmin + s_rmin[k] - a.t0) * a.fs)) - 2;
+          lo = max(0, min(lo, a.n_smp - kStageW - 1));
+          const long el = row_base + (static_cast<long>(ev) * a.n_ch + ch) * a.n_smp + lo;
+          if (el & 1L) lo = lo > 0 ? lo - 1 : lo + 1;   // 16-byte aligned source
+          bytes += kStageW * sizeof(float2);
+        }
+        s_lo[st][e][k] = lo;
+      }
+    }
+    mbar_arrive_expect_tx(&bar[st], bytes);
+    for (int e = 0; e < kE; ++e)
+      for (int k = 0; k < kG; ++k) {
+        const int lo = s_lo[st][e][k];
+        if (lo < 0) continue;
+        const float2* src = iq + (static_cast<long>(e0 + e) * a.n_ch + g + k) * a.n_smp + lo;
+        bulk_copy_g2s(&win[st][e][k][0], src, kStageW * sizeof(float2), &bar[st]);
+      }
+  };
+
+  cplx das = mk(0.f, 0.f), s = mk(0.f, 0.f), q = mk(0.f, 0.f), coh = mk(0.f, 0.f);
+  float incs = 0.0f;
+  int n_active = 0;
+  float rt[kG], ar[kG], ai[kG];
+  unsigned mask = 0u;
+  bool timed_out = false;
+  for (int i = 0; i < n_steps; ++i) {
+    const int g = (i / n_chunks) * kG, e0 = ev_first + (i % n_chunks) * kE;
+    const int st = i & 1;
+    if (i % n_chunks == 0) {
+      // A new channel group: receive delays and the tile's channel mask.
+      mask = 0u;
+#pragma unroll
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        rt[k] = 0.0f;
+        ar[k] = ai[k] = 0.0f;
+        if (live && ch < a.n_ch) {
+          const float ex = elem_x(a, ch);
+          if (aperture_weight(ex, px, pz, a.f_number, a.rx_window, a.tukey_alpha) > 0.0f) {
+            mask |= 1u << k;
+            rt[k] = dist3(ex, 0.0f, 0.0f, px, py, pz) / a.c;
+          }
+        }
+      }
+      unsigned m = mask;
+      for (int o = 16; o > 0; o >>= 1) m |= __shfl_xor_sync(0xffffffffu, m, o);
+      if (threadIdx.x == 0) s_mask = 0u;
+      __syncthreads();
+      if (lane == 0) atomicOr(&s_mask, m);
+      __syncthreads();
+      // The group's first step is issued once the tile's channel mask is known.
+      if (threadIdx.x == 0) {
+        for (int k = 0; k < kG; ++k) {  // receive delay of channel g + k at the tile point nearest it
+          const float ex = elem_x(a, min(g + k, a.n_ch - 1));
+          const float xc = fminf(fmaxf(ex, x_min), x_max);
+          s_rmin[k] = sqrtf((ex - xc) * (ex - xc) + z_min * z_min) / a.c;
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        issue(i);
+      }
+    }
+    // Prefetch the next step (its stage was released by the barrier closing step i - 1).
+    if (threadIdx.x == 0 && i + 1 < n_steps && (i + 1) % n_chunks != 0) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      issue(i + 1);
+    }
+    // Wait for this step's windows (bounded: on a timeout the samples are read
+    // from global memory and the context's status word records it).
+    {
+      long spins = 0;
+      while (!mbar_try_wait(&bar[st], phase[st])) {
+        if (++spins > (1L << 24)) {
+          timed_out = true;
+          break;
+        }
+      }
+      phase[st] ^= 1u;
+    }
+    if (mask) {
+      for (int e = 0; e < kE; ++e) {
+        const int ev = e0 + e;
+        if (ev >= ev_last) break;
+        const TxDev& t = a.tx[ev];
+        float tw;
+        if (select) {
+          tw = (best_ev == ev && best_w > 0.0f) ? 1.0f : 0.0f;
+        } else if (a.tx_weighting) {
+          tw = tx_sensitivity(t, px, pz, a.lambda, a.pitch);
+        } else {
+          tw = 1.0f;
+        }
+        if (!(tw > 0.0f)) continue;
+        const float tau = tx_arrival(t, px, py, pz, a.c);
+        float tc = 1.0f, ts = 0.0f;
+        if (a.fdem > 0.0f) sincosf(a.two_pi_f * tau, &ts, &tc);
+        const float wr = tw * tc, wi = tw * ts;
+        const long trace0 = (static_cast<long>(ev) * a.n_ch + g) * a.n_smp;
+#pragma unroll
+        for (int k = 0; k < kG; ++k) {
+          if (!(mask & (1u << k))) continue;
+          const float idx = (tau + rt[k] - a.t0) * a.fs;
+          const float fl = floorf(idx);
+          const int kk = static_cast<int>(fl);
+          if (static_cast<unsigned>(kk) >= n_last) continue;
+          const float f = idx - fl;
+          const int lo = s_lo[st][e][k];
+          const int loc = kk - lo;
+          float2 s0, s1;
+          if (!timed_out && lo >= 0 && loc >= 0 && loc + 1 < kStageW) {
+            s0 = win[st][e][k][loc];
+            s1 = win[st][e][k][loc + 1];
+          } else {
+            const float2* tr = iq + trace0 + static_cast<long>(k) * a.n_smp + kk;
+            s0 = __ldg(tr);
+            s1 = __ldg(tr + 1);
+          }
+          const float vr = fmaf(f, s1.x - s0.x, s0.x);
+          const float vi = fmaf(f, s1.y - s0.y, s0.y);
+          ar[k] = fmaf(wr, vr, fmaf(-wi, vi, ar[k]));
+          ai[k] = fmaf(wr, vi, fmaf(wi, vr, ai[k]));
+        }
+      }
+    }
+    __syncthreads();   // stage st is free for step i + 2
+    if ((i + 1) % n_chunks == 0) {
+      // The group is complete: receive phasor and aperture weight, combine.
+#pragma unroll
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        if (ch >= a.n_ch || !live) continue;
+        const bool act = (mask >> k) & 1u;
+        cplx y = mk(0.f, 0.f);
+        if (act) {
+          const float w = aperture_weight(elem_x(a, ch), px, pz, a.f_number, a.rx_window, a.tukey_alpha);
+          const float ap = a.is_mv ? 1.0f : w;
+          float rc = 1.0f, rs = 0.0f;
+          if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs, &rc);
+          const float gr = ap * rc, gi = ap * rs;
+          y = mk(fmaf(gr, ar[k], -gi * ai[k]), fmaf(gr, ai[k], gi * ar[k]));
+        }
+        if (a.is_mv) {
+          a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = make_float2(y.re, y.im);
+          continue;
+        }
+        n_active += act ? 1 : 0;
+        if (a.combiner == USX_COMB_DMAS) {
+          const float m = cabsf_(y);
+          if (m > 0.0f) {
+            const cplx v = cdivr(y, sqrtf(m));
+            s = cadd(s, v);
+            q = cadd(q, cmul(v, v));
+          }
+        } else {
+          das = cadd(das, y);
+        }
+        if (a.cf && act) {
+          coh = cadd(coh, y);
+          incs += cnorm(y);
+        }
+      }
+    }
+  }
+  if (timed_out && threadIdx.x == 0 && a.status) atomicExch(a.status, 1);
+  if (!live || a.is_mv) return;
+  cplx out;
+  if (n_active == 0) {
+    out = mk(0.f, 0.f);
+  } else if (a.combiner == USX_COMB_DMAS) {
+    const cplx acc = cscale(csub(cmul(s, s), q), 0.5f);
+    out = cdivr(acc, 0.5f * fmaxf(1.0f, static_cast<float>(n_active - 1)));
+  } else {
+    out = das;
+  }
+  if (a.cf && n_active > 0)
+    out = cscale(out, (incs > 0.0f) ? cnorm(coh) / (static_cast<float>(n_active) * incs) : 0.0f);
+  a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+}
+
 // The delay-and-sum variants the autotuner chooses from (index 0 is the
 // default): (channel group, tile lines, minimum resident CTAs per SM).
 struct DasVariant {
   int group, tile_lines, min_blocks;
   void (*iq)(BfArgs);
   void (*rf)(BfArgs);
+  bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
 template <int G, int TL, int MB, bool RTS = false>
 constexpr DasVariant das_variant() {
-  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB, RTS>, das_fast_kernel<false, 16, 4, 1>};
+  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB, RTS>, das_fast_kernel<false, 16, 4, 1>, false};
+}
+template <int G, int TL, int E>
+constexpr DasVariant das_staged_variant() {
+  return DasVariant{G, TL, 0, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
 }
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
     das_variant<8, 8, 4>(),  das_variant<16, 2, 8>(), das_variant<4, 4, 12>(), das_variant<8, 2, 16>(),
-    das_variant<16, 4, 8, true>(), das_variant<16, 2, 16, true>(),
+    das_variant<16, 4, 8, true>(), das_variant<16, 2, 16, true>(), das_staged_variant<8, 4, 1>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -654,6 +985,7 @@ struct usx_bf_plan {
   int mv_mode = USX_MV_EXACT;
   int precision = USX_BF_FAST;
   int das_variant = 0;         // index into kDasVariants (the autotuner's choice)
+  bool all_plane_waves = false;  // every event is a plane wave (the staged kernel's bound)
   int* d_mv_stats = nullptr;   // [0] FP64 re-solves, [1] factorisation failures, [2] learned-MV gate rejections
   // Learned minimum variance: the network (not owned) and the gate on |1^H w - 1|.
   usx_mlp* mlp = nullptr;
@@ -735,6 +1067,7 @@ BfArgs make_args(const usx_bf_plan* p) {
   const usx_channel_desc& cd = p->cd;
   a.points = p->d_points;
   a.tx = p->d_tx;
+  a.status = p->ctx->d_status + 12;
   a.n_ch = cd.probe.n_elements;
   a.n_smp = cd.acq.n_samples;
   a.n1 = p->n1;
@@ -790,7 +1123,13 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     return USX_OK;
   }
   const bool fast = plan->precision == USX_BF_FAST;
-  const DasVariant& dv = kDasVariants[plan->das_variant];
+  const DasVariant* dvp = &kDasVariants[plan->das_variant];
+  if (dvp->staged) {
+    const bool ok = plan->cd.is_iq && plan->all_plane_waves && a.compounding != USX_COMP_INCOHERENT &&
+                    reinterpret_cast<uintptr_t>(data) % 16 == 0 && a.n_smp >= kStageW + 2;
+    if (!ok) dvp = &kDasVariants[0];
+  }
+  const DasVariant& dv = *dvp;
   dim3 grid_das(fast ? ceil_div(plan->n0, dv.tile_lines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
                 n_frames);
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
@@ -1046,6 +1385,8 @@ int usx_cu_bf_plan_create(usx_ctx* ctx, const usx_channel_desc* cd, const usx_gr
   p->ev_end = event_end;
   std::vector<TxDev> txs(static_cast<size_t>(n_ev));
   for (int e = 0; e < n_ev; ++e) txs[static_cast<size_t>(e)] = make_txdev(cd->probe, cd->transmits[e]);
+  p->all_plane_waves = n_ev > 0;
+  for (int e = 0; e < n_ev; ++e) p->all_plane_waves = p->all_plane_waves && txs[static_cast<size_t>(e)].type == USX_TX_PLANE_WAVE;
   cudaError_t e1 = cudaMalloc(&p->d_points, sizeof(float) * 3 * n_pix);
   cudaError_t e2 = cudaMalloc(&p->d_tx, sizeof(TxDev) * std::max(1, n_ev));
   cudaError_t e3 = cudaMalloc(&p->d_mv_stats, sizeof(int) * 4);
