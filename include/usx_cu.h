@@ -213,7 +213,10 @@ int usx_cu_bf_plan_set_training_export(usx_bf_plan* plan, float* features, float
 
 /* The network: fully connected layers dims[0] -> dims[1] -> ... ->
  * dims[n_layers], ReLU between layers, FP32 master weights with a BF16 copy
- * for the GEMMs (mma.sync BF16, FP32 accumulation). Every width must be a
+ * for the GEMMs (BF16 operands, FP32 accumulation: tcgen05 with the
+ * accumulator in tensor memory for the forward layers of width 128 or 256
+ * whose input width is a multiple of 64, mma.sync for the rest and for the
+ * backward pass). Every width must be a
  * positive multiple of 128. Parameters are laid out per layer as W_l
  * [dims[l]][dims[l+1]] row-major followed by b_l [dims[l+1]]. Weights start
  * He-uniform from `seed`, biases at zero. */
@@ -250,6 +253,12 @@ int usx_cu_mlp_train_step(usx_mlp* mlp, const float* x, const float* target, con
  *     and divided by rows. */
 enum { USX_MLP_LOSS_MSE = 0, USX_MLP_LOSS_LMV_OUTPUT = 1, USX_MLP_LOSS_LMV_SUBSPACE = 2 };
 int usx_cu_mlp_set_loss(usx_mlp* mlp, int kind, float beta);
+/* Forward GEMM of the network: USX_MLP_GEMM_AUTO (default) takes the tcgen05
+ * GEMM wherever the layer's shape allows it, USX_MLP_GEMM_MMA_SYNC always the
+ * mma.sync GEMM. Both accumulate the same BF16 products in FP32; they differ
+ * only in the order of the additions. */
+enum { USX_MLP_GEMM_AUTO = 0, USX_MLP_GEMM_MMA_SYNC = 1 };
+int usx_cu_mlp_set_gemm_path(usx_mlp* mlp, int path);
 
 /* Beamformer::beamform_sequence (reference beamformer.cpp:551-569) in one
  * launch: frame f uses the plan's events [first + f*events_per_frame,

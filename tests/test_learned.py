@@ -204,6 +204,44 @@ def test_mlp_forward_matches_oracle(capi, ctx, torch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("dims,rows", [((256, 256), 128), ((256, 128), 384), ((128, 256), 152 * 128 * 3 + 256),
+                                       ((256, 384, 128), 1024), ((256, 256, 256, 256, 128), 4096)])
+def test_tcgen05_gemm_matches_mma_sync(capi, ctx, torch, dims, rows):
+    """The tcgen05 forward GEMM (accumulator in tensor memory) against the
+    mma.sync GEMM: the same BF16 products summed in FP32 in another order.
+    One layer: within FP32 rounding of a 256-term sum. Several layers: the
+    hidden activations are rounded to BF16, so a few outputs may differ by one
+    BF16 step of an input. (256, 384, 128) mixes the two paths (a 384-wide
+    layer stays on mma.sync); 152 * 128 * 3 + 256 rows give every CTA of the
+    persistent grid several tiles."""
+    rng = np.random.default_rng(len(dims) * 7 + rows)
+    mlp = capi.Mlp(ctx, dims, seed=3)
+    p = mlp.get_params()
+    for w, b in mlp.layers(p):
+        b[:] = rng.standard_normal(b.size).astype(np.float32) * 0.1
+    mlp.set_params(p)
+    x = rng.standard_normal((rows, dims[0])).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    out = []
+    for path in (capi.Mlp.GEMM_AUTO, capi.Mlp.GEMM_MMA_SYNC):
+        mlp.set_gemm_path(path)
+        dy = torch.full((rows, dims[-1]), float("nan"), dtype=torch.float32, device="cuda")
+        mlp.forward(dx.data_ptr(), rows, dy.data_ptr())
+        ctx.synchronize()
+        out.append(dy.cpu().numpy())
+    tc5, mma = out
+    assert np.isfinite(tc5).all()
+    if len(dims) == 2:
+        assert np.abs(tc5 - mma).max() <= 1e-5 * np.abs(mma).max()
+        want, _ = MO.forward(p, dims, x, quantize=True)
+        assert rel_l2(tc5, want) < 1e-5
+    else:
+        assert rel_l2(tc5, mma) < 2e-3
+        want, _ = MO.forward(p, dims, x, quantize=True)
+        assert rel_l2(tc5, want) < 2e-3
+
+
+@pytest.mark.gpu
 def test_mlp_gradients_match_oracle(capi, ctx, torch):
     """Hand-written backward GEMMs (dW split-K, dX with the ReLU mask) and the
     bias reduction against the oracle's backward with the same BF16 rounding."""

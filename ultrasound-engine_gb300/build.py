@@ -39,8 +39,8 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["ctx.cu", "demod.cu", "beamform.cu", "mv_tc.cu", "learned.cu", "mlp.cu", "post.cu", "doppler.cu",
-              "simulate.cu"]
-FMAD_SOURCES = {"mv_tc.cu", "learned.cu", "mlp.cu"}
+              "simulate.cu", "gemm_tc5.cu"]
+FMAD_SOURCES = {"mv_tc.cu", "learned.cu", "mlp.cu", "gemm_tc5.cu"}
 HOST_SOURCES = ["types.cpp", "geometry.cpp", "simulator.cpp", "demodulate.cpp", "beamformer.cpp",
                 "postprocess.cpp", "doppler.cpp", "pipeline.cpp", "runtime.cpp"]
 

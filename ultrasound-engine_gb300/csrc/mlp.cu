@@ -555,6 +555,8 @@ struct usx_mlp {
   float* m = nullptr;
   float* v = nullptr;
   __nv_bfloat16* p16 = nullptr;     // BF16 copy used by the GEMMs
+  __nv_bfloat16* p16t = nullptr;    // the same with each W_l transposed ([out][in]) for the tcgen05 GEMM
+  int gemm_path = USX_MLP_GEMM_AUTO;
   long step = 0;
   // Activation workspace for `cap` rows.
   long cap = 0;
@@ -589,18 +591,44 @@ int mlp_reserve(usx_mlp* n, long rows) {
   return USX_OK;
 }
 
+// p16t <- per-layer transposes of p16, after every change of the weights.
+int refresh_transposed(usx_mlp* n) {
+  for (int l = 0; l < n->n_layers; ++l)
+    if (int rc = transpose_bf16(n->ctx->stream, n->p16 + n->w_off[static_cast<size_t>(l)],
+                                n->dims[static_cast<size_t>(l)], n->dims[static_cast<size_t>(l + 1)],
+                                n->p16t + n->w_off[static_cast<size_t>(l)]))
+      return rc;
+  return USX_OK;
+}
+
+// Layer l forward: out = act(in W_l + b_l), ReLU on all but the last layer,
+// BF16 (dst16) and / or FP32 (dst32) output. The tcgen05 GEMM takes the
+// layers whose shape it supports; the mma.sync GEMM the rest.
+int layer_forward(usx_mlp* n, usx_ctx* ctx, int l, const __nv_bfloat16* in, long rows, __nv_bfloat16* dst16,
+                  float* dst32, const char* tc5_tag, const char* mma_tag) {
+  const int din = n->dims[static_cast<size_t>(l)], dout = n->dims[static_cast<size_t>(l + 1)];
+  const bool relu = l < n->n_layers - 1;
+  const float* bias = n->p + n->b_off[static_cast<size_t>(l)];
+  if (n->gemm_path == USX_MLP_GEMM_AUTO && gemm_tc5_supported(static_cast<int>(rows), dout, din)) {
+    prof_begin(ctx, tc5_tag);
+    const int rc = launch_gemm_tc5(ctx, in, n->p16t + n->w_off[static_cast<size_t>(l)], bias, relu, dst16, dst32,
+                                   static_cast<int>(rows), dout, din);
+    prof_end(ctx);
+    return rc;
+  }
+  prof_begin(ctx, mma_tag);
+  const int rc = launch_gemm(ctx->stream, in, din, true, n->p16 + n->w_off[static_cast<size_t>(l)], dout, true,
+                             static_cast<int>(rows), dout, din, bias, relu, nullptr, 0, dst16, dst32, dout, 1);
+  prof_end(ctx);
+  return rc;
+}
+
 int mlp_forward_rows(usx_mlp* n, long rows) {
-  cudaStream_t st = n->ctx->stream;
   for (int l = 0; l < n->n_layers; ++l) {
-    const int din = n->dims[static_cast<size_t>(l)], dout = n->dims[static_cast<size_t>(l + 1)];
     const bool last = l == n->n_layers - 1;
-    prof_begin(n->ctx, "gemm_bf16_kernel(fwd)");
-    const int rc = launch_gemm(st, n->act[static_cast<size_t>(l)], din, true, n->p16 + n->w_off[static_cast<size_t>(l)],
-                               dout, true, static_cast<int>(rows), dout, din, n->p + n->b_off[static_cast<size_t>(l)],
-                               !last, nullptr, 0, n->act[static_cast<size_t>(l + 1)], last ? n->out32 : nullptr, dout,
-                               1);
-    prof_end(n->ctx);
-    if (rc) return rc;
+    if (int rc = layer_forward(n, n->ctx, l, n->act[static_cast<size_t>(l)], rows, n->act[static_cast<size_t>(l + 1)],
+                               last ? n->out32 : nullptr, "gemm_tc5_kernel(fwd)", "gemm_bf16_kernel(fwd)"))
+      return rc;
   }
   return USX_OK;
 }
@@ -619,19 +647,14 @@ bool mlp_is_lmv(const usx_mlp* n) { return n->dims.front() == kLmvFeatures && n-
 
 int mlp_infer(usx_mlp* n, usx_ctx* ctx, const void* x16, long rows, void* t0, void* t1, float* out32) {
   if (rows % 128) return fail(USX_ERR_INVALID, "mlp_infer: rows must be a multiple of 128");
-  cudaStream_t st = ctx->stream;
   const __nv_bfloat16* in = static_cast<const __nv_bfloat16*>(x16);
   __nv_bfloat16* ping[2] = {static_cast<__nv_bfloat16*>(t0), static_cast<__nv_bfloat16*>(t1)};
   for (int l = 0; l < n->n_layers; ++l) {
-    const int din = n->dims[static_cast<size_t>(l)], dout = n->dims[static_cast<size_t>(l + 1)];
     const bool last = l == n->n_layers - 1;
     __nv_bfloat16* dst = last ? nullptr : ping[l & 1];
-    prof_begin(ctx, "gemm_bf16_kernel(lmv)");
-    const int rc = launch_gemm(st, in, din, true, n->p16 + n->w_off[static_cast<size_t>(l)], dout, true,
-                               static_cast<int>(rows), dout, din, n->p + n->b_off[static_cast<size_t>(l)], !last,
-                               nullptr, 0, dst, last ? out32 : nullptr, dout, 1);
-    prof_end(ctx);
-    if (rc) return rc;
+    if (int rc = layer_forward(n, ctx, l, in, rows, dst, last ? out32 : nullptr, "gemm_tc5_kernel(lmv)",
+                               "gemm_bf16_kernel(lmv)"))
+      return rc;
     in = dst;
   }
   return USX_OK;
@@ -665,6 +688,7 @@ int usx_cu_mlp_create(usx_ctx* ctx, int n_layers, const int* dims, uint64_t seed
   e = e == cudaSuccess ? cudaMalloc(&n->m, sizeof(float) * off) : e;
   e = e == cudaSuccess ? cudaMalloc(&n->v, sizeof(float) * off) : e;
   e = e == cudaSuccess ? cudaMalloc(&n->p16, sizeof(__nv_bfloat16) * off) : e;
+  e = e == cudaSuccess ? cudaMalloc(&n->p16t, sizeof(__nv_bfloat16) * off) : e;
   e = e == cudaSuccess ? cudaMalloc(&n->loss, sizeof(float) * 4) : e;
   if (e != cudaSuccess) {
     usx_cu_mlp_destroy(n);
@@ -683,6 +707,10 @@ int usx_cu_mlp_create(usx_ctx* ctx, int n_layers, const int* dims, uint64_t seed
   }
   f32_to_bf16_kernel<<<ceil_div(static_cast<long>(off), 256), 256, 0, st>>>(n->p, n->p16, static_cast<long>(off));
   USX_CHECK_LAUNCH("usx_cu_mlp_create");
+  if (int rc = refresh_transposed(n)) {
+    usx_cu_mlp_destroy(n);
+    return rc;
+  }
   *out = n;
   return USX_OK;
 }
@@ -701,6 +729,7 @@ int usx_cu_mlp_destroy(usx_mlp* n) {
   cudaFree(n->m);
   cudaFree(n->v);
   cudaFree(n->p16);
+  cudaFree(n->p16t);
   cudaFree(n->loss);
   delete n;
   return USX_OK;
@@ -725,7 +754,16 @@ int usx_cu_mlp_set_params(usx_mlp* n, const float* host) {
   f32_to_bf16_kernel<<<ceil_div(static_cast<long>(n->n_params), 256), 256, 0, n->ctx->stream>>>(
       n->p, n->p16, static_cast<long>(n->n_params));
   USX_CHECK_LAUNCH("f32_to_bf16_kernel");
+  if (int rc = refresh_transposed(n)) return rc;
   USX_CUDA(cudaStreamSynchronize(n->ctx->stream));
+  return USX_OK;
+}
+
+int usx_cu_mlp_set_gemm_path(usx_mlp* n, int path) {
+  if (!n) return fail(USX_ERR_INVALID, "usx_cu_mlp_set_gemm_path: null network");
+  if (path != USX_MLP_GEMM_AUTO && path != USX_MLP_GEMM_MMA_SYNC)
+    return fail(USX_ERR_INVALID, "usx_cu_mlp_set_gemm_path: unknown path");
+  n->gemm_path = path;
   return USX_OK;
 }
 
@@ -824,6 +862,7 @@ int usx_cu_mlp_train_step(usx_mlp* n, const float* x, const float* target, const
     adam_kernel<<<ceil_div(static_cast<long>(n->n_params), 256), 256, 0, st>>>(
         n->p, n->grad, n->m, n->v, static_cast<long>(n->n_params), lr, b1, b2, c1, c2, 1e-8f, n->p16);
     USX_CHECK_LAUNCH("adam_kernel");
+    if (int rc = refresh_transposed(n)) return rc;
   }
   if (grad_host) {
     USX_CUDA(cudaMemcpyAsync(grad_host, n->grad, sizeof(float) * n->n_params, cudaMemcpyDeviceToHost, st));

@@ -286,6 +286,16 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
 // Bytes per pixel of the scratch record launch_lmv_subspace passes between its two stages.
 int lmv_subspace_record_bytes(int n_beams);
 
+// Fifth-generation tensor-core GEMM (gemm_tc5.cu): C = act(A W + b) with A
+// [M][K] and W^T [N][K] BF16 (K contiguous), FP32 accumulation in tensor
+// memory, BF16 and / or FP32 output [M][N]; N = 128 or 256, K a multiple of
+// 64, M a multiple of 128.
+bool gemm_tc5_supported(int M, int N, int K);
+int launch_gemm_tc5(usx_ctx* ctx, const void* A, const void* Bt, const float* bias, bool relu, void* C16, float* C32,
+                    int M, int N, int K);
+// wt[N][K] = w[K][N] (BF16).
+int transpose_bf16(cudaStream_t st, const void* w, int K, int N, void* wt);
+
 // The network (mlp.cu). mlp_infer runs `rows` (a multiple of 128) BF16 input
 // rows through every layer with caller scratch t0, t1 (rows x widest BF16
 // each) and writes the FP32 outputs.

@@ -431,6 +431,13 @@ class Mlp:
         combiner output error + beta * weight MSE)."""
         check(lib().usx_cu_mlp_set_loss(self._h, int(kind), C.c_float(beta)), "mlp_set_loss")
 
+    GEMM_AUTO, GEMM_MMA_SYNC = 0, 1
+
+    def set_gemm_path(self, path: int) -> None:
+        """Forward GEMM: GEMM_AUTO (tcgen05 wherever the layer shape allows)
+        or GEMM_MMA_SYNC (the mma.sync GEMM for every layer)."""
+        check(lib().usx_cu_mlp_set_gemm_path(self._h, int(path)), "mlp_set_gemm_path")
+
     def forward(self, x_ptr: int, rows: int, y_ptr: int) -> None:
         check(lib().usx_cu_mlp_forward(self._h, vp(x_ptr), C.c_int64(rows), vp(y_ptr)), "mlp_forward")
 
