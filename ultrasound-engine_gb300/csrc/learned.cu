@@ -47,7 +47,7 @@ struct LmvArgs {
   __nv_bfloat16* feat16;  // [row][256] (inference) or null
   float* feat32;          // [row][256] (training export) or null
   float2* avg;            // [row][64] subarray-averaged snapshot (inference) or null
-  float4* meta;           // [row] (L, n_act, coherence factor, 0) (inference) or null
+  float4* meta;           // [row] (L, n_act, coherence factor, first active channel) (inference) or null
   float2* out;            // frames, written here for n_act < 4 (inference) or null
   long out_stride;
 };
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
       if (a.avg) a.avg[row * kLmvMaxL + m] = v;
     }
     if (lane == 0 && a.meta)
-      a.meta[row] = make_float4(static_cast<float>(L), static_cast<float>(n_act), cf_factor, 0.f);
+      a.meta[row] = make_float4(static_cast<float>(L), static_cast<float>(n_act), cf_factor, static_cast<float>(act[0]));
   }
 }
 
@@ -310,7 +310,6 @@ __global__ void __launch_bounds__(256) lmv_apply_kernel(const ApplyArgs a) {
 // network's distortionless residual |1^H w~ / L - 1| comes first; gated
 // pixels go to the exact solver.
 constexpr int kSubMaxBeams = 7;            // b = 0, +1, -1, +2, -2, +3, -3
-constexpr int kSubMaxK = kSubMaxBeams + 1; // plus the network's direction
 constexpr int kSubWarps = 4;
 constexpr int kSubMaxN = 128;              // active channels
 
@@ -319,7 +318,7 @@ struct SubArgs {
   const float* points;
   const float* net;       // [row][128]
   const float2* avg;      // [row][64] subarray-averaged snapshot of the centre row
-  const float4* meta;     // [row] (L, n_act, cf, 0)
+  const float4* meta;     // [row] (L, n_act, cf, first active channel)
   float2* out;
   long out_stride;
   int n_ch, n_pix, n1, n_dmax;
@@ -341,13 +340,22 @@ __host__ __device__ constexpr int lmv_rec_floats(int nb) {
   return ((nb + 1) * (nb + 2) + 2 * (nb + 1) + 8 + 3) / 4 * 4;
 }
 
-// Per-warp shared memory; the range rows follow it (n_dmax x kSubMaxN).
+// The beams' prefix sums are stored skewed, t at t + t / 16: conflict-free
+// both for the runs of four the scan writes (t = 4 lane + c) and for the
+// consecutive t the snapshot passes read. Two range rows (linear, zero past
+// n_act): the next one streams in (cp.async) while the current one is used.
+constexpr int kSubPre = kSubMaxN + 1 + kSubMaxN / 16;
+constexpr int kSubRing = 32;   // snapshot projections left over from full passes
+
+__device__ __forceinline__ int skw(int t) { return t + (t >> 4); }
+
 template <int NB>
 struct SubWarpSmem {
-  float2 pre[NB][kSubMaxN + 1];             // prefix sums of one row, per beam
+  float2 pre[NB][kSubPre];                  // prefix sums of one row, per beam (skewed)
   float2 tw1[kSubMaxN];                     // e^{-j 2 pi t / L}; beam b's twiddle is its b-th power
-  float2 wq[kLmvMaxL];                      // the network's direction, orthogonalised
-  float2 rows[1][kSubMaxN];                 // [n_dmax][kSubMaxN] range rows, active channels
+  float4 qq[kLmvMaxL];                      // the network's direction q, orthogonalised: (q.x, q.x, q.y, q.y), 0 past L
+  float2 ring[NB + 1][kSubRing];            // z vectors of snapshots past each row's full passes
+  float2 rows[2][kSubMaxN];
 };
 
 // e^{-j 2 pi b t / L} for b = 0, 1, -1, 2, -2, 3, -3 (k = 0..6) from
@@ -360,8 +368,14 @@ __device__ __forceinline__ float2 beam_twiddle(float2 t1, int k) {
   return (k & 1) ? t : make_float2(t.x, -t.y);
 }
 template <int NB>
-__host__ __device__ constexpr size_t sub_warp_bytes(int n_dmax) {
-  return (sizeof(SubWarpSmem<NB>) + sizeof(float2) * kSubMaxN * (n_dmax - 1) + 15) / 16 * 16;
+__host__ __device__ constexpr size_t sub_warp_bytes() {
+  return (sizeof(SubWarpSmem<NB>) + 15) / 16 * 16;
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* g, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+               "l"(g), "r"(src_bytes)
+               : "memory");
 }
 
 __device__ __forceinline__ float2 warp_sum2(float2 v) {
@@ -376,32 +390,79 @@ __device__ __forceinline__ float2 warp_sum2(float2 v) {
 // snapshot projections and the Gram matrix G = sum_s z_s z_s^H (z = Q^H y_s),
 // written with the projections of the subarray average and of 1 onto the
 // basis as one record per pixel (stage 2 solves it, one thread per pixel).
-// NB, the number of beams (1, 3, 5 or 7), is a template parameter so that
-// every loop over the basis is unrolled to its size.
+// The range rows are processed one at a time while the next streams in: the
+// beams' prefix sums, then passes of 32 snapshots (each lane one snapshot:
+// beam projections from the prefix sums, the network direction's by a
+// sliding dot product, its Gram update). The snapshots past the last full
+// pass (n_sub mod 32, often one) take the network direction's projection
+// from the whole warp and wait in a ring until 32 have gathered. NB, the
+// number of beams (1, 3, 5 or 7), is a template parameter so that every loop
+// over the basis is unrolled to its size.
+// Three CTAs per SM (168 registers, 12 warps) measured faster than four with
+// the spills a 128-register cap forces.
 template <int NB>
-__global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_gram_kernel(const SubArgs a) {
+__global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(const SubArgs a) {
   extern __shared__ float4 sub_smem_raw[];
+  constexpr int K1 = NB + 1;
+  constexpr int kG = K1 * (K1 + 1);  // upper triangle of G, (re, im)
+  constexpr int kTail = kG + 2 * K1; // record: [G][Q^H abar][w_q^H 1, eps, K, nb, has_w, L, valid]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   SubWarpSmem<NB>& sm = *reinterpret_cast<SubWarpSmem<NB>*>(reinterpret_cast<char*>(sub_smem_raw) +
-                                                           warp * sub_warp_bytes<NB>(a.n_dmax));
-  float2* srow = &sm.rows[0][0];  // [n_dmax][kSubMaxN]
-  const int nb_all = NB;
+                                                           warp * sub_warp_bytes<NB>());
+  const long stride = static_cast<long>(gridDim.x) * kSubWarps;
 
-  for (long row = static_cast<long>(blockIdx.x) * kSubWarps + warp; row < a.n_rows;
-       row += static_cast<long>(gridDim.x) * kSubWarps) {
-    const float4 meta = a.meta[row];
+  // The next pixel's metadata and network output are fetched while the
+  // current one is processed.
+  long row = static_cast<long>(blockIdx.x) * kSubWarps + warp;
+  float4 meta_n = make_float4(0.f, 0.f, 0.f, 0.f), o_n = meta_n;
+  if (row < a.n_rows) {
+    meta_n = a.meta[row];
+    o_n = reinterpret_cast<const float4*>(a.net + row * kLmvOut)[lane];
+  }
+  for (; row < a.n_rows; row += stride) {
+    const float4 meta = meta_n, o = o_n;
+    if (row + stride < a.n_rows) {
+      meta_n = a.meta[row + stride];
+      o_n = reinterpret_cast<const float4*>(a.net + (row + stride) * kLmvOut)[lane];
+    }
+    float* rec = a.rec + row * lmv_rec_floats(NB);
     const int L = static_cast<int>(meta.x);
     if (L == 0) {  // n_act < 4: written by the feature pass
-      if (lane == 0) a.rec[row * lmv_rec_floats(NB) + (NB + 1) * (NB + 2) + 2 * (NB + 1) + 7] = 0.f;
+      if (lane == 0) rec[kTail + 7] = 0.f;
       continue;
     }
     const long frame = row / a.n_pix;
     const int pix = static_cast<int>(row - frame * a.n_pix);
-    // The first nb of b = 0, 1, -1, 2, -2 are distinct modulo L when nb <= L;
-    // with nb = L they span every length-L vector (the exact solve).
-    const int nb = min(nb_all, L);
+    // The first nb of b = 0, 1, -1, 2, -2, 3, -3 are distinct modulo L when
+    // nb <= L; with nb = L they span every length-L vector (the exact solve).
+    const int nb = min(NB, L);
+
+    // Active aperture (|x_e - x_p| < z / (2 F#): one contiguous run, from the
+    // feature pass) and the range rows of the smoothing window; the first row
+    // starts streaming now.
+    const int j = pix % a.n1;
+    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+    const int n_act = min(static_cast<int>(meta.y), kSubMaxN), first = static_cast<int>(meta.w);
+    const int n_sub = n_act - L + 1;
+    int dlo = -a.range_avg, dhi = a.range_avg;
+    while (j + dlo < 0) ++dlo;
+    while (j + dhi >= a.n1) --dhi;
+    const int n_d = dhi - dlo + 1;
+    auto issue_row = [&](int d) {
+      float2* dst = sm.rows[d & 1];
+      const float2* src = Y + static_cast<long>(pix + dlo + d) * a.n_ch + first;
+#pragma unroll
+      for (int c = 0; c < kSubMaxN / 32; ++c) {
+        const int t = c * 32 + lane;
+        const bool in = t < n_act;
+        cp_async8(dst + t, in ? src + t : src, in ? 8 : 0);   // zero-fills past n_act
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    issue_row(0);
+    const float4 av4 = reinterpret_cast<const float4*>(a.avg + row * kLmvMaxL)[lane];
+
     // The network's weights (lane holds i = 2 lane, 2 lane + 1) and the gate.
-    const float4 o = reinterpret_cast<const float4*>(a.net + row * kLmvOut)[lane];
     const float inv_l = 1.0f / static_cast<float>(L);
     float2 w0 = make_float2(0.f, 0.f), w1 = make_float2(0.f, 0.f);
     if (2 * lane < L) w0 = make_float2(o.x * inv_l, o.y * inv_l);
@@ -409,195 +470,267 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_gram_kernel(const
     const float2 sw = warp_sum2(make_float2(w0.x + w1.x, w0.y + w1.y));
     const float res = sqrtf((sw.x - 1.f) * (sw.x - 1.f) + sw.y * sw.y);
     if (!(res <= a.gate)) {
+      asm volatile("cp.async.wait_all;\n" ::: "memory");
       if (lane == 0) {
         push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
         if (a.stats) atomicAdd(a.stats, 1);
-        a.rec[row * lmv_rec_floats(NB) + (NB + 1) * (NB + 2) + 2 * (NB + 1) + 7] = 0.f;
+        rec[kTail + 7] = 0.f;
       }
+      __syncwarp();
       continue;
     }
-    __syncwarp();
     // Twiddles e^{-j 2 pi t / L}, t < 128, argument reduced to one turn.
     for (int t = lane; t < kSubMaxN; t += 32) {
       float sn, cs;
       sincospif(2.0f * static_cast<float>(t % L) * inv_l, &sn, &cs);
       sm.tw1[t] = make_float2(cs, -sn);
     }
-    // w~ minus its projections on the beams: c_b = u_b^H w~ (u_b = conj(tw_b) / sqrt(L)).
     const float rs = rsqrtf(static_cast<float>(L));
     __syncwarp();
+    // w~ minus its projections on the beams: c_b = u_b^H w~ (u_b = conj(tw_b) / sqrt(L)).
     float2 wv[2];
     {
       const int i0 = 2 * lane;
       wv[0] = w0;
       wv[1] = w1;
+      // (wv is zero past L; beams past nb alias earlier ones and are left out.)
       float2 cb[NB];
+      float2 t1h[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) t1h[h] = sm.tw1[i0 + h];
 #pragma unroll
       for (int k = 0; k < NB; ++k) {
         float2 d = make_float2(0.f, 0.f);
-        if (k < nb) {
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int i = i0 + h;
-            if (i < L) {  // conj(u_b[i]) w~_i = tw_b[i] w~_i / sqrt(L)
-              const float2 t = beam_twiddle(sm.tw1[i], k);
-              d.x += (t.x * wv[h].x - t.y * wv[h].y) * rs;
-              d.y += (t.x * wv[h].y + t.y * wv[h].x) * rs;
-            }
-          }
+        for (int h = 0; h < 2; ++h) {  // conj(u_b[i]) w~_i = tw_b[i] w~_i / sqrt(L)
+          const float2 t = beam_twiddle(t1h[h], k);
+          d.x += t.x * wv[h].x - t.y * wv[h].y;
+          d.y += t.x * wv[h].y + t.y * wv[h].x;
         }
-        cb[k] = warp_sum2(d);
+        cb[k] = d;
       }
       float n0 = w0.x * w0.x + w0.y * w0.y + w1.x * w1.x + w1.y * w1.y;
+      // The beam reductions and the norm interleaved, level by level.
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int i = i0 + h;
-        if (i >= L) continue;
+      for (int o2 = 16; o2 > 0; o2 >>= 1) {
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
-          if (k >= nb) continue;
-          const float2 t = beam_twiddle(sm.tw1[i], k);  // u_b[i] = conj(t) / sqrt(L)
-          const float ux = t.x * rs, uy = -t.y * rs;
-          wv[h].x -= cb[k].x * ux - cb[k].y * uy;
-          wv[h].y -= cb[k].x * uy + cb[k].y * ux;
+          cb[k].x += __shfl_xor_sync(0xffffffffu, cb[k].x, o2);
+          cb[k].y += __shfl_xor_sync(0xffffffffu, cb[k].y, o2);
+        }
+        n0 += __shfl_xor_sync(0xffffffffu, n0, o2);
+      }
+      // c_b / L: both u_b factors' 1 / sqrt(L); zero for the aliases.
+#pragma unroll
+      for (int k = 0; k < NB; ++k)
+        cb[k] = k < nb ? make_float2(cb[k].x * inv_l, cb[k].y * inv_l) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float mi = i0 + h < L ? 1.f : 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+          const float2 t = beam_twiddle(t1h[h], k);  // u_b[i] = conj(t) / sqrt(L)
+          wv[h].x -= mi * (cb[k].x * t.x + cb[k].y * t.y);
+          wv[h].y -= mi * (cb[k].y * t.x - cb[k].x * t.y);
         }
       }
-      for (int o2 = 16; o2 > 0; o2 >>= 1) n0 += __shfl_xor_sync(0xffffffffu, n0, o2);
       float n1 = wv[0].x * wv[0].x + wv[0].y * wv[0].y + wv[1].x * wv[1].x + wv[1].y * wv[1].y;
       for (int o2 = 16; o2 > 0; o2 >>= 1) n1 += __shfl_xor_sync(0xffffffffu, n1, o2);
       const float sc = (n0 > 0.f && n1 > 1e-4f * n0) ? rsqrtf(n1) : 0.f;
-      if (i0 < kLmvMaxL) sm.wq[i0] = make_float2(wv[0].x * sc, wv[0].y * sc);
-      if (i0 + 1 < kLmvMaxL) sm.wq[i0 + 1] = make_float2(wv[1].x * sc, wv[1].y * sc);
       wv[0] = make_float2(wv[0].x * sc, wv[0].y * sc);
       wv[1] = make_float2(wv[1].x * sc, wv[1].y * sc);
+      sm.qq[i0] = make_float4(wv[0].x, wv[0].x, wv[0].y, wv[0].y);   // kLmvMaxL = 64: lanes cover every i
+      sm.qq[i0 + 1] = make_float4(wv[1].x, wv[1].x, wv[1].y, wv[1].y);
     }
     const bool has_w =
         __any_sync(0xffffffffu, wv[0].x != 0.f || wv[0].y != 0.f || wv[1].x != 0.f || wv[1].y != 0.f);
 
-    // Active aperture and the range rows of the smoothing window.
-    const int j = pix % a.n1;
-    const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
-    const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
-    // The active channels |x_e - x_p| < z / (2 F#) are one contiguous run.
-    int n_act = 0, first = -1;
-    for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
-      const int ch = c0 + lane;
-      bool on = false;
-      if (ch < a.n_ch)
-        on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
-                             a.tukey_alpha) > 0.0f;
-      const unsigned m = __ballot_sync(0xffffffffu, on);
-      if (first < 0 && m) first = c0 + __ffs(m) - 1;
-      n_act += __popc(m);
-    }
-    n_act = min(n_act, kSubMaxN);
-    const int n_sub = n_act - L + 1;
-    int dlo = -a.range_avg, dhi = a.range_avg;
-    while (j + dlo < 0) ++dlo;
-    while (j + dhi >= a.n1) --dhi;
-    const int n_d = dhi - dlo + 1;
-    for (int k = lane; k < n_d * n_act; k += 32) {
-      const int d = k / n_act, q = k - d * n_act;
-      srow[d * kSubMaxN + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + first + q];
-    }
-    __syncwarp();
-
-    // Trace of the covariance (times K): every sample weighted by the number
-    // of subarrays that contain it.
-    float tr = 0.f;
-    for (int k = lane; k < n_d * n_act; k += 32) {
-      const int d = k / n_act, t = k - d * n_act;
-      const float2 yv = srow[d * kSubMaxN + t];
-      const int c = min(t, n_sub - 1) - max(0, t - L + 1) + 1;
-      tr = fmaf(static_cast<float>(c), fmaf(yv.x, yv.x, yv.y * yv.y), tr);
-    }
-    for (int o2 = 16; o2 > 0; o2 >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o2);
-    const float K = static_cast<float>(n_d * n_sub);
-
-    // G = sum_s z_s z_s^H over the snapshots, z = (beams..., w_q)^H y_s.
-    constexpr int kG = (NB + 1) * (NB + 2);  // upper triangle, (re, im)
     float g[kG];
 #pragma unroll
     for (int e = 0; e < kG; ++e) g[e] = 0.f;
+    auto gram_add = [&](const float2 (&z)[K1]) {
+      int e = 0;
+#pragma unroll
+      for (int r = 0; r < K1; ++r)
+#pragma unroll
+        for (int c = r; c < K1; ++c, e += 2) {
+          g[e] = fmaf(z[r].x, z[c].x, fmaf(z[r].y, z[c].y, g[e]));      // z_r conj(z_c)
+          g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
+        }
+    };
+    float tr = 0.f;
+    int ring_n = 0;
     for (int d = 0; d < n_d; ++d) {
-      // Prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y_d[t']: each lane sums
-      // its run of C consecutive samples, then one warp scan of the run totals.
-      const int C = (n_act + 31) >> 5;
-      const int t_beg = lane * C;
-      if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NB; ++k)
-          if (k < nb) sm.pre[k][0] = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int k = 0; k < NB; ++k) {
-        if (k >= nb) continue;
-        float2 run = make_float2(0.f, 0.f), loc[kSubMaxN / 32];
-#pragma unroll
-        for (int c = 0; c < kSubMaxN / 32; ++c) {
-          const int t = t_beg + c;
-          if (c < C && t < n_act) {
-            const float2 yv = srow[d * kSubMaxN + t], tw = beam_twiddle(sm.tw1[t], k);
-            run.x += tw.x * yv.x - tw.y * yv.y;
-            run.y += tw.x * yv.y + tw.y * yv.x;
-          }
-          loc[c] = run;
-        }
-        float2 inc = run;
-        for (int o2 = 1; o2 < 32; o2 <<= 1) {
-          const float ux = __shfl_up_sync(0xffffffffu, inc.x, o2), uy = __shfl_up_sync(0xffffffffu, inc.y, o2);
-          if (lane >= o2) {
-            inc.x += ux;
-            inc.y += uy;
-          }
-        }
-        const float2 ex = make_float2(inc.x - run.x, inc.y - run.y);
-#pragma unroll
-        for (int c = 0; c < kSubMaxN / 32; ++c) {
-          const int t = t_beg + c;
-          if (c < C && t < n_act) sm.pre[k][t + 1] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
-        }
+      if (d + 1 < n_d) {
+        issue_row(d + 1);
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       }
       __syncwarp();
-      const float2* yr = srow + d * kSubMaxN;
-      for (int s0 = lane; s0 < n_sub; s0 += 32) {
-        float2 z[(NB + 1)];
-        // Beams: u_b^H y_s = conj(tw_b[s0]) (P_b[s0 + L] - P_b[s0]) / sqrt(L).
+      const float2* yr = sm.rows[d & 1];
+
+      // Trace of the covariance (times K): every sample weighted by the
+      // number of subarrays that contain it.
+      for (int t = lane; t < n_act; t += 32) {
+        const float2 yv = yr[t];
+        const int c = min(t, n_sub - 1) - max(0, t - L + 1) + 1;
+        tr = fmaf(static_cast<float>(c), fmaf(yv.x, yv.x, yv.y * yv.y), tr);
+      }
+
+      // The beams' prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y[t']: lane
+      // l sums its run t = 4 l .. 4 l + 3 (the row is zero past n_act), then a
+      // warp scan of the run totals, beam by beam.
+      {
+        float2 yv[4], t1v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          yv[c] = yr[4 * lane + c];
+          t1v[c] = sm.tw1[4 * lane + c];
+        }
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
-          z[k] = make_float2(0.f, 0.f);
-          if (k >= nb) continue;
-          const float2 hi = sm.pre[k][s0 + L], lo = sm.pre[k][s0];
-          const float2 df = make_float2((hi.x - lo.x) * rs, (hi.y - lo.y) * rs);
-          const float2 t = beam_twiddle(sm.tw1[s0], k);
-          z[k] = make_float2(t.x * df.x + t.y * df.y, t.x * df.y - t.y * df.x);
+          float2 run = make_float2(0.f, 0.f), loc[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const float2 tw = beam_twiddle(t1v[c], k);
+            run.x = fmaf(tw.x, yv[c].x, fmaf(-tw.y, yv[c].y, run.x));
+            run.y = fmaf(tw.x, yv[c].y, fmaf(tw.y, yv[c].x, run.y));
+            loc[c] = run;
+          }
+          float2 inc = run;
+#pragma unroll
+          for (int o2 = 1; o2 < 32; o2 <<= 1) {
+            const float ux = __shfl_up_sync(0xffffffffu, inc.x, o2), uy = __shfl_up_sync(0xffffffffu, inc.y, o2);
+            const float take = lane >= o2 ? 1.f : 0.f;
+            inc.x = fmaf(take, ux, inc.x);
+            inc.y = fmaf(take, uy, inc.y);
+          }
+          const float2 ex = make_float2(inc.x - run.x, inc.y - run.y);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) sm.pre[k][skw(4 * lane + c + 1)] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
         }
-        // The network's direction: w_q^H y_s.
-        float2 zw = make_float2(0.f, 0.f);
-        if (has_w)
-          for (int i = 0; i < L; ++i) {
-            const float2 q = sm.wq[i], yv = yr[s0 + i];
-            zw.x = fmaf(q.x, yv.x, fmaf(q.y, yv.y, zw.x));
-            zw.y = fmaf(q.x, yv.y, fmaf(-q.y, yv.x, zw.y));
-          }
-        z[NB] = zw;
-        int e = 0;
+        if (lane == 0)
 #pragma unroll
-        for (int r = 0; r < (NB + 1); ++r)
+          for (int k = 0; k < NB; ++k) sm.pre[k][0] = make_float2(0.f, 0.f);
+      }
+      __syncwarp();
+
+      // Beam projections of snapshot s without their 1 / sqrt(L) (applied to
+      // G at the end): conj(tw_b[s]) (P_b[s + L] - P_b[s]).
+      auto zbeams = [&](int s, float2 (&z)[K1]) {
+        const float2 t1 = sm.tw1[s];
+        const int hi_i = skw(s + L), lo_i = skw(s);
 #pragma unroll
-          for (int c = r; c < (NB + 1); ++c, e += 2) {
-            g[e] = fmaf(z[r].x, z[c].x, fmaf(z[r].y, z[c].y, g[e]));      // z_r conj(z_c)
-            g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
+        for (int k = 0; k < NB; ++k) {
+          const float2 hi = sm.pre[k][hi_i], lo = sm.pre[k][lo_i];
+          const float2 df = make_float2(hi.x - lo.x, hi.y - lo.y);
+          const float2 t = beam_twiddle(t1, k);
+          z[k] = make_float2(fmaf(t.x, df.x, t.y * df.y), fmaf(t.x, df.y, -t.y * df.x));
+        }
+      };
+      // w_q^H y_s by one lane: with q = (x, y), (x, x) * y and (y, y) * y
+      // accumulate in FP32 pairs and conj(q) y = (A.x + B.y, A.y - B.x).
+      auto zdir = [&](int s) {
+        float2 A = make_float2(0.f, 0.f), B = A;
+        const float2* ys = yr + s;
+#pragma unroll 4
+        for (int i = 0; i < L; ++i) {
+          const float4 q = sm.qq[i];
+          const float2 yv = ys[i];
+          A = __ffma2_rn(make_float2(q.x, q.y), yv, A);
+          B = __ffma2_rn(make_float2(q.z, q.w), yv, B);
+        }
+        return make_float2(A.x + B.y, A.y - B.x);
+      };
+      const int n_full = n_sub & ~31;
+      for (int s0 = 0; s0 < n_full; s0 += 32) {
+        float2 z[K1];
+        zbeams(s0 + lane, z);
+        z[NB] = has_w ? zdir(s0 + lane) : make_float2(0.f, 0.f);
+        gram_add(z);
+      }
+      const int rem = n_sub - n_full;
+      if (rem > 0) {
+        float2 z[K1];
+        const int s = n_full + min(lane, rem - 1);
+        zbeams(s, z);
+        z[NB] = make_float2(0.f, 0.f);
+        if (has_w) {
+          if (rem <= 4) {
+            // A few snapshots: each one's w_q^H y_s by the whole warp.
+            for (int r = 0; r < rem; ++r) {
+              float2 acc = make_float2(0.f, 0.f);
+              for (int i = lane; i < L; i += 32) {
+                const float4 q = sm.qq[i];
+                const float2 yv = yr[n_full + r + i];
+                acc.x = fmaf(q.x, yv.x, fmaf(q.z, yv.y, acc.x));
+                acc.y = fmaf(q.x, yv.y, fmaf(-q.z, yv.x, acc.y));
+              }
+              acc = warp_sum2(acc);
+              if (lane == r) z[NB] = acc;
+            }
+          } else if (lane < rem) {
+            z[NB] = zdir(s);
           }
+        }
+        if (ring_n + rem >= 32) {
+          // One full pass: the ring's entries, then this row's first leftovers.
+          const int take = 32 - ring_n;
+          float2 zp[K1];
+          const int src = lane - ring_n;   // this row's leftover in lanes ring_n ..
+#pragma unroll
+          for (int k = 0; k < K1; ++k) {
+            const float v_x = __shfl_sync(0xffffffffu, z[k].x, src & 31), v_y = __shfl_sync(0xffffffffu, z[k].y, src & 31);
+            zp[k] = lane < ring_n ? sm.ring[k][lane] : make_float2(v_x, v_y);
+          }
+          gram_add(zp);
+          __syncwarp();
+          // The rest of this row's leftovers start the ring again.
+#pragma unroll
+          for (int k = 0; k < K1; ++k) {
+            const float v_x = __shfl_sync(0xffffffffu, z[k].x, (lane + take) & 31),
+                        v_y = __shfl_sync(0xffffffffu, z[k].y, (lane + take) & 31);
+            if (lane < rem - take) sm.ring[k][lane] = make_float2(v_x, v_y);
+          }
+          ring_n = rem - take;
+        } else {
+          if (lane < rem)
+#pragma unroll
+            for (int k = 0; k < K1; ++k) sm.ring[k][ring_n + lane] = z[k];
+          ring_n += rem;
+        }
       }
       __syncwarp();
     }
+    if (ring_n > 0) {
+      float2 z[K1];
+#pragma unroll
+      for (int k = 0; k < K1; ++k) z[k] = lane < ring_n ? sm.ring[k][lane] : make_float2(0.f, 0.f);
+      gram_add(z);
+    }
+    for (int o2 = 16; o2 > 0; o2 >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o2);
+    const float K = static_cast<float>(n_d * n_sub);
 
     // G, reduced across the warp by a reduce-scatter: after five halvings each
     // lane holds kPad / 32 finished entries, written straight to the record.
     constexpr int kPad = (kG + 31) / 32 * 32;
     float v[kPad];
+    {
+      // The beams' 1 / sqrt(L) per factor; entries of beams past nb are
+      // replaced by the identity in stage 2.
+      int e = 0;
 #pragma unroll
-    for (int e = 0; e < kPad; ++e) v[e] = e < kG ? g[e] : 0.f;
+      for (int r = 0; r < K1; ++r)
+#pragma unroll
+        for (int c = r; c < K1; ++c, e += 2) {
+          const float f = (r < NB ? rs : 1.f) * (c < NB ? rs : 1.f);
+          v[e] = g[e] * f;
+          v[e + 1] = g[e + 1] * f;
+        }
+#pragma unroll
+      for (int e2 = kG; e2 < kPad; ++e2) v[e2] = 0.f;
+    }
     int base = 0;
 #pragma unroll
     for (int lvl = 0; lvl < 5; ++lvl) {
@@ -613,53 +746,60 @@ __global__ void __launch_bounds__(32 * kSubWarps) lmv_subspace_gram_kernel(const
       }
       if (up) base += half;
     }
-    float* rec = a.rec + row * lmv_rec_floats(NB);
 #pragma unroll
     for (int i = 0; i < kPad / 32; ++i)
       if (base + i < kG) rec[base + i] = v[i];
-    // Projections of the subarray average and of 1 onto the basis.
-    const float4 av4 = reinterpret_cast<const float4*>(a.avg + row * kLmvMaxL)[lane];
-    float2 ak[NB + 1];
+    // Projections of the subarray average and of 1 onto the basis, reduced
+    // together.
+    float2 ak[K1];
 #pragma unroll
-    for (int k = 0; k <= NB; ++k) {
+    for (int k = 0; k < K1; ++k) {
       float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int i = 2 * lane + h;
-        if (i >= L) continue;
-        const float ax = h ? av4.z : av4.x, ay = h ? av4.w : av4.y;
-        float2 q;   // basis vector k at i
+        const float mi = i < L ? 1.f : 0.f;   // the average is defined for i < L
+        const float ax = (h ? av4.z : av4.x) * mi, ay = (h ? av4.w : av4.y) * mi;
+        float2 q;   // basis vector k at i (beams past nb are unused by stage 2)
         if (k < NB) {
           const float2 t = beam_twiddle(sm.tw1[i], k);
           q = make_float2(t.x * rs, -t.y * rs);
-          if (k >= nb) q = make_float2(0.f, 0.f);
         } else {
           q = wv[h];
         }
         acc.x += q.x * ax + q.y * ay;   // conj(q) abar
         acc.y += q.x * ay - q.y * ax;
       }
-      ak[k] = warp_sum2(acc);
+      ak[k] = acc;
     }
     float2 bw = make_float2(0.f, 0.f);
     if (2 * lane < L) bw = make_float2(wv[0].x, -wv[0].y);
     if (2 * lane + 1 < L) bw = make_float2(bw.x + wv[1].x, bw.y - wv[1].y);
-    bw = warp_sum2(bw);   // w_q^H 1
+#pragma unroll
+    for (int o2 = 16; o2 > 0; o2 >>= 1) {
+#pragma unroll
+      for (int k = 0; k < K1; ++k) {
+        ak[k].x += __shfl_xor_sync(0xffffffffu, ak[k].x, o2);
+        ak[k].y += __shfl_xor_sync(0xffffffffu, ak[k].y, o2);
+      }
+      bw.x += __shfl_xor_sync(0xffffffffu, bw.x, o2);   // w_q^H 1
+      bw.y += __shfl_xor_sync(0xffffffffu, bw.y, o2);
+    }
     if (lane == 0) {
       float* tail = rec + kG;
 #pragma unroll
-      for (int k = 0; k <= NB; ++k) {
+      for (int k = 0; k < K1; ++k) {
         tail[2 * k] = ak[k].x;
         tail[2 * k + 1] = ak[k].y;
       }
-      tail[2 * (NB + 1) + 0] = bw.x;
-      tail[2 * (NB + 1) + 1] = bw.y;
-      tail[2 * (NB + 1) + 2] = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);   // eps
-      tail[2 * (NB + 1) + 3] = K;
-      tail[2 * (NB + 1) + 4] = static_cast<float>(nb);
-      tail[2 * (NB + 1) + 5] = has_w ? 1.f : 0.f;
-      tail[2 * (NB + 1) + 6] = static_cast<float>(L);
-      tail[2 * (NB + 1) + 7] = 1.f;   // record valid
+      tail[2 * K1 + 0] = bw.x;
+      tail[2 * K1 + 1] = bw.y;
+      tail[2 * K1 + 2] = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);   // eps
+      tail[2 * K1 + 3] = K;
+      tail[2 * K1 + 4] = static_cast<float>(nb);
+      tail[2 * K1 + 5] = has_w ? 1.f : 0.f;
+      tail[2 * K1 + 6] = static_cast<float>(L);
+      tail[2 * K1 + 7] = 1.f;   // record valid
     }
     __syncwarp();
   }
@@ -894,10 +1034,10 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
     return USX_OK;
   };
   switch (std::min(kSubMaxBeams, 1 + n_beams)) {
-    case 1: return go(lmv_subspace_gram_kernel<1>, lmv_subspace_solve_kernel<1>, sub_warp_bytes<1>(a.n_dmax));
-    case 3: return go(lmv_subspace_gram_kernel<3>, lmv_subspace_solve_kernel<3>, sub_warp_bytes<3>(a.n_dmax));
-    case 5: return go(lmv_subspace_gram_kernel<5>, lmv_subspace_solve_kernel<5>, sub_warp_bytes<5>(a.n_dmax));
-    default: return go(lmv_subspace_gram_kernel<7>, lmv_subspace_solve_kernel<7>, sub_warp_bytes<7>(a.n_dmax));
+    case 1: return go(lmv_subspace_gram_kernel<1>, lmv_subspace_solve_kernel<1>, sub_warp_bytes<1>());
+    case 3: return go(lmv_subspace_gram_kernel<3>, lmv_subspace_solve_kernel<3>, sub_warp_bytes<3>());
+    case 5: return go(lmv_subspace_gram_kernel<5>, lmv_subspace_solve_kernel<5>, sub_warp_bytes<5>());
+    default: return go(lmv_subspace_gram_kernel<7>, lmv_subspace_solve_kernel<7>, sub_warp_bytes<7>());
   }
 }
 
