@@ -238,9 +238,9 @@ WEIGHTS = PKG / "weights" / "learned_mv_128ch_l64.bin"
 # same workload (profiles/ holds the summaries these come from), scaled to a
 # full 512-line frame where the capture was a subset of lines.
 TRAFFIC_PER_FRAME = {
-    # profiles/lmv_subspace_gram_kernel_7beams_64x1024.md: 96.11 MB read + 10.08 MB written for
+    # profiles/lmv_subspace_gram_kernel_7beams_64x1024.md: 95.39 MB read + 9.67 MB written for
     # the first 64 of 512 lines, scaled by 8 (deeper lines read wider apertures: a lower bound).
-    "lmv_subspace_gram_kernel": 8 * (96.113e6 + 10.075e6),
+    "lmv_subspace_gram_kernel": 8 * (95.388e6 + 9.666e6),
 }
 
 
