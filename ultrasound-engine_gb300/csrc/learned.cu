@@ -52,11 +52,18 @@ struct LmvArgs {
   long out_stride;
 };
 
-__global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvArgs a) {
+// kStride: the shared-memory row stride when it is known at compile time
+// (n_ch <= 128: 128), else 0 (n_ch); kND: the full smoothing window's row
+// count that gets an unrolled lag loop (5 for range averaging 2), else 0.
+// Five CTAs per SM (48 registers) measured faster than the four that 59
+// registers allow.
+template <int kStride, int kND>
+__global__ void __launch_bounds__(32 * kLmvWarps, 5) lmv_features_kernel(const LmvArgs a) {
   extern __shared__ float2 lmv_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float2* rows = lmv_smem + static_cast<size_t>(warp) * a.n_dmax * a.n_ch;
-  int* act = reinterpret_cast<int*>(lmv_smem + static_cast<size_t>(kLmvWarps) * a.n_dmax * a.n_ch) + warp * a.n_ch;
+  const int rs = kStride ? kStride : a.n_ch;
+  float2* rows = lmv_smem + static_cast<size_t>(warp) * a.n_dmax * rs;
+  int* act = reinterpret_cast<int*>(lmv_smem + static_cast<size_t>(kLmvWarps) * a.n_dmax * rs) + warp * a.n_ch;
 
   for (long row = static_cast<long>(blockIdx.x) * kLmvWarps + warp; row < a.n_rows;
        row += static_cast<long>(gridDim.x) * kLmvWarps) {
@@ -92,17 +99,17 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
     if (n_act >= 4) {
       for (int k = lane; k < n_d * n_act; k += 32) {
         const int d = k / n_act, q = k - d * n_act;
-        rows[d * a.n_ch + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[q]];
+        rows[d * rs + q] = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[q]];
       }
     } else {
-      for (int q = lane; q < n_act; q += 32) rows[dc * a.n_ch + q] = Y[static_cast<long>(pix) * a.n_ch + act[q]];
+      for (int q = lane; q < n_act; q += 32) rows[dc * rs + q] = Y[static_cast<long>(pix) * a.n_ch + act[q]];
     }
     __syncwarp();
 
     // Coherence factor terms over the active aperture of the centre row.
     float cre = 0.f, cim = 0.f, inc = 0.f;
     for (int q = lane; q < n_act; q += 32) {
-      const float2 v = rows[dc * a.n_ch + q];
+      const float2 v = rows[dc * rs + q];
       cre += v.x;
       cim += v.y;
       inc = fmaf(v.x, v.x, fmaf(v.y, v.y, inc));
@@ -139,17 +146,34 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
       const int lm1 = L - m - 1;
       // The trapezoid weight depends on t only: sum the range rows first.
       float are = 0.f, aim = 0.f;
-      for (int t = 0; t < n_act - m; ++t) {
-        const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
-        float sre = 0.f, sim = 0.f;
-#pragma unroll 5
-        for (int d = 0; d < n_d; ++d) {
-          const float2 p = rows[d * a.n_ch + t + m], q = rows[d * a.n_ch + t];
-          sre = fmaf(p.x, q.x, fmaf(p.y, q.y, sre));
-          sim = fmaf(p.y, q.x, fmaf(-p.x, q.y, sim));
+      const float2* pp = rows + m;
+      if (kND > 0 && n_d == kND) {
+        // The full window with a compile-time row stride: immediate offsets.
+        for (int t = 0; t < n_act - m; ++t) {
+          const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
+          float sre = 0.f, sim = 0.f;
+#pragma unroll
+          for (int d = 0; d < kND; ++d) {
+            const float2 pv = pp[d * rs + t], q = rows[d * rs + t];
+            sre = fmaf(pv.x, q.x, fmaf(pv.y, q.y, sre));
+            sim = fmaf(pv.y, q.x, fmaf(-pv.x, q.y, sim));
+          }
+          are = fmaf(w, sre, are);
+          aim = fmaf(w, sim, aim);
         }
-        are = fmaf(w, sre, are);
-        aim = fmaf(w, sim, aim);
+      } else {
+        for (int t = 0; t < n_act - m; ++t) {
+          const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
+          float sre = 0.f, sim = 0.f;
+#pragma unroll 5
+          for (int d = 0; d < n_d; ++d) {
+            const float2 pv = pp[d * rs + t], q = rows[d * rs + t];
+            sre = fmaf(pv.x, q.x, fmaf(pv.y, q.y, sre));
+            sim = fmaf(pv.y, q.x, fmaf(-pv.x, q.y, sim));
+          }
+          are = fmaf(w, sre, are);
+          aim = fmaf(w, sim, aim);
+        }
       }
       rre[s2] += are;
       rim[s2] += aim;
@@ -167,7 +191,7 @@ __global__ void __launch_bounds__(32 * kLmvWarps) lmv_features_kernel(const LmvA
       const int i = lane + 32 * s2;
       float xr = 0.f, xi = 0.f;
       if (i < L) {
-        const float2* yr = rows + dc * a.n_ch + i;
+        const float2* yr = rows + dc * rs + i;
         for (int s = 0; s < n_sub; ++s) {
           xr += yr[s].x;
           xi += yr[s].y;
@@ -918,7 +942,8 @@ __global__ void lmv_subspace_solve_kernel(const SubArgs a) {
 
 int lmv_features_smem(int n_ch, int range_avg) {
   const int n_dmax = 2 * range_avg + 1;
-  return static_cast<int>(sizeof(float2) * kLmvWarps * n_dmax * n_ch + sizeof(int) * kLmvWarps * n_ch);
+  const int rs = n_ch <= 128 ? 128 : n_ch;
+  return static_cast<int>(sizeof(float2) * kLmvWarps * n_dmax * rs + sizeof(int) * kLmvWarps * n_ch);
 }
 
 int launch_lmv_features(usx_ctx* ctx, const LmvLaunch& l) {
@@ -945,17 +970,21 @@ int launch_lmv_features(usx_ctx* ctx, const LmvLaunch& l) {
   a.out = l.out;
   a.out_stride = l.out_stride;
   const int smem = lmv_features_smem(l.n_ch, l.range_avg);
-  if (int rc_ = smem_limit(reinterpret_cast<const void*>(lmv_features_kernel), static_cast<size_t>(smem))) return rc_;
-  int per_sm = 0;
-  if (int rc_ = occupancy(reinterpret_cast<const void*>(lmv_features_kernel), 32 * kLmvWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
-  const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
-  const long need = (a.n_rows + kLmvWarps - 1) / kLmvWarps;
-  prof_begin(ctx, "lmv_features_kernel");
-  lmv_features_kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kLmvWarps, smem,
-                        ctx->stream>>>(a);
-  prof_end(ctx);
-  USX_CHECK_LAUNCH("lmv_features_kernel");
-  return USX_OK;
+  auto go = [&](auto kernel) -> int {
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(kernel), static_cast<size_t>(smem))) return rc_;
+    int per_sm = 0;
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(kernel), 32 * kLmvWarps, static_cast<size_t>(smem), &per_sm))
+      return rc_;
+    const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 8;
+    const long need = (a.n_rows + kLmvWarps - 1) / kLmvWarps;
+    prof_begin(ctx, "lmv_features_kernel");
+    kernel<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kLmvWarps, smem, ctx->stream>>>(a);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("lmv_features_kernel");
+    return USX_OK;
+  };
+  if (l.n_ch <= 128) return l.range_avg == 2 ? go(lmv_features_kernel<128, 5>) : go(lmv_features_kernel<128, 0>);
+  return go(lmv_features_kernel<0, 0>);
 }
 
 int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const float4* meta, float2* out,
