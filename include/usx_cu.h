@@ -151,7 +151,7 @@ int usx_cu_bf_plan_set_precision(usx_bf_plan* plan, int precision);
  * NULL; usx_cu_bf_variant_count() entries), leaves the frame of the chosen
  * variant in `frame` and synchronises. Variant 0 is the default. */
 int usx_cu_bf_variant_count(void);
-int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks);
+int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks, int* warp_lines);
 int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
 int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);
 int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, int repeats, float* ms_out);

@@ -251,20 +251,27 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
 //     overlapping windows of every trace and share them in L1.
 // The result differs from the reference's rounding by ~1e-7 relative L2.
 //
-// The group size G, the tile's line count TL (a CTA is TL warps) and the
-// register cap (MINB resident CTAs per SM) are template parameters; every
-// variant computes the same sums in the same order (bit-identical frames),
-// and the plan's autotuner picks the fastest for its geometry.
-template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false>
+// The group size G, the tile's line count TL (a CTA is TL warps), the
+// register cap (MINB resident CTAs per SM) and the warp's shape within the
+// tile (kWarpLines lines x 32 / kWarpLines depths: a warp spanning several
+// lines and fewer depths gathers from a narrower window of each trace, the
+// transmit-plus-receive delay changing less across lines than along depth)
+// are template parameters; every variant computes the same sums in the same
+// order (bit-identical frames), and the plan's autotuner picks the fastest
+// for its geometry.
+template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1>
 __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
+  static_assert(kTileLines % kWarpLines == 0 && 32 % kWarpLines == 0, "warp shape must tile the CTA");
   // kRtShared: the group's receive delays live in shared memory instead of
   // registers, so that a larger group fits the register cap.
   __shared__ float rt_s[kRtShared ? 32 * kTileLines * kFastGroup : 1];
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
   const int tile = blockIdx.x;
-  const int line = (tile / tiles_depth) * kTileLines + (threadIdx.x >> 5);
-  const int depth = (tile % tiles_depth) * 32 + (threadIdx.x & 31);
+  constexpr int kWarpDepths = 32 / kWarpLines;
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int line = (tile / tiles_depth) * kTileLines + (w / kWarpLines) * kWarpLines + ln / kWarpDepths;
+  const int depth = (tile % tiles_depth) * 32 + (w % kWarpLines) * kWarpDepths + ln % kWarpDepths;
   if (line >= n0 || depth >= a.n1) return;
   const int pix = line * a.n1 + depth;
   const long frame = blockIdx.y;
@@ -749,27 +756,30 @@ __global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
 }
 
 // The delay-and-sum variants the autotuner chooses from (index 0 is the
-// default): (channel group, tile lines, minimum resident CTAs per SM).
+// default): (channel group, tile lines, minimum resident CTAs per SM, lines
+// per warp).
 struct DasVariant {
-  int group, tile_lines, min_blocks;
+  int group, tile_lines, min_blocks, warp_lines;
   void (*iq)(BfArgs);
   void (*rf)(BfArgs);
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
-template <int G, int TL, int MB, bool RTS = false>
+template <int G, int TL, int MB, bool RTS = false, int WL = 1>
 constexpr DasVariant das_variant() {
-  return DasVariant{G, TL, MB, das_fast_kernel<true, G, TL, MB, RTS>, das_fast_kernel<false, 16, 4, 1>, false};
+  return DasVariant{G, TL, MB, WL, das_fast_kernel<true, G, TL, MB, RTS, WL>, das_fast_kernel<false, 16, 4, 1>, false};
 }
 template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
-  return DasVariant{G, TL, 0, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
+  return DasVariant{G, TL, 0, 1, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
 }
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
     das_variant<8, 8, 4>(),  das_variant<16, 2, 8>(), das_variant<4, 4, 12>(), das_variant<8, 2, 16>(),
     das_variant<16, 4, 8, true>(), das_variant<16, 2, 16, true>(), das_staged_variant<8, 4, 1>(),
+    das_variant<8, 4, 8, false, 4>(), das_variant<4, 4, 12, false, 4>(), das_variant<4, 4, 12, false, 2>(),
+    das_variant<8, 2, 16, false, 2>(), das_variant<8, 8, 4, false, 4>(), das_variant<8, 8, 4, false, 8>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -1460,11 +1470,12 @@ int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode) {
 
 int usx_cu_bf_variant_count(void) { return kNumDasVariants; }
 
-int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks) {
+int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks, int* warp_lines) {
   if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_info: no such variant");
   if (channel_group) *channel_group = kDasVariants[index].group;
   if (tile_lines) *tile_lines = kDasVariants[index].tile_lines;
   if (min_blocks) *min_blocks = kDasVariants[index].min_blocks;
+  if (warp_lines) *warp_lines = kDasVariants[index].warp_lines;
   return USX_OK;
 }
 
