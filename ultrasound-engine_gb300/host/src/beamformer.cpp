@@ -102,13 +102,16 @@ LearnedNet learned_net(usx_ctx* ctx) {
 
 }  // namespace
 
-// The key of a plan is everything that is frozen into it.
+// The key of a plan is everything that is frozen into it. The grid's points
+// (6 MB for 512 x 1024 pixels) are compared in place, not copied, on every
+// lookup; only a new plan keeps a copy.
 struct PlanKey {
   usx_ctx* ctx = nullptr;
   std::vector<unsigned char> meta;   // POD bytes of probe/medium/acq/config/tx geometry
   std::vector<real> points;
-  bool operator==(const PlanKey& o) const {
-    return ctx == o.ctx && meta == o.meta && points == o.points;
+  bool matches(usx_ctx* c, const std::vector<unsigned char>& m, const real* pts, std::size_t n) const {
+    return ctx == c && meta == m && points.size() == n &&
+           (n == 0 || std::memcmp(points.data(), pts, n * sizeof(real)) == 0);
   }
 };
 
@@ -155,15 +158,17 @@ class PlanCache {
       put(&na, sizeof na);
       if (na) put(t.apodization.data(), sizeof(real) * t.apodization.size());
     }
-    key.points.assign(desc::points(grid), desc::points(grid) + 3 * grid.points.size());
+    const real* pts = desc::points(grid);
+    const std::size_t n_pts = 3 * grid.points.size();
 
     std::lock_guard<std::mutex> lock(mu_);
     for (auto it = entries_.begin(); it != entries_.end(); ++it) {
-      if (it->first == key) {
+      if (it->first.matches(key.ctx, key.meta, pts, n_pts)) {
         entries_.splice(entries_.begin(), entries_, it);
         return entries_.front().second;
       }
     }
+    key.points.assign(pts, pts + n_pts);
     desc::Channel ch(data);
     const usx_grid_desc g = desc::grid(grid);
     usx_bf_plan* plan = nullptr;
