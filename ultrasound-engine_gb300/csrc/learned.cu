@@ -25,6 +25,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "usx_internal.cuh"
 
@@ -366,8 +367,8 @@ __host__ __device__ constexpr int lmv_rec_floats(int nb) {
 
 // The beams' prefix sums are stored skewed, t at t + t / 16: conflict-free
 // both for the runs of four the scan writes (t = 4 lane + c) and for the
-// consecutive t the snapshot passes read. Two range rows (linear, zero past
-// n_act): the next one streams in (cp.async) while the current one is used.
+// consecutive t the snapshot passes read. Three range rows (linear, zero past
+// n_act): the next two stream in (cp.async) while the current one is used.
 constexpr int kSubPre = kSubMaxN + 1 + kSubMaxN / 16;
 constexpr int kSubRing = 32;   // snapshot projections left over from full passes
 
@@ -379,7 +380,7 @@ struct SubWarpSmem {
   float2 tw1[kSubMaxN];                     // e^{-j 2 pi t / L}; beam b's twiddle is its b-th power
   float4 qq[kLmvMaxL];                      // the network's direction q, orthogonalised: (q.x, q.x, q.y, q.y), 0 past L
   float2 ring[NB + 1][kSubRing];            // z vectors of snapshots past each row's full passes
-  float2 rows[2][kSubMaxN];
+  float2 rows[3][kSubMaxN];
 };
 
 // e^{-j 2 pi b t / L} for b = 0, 1, -1, 2, -2, 3, -3 (k = 0..6) from
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
     while (j + dhi >= a.n1) --dhi;
     const int n_d = dhi - dlo + 1;
     auto issue_row = [&](int d) {
-      float2* dst = sm.rows[d & 1];
+      float2* dst = sm.rows[d % 3];
       const float2* src = Y + static_cast<long>(pix + dlo + d) * a.n_ch + first;
 #pragma unroll
       for (int c = 0; c < kSubMaxN / 32; ++c) {
@@ -484,6 +485,7 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       asm volatile("cp.async.commit_group;\n" ::: "memory");
     };
     issue_row(0);
+    if (n_d > 1) issue_row(1);
     const float4 av4 = reinterpret_cast<const float4*>(a.avg + row * kLmvMaxL)[lane];
 
     // The network's weights (lane holds i = 2 lane, 2 lane + 1) and the gate.
@@ -585,14 +587,17 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
     float tr = 0.f;
     int ring_n = 0;
     for (int d = 0; d < n_d; ++d) {
-      if (d + 1 < n_d) {
-        issue_row(d + 1);
+      // Row d + 2 starts streaming; row d is the oldest copy in flight.
+      if (d + 2 < n_d) {
+        issue_row(d + 2);
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+      } else if (d + 1 < n_d) {
         asm volatile("cp.async.wait_group 1;\n" ::: "memory");
       } else {
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       }
       __syncwarp();
-      const float2* yr = sm.rows[d & 1];
+      const float2* yr = sm.rows[d % 3];
 
       // Trace of the covariance (times K): every sample weighted by the
       // number of subarrays that contain it.
@@ -603,20 +608,22 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       }
 
       // The beams' prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y[t']: lane
-      // l sums its run t = 4 l .. 4 l + 3 (the row is zero past n_act), then a
-      // warp scan of the run totals, beam by beam.
-      {
-        float2 yv[4], t1v[4];
+      // l sums its run of C samples t = C l .. C l + C - 1 (C = 2 when the
+      // aperture fits 64 channels, else 4; the row is zero past n_act), then
+      // a warp scan of the run totals, beam by beam.
+      auto scan_row = [&](auto run_len) {
+        constexpr int C = decltype(run_len)::value;
+        float2 yv[C], t1v[C];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          yv[c] = yr[4 * lane + c];
-          t1v[c] = sm.tw1[4 * lane + c];
+        for (int c = 0; c < C; ++c) {
+          yv[c] = yr[C * lane + c];
+          t1v[c] = sm.tw1[C * lane + c];
         }
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
-          float2 run = make_float2(0.f, 0.f), loc[4];
+          float2 run = make_float2(0.f, 0.f), loc[C];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
+          for (int c = 0; c < C; ++c) {
             const float2 tw = beam_twiddle(t1v[c], k);
             run.x = fmaf(tw.x, yv[c].x, fmaf(-tw.y, yv[c].y, run.x));
             run.y = fmaf(tw.x, yv[c].y, fmaf(tw.y, yv[c].x, run.y));
@@ -632,12 +639,16 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
           }
           const float2 ex = make_float2(inc.x - run.x, inc.y - run.y);
 #pragma unroll
-          for (int c = 0; c < 4; ++c) sm.pre[k][skw(4 * lane + c + 1)] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
+          for (int c = 0; c < C; ++c) sm.pre[k][skw(C * lane + c + 1)] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
         }
-        if (lane == 0)
+      };
+      if (n_act <= 64)
+        scan_row(std::integral_constant<int, 2>{});
+      else
+        scan_row(std::integral_constant<int, 4>{});
+      if (lane == 0)
 #pragma unroll
-          for (int k = 0; k < NB; ++k) sm.pre[k][0] = make_float2(0.f, 0.f);
-      }
+        for (int k = 0; k < NB; ++k) sm.pre[k][0] = make_float2(0.f, 0.f);
       __syncwarp();
 
       // Beam projections of snapshot s without their 1 / sqrt(L) (applied to
