@@ -226,7 +226,11 @@ def run_reference(args) -> None:
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": "mv_l64_75pw_512x1024", "combiner": "mv"},
+            "data": "synthetic",
+            "config": {"workload": f"{args.workload}_75pw_512x1024", "beamformer": dict(WORKLOADS.get(args.workload, {})),
+                       "n_tx": N_TX, "n_ch": N_EL, "grid": [N0, N1],
+                       "reference_path": "the reference has no learned combiner: its minimum variance "
+                                         "(combine_mv_windowed, beamformer.cpp:137-214) on the same frame"},
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": kind,
                              "sample": f"{lines} of {N0} lateral lines per step, scaled to a frame"},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
