@@ -227,8 +227,8 @@ def run_reference(args) -> None:
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"{args.workload}_75pw_512x1024", "beamformer": dict(WORKLOADS.get(args.workload, {})),
-                       "n_tx": N_TX, "n_ch": N_EL, "grid": [N0, N1],
+            "config": {"workload": f"{args.workload}_75pw_512x1024",
+                       "beamformer": dict(WORKLOADS.get(args.workload, {})), "n_tx": N_TX, "n_ch": N_EL, "grid": [N0, N1],
                        "reference_path": "the reference has no learned combiner: its minimum variance "
                                          "(combine_mv_windowed, beamformer.cpp:137-214) on the same frame"},
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": kind,
