@@ -269,6 +269,37 @@ def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_k
     plan.close()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg_kw", [dict(f_number=1.5), dict(f_number=1.5, combiner=1, coherence_factor=1)])
+def test_das_variants_ragged_grid(capi, ctx, torch, golden, cfg_kw):
+    """A grid whose lines and depths do not fill the CTA tiles (13 x 37, tiles
+    of 2-8 lines x 32 depths, warps of 1-8 lines): every launch shape gives
+    the same frame, bit for bit the same pixels of the full grid."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    ax0, ax1 = np.asarray(g["ax0"]), np.asarray(g["ax1"])
+    pts = np.asarray(g["pts"], dtype=np.float32).reshape(len(ax0), len(ax1), 3)
+    full = capi.Grid(0, ax0, ax1, pts.reshape(-1, 3))
+    sub = capi.Grid(0, ax0[:13], ax1[:37], pts[:13, :37].reshape(-1, 3))
+    cfg = capi.bf_config(**cfg_kw)
+    d = dev(torch, g["iq"])
+    plan_full = ctx.plan(ch, full, cfg)
+    out_full = torch.empty(full.shape, dtype=torch.complex64, device="cuda")
+    plan_full.execute(d.data_ptr(), out_full.data_ptr())
+    want = host(torch, out_full)[:13, :37]
+    plan_full.close()
+    plan = ctx.plan(ch, sub, cfg)
+    out = torch.empty(sub.shape, dtype=torch.complex64, device="cuda")
+    for v in range(len(capi.das_variants())):
+        plan.set_variant(v)
+        out.fill_(float("nan"))
+        plan.execute(d.data_ptr(), out.data_ptr())
+        assert np.array_equal(host(torch, out), want), f"variant {v}"
+    plan.close()
+
+
 def test_batch_and_sequence_equal_single_frames(capi, ctx, torch, golden):
     g = golden("bf")
     s = golden("sim")
