@@ -506,7 +506,9 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       continue;
     }
     // Twiddles e^{-j 2 pi t / L}, t < 128, argument reduced to one turn.
-    for (int t = lane; t < kSubMaxN; t += 32) {
+    // (Read up to t < 64 when the aperture fits 64 channels, else t < 128.)
+    const int n_tw = n_act <= 64 ? 64 : kSubMaxN;
+    for (int t = lane; t < n_tw; t += 32) {
       float sn, cs;
       sincospif(2.0f * static_cast<float>(t % L) * inv_l, &sn, &cs);
       sm.tw1[t] = make_float2(cs, -sn);
@@ -581,7 +583,8 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
 #pragma unroll
         for (int c = r; c < K1; ++c, e += 2) {
           g[e] = fmaf(z[r].x, z[c].x, fmaf(z[r].y, z[c].y, g[e]));      // z_r conj(z_c)
-          g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
+          if (r != c)  // the diagonal is real
+            g[e + 1] = fmaf(z[r].y, z[c].x, fmaf(-z[r].x, z[c].y, g[e + 1]));
         }
     };
     float tr = 0.f;
