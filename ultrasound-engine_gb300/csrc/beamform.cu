@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
   float best_w = 0.0f;
   if (select) {
     for (int ev = ev_first; ev < ev_last; ++ev) {
-      const float tw = tx_sensitivity(a.tx[ev], px, pz, a.lambda, a.pitch);
+      const float tw = tx_sensitivity_fast(a.tx[ev], px, pz, a.lambda);
       if (tw > best_w) {
         best_w = tw;
         best_ev = ev;
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
           if (select) {
             tw = (best_ev == ev && best_w > 0.0f) ? 1.0f : 0.0f;
           } else if (a.tx_weighting) {
-            tw = tx_sensitivity(t, px, pz, a.lambda, a.pitch);
+            tw = tx_sensitivity_fast(t, px, pz, a.lambda);
           } else {
             tw = 1.0f;
           }
@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
   float best_w = 0.0f;
   if (select && live) {
     for (int ev = ev_first; ev < ev_last; ++ev) {
-      const float tw = tx_sensitivity(a.tx[ev], px, pz, a.lambda, a.pitch);
+      const float tw = tx_sensitivity_fast(a.tx[ev], px, pz, a.lambda);
       if (tw > best_w) {
         best_w = tw;
         best_ev = ev;
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
         if (select) {
           tw = (best_ev == ev && best_w > 0.0f) ? 1.0f : 0.0f;
         } else if (a.tx_weighting) {
-          tw = tx_sensitivity(t, px, pz, a.lambda, a.pitch);
+          tw = tx_sensitivity_fast(t, px, pz, a.lambda);
         } else {
           tw = 1.0f;
         }

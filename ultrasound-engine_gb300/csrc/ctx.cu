@@ -1,6 +1,7 @@
 // ctx.cu — context, memory and error plumbing of the C-ABI, plus the host-side
 // helpers (transmit tables, pulse, low-pass design) whose float arithmetic must
 // match the reference exactly and therefore runs on the host's libm.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -88,6 +89,12 @@ TxDev make_txdev(const usx_probe& probe, const usx_transmit& tx) {
   // Diverging: |O - focus| (geometry.cpp:104-106).
   const float ox = t.ox - t.fx, oy = 0.0f - t.fy, oz = 0.0f - t.fz;
   t.d_origin_focus = std::sqrt(ox * ox + oy * oy + oz * oz);
+  // Reciprocal and slopes for tx_sensitivity_fast.
+  t.inv_aperture = 1.0f / std::max(t.x_hi - t.x_lo, probe.pitch);
+  if (std::fabs(t.fz) >= 1e-9f) {
+    t.slope_lo = (t.fx - t.x_lo) / t.fz;
+    t.slope_hi = (t.fx - t.x_hi) / t.fz;
+  }
   return t;
 }
 

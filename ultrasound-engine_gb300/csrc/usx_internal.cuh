@@ -170,6 +170,9 @@ struct TxDev {
   float x_lo, x_hi; // firing aperture extent (beamformer.cpp:238-247)
   float axis_len, dx, dy, dz;  // focused: unit axis from origin to focus
   float d_origin_focus;        // diverging: |O - focus|
+  // For the fast paths' illumination weight: 1 / max(x_hi - x_lo, pitch) and
+  // the focused/diverging band's edge slopes (fx - x_lo) / fz, (fx - x_hi) / fz.
+  float inv_aperture, slope_lo, slope_hi;
 };
 
 // Ideal transmit arrival time at a point (reference geometry.cpp:82-109).
@@ -212,6 +215,41 @@ __device__ __forceinline__ float tx_sensitivity(const TxDev& t, float px, float 
   const float half = 0.5f * (b - a);
   if (half <= 0.0f) return 0.0f;
   return window_value(USX_WIN_TUKEY, (px - centre) / half, 0.4f);
+}
+
+// tx_sensitivity with the per-transmit divisions replaced by products with
+// host-computed reciprocals, the per-pixel one by __fdividef and the Tukey
+// taper's cosine by __cosf: the weight moves by ~1e-6 relative, the delay
+// indices and phases (which do not use it) not at all. The fast
+// delay-and-sum kernels (every launch shape) use it; the exact-order kernel
+// keeps tx_sensitivity.
+__device__ __forceinline__ float tx_sensitivity_fast(const TxDev& t, float px, float pz, float lambda) {
+  if (!t.valid || pz <= 0.0f) return 0.0f;
+  float a, b;
+  if (t.type == USX_TX_PLANE_WAVE) {
+    const float shift = pz * t.tan_a;
+    a = t.x_lo + shift;
+    b = t.x_hi + shift;
+  } else {
+    if (fabsf(t.fz) < 1e-9f) return 1.0f;
+    a = t.x_lo + pz * t.slope_lo;
+    b = t.x_hi + pz * t.slope_hi;
+    if (a > b) { const float s = a; a = b; b = s; }
+  }
+  const float f_num_eff = fclamp(pz * t.inv_aperture, 0.5f, 20.0f);
+  const float diffraction = f_num_eff * lambda;
+  a -= diffraction;
+  b += diffraction;
+  const float centre = 0.5f * (a + b);
+  const float half = 0.5f * (b - a);
+  if (half <= 0.0f) return 0.0f;
+  const float u = __fdividef(px - centre, half);
+  if (u < -1.0f || u > 1.0f) return 0.0f;
+  const float tt = 0.5f * (u + 1.0f);   // Tukey, alpha 0.4
+  constexpr float kA = 0.4f, kW = 2.0f * kPi / kA;
+  if (tt < 0.5f * kA) return 0.5f * (1.0f + __cosf(kW * (tt - 0.5f * kA)));
+  if (tt > 1.0f - 0.5f * kA) return 0.5f * (1.0f + __cosf(kW * (tt - 1.0f + 0.5f * kA)));
+  return 1.0f;
 }
 
 // ChannelData::validate (reference types.cpp:8-124) on the metadata half.
