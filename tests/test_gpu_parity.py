@@ -407,6 +407,47 @@ def test_postprocess_matches_reference(capi, ctx, torch, golden):
     assert rel_l2(host(torch, px), g["sc_cart"]) < TOL
 
 
+def test_scan_convert_tiles_and_extent_match_oracle(capi, ctx, torch, oracle):
+    """Rasters of several 32 x 32 tiles with ragged edges (75 x 131, 33 x 64,
+    1 x 1), a Cartesian grid (bit-exact: no transcendental on that path) and a
+    sector grid (atan2f, 1e-5); and the extent scan's tie rule: with +0.0 and
+    -0.0 both minimal depths, the first in point order is returned, as by one
+    sequential std::min pass."""
+    rng = np.random.default_rng(11)
+    n0, n1 = 97, 161  # 15617 points: the extent scan's quarters leave a tail
+    ax0 = np.linspace(-0.019, 0.019, n0, dtype=np.float32)
+    ax1 = np.linspace(0.0, 0.045, n1, dtype=np.float32)
+    pts = np.zeros((n0 * n1, 3), np.float32)
+    pts[:, 0] = np.repeat(ax0, n1)
+    pts[:, 2] = np.tile(ax1, n0)
+    img = rng.random((n0, n1), dtype=np.float32)
+    d_img = dev(torch, img)
+    for first_sign in (1.0, -1.0):
+        p = pts.copy()
+        p[::n1, 2] = 0.0
+        p[0, 2] = first_sign * 0.0
+        p[(n0 - 3) * n1, 2] = -first_sign * 0.0
+        cgrid = capi.Grid(0, ax0, ax1, p)
+        for w, h in ((75, 131), (33, 64), (1, 1)):
+            px = torch.empty((h, w), dtype=torch.float32, device="cuda")
+            ext = ctx.scan_convert(d_img.data_ptr(), cgrid, w, h, -2.0, px.data_ptr())
+            want, want_ext = oracle.scan_convert(img, 0, ax0, ax1, (0, 0, 0), p, w, h, -2.0)
+            assert np.array_equal(host(torch, px), want), (w, h)
+            assert np.array_equal(ext, want_ext)
+            assert np.signbit(ext[2]) == (first_sign < 0)
+    th = np.linspace(-0.6, 0.6, n0, dtype=np.float32)
+    r = np.linspace(0.01, 0.08, n1, dtype=np.float32)
+    sp = np.zeros((n0 * n1, 3), np.float32)
+    sp[:, 0] = (np.sin(th)[:, None] * r[None, :]).ravel()
+    sp[:, 2] = (np.cos(th)[:, None] * r[None, :]).ravel()
+    sgrid = capi.Grid(1, th, r, sp)
+    px = torch.empty((131, 75), dtype=torch.float32, device="cuda")
+    ext = ctx.scan_convert(d_img.data_ptr(), sgrid, 75, 131, -1.0, px.data_ptr())
+    want, want_ext = oracle.scan_convert(img, 1, th, r, (0, 0, 0), sp, 75, 131, -1.0)
+    assert np.array_equal(ext, want_ext)
+    assert rel_l2(host(torch, px), want) < TOL
+
+
 # ---------------------------------------------------------- Doppler / strain
 
 @pytest.mark.parametrize("key,wt,order", [("w0o1", 0, 1), ("w1o1", 1, 1), ("w1o2", 1, 2), ("w2o0", 2, 0)])

@@ -92,14 +92,23 @@ __global__ void tgc_kernel(const float* env, const float* points, float atten, f
   out[i] = env[i] * powf(10.0f, gain_db / 20.0f);
 }
 
-__global__ void max_kernel(const float* x, long n, unsigned* out_bits) {
+// Launched with 256 threads. The block reduces in shared memory and issues one
+// atomic: one atomic per warp onto a single word serialises thousands of them.
+__global__ void __launch_bounds__(256) max_kernel(const float* x, long n, unsigned* out_bits) {
+  __shared__ float warp_max[8];
   float m = 0.0f;
   for (long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long>(gridDim.x) * blockDim.x)
     m = fmaxf(m, x[i]);
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  // Non-negative floats order like their bit patterns.
-  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(out_bits, __float_as_uint(m));
+  if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < 8 ? warp_max[threadIdx.x] : 0.0f;
+    for (int o = 4; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    // Non-negative floats order like their bit patterns.
+    if (threadIdx.x == 0 && m > 0.0f) atomicMax(out_bits, __float_as_uint(m));
+  }
 }
 
 __global__ void log_compress_kernel(const float* env, long n, float dr_db, float gain_db,
@@ -127,10 +136,9 @@ struct ScanArgs {
   float fill;
 };
 
-__global__ void scan_convert_kernel(const ScanArgs s) {
-  const long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
-  if (i >= static_cast<long>(s.width) * s.height) return;
-  const int py = static_cast<int>(i / s.width), px = static_cast<int>(i - static_cast<long>(py) * s.width);
+// One output pixel of the backward mapping (postprocess.cpp:139-176):
+// `fill` outside the grid, else the bilinear interpolation of the image.
+__device__ __forceinline__ float scan_pixel(const ScanArgs& s, int px, int py) {
   float val = s.fill;
   const float z = s.z_min + (s.z_max - s.z_min) *
                                 (s.height == 1 ? 0.0f : static_cast<float>(py) / static_cast<float>(s.height - 1));
@@ -163,13 +171,57 @@ __global__ void scan_convert_kernel(const ScanArgs s) {
       val = (a * (1.0f - fu) + b * fu) * (1.0f - fv) + (cc * (1.0f - fu) + d * fu) * fv;
     }
   }
-  s.pixels[i] = val;
+  return val;
+}
+
+// A 32 x 32 tile of the raster per 256-thread block. The image is stored
+// lateral-major (axis 1, depth, contiguous) while the raster is row-major in
+// depth, so the lanes of a warp first walk depth (py) at one px, which makes
+// the four bilinear taps contiguous reads along the image's rows; the tile is
+// then transposed through shared memory so that each warp writes 32
+// consecutive raster pixels.
+constexpr int kScanTile = 32;
+__global__ void __launch_bounds__(256) scan_convert_kernel(const ScanArgs s) {
+  __shared__ float tile[kScanTile][kScanTile + 1];
+  const int lane = threadIdx.x & 31, row = threadIdx.x >> 5;
+  const int px0 = blockIdx.x * kScanTile, py0 = blockIdx.y * kScanTile;
+#pragma unroll
+  for (int k = 0; k < kScanTile / 8; ++k) {
+    const int lx = row + 8 * k, px = px0 + lx, py = py0 + lane;
+    if (px < s.width && py < s.height) tile[lx][lane] = scan_pixel(s, px, py);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanTile / 8; ++k) {
+    const int ly = row + 8 * k, px = px0 + lane, py = py0 + ly;
+    if (px < s.width && py < s.height) s.pixels[static_cast<long>(py) * s.width + px] = tile[lane][ly];
+  }
 }
 
 }  // namespace
 }  // namespace usxcu
 
 using namespace usxcu;
+
+namespace {
+// Running extent of (x, z) over sample points [x, y, z].
+struct Extent {
+  float x_min = std::numeric_limits<float>::max(), x_max = -std::numeric_limits<float>::max();
+  float z_min = std::numeric_limits<float>::max(), z_max = -std::numeric_limits<float>::max();
+  void add(const float* p) {
+    x_min = std::min(x_min, p[0]);
+    x_max = std::max(x_max, p[0]);
+    z_min = std::min(z_min, p[2]);
+    z_max = std::max(z_max, p[2]);
+  }
+  void merge(const Extent& o) {
+    x_min = std::min(x_min, o.x_min);
+    x_max = std::max(x_max, o.x_max);
+    z_min = std::min(z_min, o.z_min);
+    z_max = std::max(z_max, o.z_max);
+  }
+};
+}  // namespace
 
 extern "C" {
 
@@ -178,8 +230,10 @@ int usx_cu_envelope(usx_ctx* ctx, const float* frame, int n0, int n1, float fdem
   if (n0 <= 0 || n1 <= 0) return fail(USX_ERR_INVALID, "usx_cu_envelope: empty frame");
   const long n = static_cast<long>(n0) * n1;
   if (fdem > 0.0f) {
+    prof_begin(ctx, "envelope_iq_kernel");
     envelope_iq_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(
         reinterpret_cast<const float2*>(frame), env, n);
+    prof_end(ctx);
     USX_CHECK_LAUNCH("envelope_iq_kernel");
     return USX_OK;
   }
@@ -191,8 +245,10 @@ int usx_cu_envelope(usx_ctx* ctx, const float* frame, int n0, int n1, float fdem
   if (n_fft > 16384) return fail(USX_ERR_UNSUPPORTED, "usx_cu_envelope: lines longer than 16384");
   if (n_fft < 2) {
     // A one-sample line: the reference's FFT is the identity.
+    prof_begin(ctx, "envelope_iq_kernel");
     envelope_iq_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(
         reinterpret_cast<const float2*>(frame), env, n);
+    prof_end(ctx);
     USX_CHECK_LAUNCH("envelope_iq_kernel");
     return USX_OK;
   }
@@ -219,8 +275,10 @@ int usx_cu_envelope(usx_ctx* ctx, const float* frame, int n0, int n1, float fdem
   const size_t smem = sizeof(float2) * n_fft;
   if (smem > 48 * 1024)
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(hilbert_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
+  prof_begin(ctx, "hilbert_kernel");
   hilbert_kernel<<<n0, 256, smem, ctx->stream>>>(reinterpret_cast<const float2*>(frame), n1, n_fft,
                                                  log2n, static_cast<const float2*>(ws), env);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("hilbert_kernel");
   // The host table must outlive the asynchronous copy.
   USX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -232,8 +290,10 @@ int usx_cu_apply_tgc(usx_ctx* ctx, const float* env, int n0, int n1, const float
   if (!ctx || !env || !points || !out) return fail(USX_ERR_INVALID, "usx_cu_apply_tgc: null argument");
   const long n = static_cast<long>(n0) * n1;
   if (n <= 0) return USX_OK;
+  prof_begin(ctx, "tgc_kernel");
   tgc_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(env, points, attenuation_db_cm_mhz,
                                                         center_frequency_hz * 1e-6f, n, out);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("tgc_kernel");
   return USX_OK;
 }
@@ -246,11 +306,15 @@ int usx_cu_log_compress(usx_ctx* ctx, const float* env, int64_t n, float dynamic
   if (reference <= 0.0f) {
     USX_CUDA(cudaMemsetAsync(ref_bits, 0, sizeof(unsigned), ctx->stream));
     const int blocks = std::max(1, std::min(ceil_div(n, 256), ctx->sm_count * 8));
+    prof_begin(ctx, "max_kernel");
     max_kernel<<<blocks, 256, 0, ctx->stream>>>(env, n, ref_bits);
+    prof_end(ctx);
     USX_CHECK_LAUNCH("max_kernel");
   }
+  prof_begin(ctx, "log_compress_kernel");
   log_compress_kernel<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(env, n, dynamic_range_db, gain_db,
                                                                  reference, ref_bits, out);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("log_compress_kernel");
   return USX_OK;
 }
@@ -283,14 +347,26 @@ int usx_cu_scan_convert(usx_ctx* ctx, const float* image, const usx_grid_desc* g
   if (n0 <= 0 || n1 <= 0 || !grid->axis0 || !grid->axis1)
     return fail(USX_ERR_INVALID, "usx_cu_scan_convert: invalid grid");
   ScanArgs s;
-  float x_min = std::numeric_limits<float>::max(), x_max = -x_min, z_min = x_min, z_max = -x_min;
+  // The extent of the sample points (postprocess.cpp:126-132). The points are
+  // scanned as four contiguous quarters side by side (independent dependency
+  // chains; the tail joins the last quarter), then the quarters' extents are
+  // combined in order: with std::min/max keeping the earlier of equal values,
+  // that returns the same value (down to the sign of a zero) as one
+  // sequential pass.
   const long n = static_cast<long>(n0) * n1;
-  for (long k = 0; k < n; ++k) {
-    x_min = std::min(x_min, points_host[3 * k]);
-    x_max = std::max(x_max, points_host[3 * k]);
-    z_min = std::min(z_min, points_host[3 * k + 2]);
-    z_max = std::max(z_max, points_host[3 * k + 2]);
+  const long q = n / 4;
+  Extent e0, e1, e2, e3;
+  for (long k = 0; k < q; ++k) {
+    e0.add(points_host + 3 * k);
+    e1.add(points_host + 3 * (q + k));
+    e2.add(points_host + 3 * (2 * q + k));
+    e3.add(points_host + 3 * (3 * q + k));
   }
+  for (long k = 4 * q; k < n; ++k) e3.add(points_host + 3 * k);
+  e0.merge(e1);
+  e0.merge(e2);
+  e0.merge(e3);
+  const float x_min = e0.x_min, x_max = e0.x_max, z_min = e0.z_min, z_max = e0.z_max;
   s.image = image;
   s.pixels = pixels;
   s.n0 = n0;
@@ -315,8 +391,10 @@ int usx_cu_scan_convert(usx_ctx* ctx, const float* image, const usx_grid_desc* g
     extent[2] = z_min;
     extent[3] = z_max;
   }
-  const long m = static_cast<long>(width) * height;
-  scan_convert_kernel<<<ceil_div(m, 256), 256, 0, ctx->stream>>>(s);
+  const dim3 tiles(ceil_div(width, kScanTile), ceil_div(height, kScanTile));
+  prof_begin(ctx, "scan_convert_kernel");
+  scan_convert_kernel<<<tiles, 256, 0, ctx->stream>>>(s);
+  prof_end(ctx);
   USX_CHECK_LAUNCH("scan_convert_kernel");
   return USX_OK;
 }
