@@ -67,7 +67,7 @@ from ._usx import (  # noqa: F401
     __backend__,
 )
 
-from . import metrics, phantoms, presets  # noqa: E402,F401
+from . import ingest, metrics, phantoms, presets  # noqa: E402,F401
 
 __all__ = [n for n in dir() if not n.startswith("_")] + [
     "angles_deg", "to_bmode", "grid_for", "extent_mm",
