@@ -262,3 +262,26 @@ def test_device_feed_into_a_device_plan_matches_the_host_path(setup):
         assert np.linalg.norm(got - w) <= 1e-5 * np.linalg.norm(w)
     plan.close()
     ctx.close()
+
+
+def test_device_feed_rejects_a_frame_of_another_shape(setup):
+    """A feed carries frames of one shape: a source that changes shape mid-way
+    raises ValueError at that frame, after delivering the frames before it."""
+    import torch
+    probe, medium, acq, sim, _ = setup
+    txs = sim.make_plane_waves([0.0])
+    a = np.ones((1, probe.n_elements, acq.n_samples), np.float32)
+
+    class Ragged(ingest.ArraySource):
+        def frames(self):
+            yield from super().frames()
+            yield usx.ChannelData.from_rf(np.ones((2, probe.n_elements, acq.n_samples), np.float32), probe,
+                                          medium, acq, list(txs) * 2)
+
+    feed = ingest.DeviceFeed(Ragged([a, a], probe, medium, acq, txs), depth=1)
+    got = []
+    with pytest.raises(ValueError, match="shape"):
+        for fr in feed:
+            got.append(float(fr.rf.sum()))
+    torch.cuda.synchronize()
+    assert got == [float(a.sum())] * 2

@@ -555,3 +555,29 @@ def test_full_size_das_is_linear_and_matches_oracle_on_lines(capi, ctx, torch, o
     got = host(torch, fx)[lines]
     assert rel_l2(got, want) < TOL
     plan.close()
+
+
+def test_postprocess_empty_and_invalid_sizes(capi, ctx, torch):
+    """Empty element counts are no-ops where the reference's loops simply do
+    not run (TGC, log compression, maximum); an empty frame or raster, or a
+    grid without samples, is an invalid argument (ValueError), and nothing
+    is written."""
+    buf = torch.full((64,), 3.0, device="cuda")
+    out = torch.full((64,), 7.0, device="cuda")
+    pts = torch.zeros((64, 3), device="cuda")
+    ctx.apply_tgc(buf.data_ptr(), 0, 64, pts.data_ptr(), 0.5, 5e6, out.data_ptr())
+    ctx.log_compress(buf.data_ptr(), 0, 60.0, 0.0, 0.0, out.data_ptr())
+    assert bool((out == 7.0).all())
+    with pytest.raises(ValueError):
+        ctx.envelope(buf.data_ptr(), 0, 8, 5e6, out.data_ptr())
+    ax = np.linspace(0.0, 0.01, 8, dtype=np.float32)
+    p = np.zeros((64, 3), np.float32)
+    p[:, 0] = np.repeat(ax, 8)
+    p[:, 2] = np.tile(ax, 8)
+    grid = capi.Grid(0, ax, ax, p)
+    with pytest.raises(ValueError):
+        ctx.scan_convert(buf.data_ptr(), grid, 0, 10, 0.0, out.data_ptr())
+    with pytest.raises(ValueError):
+        ctx.scan_convert(buf.data_ptr(), grid, 10, 0, 0.0, out.data_ptr())
+    torch.cuda.synchronize()
+    assert bool((out == 7.0).all())
