@@ -297,6 +297,10 @@ class DeviceFeed:
         with self._torch.cuda.stream(self._copy):
             self._dev[slot].copy_(self._host[slot], non_blocking=True)
             self._copied[slot].record(self._copy)
+        # The slot was allocated on another stream: tell the caching allocator
+        # that the copy stream writes it, so that it is not handed out again
+        # while a copy is in flight if the feed is dropped early.
+        self._dev[slot].record_stream(self._copy)
 
     def __iter__(self):
         frames = iter(self._source.frames())
