@@ -766,6 +766,184 @@ def run_strain(args) -> None:
     ctx.close()
 
 
+BATCH_BEAMFORMERS = {
+    "das": dict(f_number=1.5),
+    "cf": dict(f_number=1.5, coherence_factor=1),
+    "dmas": dict(f_number=1.5, combiner=1),
+    "mv": MV_KW,
+}
+
+
+def cpu_leg_batch(iq0: np.ndarray, pts: np.ndarray, txs, probe, acq, gpu_lines: dict, line_idx, threads: int):
+    """CPU side of the batched workload: the reference's CPU beamformers (its
+    own build when present, else the oracle's port) timed on a sample of
+    lateral lines and scaled to a frame, and the FP64 oracle on `line_idx` as
+    the checker of each GPU beamformer's frame 0 (relative L2)."""
+    from oracle import oracle as O
+    pr = O.probe(N_EL, probe.pitch, probe.element_width, 5e-3, F0, probe.bandwidth)
+    oacq = O.acquisition(fs=acq.sampling_frequency, n_samples=acq.n_samples, t0=acq.t0, prf=acq.prf)
+    tx = O.TxSet(np.ones(len(txs), np.int32), np.asarray([t.angle for t in txs], np.float32),
+                 np.tile([0, 0, 0.03], (len(txs), 1)).astype(np.float32), np.zeros((len(txs), 3), np.float32),
+                 np.asarray([t.delays for t in txs], np.float32), np.asarray([t.apodization for t in txs], np.float32))
+    cd = O.channel_desc(pr, O.medium(), oacq, tx, is_iq=True, fdem=F0)
+    grid_pts = pts.reshape(N0, N1, 3)
+    orc = O.Lib("oracle")
+    orc.set_threads(threads)
+    n_time = max(2, min(threads, 16))
+    t_idx = np.linspace(0, N0 - 1, n_time).astype(int)
+    sub_t = grid_pts[t_idx].reshape(-1, 3)
+    sub_e = grid_pts[list(line_idx)].reshape(-1, 3)
+    ref = O.RefLib() if O.REF_SO.exists() else None
+    seconds, errors = {}, {}
+    for name, kw in BATCH_BEAMFORMERS.items():
+        t = time.perf_counter()
+        if ref is not None:
+            ref.beamform(cd, iq0, 0, sub_t[::N1, 0], sub_t[:N1, 2], (0, 0, 0), sub_t, O.bf_config(**kw))
+        else:
+            orc.beamform(cd, iq0, sub_t, n_time, N1, O.bf_config(**kw))
+        seconds[name] = (time.perf_counter() - t) * N0 / n_time
+        want = orc.beamform(cd, iq0, sub_e, len(line_idx), N1, O.bf_config(**kw), prec="f64")
+        got = gpu_lines[name].astype(np.complex128)
+        errors[name] = float(np.linalg.norm(got - want) / max(1e-300, np.linalg.norm(want)))
+    total = sum(seconds.values())
+    cpu = {"value": len(seconds) / total, "unit": "frames/s", "cores": threads,
+           "kind": "reference" if ref is not None else "port",
+           "sample": f"{', '.join(seconds)} on {n_time} of {N0} lateral lines of frame 0, scaled to a frame",
+           "seconds_per_frame": seconds}
+    return cpu, errors
+
+
+def run_batch(args) -> None:
+    """Batched plain beamformers: 64 acquisitions of distinct seeded phantoms
+    (100,000 scatterers each, three cysts of radius 2-4 mm, 75 plane waves at
+    -16..16 degrees, 60 mm, simulated and demodulated on the GPU), beamformed
+    onto 512 x 1024 by delay-and-sum, coherence-factor DAS, DMAS and minimum
+    variance (L = 64, range averaging 2, loading tr(R) / (100 L); tensor-core
+    covariance). Each beamformer's 64 frames are captured once into a CUDA
+    graph (DAS, CF and DMAS as one batched launch sequence; MV as 64 frame
+    executions, whose channel export is 0.5 GB a frame) and one step replays
+    the four graphs. Reported per beamformer: frames/s and the relative L2
+    error of frame 0 against the FP64 oracle on four lateral lines."""
+    import torch
+    import usx
+    from usx import capi
+    torch.cuda.set_device(0)
+    n_frames = 64
+    _, probe, medium, acq, _, txs, _, grid = workload_setup()
+    stream = torch.cuda.Stream()
+    ctx = capi.Context(0, stream=stream.cuda_stream)
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    ch_iq = _capi_channel(capi, probe, medium, acq, txs, is_iq=True, fdem=F0)
+    half = 0.5 * probe.aperture_width()
+    iq = torch.empty((n_frames, N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    d_rf = torch.empty((N_TX, N_EL, N_SMP), device="cuda")
+    t_sim = time.perf_counter()
+    for f in range(n_frames):
+        ph = usx.Phantom.speckle_box(-half * 1.1, half * 1.1, 0.004, 0.062, 0.0, 100_000, 2026 + f)
+        for x, z, r in CYSTS:
+            ph.scale_amplitude_in_circle(usx.Vec3(x, 0.0, z), r, 0.0)
+        d_sc = torch.from_numpy(_scatterers(ph)).cuda()
+        with torch.cuda.stream(stream):
+            ctx.simulate(ch_rf, capi.sim_config(noise_db=-200.0), d_sc.data_ptr(), len(d_sc), None,
+                         d_rf.data_ptr())
+            ctx.demodulate(ch_rf, capi.demod_config(), d_rf.data_ptr(), iq[f].data_ptr())
+        ctx.synchronize()
+    t_sim = time.perf_counter() - t_sim
+    del d_rf
+    pts = np.asarray(grid.points, np.float32).reshape(-1, 3)
+    cgrid = capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1), pts)
+    frames = torch.empty((n_frames, N0, N1), dtype=torch.complex64, device="cuda")
+    iq_stride, fr_stride = N_TX * N_EL * N_SMP, N0 * N1
+    line_idx = (0, 170, 341, 511)
+    plans, graphs, lines0, prof_all = {}, {}, {}, {}
+    for name, kw in BATCH_BEAMFORMERS.items():
+        plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**kw))
+        if name == "mv":
+            plan.set_mv_mode(1)
+        with torch.cuda.stream(stream):
+            plan.autotune(iq[0].data_ptr(), frames[0].data_ptr(), repeats=1)
+
+        def run(plan=plan, name=name):
+            if name == "mv":
+                for f in range(n_frames):
+                    plan.execute(iq[f].data_ptr(), frames[f].data_ptr())
+            else:
+                plan.execute_batch(n_frames, iq.data_ptr(), iq_stride, frames.data_ptr(), fr_stride)
+
+        with torch.cuda.stream(stream):
+            run()                                  # sizes the scratch arena
+            stream.synchronize()
+            capi.profile(ctx, True)
+            capi.profile_reset(ctx)
+            run()                                  # one direct pass: per-kernel device times
+            stream.synchronize()
+            prof_all[name] = capi.profile_read(ctx)
+            capi.profile(ctx, False)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                run()
+            stream.synchronize()
+            g.replay()
+            stream.synchronize()
+        lines0[name] = frames[0].cpu().numpy()[list(line_idx)]
+        plans[name], graphs[name] = plan, g
+    # Replays go to the current stream: every replay below runs on `stream`,
+    # where the events are recorded.
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            for g in graphs.values():
+                g.replay()
+    stream.synchronize()
+    per_bf = {}
+    with ClockSampler(0) as clocks, torch.cuda.stream(stream):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(graphs) + 1)]
+        torch.cuda.synchronize()
+        ms = {n: 0.0 for n in graphs}
+        for _ in range(args.steps):
+            ev[0].record(stream)
+            for i, g in enumerate(graphs.values()):
+                g.replay()
+                ev[i + 1].record(stream)
+            ev[-1].synchronize()
+            for i, n in enumerate(graphs):
+                ms[n] += ev[i].elapsed_time(ev[i + 1])
+    total_ms = sum(ms.values())
+    for n in graphs:
+        per_bf[n] = {"frames_per_s": n_frames * args.steps / (ms[n] / 1e3), "ms_per_frame": ms[n] / (n_frames * args.steps),
+                     "graph_launches_per_step": 1}
+    peaks = load_peaks()
+    prof = {}
+    for p in prof_all.values():
+        for k, v in p.items():
+            a = prof.setdefault(k, [0.0, 0])
+            a[0] += v[0]
+            a[1] += v[1]
+    roof = kernel_roofline(prof, n_frames, pts, txs, probe, peaks)
+    cpu, errors = (None, None)
+    if not args.no_cpu:
+        cpu, errors = cpu_leg_batch(iq[0].cpu().numpy(), pts, txs, probe, acq, lines0, line_idx,
+                                    os.cpu_count() or 1)
+        for n, e in errors.items():
+            per_bf[n]["fp64_oracle_rel_l2_frame0"] = e
+    launches = sum(v[1] for v in prof.values()) * args.steps  # one pass of the four graphs per step
+    line = {"metric": "beamformed frames/s, 64-frame batch of 128ch 75-PW 512x1024 (DAS, CF, DMAS, MV; one CUDA "
+                      "graph per beamformer)",
+            "value": len(graphs) * n_frames * args.steps / (total_ms / 1e3), "unit": "frames/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (64 GPU-simulated 100k-scatterer cyst phantoms, seeds 2026-2089)",
+            "config": {"workload": "batch_64x_75pw_512x1024", "beamformers": BATCH_BEAMFORMERS,
+                       "mv_solver": "tensor", "frames": n_frames, "iq_bytes": int(iq.numel() * 8),
+                       "l2": "inputs larger than L2 (10.2 GB IQ), no flush"},
+            "gpu_launches": launches, "graph_replays_per_step": len(graphs), "beamformers": per_bf,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": None, "clocks": clocks.summary(),
+            "simulation_s": t_sim}
+    print(json.dumps(line))
+    for p in plans.values():
+        p.close()
+    ctx.close()
+
+
 def run_post(args) -> None:
     """B-mode post-processing of a cine loop: 48 distinct 512 x 1024 IQ frames
     (192 MB, larger than L2), each through envelope (|IQ|), time-gain
@@ -1062,7 +1240,8 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="learned",
-                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "post", "sector", "mixed"])
+                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "post", "batch", "sector",
+                                                   "mixed"])
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
     ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
@@ -1080,6 +1259,8 @@ def main() -> int:
         run_strain(args)
     elif args.workload == "post":
         run_post(args)
+    elif args.workload == "batch":
+        run_batch(args)
     elif args.workload == "sector":
         run_sector(args)
     elif args.workload == "mixed":
