@@ -1110,11 +1110,13 @@ def run_sector(args) -> None:
 
 def run_mixed(args) -> None:
     """Mixed-probe streaming: per step one 128-element linear frame (75 plane
-    waves, 512 x 1024, learned MV with plain-MV fallback) and one 64-element
-    phased-array sector frame (31 diverging waves, 256 x 1024, tensor-core MV,
-    envelope, log compression, scan conversion to 800 x 800), both captured
-    once into a single CUDA graph that each step replays (one launch for the
-    whole mixed batch)."""
+    waves, 512 x 1024) and one 64-element phased-array sector frame (31
+    diverging waves, 256 x 1024, L = 32, then envelope, log compression and
+    scan conversion to 800 x 800), both by learned MV with the plain-MV
+    fallback (the shipped network and gate), captured once into a single CUDA
+    graph that each step replays (one launch for the whole mixed batch). The
+    sector frame's distance from plain tensor-core MV and both frames'
+    fallback rates are reported from one direct execution."""
     import torch
     import usx
     from usx import capi, learned
@@ -1162,10 +1164,18 @@ def run_mixed(args) -> None:
     sgrid = usx.ScanGrid.sector(float(np.deg2rad(-45.0)), float(np.deg2rad(45.0)), 256, 0.005, 0.08, 1024,
                                 usx.Vec3(0.0, 0.0, 0.0))
     scg = capi.Grid(1, np.asarray(sgrid.axis0), np.asarray(sgrid.axis1), np.asarray(sgrid.points).reshape(-1, 3))
-    sec = ctx.plan(sch_iq, scg, capi.bf_config(f_number=1.5, combiner=2, mv_subarray=32,
-                                                mv_diagonal_loading=0.01, mv_range_average=2))
-    sec.set_mv_mode(1)
+    sector_mv = dict(f_number=1.5, mv_subarray=32, mv_diagonal_loading=0.01, mv_range_average=2)
     f_sec = torch.empty((256, 1024), dtype=torch.complex64, device="cuda")
+    plain = ctx.plan(sch_iq, scg, capi.bf_config(combiner=2, **sector_mv))
+    plain.set_mv_mode(1)
+    plain.execute(iq_sec.data_ptr(), f_sec.data_ptr())
+    ctx.synchronize()                    # the plan ran on the context's stream
+    f_sec_plain = f_sec.clone()
+    torch.cuda.synchronize()
+    plain.close()
+    sec = ctx.plan(sch_iq, scg, capi.bf_config(combiner=learned.COMB_LEARNED_MV, **sector_mv))
+    sec.set_learned(mlp, learned.trained_gate(WEIGHTS))
+    sec.set_learned_refine(learned.trained_refine(WEIGHTS))
     sec.autotune(iq_sec.data_ptr(), f_sec.data_ptr(), repeats=1)
     env, logi = torch.empty((256, 1024), device="cuda"), torch.empty((256, 1024), device="cuda")
     img = torch.empty((800, 800), device="cuda")
@@ -1190,13 +1200,48 @@ def run_mixed(args) -> None:
         with ClockSampler(0) as clocks:
             ms = timed(stream, graph.replay, args.steps)
         ms_direct = timed(stream, batch, args.steps)
-    line = {"metric": "mixed-batch frames/s (128-el linear learned-MV 512x1024 + 64-el sector MV 256x1024 -> 800x800)",
+        stream.synchronize()
+        # Fallback rates from one direct execution (graph replays bypass the
+        # plans' host-side pixel counters).
+        lin.learned_stats()
+        sec.learned_stats()
+        batch()
+        stream.synchronize()
+        g_lin, p_lin = lin.learned_stats()
+        g_sec, p_sec = sec.learned_stats()
+        # Per-kernel device times of each frame type from one profiled direct pass.
+        profs = {}
+        for name, fn in (("linear", lambda: lin.execute(iq_lin.data_ptr(), f_lin.data_ptr())),
+                         ("sector", lambda: (sec.execute(iq_sec.data_ptr(), f_sec.data_ptr()),
+                                             ctx.envelope(f_sec.data_ptr(), 256, 1024, sp.center_frequency,
+                                                          env.data_ptr()),
+                                             ctx.log_compress(env.data_ptr(), 256 * 1024, 60.0, 0.0, -1.0,
+                                                              logi.data_ptr()),
+                                             ctx.scan_convert(logi.data_ptr(), scg, 800, 800, 0.0,
+                                                              img.data_ptr())))):
+            capi.profile(ctx, True)
+            capi.profile_reset(ctx)
+            fn()
+            stream.synchronize()
+            profs[name] = capi.profile_read(ctx)
+            capi.profile(ctx, False)
+    peaks = load_peaks()
+    roof = kernel_roofline(profs["linear"], 1, pts, txs, probe, peaks, learned.trained_refine(WEIGHTS))
+    roof["sector_kernels_ms_per_frame"] = {k: v[0] for k, v in profs["sector"].items()}
+    launches = sum(v[1] for p in profs.values() for v in p.values()) * args.steps
+    torch.cuda.synchronize()
+    rel_sec = float((f_sec - f_sec_plain).abs().pow(2).sum().sqrt() / f_sec_plain.abs().pow(2).sum().sqrt())
+    line = {"metric": "mixed-batch frames/s (128-el linear 512x1024 + 64-el sector 256x1024 -> 800x800, both "
+                      "learned MV with plain-MV fallback)",
             "value": 2 * args.steps / (ms / 1e3), "unit": "frames/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (GPU-simulated phantoms)",
-            "config": {"workload": "mixed_linear_learned_512x1024_sector_mv_256x1024", "frames_per_step": 2,
-                       "launch": "one CUDA graph per step"},
-            "direct_launch_ms_per_step": ms_direct / args.steps, "clocks": clocks.summary()}
+            "config": {"workload": "mixed_linear_learned_512x1024_sector_learned_256x1024", "frames_per_step": 2,
+                       "launch": "one CUDA graph per step", "sector_mv": sector_mv},
+            "direct_launch_ms_per_step": ms_direct / args.steps, "clocks": clocks.summary(),
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": None, "e2e": None,
+            "fallback_rate": {"linear": g_lin / max(1, p_lin), "sector": g_sec / max(1, p_sec)},
+            "sector_rel_l2_vs_plain_mv": rel_sec}
     print(json.dumps(line))
     lin.close()
     sec.close()
