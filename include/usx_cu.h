@@ -152,6 +152,10 @@ int usx_cu_bf_plan_set_precision(usx_bf_plan* plan, int precision);
  * variant in `frame` and synchronises. Variant 0 is the default. */
 int usx_cu_bf_variant_count(void);
 int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* min_blocks, int* warp_lines);
+/* The order in which variant i dispatches its CTA tiles: *deep_first = 1 when
+ * every line group's deepest depth tile goes first (the lightest tiles form
+ * the grid's tail), 0 for depth tiles in ascending order. */
+int usx_cu_bf_variant_order(int index, int* deep_first);
 int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
 int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);
 int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, int repeats, float* ms_out);

@@ -259,7 +259,8 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
 // are template parameters; every variant computes the same sums in the same
 // order (bit-identical frames), and the plan's autotuner picks the fastest
 // for its geometry.
-template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1>
+template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1,
+          bool kDeepFirst = false>
 __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
   static_assert(kTileLines % kWarpLines == 0 && 32 % kWarpLines == 0, "warp shape must tile the CTA");
   // kRtShared: the group's receive delays live in shared memory instead of
@@ -270,8 +271,17 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
   const int tile = blockIdx.x;
   constexpr int kWarpDepths = 32 / kWarpLines;
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  const int line = (tile / tiles_depth) * kTileLines + (w / kWarpLines) * kWarpLines + ln / kWarpDepths;
-  const int depth = (tile % tiles_depth) * 32 + (w % kWarpLines) * kWarpDepths + ln % kWarpDepths;
+  // Tile order. Default: depth tiles of a group of lines, then the next lines.
+  // kDeepFirst: every line group's deepest depth tile first, the shallowest
+  // last. A pixel's work grows with depth (the aperture widens as z / F#), so
+  // the CTAs dispatched last, which form the tail of the grid, are the
+  // lightest (longest-processing-time-first order). Both orders visit each of
+  // the n_line_tiles x tiles_depth tiles once.
+  const int n_line_tiles = (n0 + kTileLines - 1) / kTileLines;
+  const int line_tile = kDeepFirst ? tile % n_line_tiles : tile / tiles_depth;
+  const int depth_tile = kDeepFirst ? tiles_depth - 1 - tile / n_line_tiles : tile % tiles_depth;
+  const int line = line_tile * kTileLines + (w / kWarpLines) * kWarpLines + ln / kWarpDepths;
+  const int depth = depth_tile * 32 + (w % kWarpLines) * kWarpDepths + ln % kWarpDepths;
   if (line >= n0 || depth >= a.n1) return;
   const int pix = line * a.n1 + depth;
   const long frame = blockIdx.y;
@@ -760,19 +770,21 @@ __global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
 // per warp).
 struct DasVariant {
   int group, tile_lines, min_blocks, warp_lines;
+  bool deep_first;  // deepest depth tiles dispatched first
   void (*iq)(BfArgs);
   void (*rf)(BfArgs);
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
-template <int G, int TL, int MB, bool RTS = false, int WL = 1>
+template <int G, int TL, int MB, bool RTS = false, int WL = 1, bool DF = false>
 constexpr DasVariant das_variant() {
-  return DasVariant{G, TL, MB, WL, das_fast_kernel<true, G, TL, MB, RTS, WL>, das_fast_kernel<false, 16, 4, 1>, false};
+  return DasVariant{G,     TL, MB, WL, DF, das_fast_kernel<true, G, TL, MB, RTS, WL, DF>,
+                    das_fast_kernel<false, 16, 4, 1>, false};
 }
 template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
-  return DasVariant{G, TL, 0, 1, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
+  return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
 }
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
@@ -780,6 +792,8 @@ const DasVariant kDasVariants[] = {
     das_variant<16, 4, 8, true>(), das_variant<16, 2, 16, true>(), das_staged_variant<8, 4, 1>(),
     das_variant<8, 4, 8, false, 4>(), das_variant<4, 4, 12, false, 4>(), das_variant<4, 4, 12, false, 2>(),
     das_variant<8, 2, 16, false, 2>(), das_variant<8, 8, 4, false, 4>(), das_variant<8, 8, 4, false, 8>(),
+    das_variant<4, 4, 12, false, 2, true>(), das_variant<4, 4, 12, false, 4, true>(),
+    das_variant<8, 4, 8, false, 4, true>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -1476,6 +1490,12 @@ int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* 
   if (tile_lines) *tile_lines = kDasVariants[index].tile_lines;
   if (min_blocks) *min_blocks = kDasVariants[index].min_blocks;
   if (warp_lines) *warp_lines = kDasVariants[index].warp_lines;
+  return USX_OK;
+}
+
+int usx_cu_bf_variant_order(int index, int* deep_first) {
+  if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_order: no such variant");
+  if (deep_first) *deep_first = kDasVariants[index].deep_first ? 1 : 0;
   return USX_OK;
 }
 

@@ -465,13 +465,14 @@ class Mlp:
 
 
 def das_variants() -> list:
-    """(channel group, tile lines, min resident CTAs, lines per warp) of each
-    delay-and-sum variant."""
+    """(channel group, tile lines, min resident CTAs, lines per warp, deepest
+    tiles first) of each delay-and-sum variant."""
     out = []
     for i in range(lib().usx_cu_bf_variant_count()):
-        g, t, m, w = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        g, t, m, w, d = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(lib().usx_cu_bf_variant_info(i, C.byref(g), C.byref(t), C.byref(m), C.byref(w)), "bf_variant_info")
-        out.append((g.value, t.value, m.value, w.value))
+        check(lib().usx_cu_bf_variant_order(i, C.byref(d)), "bf_variant_order")
+        out.append((g.value, t.value, m.value, w.value, d.value))
     return out
 
 
