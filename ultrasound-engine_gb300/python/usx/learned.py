@@ -9,7 +9,8 @@ pairs come from the plain tensor-core minimum variance run on simulated
 phantoms (the plan's training export); training runs on the device through
 usx_cu_mlp_train_step (hand-written forward/backward GEMMs and Adam). At
 inference the plan gates each pixel on |1^H w - 1| and solves the rejected
-ones exactly, so plain minimum variance is both the fallback and the judge.
+ones exactly, so plain minimum variance is both the fallback and the
+reference the image metrics are compared against.
 
     python -m usx.learned train --phantoms 200 --out weights.bin
     python -m usx.learned evaluate --weights weights.bin --phantoms 16
