@@ -778,7 +778,9 @@ def cpu_leg_batch(iq0: np.ndarray, pts: np.ndarray, txs, probe, acq, gpu_lines: 
     """CPU side of the batched workload: the reference's CPU beamformers (its
     own build when present, else the oracle's port) timed on a sample of
     lateral lines and scaled to a frame, and the FP64 oracle on `line_idx` as
-    the checker of each GPU beamformer's frame 0 (relative L2)."""
+    the checker of each GPU beamformer's frame 0 (relative L2), beside the
+    distance of the reference's own FP32 arithmetic (the oracle's f32
+    restatement) from the FP64 oracle on the same lines."""
     from oracle import oracle as O
     pr = O.probe(N_EL, probe.pitch, probe.element_width, 5e-3, F0, probe.bandwidth)
     oacq = O.acquisition(fs=acq.sampling_frequency, n_samples=acq.n_samples, t0=acq.t0, prf=acq.prf)
@@ -794,7 +796,7 @@ def cpu_leg_batch(iq0: np.ndarray, pts: np.ndarray, txs, probe, acq, gpu_lines: 
     sub_t = grid_pts[t_idx].reshape(-1, 3)
     sub_e = grid_pts[list(line_idx)].reshape(-1, 3)
     ref = O.RefLib() if O.REF_SO.exists() else None
-    seconds, errors = {}, {}
+    seconds, errors, ref_errors = {}, {}, {}
     for name, kw in BATCH_BEAMFORMERS.items():
         t = time.perf_counter()
         if ref is not None:
@@ -803,14 +805,16 @@ def cpu_leg_batch(iq0: np.ndarray, pts: np.ndarray, txs, probe, acq, gpu_lines: 
             orc.beamform(cd, iq0, sub_t, n_time, N1, O.bf_config(**kw))
         seconds[name] = (time.perf_counter() - t) * N0 / n_time
         want = orc.beamform(cd, iq0, sub_e, len(line_idx), N1, O.bf_config(**kw), prec="f64")
+        ref32 = orc.beamform(cd, iq0, sub_e, len(line_idx), N1, O.bf_config(**kw), prec="f32")
         got = gpu_lines[name].astype(np.complex128)
         errors[name] = float(np.linalg.norm(got - want) / max(1e-300, np.linalg.norm(want)))
+        ref_errors[name] = float(np.linalg.norm(ref32 - want) / max(1e-300, np.linalg.norm(want)))
     total = sum(seconds.values())
     cpu = {"value": len(seconds) / total, "unit": "frames/s", "cores": threads,
            "kind": "reference" if ref is not None else "port",
            "sample": f"{', '.join(seconds)} on {n_time} of {N0} lateral lines of frame 0, scaled to a frame",
            "seconds_per_frame": seconds}
-    return cpu, errors
+    return cpu, errors, ref_errors
 
 
 def run_batch(args) -> None:
@@ -919,12 +923,13 @@ def run_batch(args) -> None:
             a[0] += v[0]
             a[1] += v[1]
     roof = kernel_roofline(prof, n_frames, pts, txs, probe, peaks)
-    cpu, errors = (None, None)
+    cpu = None
     if not args.no_cpu:
-        cpu, errors = cpu_leg_batch(iq[0].cpu().numpy(), pts, txs, probe, acq, lines0, line_idx,
-                                    os.cpu_count() or 1)
+        cpu, errors, ref_errors = cpu_leg_batch(iq[0].cpu().numpy(), pts, txs, probe, acq, lines0, line_idx,
+                                                os.cpu_count() or 1)
         for n, e in errors.items():
             per_bf[n]["fp64_oracle_rel_l2_frame0"] = e
+            per_bf[n]["reference_fp32_rel_l2_vs_fp64_frame0"] = ref_errors[n]
     launches = sum(v[1] for v in prof.values()) * args.steps  # one pass of the four graphs per step
     line = {"metric": "beamformed frames/s, 64-frame batch of 128ch 75-PW 512x1024 (DAS, CF, DMAS, MV; one CUDA "
                       "graph per beamformer)",
