@@ -101,3 +101,112 @@ def test_device_feed_fails_loudly_without_a_gpu(geometry):
     probe, medium, acq, txs = geometry
     with pytest.raises(RuntimeError, match="no CPU path"):
         ingest.DeviceFeed(ingest.ArraySource(_blocks(acq, txs, 1), probe, medium, acq, txs))
+
+
+class _FakeCuda:
+    """Records the stream operations DeviceFeed issues (no GPU involved)."""
+
+    def __init__(self, log):
+        self.log = log
+        fake = self
+
+        class Event:
+            n = 0
+
+            def __init__(self, *a, **k):
+                Event.n += 1
+                self.id = Event.n
+
+            def record(self, stream):
+                fake.log.append(("record", self.id, stream.name))
+
+            def synchronize(self):
+                fake.log.append(("host_wait", self.id))
+
+        class Stream:
+            def __init__(self, *a, name="copy", **k):
+                self.name = name
+
+            def wait_event(self, ev):
+                fake.log.append(("wait", self.name, ev.id))
+
+        class _Ctx:
+            def __init__(self, s):
+                self.s = s
+
+            def __enter__(self):
+                fake.current = self.s
+
+            def __exit__(self, *a):
+                fake.current = None
+
+        self.Event, self.Stream = Event, Stream
+        self.current = None
+        self.stream = _Ctx
+
+    def is_available(self):
+        return True
+
+    def current_device(self):
+        return 0
+
+    def current_stream(self, device=None):
+        return self.Stream(name="consumer")
+
+
+class _FakeTensor:
+    def __init__(self, shape, log, kind):
+        self.a = np.zeros(shape, np.float32)
+        self.log, self.kind = log, kind
+
+    def numpy(self):
+        return self.a
+
+    def copy_(self, src, non_blocking=False):
+        self.a[...] = src.a
+        self.log.append(("copy", int(src.a.flat[0])))
+
+    def record_stream(self, s):
+        pass
+
+
+def test_device_feed_orders_copies_and_slot_reuse(monkeypatch, geometry):
+    """With depth 2: frame k's copy waits for the consumer's release of its
+    slot (recorded when the consumer asked for frame k - 1), each frame is
+    handed over behind the event of its own copy, and the copies run ahead of
+    the consumer by one frame."""
+    import sys
+    import types
+    log = []
+    cuda = _FakeCuda(log)
+    fake = types.SimpleNamespace(
+        cuda=cuda, float32=np.float32, device=lambda *a: "cuda:0",
+        empty=lambda shape, dtype=None, pin_memory=False, device=None: _FakeTensor(
+            shape, log, "host" if pin_memory else "device"))
+    monkeypatch.setitem(sys.modules, "torch", fake)
+    probe, medium, acq, txs = geometry
+    blocks = [np.full((len(txs), 32, acq.n_samples), k, np.float32) for k in range(5)]
+    feed = ingest.DeviceFeed(ingest.ArraySource(blocks, probe, medium, acq, txs), depth=2)
+    seen = []
+    for fr in feed:
+        log.append(("consume", fr.index))
+        seen.append(int(fr.rf.numpy().flat[0]))
+    assert seen == [0, 1, 2, 3, 4]
+    copies = [i for i, e in enumerate(log) if e[0] == "copy"]
+    consumes = [i for i, e in enumerate(log) if e[0] == "consume"]
+    assert [log[i][1] for i in copies] == [0, 1, 2, 3, 4]
+    # Frame k + 1 is copied before frame k is consumed (one frame ahead).
+    for k in range(4):
+        assert copies[k + 1] < consumes[k]
+    # Before copying frame k >= 2 into its slot, the copy stream waited on an
+    # event the consumer recorded after consuming frame k - 2.
+    for k in range(2, 5):
+        waits = [i for i in range(consumes[k - 2], copies[k]) if log[i][0] == "wait" and log[i][1] == "copy"]
+        assert waits, k
+        ev = log[waits[-1]][2]
+        rec = [i for i in range(consumes[k - 2], waits[-1]) if log[i] == ("record", ev, "consumer")]
+        assert rec, k
+    # The consumer waits on some copy event before each frame is handed over.
+    for k in range(5):
+        start = consumes[k - 1] if k else 0
+        assert any(log[i][0] == "wait" and log[i][1] == "consumer" for i in range(start, consumes[k])), k
