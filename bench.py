@@ -175,21 +175,54 @@ def mv_flops_per_frame(grid_pts: np.ndarray, cfg: dict) -> float:
     return float(np.sum(f[ok]))
 
 
-def cpu_baseline_mv(iq: np.ndarray, pts: np.ndarray, txs, probe, acq, lines: int, threads: int):
-    """Time the CPU minimum variance on `lines` lateral lines; returns (s, kind)."""
+def plane_wave_table(angles: np.ndarray, n_el: int = N_EL, pitch: float = 300e-6, width: float = 270e-6,
+                     c: float = C0):
+    """Plane-wave delays and Hann transmit apodisation over the whole aperture,
+    the reference's compute_transmit_delays (core/src/geometry.cpp:17-80) for
+    PlaneWave with origin 0, restated in float32 for the CPU arm."""
+    import ctypes
+    libm = ctypes.CDLL("libm.so.6")  # the C library's sinf/cosf, as the reference's std::sin/std::cos
+    for fn in (libm.sinf, libm.cosf):
+        fn.argtypes, fn.restype = [ctypes.c_float], ctypes.c_float
+    f = np.float32
+    ex = ((np.arange(n_el, dtype=f) - f(0.5) * f(n_el - 1)) * f(pitch)).astype(f)
+    half = f(0.5) * (f(n_el - 1) * f(pitch) + f(width))
+    two_pi = f(2.0) * f(np.pi)
+    apod = np.zeros(n_el, f)
+    for i, x in enumerate(ex):
+        u = x / max(half, f(1e-9))
+        if -1 <= u <= 1:  # window_value(Hann, u), core/src/types.cpp:126-148
+            t = f(0.5) * (u + f(1))
+            apod[i] = f(0.5) * (f(1) - f(libm.cosf(two_pi * t)))
+    sin = np.array([libm.sinf(float(a)) for a in angles], f)
+    delays = np.where(apod[None, :] > 0, ex[None, :] * sin[:, None] / f(c), f(0)).astype(f)
+    return delays, np.repeat(apod[None, :], len(angles), 0)
+
+
+def baseline_lines(threads: int) -> np.ndarray:
+    """Lateral lines of the CPU sample: two per host thread (the reference's
+    beamformer splits its work across threads by blocks of pixels), evenly
+    spread over the grid, at least 32."""
+    n = int(min(N0, max(32, 2 * threads)))
+    return np.linspace(0, N0 - 1, n).round().astype(int)
+
+
+def cpu_baseline_mv(iq: np.ndarray, pts: np.ndarray, angles: np.ndarray, delays: np.ndarray, apod: np.ndarray,
+                    fs: float, n_samples: int, prf: float, lines: np.ndarray, threads: int):
+    """Time the CPU minimum variance on the given lateral lines; returns (s, kind)."""
     from oracle import oracle as O
-    pr = O.probe(N_EL, probe.pitch, probe.element_width, 5e-3, F0, probe.bandwidth)
-    oacq = O.acquisition(fs=acq.sampling_frequency, n_samples=acq.n_samples, t0=acq.t0, prf=acq.prf)
-    tx = O.TxSet(np.ones(len(txs), np.int32), np.asarray([t.angle for t in txs], np.float32),
-                 np.tile([0, 0, 0.03], (len(txs), 1)).astype(np.float32), np.zeros((len(txs), 3), np.float32),
-                 np.asarray([t.delays for t in txs], np.float32), np.asarray([t.apodization for t in txs], np.float32))
+    pr = O.probe(N_EL, 300e-6, 270e-6, 5e-3, F0, 0.6)
+    oacq = O.acquisition(fs=fs, n_samples=n_samples, t0=0.0, prf=prf)
+    n_tx = len(angles)
+    tx = O.TxSet(np.ones(n_tx, np.int32), np.asarray(angles, np.float32),
+                 np.tile([0, 0, 0.03], (n_tx, 1)).astype(np.float32), np.zeros((n_tx, 3), np.float32),
+                 np.asarray(delays, np.float32), np.asarray(apod, np.float32))
     cd = O.channel_desc(pr, O.medium(), oacq, tx, is_iq=True, fdem=F0)
-    idx = np.linspace(0, N0 - 1, lines).astype(int)
-    sub = pts.reshape(N0, N1, 3)[idx].reshape(-1, 3)
+    sub = np.ascontiguousarray(pts.reshape(N0, N1, 3)[lines].reshape(-1, 3), dtype=np.float32)
     if O.REF_SO.exists():
         ref = O.RefLib()
         kind = "reference"
-        axis1 = sub.reshape(lines, N1, 3)[0, :, 2]
+        axis1 = sub.reshape(len(lines), N1, 3)[0, :, 2]
         t = time.perf_counter()
         ref.beamform(cd, iq, 0, sub[::N1, 0], axis1, (0, 0, 0), sub, O.bf_config(**MV_KW))
         dt = time.perf_counter() - t
@@ -198,9 +231,26 @@ def cpu_baseline_mv(iq: np.ndarray, pts: np.ndarray, txs, probe, acq, lines: int
         orc.set_threads(threads)
         kind = "port"
         t = time.perf_counter()
-        orc.beamform(cd, iq, sub, lines, N1, O.bf_config(**MV_KW))
+        orc.beamform(cd, iq, sub, len(lines), N1, O.bf_config(**MV_KW))
         dt = time.perf_counter() - t
     return dt, kind
+
+
+def reference_workload():
+    """The headline acquisition's geometry for the CPU arm, built with numpy
+    alone (this engine's library is not loaded by the reference arm): 75
+    plane waves at -16..16 deg, 2073 samples at 20 MHz, the 512 x 1024 grid
+    over the aperture and z = 5-60 mm."""
+    f = np.float32
+    angles = np.deg2rad(np.linspace(-16, 16, N_TX)).astype(f)
+    delays, apod = plane_wave_table(angles)
+    half = f(0.5) * (f(N_EL - 1) * f(300e-6) + f(270e-6))
+    ax0 = np.array([-half + (half - -half) * f(i) / f(N0 - 1) for i in range(N0)], f)
+    ax1 = np.array([f(0.005) + (f(0.060) - f(0.005)) * f(i) / f(N1 - 1) for i in range(N1)], f)
+    pts = np.zeros((N0, N1, 3), f)
+    pts[:, :, 0] = ax0[:, None]
+    pts[:, :, 2] = ax1[None, :]
+    return angles, delays, apod, pts.reshape(-1, 3)
 
 
 def run_reference(args) -> None:
@@ -209,30 +259,36 @@ def run_reference(args) -> None:
         return
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     threads = int(os.environ["OMP_NUM_THREADS"])
-    usx, probe, medium, acq, sim, txs, ph, grid = workload_setup()
+    angles, delays, apod, pts = reference_workload()
     rng = np.random.default_rng(1)
-    # The CPU path's cost does not depend on the sample values; random IQ of the workload's shape.
+    # The CPU minimum variance does the same work whatever the sample values
+    # (every pixel forms its covariance and runs its Cholesky), so the arm
+    # beamforms seeded random IQ of the workload's shape: the GPU arm's
+    # simulated acquisition does not exist yet when this arm runs.
     iq = (rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)
           + 1j * rng.standard_normal((N_TX, N_EL, N_SMP), dtype=np.float32)).astype(np.complex64)
-    pts = np.asarray(grid.points)
-    lines = max(2, min(threads, 16))  # the reference parallelises over lines: one per core
+    lines = baseline_lines(threads) if args.lines >= N0 else np.linspace(0, N0 - 1, args.lines).round().astype(int)
     times = []
     for i in range(args.warmup + args.steps):
-        dt, kind = cpu_baseline_mv(iq, pts, txs, probe, acq, lines, threads)
+        dt, kind = cpu_baseline_mv(iq, pts, angles, delays, apod, FS, N_SMP, 5000.0, lines, threads)
         if i >= args.warmup:
             times.append(dt)
-    sec_per_frame = float(np.mean(times)) * N0 / lines
-    v = 1.0 / sec_per_frame
+    step_s = float(np.mean(times))
+    v = len(lines) / N0 / step_s
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_frame * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "data": "synthetic (seeded random IQ of the workload's shape)",
             "config": {"workload": f"{args.workload}_75pw_512x1024",
                        "beamformer": dict(WORKLOADS.get(args.workload, {})), "n_tx": N_TX, "n_ch": N_EL, "grid": [N0, N1],
+                       "step": f"{len(lines)} of {N0} lateral lines (1/{N0 // len(lines)} frame); "
+                               "value = frames/s = lines per second / 512",
                        "reference_path": "the reference has no learned combiner: its minimum variance "
-                                         "(combine_mv_windowed, beamformer.cpp:137-214) on the same frame"},
+                                         "(combine_mv_windowed, beamformer.cpp:137-214) on the same geometry"},
             "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": kind,
-                             "sample": f"{lines} of {N0} lateral lines per step, scaled to a frame"},
+                             "sample": f"{len(lines)} of {N0} lateral lines per step, full depth "
+                                       f"({len(lines) * N1} pixels), {threads} threads",
+                             "s_per_line": step_s / len(lines)},
             "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -452,11 +508,14 @@ def run_ours(args) -> None:
         if world == 1 and not args.no_cpu:
             threads = os.cpu_count() or 1
             iq_host = d_iq.cpu().numpy()
-            lines = max(2, min(threads, 16))
-            dt, kind = cpu_baseline_mv(iq_host, np.asarray(grid.points), txs, probe, acq, lines, threads)
-            cpu = {"value": 1.0 / (dt * N0 / lines), "unit": "frames/s", "cores": threads, "kind": kind,
-                   "sample": f"minimum variance on {lines} of {N0} lateral lines (one per core), "
-                             f"scaled to a frame"}
+            lines = baseline_lines(threads)
+            dt, kind = cpu_baseline_mv(iq_host, np.asarray(grid.points), np.asarray([t.angle for t in txs]),
+                                       np.asarray([t.delays for t in txs]), np.asarray([t.apodization for t in txs]),
+                                       acq.sampling_frequency, acq.n_samples, acq.prf, lines, threads)
+            cpu = {"value": len(lines) / N0 / dt, "unit": "frames/s", "cores": threads, "kind": kind,
+                   "sample": f"minimum variance on {len(lines)} of {N0} lateral lines (full depth, "
+                             f"{threads} threads) of the same acquisition, lines per second / 512",
+                   "s_per_line": dt / len(lines)}
         frames_per_s = value * N0 / n0
         line = {"metric": METRIC, "value": frames_per_s, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step * N0 / n0, "higher_is_better": True,

@@ -8,8 +8,10 @@
 # Flags follow the reference's Release build (CMakeLists.txt: -O3, OpenMP, no
 # -ffast-math, no -march) plus -ffp-contract=off so that a compiler which
 # contracts by default (GCC on aarch64) keeps the reference's float arithmetic.
+# The checkout is the first argument, else $USX_REFERENCE_DIR, else the
+# location this container mounts it at; exit status 3 = no sources there.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${USX_REFERENCE_DIR:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/core/src" ]; then

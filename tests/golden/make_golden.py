@@ -12,6 +12,7 @@ pin both the CPU oracle (tests/test_oracle_golden.py) and the CUDA kernels
 from __future__ import annotations
 
 import sys
+import os
 from pathlib import Path
 
 import numpy as np
@@ -21,7 +22,8 @@ sys.path.insert(0, str(HERE.parents[1]))
 
 from oracle import oracle as O  # noqa: E402
 
-REF_DIR = Path("/root/reference")
+# The reference checkout: $USX_REFERENCE_DIR, else where this container mounts it.
+REF_DIR = Path(os.environ.get("USX_REFERENCE_DIR", "/root/reference"))
 
 
 def tx_arrays(txs: O.TxSet, prefix: str) -> dict:

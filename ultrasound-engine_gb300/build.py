@@ -135,13 +135,21 @@ def build_oracle() -> Path:
     return out
 
 
-def build_reference(ref_dir: str = "/root/reference") -> Path | None:
-    """The reference engine from its own sources, only where they exist."""
+def build_reference(ref_dir: str | None = None) -> Path | None:
+    """The reference engine from its own sources, only where they exist.
+
+    The checkout's location is the recipe's business (oracle/build_ref.sh:
+    its argument, else USX_REFERENCE_DIR, else its default); the recipe exits
+    with status 3 when there are no sources to build."""
     out = ORACLE / "_ref" / "libusx_ref.so"
-    if not Path(ref_dir, "core", "src").is_dir():
+    if not _stale(out, [ORACLE / "ref_shim.cpp", ORACLE / "build_ref.sh"]):
+        return out
+    cmd = ["bash", str(ORACLE / "build_ref.sh")] + ([ref_dir] if ref_dir else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode == 3:
         return None
-    if _stale(out, [ORACLE / "ref_shim.cpp", ORACLE / "build_ref.sh"]):
-        _run(["bash", str(ORACLE / "build_ref.sh"), ref_dir])
+    if r.returncode != 0:
+        raise RuntimeError(f"command failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return out
 
 
