@@ -604,7 +604,8 @@ def run_stage(args) -> None:
     else:
         nbytes = 4.0 * N_TX * N_EL * N_SMP + 8.0 * N_TX * N_EL * N_SMP
         kms = per[top]
-        line["config"] = {"workload": "demod_75x128x2073_33taps_dec1"}
+        line["config"] = {"workload": "demod_75x128x2073_33taps_dec1",
+                          "l2": "80 MB of RF in and 159 MB of IQ out per step (more than the 129 MB L2), no flush"}
         line["roofline"] = {"kernel": top, "bound": "hbm", "achieved": nbytes / (kms / 1e3) / 1e9,
                             "peak": peaks["hbm_gbs"], "unit": "GB/s",
                             "frac": nbytes / (kms / 1e3) / 1e9 / peaks["hbm_gbs"], "traffic": None,

@@ -309,9 +309,13 @@ int usx_cu_color_flow(usx_ctx* ctx, const float* ens, int n_frames, int n0, int 
                       const float* axis1_host, float fdem, float prf, float speed_of_sound,
                       const usx_doppler_config* cfg, float* velocity, float* power,
                       float* variance, uint8_t* valid, float* nyquist);
-/* Many colour-flow ensembles of uneven length in one launch sequence:
- * ensemble e has n_frames[e] frames starting at frame offset frame_offset[e]
- * of `ens` (all the same grid); outputs are [n_ens][n0*n1]. */
+/* Many colour-flow ensembles of uneven length in one launch sequence
+ * (reference: color_flow per ensemble, doppler.cpp:77-176): ensemble e has
+ * n_frames[e] frames starting at frame offset frame_offset[e] of `ens` (all
+ * the same grid); outputs are [n_ens][n0*n1], each map bit for bit what
+ * usx_cu_color_flow gives for that ensemble. One wall-filter and one flow
+ * launch per 64 ensembles (fewer when many distinct lengths share a call),
+ * then one power-gate launch for all; n_ens <= 65535. */
 int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int* n_frames_host,
                             const int64_t* frame_offset_host, int n0, int n1,
                             const float* axis1_host, float fdem, float prf,

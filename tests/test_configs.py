@@ -206,6 +206,12 @@ def test_cfg1_process_frame_and_display_match_oracle_chain(cfg1_run, orc):
         want_img = orc.log_compress(env, 60.0, 0.0, float(reference))
         assert img.shape == (256, 640)
         assert rel_l2(img, want_img) < TOL
+        if raw is r["raw"]:
+            first = want_img
+    # to_display of a host frame takes the same device chain (frame uploaded once).
+    pipe2 = usx.ImagingPipeline(s.grid, pcfg)
+    img2 = np.asarray(pipe2.to_display(pipe2.process_frame(r["raw"]), s.medium))
+    assert rel_l2(img2, first) < TOL
 
 
 # ---------------------------------------------------------------- config 2

@@ -495,6 +495,40 @@ def test_color_flow_batch_of_uneven_ensembles(capi, ctx, torch, golden, oracle):
         assert rel_l2(P[e], p) < TOL
 
 
+@pytest.mark.parametrize("wt,order", [(1, 2), (0, 1), (2, 0)])
+def test_color_flow_batch_equals_one_ensemble_at_a_time(capi, ctx, torch, wt, order):
+    """The batched call (one wall-filter, one flow and one gate launch per
+    chunk of ensembles) gives every map of every ensemble bit for bit as the
+    one-ensemble call does: lengths from 2 to 64 frames, ensembles that share
+    frames, enough distinct lengths to split the projector pool (64, 40 and
+    30 frames) and more ensembles than one launch takes (70)."""
+    rng = np.random.default_rng(5)
+    n0, n1, n_all = 6, 40, 64
+    ph = np.exp(-1j * 0.35 * np.arange(n_all))[:, None, None] * np.exp(-1j * 0.85 * np.arange(n1))[None, None, :]
+    noise = rng.normal(size=(n_all, n0, n1)) + 1j * rng.normal(size=(n_all, n0, n1))
+    ens = (8.0 * np.exp(0.02j * np.arange(n_all))[:, None, None] + 2.0 * ph + 0.2 * noise).astype(np.complex64)
+    ens[:, :, :10] *= 0.01
+    d = dev(torch, ens)
+    axis1 = np.linspace(0.02, 0.03, n1).astype(np.float32)
+    cfg = capi.doppler_config(wall_filter=wt, polynomial_order=order)
+    lens = [2, 5, 64, 40, 30, 7, 12] + [3] * 63
+    offs = [int(rng.integers(0, n_all - n + 1)) for n in lens]
+    m = len(lens)
+    vel, pwr, var = (torch.empty((m, n0, n1), dtype=torch.float32, device="cuda") for _ in range(3))
+    valid = torch.empty((m, n0, n1), dtype=torch.uint8, device="cuda")
+    ctx.color_flow_batch(d.data_ptr(), lens, offs, n0, n1, axis1, 5e6, 5000.0, 1540.0, cfg, vel.data_ptr(),
+                         pwr.data_ptr(), var.data_ptr(), valid.data_ptr())
+    got = [host(torch, t) for t in (vel, pwr, var, valid)]
+    one = [torch.empty((n0, n1), dtype=torch.float32, device="cuda") for _ in range(3)]
+    one.append(torch.empty((n0, n1), dtype=torch.uint8, device="cuda"))
+    for e, (n, o) in enumerate(zip(lens, offs)):
+        sub = d[o:o + n].contiguous()
+        ctx.color_flow(sub.data_ptr(), n, n0, n1, axis1, 5e6, 5000.0, 1540.0, cfg, *[t.data_ptr() for t in one])
+        for g, w in zip(got, one):
+            assert np.array_equal(g[e], host(torch, w)), (e, n)
+    assert got[3].sum() > 0
+
+
 def test_displacement_and_strain_match_reference(capi, ctx, torch, golden):
     g = golden("doppler")
     a, b = g["disp_a"], g["disp_b"]

@@ -63,6 +63,33 @@ def test_noalloc_color_flow_equals_color_flow_on_two_calls():
     ctx.close()
 
 
+@pytest.mark.parametrize("n,n0,n1,wt", [(64, 128, 128, 1), (16, 64, 96, 0)])
+def test_noalloc_color_flow_at_the_limit_and_without_wall_filter(n, n0, n1, wt):
+    """Exactly the 1,048,576 complex samples the scratch holds (64 frames,
+    whose wall filter needs more than 48 KiB of shared memory per block), and
+    the wall filter switched off, each twice in a row."""
+    import torch
+    from usx import capi
+
+    ctx = capi.Context(0, stream=torch.cuda.current_stream().cuda_stream)
+    rng = np.random.default_rng(11)
+    cfg = capi.doppler_config(wall_filter=wt, polynomial_order=2)
+    ens = _ensemble(rng, n, n0, n1)
+    axis1 = np.linspace(0.02, 0.03, n1).astype(np.float32)
+    d = torch.from_numpy(ens).cuda()
+    ref = _maps(torch, n0, n1)
+    ctx.color_flow(d.data_ptr(), n, n0, n1, axis1, 5e6, 5000.0, 1540.0, cfg, *[t.data_ptr() for t in ref])
+    for _ in range(2):
+        got = _maps(torch, n0, n1)
+        capi.color_flow_noalloc(torch.cuda.current_stream().cuda_stream, d.data_ptr(), n, n0, n1, axis1,
+                                5e6, 5000.0, 1540.0, cfg, *[t.data_ptr() for t in got])
+        torch.cuda.synchronize()
+        for a, b in zip(got[:3], ref[:3]):
+            assert rel_l2(a.cpu().numpy(), b.cpu().numpy()) <= 1e-5
+        assert np.array_equal(got[3].cpu().numpy(), ref[3].cpu().numpy())
+    ctx.close()
+
+
 def test_noalloc_color_flow_rejects_ensembles_beyond_its_scratch():
     import torch
     from usx import capi

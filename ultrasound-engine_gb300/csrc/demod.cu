@@ -1,19 +1,33 @@
 // demod.cu — quadrature demodulation + decimating FIR (reference
-// demodulate.cpp:36-121) as one HBM-bound kernel.
+// demodulate.cpp:36-121), HBM-bound.
 //
 // Layout: RF [trace][n_in] float -> IQ [trace][n_out] complex, trace =
-// event*n_channels + channel. A block owns kTraces traces x kOut output
-// samples. It stages the input span those outputs need (kOut*dec + taps - 1
-// samples per trace) in shared memory already mixed to baseband, then every
-// thread runs the FIR for one output sample of each of its traces. Each input
-// sample is read from HBM once per block; blocks overlap by taps-1 samples,
-// which is the only re-read (3% at 33 taps, dec 1).
+// event*n_channels + channel.
+//
+// demod_slide_kernel<NT> (no decimation, NT taps; the default 33-tap filter):
+// a block of 8 warps owns 8 traces x 256 output samples. It stages the 288
+// input samples those outputs need for each trace in shared memory, already
+// mixed to baseband (the rotator once per block for all 8 traces), with one
+// pad word every 8 samples so that lanes reading 8-sample strides hit distinct
+// banks. Each warp then filters one trace: lane l produces outputs 8l..8l+7
+// from one descending pass over its 8+NT-1 window samples, each sample read
+// from shared memory once and multiplied into every output it reaches (the
+// taps are compile-time constant-bank operands). Every output still sums its
+// taps in ascending order, as the reference does. The outputs go back through
+// the warp's own shared-memory row so the IQ stores are coalesced. Samples
+// outside the trace are staged as zeros: an output whose tap range the
+// reference clips (j_lo > 0 or j_hi < NT-1) then adds exact zeros outside
+// that range, which leaves its sum unchanged.
+//
+// demod_kernel (any decimation or tap count): a block owns 8 traces x 128
+// outputs, one output per thread per trace, taps read from the parameter
+// block in a runtime loop.
 //
 // Arithmetic follows the reference term by term (mix, then tap product and
 // accumulation in ascending tap order, then x2); the tap product and the
 // accumulation are one FMA (~1e-7 relative from the reference's separate
 // multiply and add); the mixing phase -2*pi*f*t(n) is evaluated on the device
-// with sincosf once per block for all of its traces.
+// with sincosf.
 #include <algorithm>
 #include <vector>
 
@@ -94,6 +108,93 @@ __global__ void __launch_bounds__(kOut) demod_kernel(const DemodParams p) {
   }
 }
 
+constexpr int kSlideR = 8;                       // outputs per lane
+constexpr int kSlideWarps = 8;                   // traces per block
+constexpr int kSlideOut = 32 * kSlideR;          // outputs per trace segment
+
+// Shared-memory slot of window sample s: one pad word after every 8 samples.
+__device__ __forceinline__ int slide_pos(int s) { return s + (s >> 3); }
+
+template <int NT>
+__global__ void __launch_bounds__(32 * kSlideWarps) demod_slide_kernel(const DemodParams p) {
+  constexpr int W = kSlideOut + NT - 1;          // window samples per trace
+  constexpr int ROW = W + W / 8 + 1;             // padded row length (float2)
+  __shared__ float2 rot[W];
+  __shared__ float2 mixed[kSlideWarps][ROW];
+
+  const int k0 = blockIdx.y * kSlideOut;
+  const long tr0 = static_cast<long>(blockIdx.x) * kSlideWarps;
+  const int n_base = k0 + p.gd - (NT - 1);       // input index of window sample 0
+
+  for (int s = threadIdx.x; s < W; s += blockDim.x) {
+    const int n = n_base + s;
+    float2 r = make_float2(0.f, 0.f);
+    if (n >= 0 && n < p.n_in) {
+      const float t = p.t0 + static_cast<float>(n) / p.fs;
+      const float ph = p.neg_two_pi_f * t;
+      float sv, cv;
+      sincosf(ph, &sv, &cv);
+      r = make_float2(cv, sv);
+    }
+    rot[s] = r;
+  }
+  // Raw samples first (independent loads in flight), then mix once the rotator is in.
+  constexpr int kPer = (kSlideWarps * W + 32 * kSlideWarps - 1) / (32 * kSlideWarps);
+  float x[kPer];
+#pragma unroll
+  for (int m = 0; m < kPer; ++m) {
+    const int q = threadIdx.x + m * 32 * kSlideWarps;
+    const int t = q / W, s = q - t * W;
+    const long tr = tr0 + t;
+    const int n = n_base + s;
+    x[m] = (q < kSlideWarps * W && tr < p.n_traces && n >= 0 && n < p.n_in) ? __ldg(p.rf + tr * p.n_in + n) : 0.f;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < kPer; ++m) {
+    const int q = threadIdx.x + m * 32 * kSlideWarps;
+    if (q < kSlideWarps * W) {
+      const int t = q / W, s = q - t * W;
+      const float2 r = rot[s];
+      mixed[t][slide_pos(s)] = make_float2(r.x * x[m], r.y * x[m]);
+    }
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long tr = tr0 + warp;
+  if (tr >= p.n_traces) return;
+  float2* row = mixed[warp];
+  float ar[kSlideR], ai[kSlideR];
+#pragma unroll
+  for (int r = 0; r < kSlideR; ++r) ar[r] = ai[r] = 0.f;
+  // Window sample i of this lane is s = 8*lane + i; output r uses tap
+  // j = r + NT - 1 - i, so descending i visits each output's taps in ascending j.
+#pragma unroll
+  for (int i = kSlideR + NT - 2; i >= 0; --i) {
+    const float2 v = row[slide_pos(kSlideR * lane + i)];
+#pragma unroll
+    for (int r = 0; r < kSlideR; ++r) {
+      const int j = r + NT - 1 - i;
+      if (j >= 0 && j < NT) {
+        ar[r] = fmaf(v.x, p.h[j], ar[r]);
+        ai[r] = fmaf(v.y, p.h[j], ai[r]);
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int r = 0; r < kSlideR; ++r) row[slide_pos(kSlideR * lane + r)] = make_float2(ar[r] * 2.0f, ai[r] * 2.0f);
+  __syncwarp();
+  float2* dst = p.iq + tr * p.n_out + k0;
+  const int n_here = min(kSlideOut, p.n_out - k0);
+#pragma unroll
+  for (int q = 0; q < kSlideR; ++q) {
+    const int o = lane + 32 * q;
+    if (o < n_here) dst[o] = row[slide_pos(o)];
+  }
+}
+
 }  // namespace
 }  // namespace usxcu
 
@@ -127,6 +228,20 @@ extern "C" int usx_cu_demodulate(usx_ctx* ctx, const usx_channel_desc* cd,
   p.t0 = cd->acq.t0;
   p.fs = fs;
   if (out_fdem) *out_fdem = fdem;
+  if (dec == 1 && (n_taps == 33 || n_taps == 21)) {
+    const long gx = (p.n_traces + kSlideWarps - 1) / kSlideWarps;
+    const int gy = ceil_div(p.n_out, kSlideOut);
+    if (gx > 0x7fffffffL || gy > 65535) return fail(USX_ERR_UNSUPPORTED, "usx_cu_demodulate: acquisition too large");
+    dim3 grid(static_cast<unsigned>(gx), static_cast<unsigned>(gy));
+    prof_begin(ctx, "demod_slide_kernel");
+    if (n_taps == 33)
+      demod_slide_kernel<33><<<grid, 32 * kSlideWarps, 0, ctx->stream>>>(p);
+    else
+      demod_slide_kernel<21><<<grid, 32 * kSlideWarps, 0, ctx->stream>>>(p);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("demod_slide_kernel");
+    return USX_OK;
+  }
   const int span = kOut * dec + n_taps - 1;
   const size_t smem = sizeof(float2) * static_cast<size_t>(span) * (1 + kTraces);
   if (smem > 48 * 1024)

@@ -98,7 +98,7 @@ struct FlowArgs {
   unsigned* pmax_bits;
 };
 
-__global__ void flow_kernel(const FlowArgs a) {
+__device__ __forceinline__ void flow_pixel(const FlowArgs& a) {
   const long k0 = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
   const long n_pix = static_cast<long>(a.n0) * a.n1;
   // Out-of-range lanes evaluate the last pixel but do not store, so that the
@@ -161,6 +161,8 @@ __global__ void flow_kernel(const FlowArgs a) {
   if ((threadIdx.x & 31) == 0) atomicMax(a.pmax_bits, m);
 }
 
+__global__ void flow_kernel(const FlowArgs a) { flow_pixel(a); }
+
 __global__ void power_gate_kernel(const float* power, uint8_t* valid, long n, float ratio,
                                   const unsigned* pmax_bits) {
   const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
@@ -169,6 +171,88 @@ __global__ void power_gate_kernel(const float* power, uint8_t* valid, long n, fl
   if (pmax > 0.0f) {
     const float thr = pmax * ratio;
     if (power[k] < thr) valid[k] = 0;
+  }
+}
+
+// Batched colour flow (usx_cu_color_flow_batch): all ensembles of one call
+// in one wall-filter launch, one flow launch and one gate launch. blockIdx.y
+// is the ensemble within a chunk; the per-ensemble lengths and offsets, and
+// the clutter projector of every distinct length (they depend only on the
+// length), ride in the kernel parameters. Per pixel the arithmetic is that
+// of wall_kernel / flow_kernel / power_gate_kernel, so every map equals the
+// one-ensemble path bit for bit.
+constexpr int kBatchEns = 64;      // ensembles per launch
+constexpr int kBatchPool = 6144;   // floats of projectors per launch (24 KB)
+
+struct WallBatchArgs {
+  const float2* ens;       // input frames, where the caller packed them
+  float2* out;             // filtered frames, packed back to back
+  long n_pix;
+  int identity;
+  int n[kBatchEns];
+  int m_off[kBatchEns];    // projector offset in M
+  long in_off[kBatchEns];  // first input frame of the ensemble
+  long out_off[kBatchEns]; // first filtered frame of the ensemble
+  float M[kBatchPool];
+};
+
+__global__ void wall_batch_kernel(const WallBatchArgs a) {
+  extern __shared__ float2 zs[];   // [n][blockDim]
+  const int e = blockIdx.y;
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= a.n_pix) return;
+  const int n = a.n[e];
+  const float2* src = a.ens + a.in_off[e] * a.n_pix;
+  float2* dst = a.out + a.out_off[e] * a.n_pix;
+  const float* M = a.M + a.m_off[e];
+  for (int j = 0; j < n; ++j) zs[j * blockDim.x + threadIdx.x] = src[j * a.n_pix + k];
+  for (int i = 0; i < n; ++i) {
+    cplx acc;
+    if (a.identity) {
+      const float2 z = zs[i * blockDim.x + threadIdx.x];
+      acc = mk(z.x, z.y);
+    } else {
+      acc = mk(0.f, 0.f);
+      for (int j = 0; j < n; ++j) {
+        const float2 z = zs[j * blockDim.x + threadIdx.x];
+        acc = cadd(acc, cscale(mk(z.x, z.y), M[i * n + j]));
+      }
+    }
+    dst[i * a.n_pix + k] = make_float2(acc.re, acc.im);
+  }
+}
+
+struct FlowBatchArgs {
+  FlowArgs base;         // filt = packed filtered frames; maps = [ensemble][pixel]
+  int n[kBatchEns];
+  int ens[kBatchEns];    // ensemble index of this chunk's entry (map row)
+  long f_off[kBatchEns];
+};
+
+__global__ void flow_batch_kernel(const FlowBatchArgs b) {
+  const int e = blockIdx.y;
+  FlowArgs a = b.base;
+  const long n_pix = static_cast<long>(a.n0) * a.n1;
+  const long row = b.ens[e];
+  a.n = b.n[e];
+  a.filt = b.base.filt + b.f_off[e] * n_pix;
+  a.velocity += row * n_pix;
+  a.power += row * n_pix;
+  a.variance += row * n_pix;
+  a.valid += row * n_pix;
+  a.pmax_bits += row;
+  flow_pixel(a);
+}
+
+__global__ void power_gate_batch_kernel(const float* power, uint8_t* valid, long n, float ratio,
+                                        const unsigned* pmax_bits) {
+  const long row = blockIdx.y;
+  const long k = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (k >= n) return;
+  const float pmax = __uint_as_float(pmax_bits[row]);
+  if (pmax > 0.0f) {
+    const float thr = pmax * ratio;
+    if (power[row * n + k] < thr) valid[row * n + k] = 0;
   }
 }
 
@@ -418,26 +502,109 @@ int usx_cu_color_flow_batch(usx_ctx* ctx, const float* ens, int n_ens, const int
                             float* power, float* variance, uint8_t* valid) {
   if (!ctx || !ens || !n_frames_host || !frame_offset_host || !cfg)
     return fail(USX_ERR_INVALID, "usx_cu_color_flow_batch: null argument");
+  if (n_ens <= 0) return USX_OK;
+  if (n_ens > 65535) return fail(USX_ERR_UNSUPPORTED, "usx_cu_color_flow_batch: more than 65535 ensembles");
+  if (!velocity || !power || !variance || !valid)
+    return fail(USX_ERR_INVALID, "usx_cu_color_flow_batch: null argument");
+  if (n0 <= 0 || n1 <= 0) return fail(USX_ERR_INVALID, "color_flow: empty grid");
   const long n_pix = static_cast<long>(n0) * n1;
-  long max_frames = 0;
+  int max_frames = 0;
+  long total_frames = 0;
   for (int e = 0; e < n_ens; ++e) {
     if (n_frames_host[e] < 2) return fail(USX_ERR_INVALID, "color_flow: need at least 2 frames in the ensemble");
-    max_frames = std::max<long>(max_frames, n_frames_host[e]);
+    if (frame_offset_host[e] < 0) return fail(USX_ERR_INVALID, "usx_cu_color_flow_batch: negative frame offset");
+    max_frames = std::max(max_frames, n_frames_host[e]);
+    total_frames += n_frames_host[e];
   }
+  if (max_frames > kMaxEns) return fail(USX_ERR_UNSUPPORTED, "ensembles longer than 64 frames are not supported");
+  // Filtered ensembles packed back to back, then one power maximum per ensemble.
+  const size_t filt_bytes = sizeof(float2) * static_cast<size_t>(n_pix) * static_cast<size_t>(total_frames);
   void* ws = nullptr;
-  if (int rc = scratch(ctx, sizeof(float2) * n_pix * max_frames + 256, &ws)) return rc;
-  float* filt = static_cast<float*>(ws);
-  for (int e = 0; e < n_ens; ++e) {
-    const float* src = ens + 2 * frame_offset_host[e] * n_pix;
-    if (int rc = launch_wall(ctx, src, n_frames_host[e], n_pix, cfg->wall_filter, cfg->polynomial_order,
-                             filt, nullptr))
-      return rc;
-    if (int rc = launch_flow(ctx, filt, n_frames_host[e], n0, n1, axial_step(axis1_host, n1), fdem, prf,
-                             speed_of_sound, *cfg, velocity + e * n_pix, power + e * n_pix,
-                             variance + e * n_pix, valid + e * n_pix,
-                             reinterpret_cast<unsigned*>(ctx->d_status + 10)))
-      return rc;
+  if (int rc = scratch(ctx, filt_bytes + sizeof(unsigned) * n_ens + 256, &ws)) return rc;
+  float2* filt = static_cast<float2*>(ws);
+  unsigned* pmax = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + filt_bytes);
+  USX_CUDA(cudaMemsetAsync(pmax, 0, sizeof(unsigned) * n_ens, ctx->stream));
+
+  const int type = cfg->wall_filter;
+  const int order = type == USX_WALL_MEAN ? 0 : cfg->polynomial_order;
+  const int threads = 128;
+  FlowBatchArgs fb;
+  FlowArgs& f = fb.base;
+  f.filt = filt;
+  f.n0 = n0;
+  f.n1 = n1;
+  f.ka = std::max(0, cfg->kernel_axial);
+  f.kl = std::max(0, cfg->kernel_lateral);
+  f.loupas = cfg->loupas;
+  f.dz = axial_step(axis1_host, n1);
+  f.fdem = fdem;
+  f.prf = prf;
+  f.c = speed_of_sound;
+  f.coh_thr = cfg->coherence_threshold;
+  f.velocity = velocity;
+  f.power = power;
+  f.variance = variance;
+  f.valid = valid;
+  f.pmax_bits = pmax;
+
+  // Chunks of at most kBatchEns ensembles whose distinct projectors fit the pool.
+  long packed = 0;  // first filtered frame of the next ensemble
+  int e0 = 0;
+  while (e0 < n_ens) {
+    WallBatchArgs w;
+    w.ens = reinterpret_cast<const float2*>(ens);
+    w.out = filt;
+    w.n_pix = n_pix;
+    w.identity = type == USX_WALL_NONE;
+    int pool = 0, count = 0, chunk_max = 0, n_have = 0;
+    int have_n[kBatchEns], have_off[kBatchEns];
+    for (int e = e0; e < n_ens && count < kBatchEns; ++e) {
+      const int n = n_frames_host[e];
+      int off = 0;
+      if (!w.identity) {
+        off = -1;
+        for (int q = 0; q < n_have; ++q)
+          if (have_n[q] == n) off = have_off[q];
+        if (off < 0) {
+          if (pool + n * n > kBatchPool) break;  // 64 x 64 alone always fits
+          const std::vector<float> M = reject_matrix(n, order);
+          std::copy(M.begin(), M.end(), w.M + pool);
+          off = pool;
+          have_n[n_have] = n;
+          have_off[n_have++] = pool;
+          pool += n * n;
+        }
+      }
+      w.n[count] = n;
+      w.m_off[count] = off;
+      w.in_off[count] = frame_offset_host[e];
+      w.out_off[count] = packed;
+      fb.n[count] = n;
+      fb.ens[count] = e;
+      fb.f_off[count] = packed;
+      packed += n;
+      chunk_max = std::max(chunk_max, n);
+      ++count;
+    }
+    const size_t smem = sizeof(float2) * static_cast<size_t>(chunk_max) * threads;
+    if (smem > 48 * 1024)
+      if (int rc_ = smem_limit(reinterpret_cast<const void*>(wall_batch_kernel), smem)) return rc_;
+    prof_begin(ctx, "wall_batch_kernel");
+    wall_batch_kernel<<<dim3(ceil_div(n_pix, threads), count), threads, smem, ctx->stream>>>(w);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("wall_batch_kernel");
+    prof_begin(ctx, "flow_batch_kernel");
+    flow_batch_kernel<<<dim3(ceil_div(n_pix, 128), count), 128, 0, ctx->stream>>>(fb);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("flow_batch_kernel");
+    e0 += count;
   }
+  const float ratio = std::pow(10.0f, cfg->power_threshold_db / 10.0f);
+  prof_begin(ctx, "power_gate_batch_kernel");
+  power_gate_batch_kernel<<<dim3(ceil_div(n_pix, 256), n_ens), 256, 0, ctx->stream>>>(power, valid, n_pix, ratio,
+                                                                                       pmax);
+  prof_end(ctx);
+  USX_CHECK_LAUNCH("power_gate_batch_kernel");
   return USX_OK;
 }
 

@@ -251,8 +251,8 @@ Frame Beamformer::beamform(const ChannelData& data, const ScanGrid& grid, int ev
   return beamform_device(data, upload(data), grid, event_begin, event_end);
 }
 
-Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, const ScanGrid& grid,
-                                  int event_begin, int event_end) const {
+void Beamformer::beamform_into(const ChannelData& data, const void* d_in, const ScanGrid& grid, void* d_out,
+                               int event_begin, int event_end) const {
   data.validate();
   grid.validate();
   config_.validate();
@@ -260,12 +260,7 @@ Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, con
   if (event_end < 0) event_end = n_ev;
   event_begin = std::clamp(event_begin, 0, n_ev);
   event_end = std::clamp(event_end, event_begin, n_ev);
-  Frame frame;
-  frame.grid = grid;
-  frame.demodulation_frequency = data.is_iq ? data.demodulation_frequency : 0.0f;
-  frame.allocate();
   usx_bf_plan* plan = plans_->get(data, grid, config_, event_begin, event_end);
-  void* d_out = rt::slot(4, frame.data.size() * sizeof(cplx));
   // A plan's first frame of a large acquisition picks the delay-and-sum launch
   // shape by timing each variant on it (the frame is the chosen variant's).
   const double work = static_cast<double>(grid.n_pixels()) * (event_end - event_begin) * data.n_channels();
@@ -273,6 +268,16 @@ Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, con
     rt::check(usx_cu_bf_plan_autotune(plan, d_in, static_cast<float*>(d_out), 1, nullptr), "beamform autotune");
   else
     rt::check(usx_cu_bf_execute(plan, d_in, static_cast<float*>(d_out)), "beamform");
+}
+
+Frame Beamformer::beamform_device(const ChannelData& data, const void* d_in, const ScanGrid& grid,
+                                  int event_begin, int event_end) const {
+  Frame frame;
+  frame.grid = grid;
+  frame.demodulation_frequency = data.is_iq ? data.demodulation_frequency : 0.0f;
+  frame.allocate();
+  void* d_out = rt::slot(4, frame.data.size() * sizeof(cplx));
+  beamform_into(data, d_in, grid, d_out, event_begin, event_end);
   rt::d2h(frame.data.data(), d_out, frame.data.size() * sizeof(cplx));
   return frame;
 }

@@ -49,6 +49,10 @@ class Beamformer {
   // points at the matching samples already in GPU memory.
   Frame beamform_device(const ChannelData& meta, const void* device_data, const ScanGrid& grid,
                         int event_begin = 0, int event_end = -1) const;
+  // As beamform_device, but the frame stays on the device: written to
+  // `device_frame` ([n_axis0][n_axis1] complex), nothing is copied back.
+  void beamform_into(const ChannelData& meta, const void* device_data, const ScanGrid& grid,
+                     void* device_frame, int event_begin = 0, int event_end = -1) const;
 
   const BeamformerConfig& config() const { return config_; }
   BeamformerConfig& config() { return config_; }

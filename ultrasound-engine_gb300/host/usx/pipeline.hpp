@@ -11,6 +11,7 @@
 #include "usx/demodulate.hpp"
 #include "usx/doppler.hpp"
 #include "usx/postprocess.hpp"
+#include "usx/runtime.hpp"
 #include "usx/types.hpp"
 
 namespace usx {
@@ -48,12 +49,19 @@ class ImagingPipeline {
   void reset();
 
  private:
+  // The acquisition on the device, demodulated if it was RF; `meta` describes it.
+  const void* to_device_iq(const ChannelData& data, ChannelData& meta);
+  // Envelope, TGC, peak and log compression of a device frame on `grid`; only
+  // the peak (4 bytes) and the display image come back to the host.
+  std::vector<real> display_device(const void* d_frame, const ScanGrid& grid, real fdem, const Medium& medium);
+
   ScanGrid grid_;
   PipelineConfig config_;
   Beamformer beamformer_;
   PipelineStats stats_;
   real reference_ = 0.0f;
   std::int64_t frame_count_ = 0;
+  std::shared_ptr<rt::DeviceBuffer> grid_points_;  // grid_'s points on the device, uploaded once
 };
 
 }  // namespace usx
