@@ -431,6 +431,7 @@ def run_ours(args) -> None:
         mlp = learned.load_mlp(ctx, WEIGHTS)
         gate = learned.trained_gate(WEIGHTS) if args.gate is None else args.gate
         refine = learned.trained_refine(WEIGHTS) if args.refine is None else args.refine
+        share = learned.trained_share_gate(WEIGHTS) if args.share_gate is None else args.share_gate
         # Plain minimum variance (tensor-core solver) on the same frame, timed first.
         plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
         plain.set_mv_mode(1)
@@ -444,10 +445,12 @@ def run_ours(args) -> None:
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         plan.set_learned(mlp, gate)
         plan.set_learned_refine(refine)
+        plan.set_learned_subspace(True, share)
         extra["plain_mv"] = {"value": world * args.steps / (plain_ms / 1e3) * N0 / n0, "unit": "frames/s",
                              "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": "tensor"}
         extra["gate"] = gate
         extra["refine_beams"] = refine
+        extra["share_gate"] = share
     else:
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         if args.workload == "mv":
@@ -485,19 +488,29 @@ def run_ours(args) -> None:
         rep = WEIGHTS.with_suffix(".json")
         if rep.exists():
             r = json.loads(rep.read_text())
-            ev = r.get("eval", {}).get(str(gate)) or r.get("eval", {}).get(repr(gate))
+            label = learned.Mode(gate=float(gate), share=float(share)).label
+            ev = r.get("eval", {}).get(label)
             if ev:
                 extra["held_out_quality"] = {
-                    "phantoms": ev.get("phantoms"), "fallback_rate": ev.get("fallback_rate"),
+                    "mode": label, "phantoms": ev.get("phantoms"), "fallback_rate": ev.get("fallback_rate"),
                     "max_abs_delta_gcnr": ev.get("gcnr", {}).get("max_abs_delta"),
                     "max_rel_delta_lateral_fwhm": ev.get("lateral_fwhm_mm", {}).get("max_rel_delta"),
+                    "max_rel_delta_axial_fwhm": ev.get("axial_fwhm_mm", {}).get("max_rel_delta"),
+                    "meets_bar": r.get("meets_bar") if r.get("chosen") == label else None,
                     "source": str(rep.relative_to(ROOT))}
+            ab = r.get("eval", {}).get("beams_only")
+            if ab:
+                extra["held_out_beams_only"] = {
+                    "max_abs_delta_gcnr": ab.get("gcnr", {}).get("max_abs_delta"),
+                    "max_rel_delta_lateral_fwhm": ab.get("lateral_fwhm_mm", {}).get("max_rel_delta"),
+                    "rel_l2_mean": ab.get("rel_l2_mean")}
 
     peaks = load_peaks()
     launches_in_region = sum(n for _, n in prof.values())
     roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks, extra.get("refine_beams", -1))
 
-    e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world)
+    e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world,
+                                           (gate, refine, share) if args.workload == "learned" else None)
     if bkw.get("combiner") == 2:
         fp64, failed = plan.mv_stats()
         roofline["mv_fp64_resolves_per_frame"] = fp64 / max(1, args.steps + args.warmup)
@@ -1207,6 +1220,7 @@ def run_mixed(args) -> None:
     lin = ctx.plan(ch_iq, cgrid, capi.bf_config(**LEARNED_KW))
     lin.set_learned(mlp, learned.trained_gate(WEIGHTS))
     lin.set_learned_refine(learned.trained_refine(WEIGHTS))
+    lin.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
     f_lin = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
     lin.autotune(iq_lin.data_ptr(), f_lin.data_ptr(), repeats=1)
     # Sector: 64-element phased array.
@@ -1241,6 +1255,7 @@ def run_mixed(args) -> None:
     sec = ctx.plan(sch_iq, scg, capi.bf_config(combiner=learned.COMB_LEARNED_MV, **sector_mv))
     sec.set_learned(mlp, learned.trained_gate(WEIGHTS))
     sec.set_learned_refine(learned.trained_refine(WEIGHTS))
+    sec.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
     sec.autotune(iq_sec.data_ptr(), f_sec.data_ptr(), repeats=1)
     env, logi = torch.empty((256, 1024), device="cuda"), torch.empty((256, 1024), device="cuda")
     img = torch.empty((800, 800), device="cuda")
@@ -1314,12 +1329,15 @@ def run_mixed(args) -> None:
     ctx.close()
 
 
-def run_e2e(usx, grid, raw, rf_host, args, world):
-    """The same frame through the public API with host buffers: RF up, frame back."""
+def run_e2e(usx, grid, raw, rf_host, args, world, learned=None):
+    """The same frame through the public API with host buffers: RF up, frame back.
+    `learned` = (gate, refine beams, share gate) of the device-timed plan."""
     import torch
-    os.environ["USX_MV_SOLVER"] = "exact" if args.workload == "mv_exact" else "tensor"
     pcfg = usx.PipelineConfig()
     b = pcfg.beamformer
+    b.mv_solver = usx.MvSolver.EXACT if args.workload == "mv_exact" else usx.MvSolver.TENSOR
+    if learned is not None:
+        b.learned_gate, b.learned_refine, b.learned_share_gate = learned
     kw = WORKLOADS[args.workload]
     b.f_number = kw["f_number"]
     b.combiner = usx.Combiner(kw.get("combiner", 0))
@@ -1355,6 +1373,8 @@ def main() -> int:
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
     ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
+    ap.add_argument("--share-gate", type=float, default=None,
+                    help="learned workload: gate on the network direction's share (default: report)")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -204,6 +204,15 @@ int usx_cu_bf_plan_set_learned(usx_bf_plan* plan, usx_mlp* mlp, float gate);
  *                    variance when w~ is the Capon direction; always
  *                    distortionless. */
 int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams);
+/* The refinement's second gate and its ablation (no counterpart in the
+ * reference). With y = L^-1 Q^H 1 from the factor of the subspace system,
+ * the subspace's Capon output power is 1/|y|^2 and that of the DFT beams
+ * alone 1/|y_beams|^2, so s = |y_net|^2 / |y|^2 is the share of the output
+ * power the network's direction removed. A pixel whose s exceeds
+ * max_network_share goes to the exact minimum variance (its optimum lies well
+ * outside the beams' span). use_network = 0 solves within the beams alone.
+ * Defaults: use_network = 1, max_network_share = +inf (no second gate). */
+int usx_cu_bf_plan_set_learned_subspace(usx_bf_plan* plan, int use_network, float max_network_share);
 /* Pixels gated to the exact solver and pixels beamformed by the learned path
  * since the last call (synchronises). */
 int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels);

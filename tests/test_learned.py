@@ -528,3 +528,68 @@ def test_training_gains_over_uniform_weights(capi, torch):
         assert res["trained"][1] < res["uniform"][1], res
     finally:
         im.close()
+
+
+@pytest.mark.gpu
+def test_shipped_network_gains_over_the_beams_alone(capi, torch):
+    """The shipped configuration (the shipped network, the subspace refinement
+    with its recorded beams, 128 channels, 75 plane waves, 512 x 1024) against
+    the same refinement without the network's direction, on two held-out
+    phantoms: with the network the frame is closer to plain minimum variance
+    (relative L2), i.e. the trained network is what the method gains over the
+    DFT beams alone."""
+    from usx import learned
+    if not learned.DEFAULT_WEIGHTS.exists():
+        pytest.fail("the shipped network weights are missing")
+    im = learned.Imager(learned.Setup())
+    try:
+        mlp = learned.load_mlp(im.ctx)
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        plan.set_learned(mlp, float("inf"))
+        plan.set_learned_refine(max(0, learned.trained_refine()))
+        err = {True: [], False: []}
+        for seed in (900_000, 900_001):
+            im.acquire(learned.phantom(seed, im.setup), noise_seed=seed)
+            mv = im.beamform(learned.COMB_MV)
+            for use_net in (True, False):
+                plan.set_learned_subspace(use_net, float("inf"))
+                lf = im.beamform(learned.COMB_LEARNED_MV)
+                err[use_net].append(float((lf - mv).abs().pow(2).sum().sqrt() / mv.abs().pow(2).sum().sqrt()))
+        assert np.mean(err[True]) < 0.9 * np.mean(err[False]), err
+        mlp.close()
+    finally:
+        im.close()
+
+
+@pytest.mark.gpu
+def test_share_gate_sends_pixels_to_the_exact_solver(capi, torch):
+    """The gate on the network direction's share of the power reduction: at 0
+    every pixel whose refinement used the network goes to the exact solver,
+    and the frame is then plain minimum variance wherever it did; at +inf no
+    pixel is gated by it; in between the fallback rate falls as the gate rises."""
+    from usx import learned
+    im = learned.Imager(learned.Setup(n_tx=15, depth=0.04, n0=128, n1=256))
+    try:
+        mlp = learned.load_mlp(im.ctx)
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        plan.set_learned(mlp, float("inf"))
+        plan.set_learned_refine(6)
+        im.acquire(learned.phantom(31, im.setup))
+        mv = im.beamform(learned.COMB_MV)
+        rates = []
+        for share in (0.0, 0.05, 0.3, float("inf")):
+            plan.set_learned_subspace(True, share)
+            plan.learned_stats()
+            lf = im.beamform(learned.COMB_LEARNED_MV)
+            gated, pixels = plan.learned_stats()
+            rates.append(gated / max(1, pixels))
+            if share == 0.0:
+                err0 = float((lf - mv).abs().pow(2).sum().sqrt() / mv.abs().pow(2).sum().sqrt())
+        assert rates[0] > 0.5 and rates[-1] < 1e-3, rates
+        assert rates[0] >= rates[1] >= rates[2] >= rates[3], rates
+        assert err0 < 2e-3, err0
+        with pytest.raises(ValueError):
+            plan.set_learned_subspace(True, -1.0)
+        mlp.close()
+    finally:
+        im.close()

@@ -1015,6 +1015,8 @@ struct usx_bf_plan {
   usx_mlp* mlp = nullptr;
   float lmv_gate = 0.05f;
   int lmv_beams = -1;   // < 0: the network's weights as predicted; >= 0: subspace refinement
+  int lmv_use_net = 1;  // 0: the refinement's basis without the network's direction
+  float lmv_share_gate = INFINITY;  // largest share of the refinement's power reduction from the network
   int64_t lmv_pixels = 0;      // pixels beamformed by the learned path since the last stats read
   // Training export (minimum variance plans): features, weights, valid flags.
   float* exp_feat = nullptr;
@@ -1250,7 +1252,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       if (int rc = mlp_infer(plan->mlp, ctx, feat16, npad, bufs[4], bufs[5], net)) return rc;
       USX_CUDA(cudaMemsetAsync(counters, 0, (kLmvGateClasses + 2) * sizeof(int), ctx->stream));
       if (plan->lmv_beams >= 0) {
-        if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate, counters,
+        if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate,
+                                         plan->lmv_use_net, plan->lmv_share_gate, counters,
                                          gated, static_cast<int>(nrows), plan->d_mv_stats + 2,
                                          static_cast<float*>(bufs[10])))
           return rc;
@@ -1591,6 +1594,15 @@ int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams) {
   if (n_beams > 6 || (n_beams >= 0 && n_beams % 2 != 0))
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_refine: n_beams must be negative, 0, 2, 4 or 6");
   plan->lmv_beams = n_beams < 0 ? -1 : n_beams;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_learned_subspace(usx_bf_plan* plan, int use_network, float max_network_share) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_subspace: null plan");
+  if (!(max_network_share >= 0.0f))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_subspace: max_network_share must be >= 0");
+  plan->lmv_use_net = use_network ? 1 : 0;
+  plan->lmv_share_gate = max_network_share;
   return USX_OK;
 }
 

@@ -165,9 +165,11 @@ __global__ void __launch_bounds__(32 * kSlideWarps) demod_slide_kernel(const Dem
   const long tr = tr0 + warp;
   if (tr >= p.n_traces) return;
   float2* row = mixed[warp];
-  float ar[kSlideR], ai[kSlideR];
+  // (re, im) of each output accumulate as one packed pair (two FP32 FMAs per
+  // instruction, each rounded as fmaf).
+  float2 acc[kSlideR];
 #pragma unroll
-  for (int r = 0; r < kSlideR; ++r) ar[r] = ai[r] = 0.f;
+  for (int r = 0; r < kSlideR; ++r) acc[r] = make_float2(0.f, 0.f);
   // Window sample i of this lane is s = 8*lane + i; output r uses tap
   // j = r + NT - 1 - i, so descending i visits each output's taps in ascending j.
 #pragma unroll
@@ -176,15 +178,13 @@ __global__ void __launch_bounds__(32 * kSlideWarps) demod_slide_kernel(const Dem
 #pragma unroll
     for (int r = 0; r < kSlideR; ++r) {
       const int j = r + NT - 1 - i;
-      if (j >= 0 && j < NT) {
-        ar[r] = fmaf(v.x, p.h[j], ar[r]);
-        ai[r] = fmaf(v.y, p.h[j], ai[r]);
-      }
+      if (j >= 0 && j < NT) acc[r] = __ffma2_rn(v, make_float2(p.h[j], p.h[j]), acc[r]);
     }
   }
   __syncwarp();
 #pragma unroll
-  for (int r = 0; r < kSlideR; ++r) row[slide_pos(kSlideR * lane + r)] = make_float2(ar[r] * 2.0f, ai[r] * 2.0f);
+  for (int r = 0; r < kSlideR; ++r)
+    row[slide_pos(kSlideR * lane + r)] = make_float2(acc[r].x * 2.0f, acc[r].y * 2.0f);
   __syncwarp();
   float2* dst = p.iq + tr * p.n_out + k0;
   const int n_here = min(kSlideOut, p.n_out - k0);

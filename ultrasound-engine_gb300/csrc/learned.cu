@@ -351,6 +351,8 @@ struct SubArgs {
   int range_avg, n_beams;
   float f_number, tukey_alpha, half_nm1, pitch, loading, gate;
   int rx_window;
+  int use_net;            // 0: the beams alone (the network's direction left out)
+  float share_gate;       // largest share of the power reduction the network's direction may carry
   int* gated_count;
   int2* gated;
   int gated_cap;
@@ -564,7 +566,7 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       }
       float n1 = wv[0].x * wv[0].x + wv[0].y * wv[0].y + wv[1].x * wv[1].x + wv[1].y * wv[1].y;
       for (int o2 = 16; o2 > 0; o2 >>= 1) n1 += __shfl_xor_sync(0xffffffffu, n1, o2);
-      const float sc = (n0 > 0.f && n1 > 1e-4f * n0) ? rsqrtf(n1) : 0.f;
+      const float sc = (a.use_net && n0 > 0.f && n1 > 1e-4f * n0) ? rsqrtf(n1) : 0.f;
       wv[0] = make_float2(wv[0].x * sc, wv[0].y * sc);
       wv[1] = make_float2(wv[1].x * sc, wv[1].y * sc);
       sm.qq[i0] = make_float4(wv[0].x, wv[0].x, wv[0].y, wv[0].y);   // kLmvMaxL = 64: lanes cover every i
@@ -914,6 +916,21 @@ __global__ void lmv_subspace_solve_kernel(const SubArgs a) {
     }
     cv[r] = make_float2(sv.x / A[r][r].x, sv.y / A[r][r].x);
   }
+  // The gate on the network's share: with y = L^-1 Q^H 1, the subspace's
+  // Capon output power is 1 / |y|^2, and that of the beams alone is
+  // 1 / |y_beams|^2 (the leading block of the factor is the beams' factor),
+  // so |y_w|^2 / |y|^2 is the fraction of the output power the network's
+  // direction removed. Where that fraction is large the optimum lies well
+  // outside the beams' span and the subspace solve may still miss it: the
+  // pixel goes to the exact solver.
+  bool share_ok = true;
+  if (has_w) {
+    float tot = 0.f;
+#pragma unroll
+    for (int k = 0; k < K1; ++k) tot += cv[k].x * cv[k].x + cv[k].y * cv[k].y;
+    const float net = cv[NB].x * cv[NB].x + cv[NB].y * cv[NB].y;
+    share_ok = !(net > a.share_gate * tot);
+  }
 #pragma unroll
   for (int r = K1 - 1; r >= 0; --r) {
     float2 sv = cv[r];
@@ -941,7 +958,7 @@ __global__ void lmv_subspace_solve_kernel(const SubArgs a) {
   const long frame = row / a.n_pix;
   const int pix = static_cast<int>(row - frame * a.n_pix);
   const float dn = den.x * den.x + den.y * den.y;
-  if (!ok || !(dn > 1e-30f)) {
+  if (!ok || !(dn > 1e-30f) || !share_ok) {
     push_gated(a.gated_count, a.gated, a.gated_cap, L, pix, frame);
     if (a.stats) atomicAdd(a.stats, 1);
     return;
@@ -1028,7 +1045,8 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 
 
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats, float* rec) {
+                        float gate, int use_net, float share_gate, int* gated_count, int2* gated, int gated_cap,
+                        int* stats, float* rec) {
   SubArgs a;
   a.y = l.y;
   a.points = l.points;
@@ -1050,6 +1068,8 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.pitch = l.pitch;
   a.loading = loading;
   a.gate = gate;
+  a.use_net = use_net;
+  a.share_gate = share_gate;
   a.rx_window = l.rx_window;
   a.gated_count = gated_count;
   a.gated = gated;

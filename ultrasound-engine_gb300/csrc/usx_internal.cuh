@@ -318,9 +318,12 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
                      int gated_cap, int* stats);
 // Learned-subspace refinement: gate on the network's distortionless residual,
 // then the exact Capon solve within span{1, network weights, n_beams DFT
-// beams} through the pixel's snapshots (learned.cu).
+// beams} through the pixel's snapshots, gated again on the share of the
+// output-power reduction the network's direction carries (learned.cu).
+// use_net = 0 leaves the network's direction out (the beams alone).
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int* gated_count, int2* gated, int gated_cap, int* stats, float* rec);
+                        float gate, int use_net, float share_gate, int* gated_count, int2* gated, int gated_cap,
+                        int* stats, float* rec);
 // Bytes per pixel of the scratch record launch_lmv_subspace passes between its two stages.
 int lmv_subspace_record_bytes(int n_beams);
 

@@ -66,6 +66,8 @@ PYBIND11_MODULE(_usx, m) {
       .value("PLANE_WAVE", TransmitType::PlaneWave)
       .value("DIVERGING", TransmitType::Diverging);
   py::enum_<GridType>(m, "GridType").value("CARTESIAN", GridType::Cartesian).value("SECTOR", GridType::Sector);
+  py::enum_<MvSolver>(m, "MvSolver").value("TENSOR", MvSolver::Tensor).value("EXACT", MvSolver::Exact);
+
   py::enum_<Combiner>(m, "Combiner")
       .value("DAS", Combiner::DAS)
       .value("DMAS", Combiner::DMAS)
@@ -371,7 +373,11 @@ PYBIND11_MODULE(_usx, m) {
       .def_readwrite("coherence_factor", &BeamformerConfig::coherence_factor)
       .def_readwrite("mv_subarray", &BeamformerConfig::mv_subarray)
       .def_readwrite("mv_diagonal_loading", &BeamformerConfig::mv_diagonal_loading)
-      .def_readwrite("mv_range_average", &BeamformerConfig::mv_range_average);
+      .def_readwrite("mv_range_average", &BeamformerConfig::mv_range_average)
+      .def_readwrite("mv_solver", &BeamformerConfig::mv_solver)
+      .def_readwrite("learned_gate", &BeamformerConfig::learned_gate)
+      .def_readwrite("learned_refine", &BeamformerConfig::learned_refine)
+      .def_readwrite("learned_share_gate", &BeamformerConfig::learned_share_gate);
 
   py::class_<Beamformer>(m, "Beamformer")
       .def(py::init<BeamformerConfig>(), py::arg("config") = BeamformerConfig{})

@@ -8,6 +8,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -37,16 +38,17 @@ namespace {
 
 // The learned minimum-variance network of a context: read once from
 // USX_LEARNED_MV_WEIGHTS, else the weights shipped beside the library
-// (<package>/weights/learned_mv_128ch_l64.bin); its gate and subspace
-// refinement from the ".gate" file written with the weights ("<gate>
-// [<beams>]"), overridden by USX_LEARNED_MV_GATE / USX_LEARNED_MV_REFINE;
-// without either, gate 0.05 and no refinement. The weights file is the
-// trainer's raw format: "USXMLP1\0", int32 n_layers, int32 dims[n_layers + 1],
-// float32 parameters.
+// (<package>/weights/learned_mv_128ch_l64.bin), with the gates and subspace
+// refinement recorded in the ".gate" file written with the weights
+// ("<gate> [<beams> [<share gate>]]"); without it, gate 0.05, no refinement
+// and no share gate. BeamformerConfig's learned_* fields override these per
+// beamformer. The weights file is the trainer's raw format: "USXMLP1\0",
+// int32 n_layers, int32 dims[n_layers + 1], float32 parameters.
 struct LearnedNet {
   usx_mlp* mlp = nullptr;
   float gate = 0.05f;
   int refine = -1;   // DFT beams of the subspace refinement (< 0: none)
+  float share_gate = INFINITY;
 };
 
 std::string library_dir() {
@@ -87,15 +89,14 @@ LearnedNet learned_net(usx_ctx* ctx) {
   rt::check(usx_cu_mlp_create(ctx, n_layers, dims.data(), 0, &net.mlp), "learned network");
   rt::check(usx_cu_mlp_set_params(net.mlp, params.data()), "learned network weights");
   {
-    // "<gate> [<refine beams>]", as written by the trainer's evaluation.
+    // "<gate> [<refine beams> [<share gate>]]", as written by the trainer's evaluation.
     std::ifstream gf(path.substr(0, path.size() - 4) + ".gate");
     std::string gs;
     if (gf >> gs) net.gate = std::strtof(gs.c_str(), nullptr);
     int rv = 0;
     if (gf >> rv) net.refine = rv;
+    if (gf >> gs) net.share_gate = std::strtof(gs.c_str(), nullptr);
   }
-  if (const char* g = std::getenv("USX_LEARNED_MV_GATE")) net.gate = std::strtof(g, nullptr);
-  if (const char* r = std::getenv("USX_LEARNED_MV_REFINE")) net.refine = std::atoi(r);
   nets.emplace(ctx, net);
   return net;
 }
@@ -138,9 +139,12 @@ class PlanCache {
     put(&b, sizeof b);
     const int iq = data.is_iq ? 1 : 0;
     put(&iq, sizeof iq);
-    const char* solver = std::getenv("USX_MV_SOLVER");
-    const int exact_mv = solver && std::string(solver) == "exact" ? 1 : 0;
-    put(&exact_mv, sizeof exact_mv);  // the solver is frozen into the plan
+    // Settings frozen into the plan that the C descriptor does not carry.
+    const int solver = static_cast<int>(cfg.mv_solver);
+    put(&solver, sizeof solver);
+    put(&cfg.learned_gate, sizeof(real));
+    put(&cfg.learned_refine, sizeof(int));
+    put(&cfg.learned_share_gate, sizeof(real));
     put(&data.demodulation_frequency, sizeof(real));
     put(&ev_begin, sizeof ev_begin);
     put(&ev_end, sizeof ev_end);
@@ -175,18 +179,19 @@ class PlanCache {
     rt::check(usx_cu_bf_plan_create(key.ctx, &ch.cd, &g, desc::points(grid), &b, ev_begin, ev_end, &plan),
               "beamformer plan");
     // Minimum variance runs on the tensor cores (BF16 covariance, FP32
-    // refinement, FP64 re-solve where needed) unless USX_MV_SOLVER=exact asks
-    // for the reference's FP32 operation order.
-    if (cfg.combiner == Combiner::MV) {
-      const char* solver = std::getenv("USX_MV_SOLVER");
-      const bool exact = solver && std::string(solver) == "exact";
-      if (!exact) usx_cu_bf_plan_set_mv_mode(plan, USX_MV_TENSOR);  // unsupported shapes stay exact
-    }
+    // refinement, FP64 re-solve where needed) unless the config asks for the
+    // reference's FP32 operation order.
+    if (cfg.combiner == Combiner::MV && cfg.mv_solver == MvSolver::Tensor)
+      usx_cu_bf_plan_set_mv_mode(plan, USX_MV_TENSOR);  // unsupported shapes stay exact
     if (cfg.combiner == Combiner::LearnedMV) {
       try {
         const LearnedNet net = learned_net(key.ctx);
-        rt::check(usx_cu_bf_plan_set_learned(plan, net.mlp, net.gate), "learned minimum variance");
-        rt::check(usx_cu_bf_plan_set_learned_refine(plan, net.refine), "learned minimum variance refinement");
+        const float gate = cfg.learned_gate >= 0.0f ? cfg.learned_gate : net.gate;
+        const int refine = cfg.learned_refine != -2 ? cfg.learned_refine : net.refine;
+        const float share = cfg.learned_share_gate >= 0.0f ? cfg.learned_share_gate : net.share_gate;
+        rt::check(usx_cu_bf_plan_set_learned(plan, net.mlp, gate), "learned minimum variance");
+        rt::check(usx_cu_bf_plan_set_learned_refine(plan, refine), "learned minimum variance refinement");
+        rt::check(usx_cu_bf_plan_set_learned_subspace(plan, 1, share), "learned minimum variance share gate");
       } catch (...) {
         usx_cu_bf_plan_destroy(plan);
         throw;

@@ -16,6 +16,13 @@ namespace usx {
 enum class Combiner : std::uint8_t { DAS = 0, DMAS = 1, MV = 2, LearnedMV = 3 };
 enum class Compounding : std::uint8_t { Coherent = 0, Incoherent = 1, Select = 2 };
 
+// How minimum variance is solved (no counterpart in the reference, whose
+// solver is its FP32 Cholesky): Tensor = BF16 covariance on the tensor cores
+// with FP32 accumulation, one refinement step against the FP32 covariance and
+// an FP64 re-solve where it fails (within 1e-3 of the reference); Exact = the
+// reference's FP32 operation order (within 1e-4, several times slower).
+enum class MvSolver { Tensor = 0, Exact = 1 };
+
 struct BeamformerConfig {
   real f_number = 1.75f;
   Window rx_window = Window::Hann;
@@ -27,6 +34,16 @@ struct BeamformerConfig {
   int mv_subarray = 16;
   real mv_diagonal_loading = 1e-2f;
   int mv_range_average = 2;
+  // Fields below have no counterpart in the reference.
+  MvSolver mv_solver = MvSolver::Tensor;
+  // Learned minimum variance: the gate on the network's distortionless
+  // residual, the DFT beams of the subspace refinement (< 0: none) and the
+  // gate on the network direction's share of the power reduction. Negative
+  // gates and a refinement of -2 mean "as recorded with the weights" (their
+  // ".gate" file).
+  real learned_gate = -1.0f;
+  int learned_refine = -2;
+  real learned_share_gate = -1.0f;
   void validate() const;
 };
 

@@ -33,6 +33,7 @@ from ._usx import (  # noqa: F401
     GridType,
     ImagingPipeline,
     Medium,
+    MvSolver,
     Phantom,
     PipelineConfig,
     PipelineStats,

@@ -348,6 +348,14 @@ class Plan:
         solve within span{1, network weights, n_beams DFT beams}."""
         check(lib().usx_cu_bf_plan_set_learned_refine(self._h, int(n_beams)), "bf_plan_set_learned_refine")
 
+    def set_learned_subspace(self, use_network: bool = True, max_network_share: float = float("inf")) -> None:
+        """The refinement's basis with or without the network's direction, and
+        the gate on the share of the output-power reduction that direction
+        carries (pixels above it go to the exact solver)."""
+        check(lib().usx_cu_bf_plan_set_learned_subspace(self._h, int(bool(use_network)),
+                                                         C.c_float(max_network_share)),
+              "bf_plan_set_learned_subspace")
+
     def learned_stats(self):
         """(pixels gated to the exact solver, pixels beamformed) since the last call."""
         a, b = C.c_int64(), C.c_int64()

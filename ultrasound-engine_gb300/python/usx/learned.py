@@ -356,54 +356,97 @@ def image_metrics(frame, imager: Imager, spec: PhantomSpec) -> dict:
     return out
 
 
-def evaluate(imager: Imager, mlp: capi.Mlp, seeds, gates=(DEFAULT_GATE,), log=print,
+@dataclass(frozen=True)
+class Mode:
+    """One learned-MV setting evaluated against plain minimum variance: the gate
+    on the network's distortionless residual, the gate on the share of the
+    refinement's power reduction carried by the network's direction, and
+    whether that direction is in the refinement's basis at all (False: the
+    DFT beams alone, the ablation of the network)."""
+    gate: float = math.inf
+    share: float = math.inf
+    use_net: bool = True
+
+    @property
+    def label(self) -> str:
+        if not self.use_net:
+            return "beams_only"
+        return f"gate={self.gate:g},share={self.share:g}"
+
+
+def modes_for(gates=(), shares=(), ablation: bool = True) -> list:
+    out = [Mode(gate=float(g)) for g in gates] + [Mode(share=float(x)) for x in shares]
+    if ablation:
+        out.append(Mode(use_net=False))
+    seen, uniq = set(), []
+    for m in out:
+        if m.label not in seen:
+            seen.add(m.label)
+            uniq.append(m)
+    return uniq
+
+
+def evaluate(imager: Imager, mlp: capi.Mlp, seeds, modes=(Mode(),), log=print,
              refine: int = DEFAULT_REFINE) -> dict:
-    """Image metrics of plain MV and of the learned MV at each gate on the
-    held-out phantoms `seeds`: {gate: summary}."""
+    """Image metrics of plain MV and of the learned MV in each mode on the
+    held-out phantoms `seeds`: {mode label: summary}."""
     learned = imager.plan(COMB_LEARNED_MV)
     learned.set_learned_refine(refine)
-    rows = {g: [] for g in gates}
+    rows = {m.label: [] for m in modes}
     for s in seeds:
         spec = phantom(int(s), imager.setup)
         imager.acquire(spec, noise_seed=int(s))
         ref = imager.beamform(COMB_MV)
         a = image_metrics(ref, imager, spec)
-        for g in gates:
-            learned.set_learned(mlp, g)
+        for m in modes:
+            learned.set_learned(mlp, m.gate)
+            learned.set_learned_subspace(m.use_net, m.share)
             learned.learned_stats()
             lf = imager.beamform(COMB_LEARNED_MV)
             gated, pixels = learned.learned_stats()
             b = image_metrics(lf, imager, spec)
             d = {k: [y - x for x, y in zip(a[k], b[k])] for k in a}
-            rows[g].append({"seed": int(s), "plain": a, "learned": b, "delta": d,
-                            "fallback_rate": gated / max(1, pixels),
-                            "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt() / ref.abs().pow(2).sum().sqrt())})
+            rows[m.label].append({"seed": int(s), "plain": a, "learned": b, "delta": d,
+                                  "fallback_rate": gated / max(1, pixels),
+                                  "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt()
+                                                  / ref.abs().pow(2).sum().sqrt())})
+        learned.set_learned_subspace(True, math.inf)
         if log:
             log(f"phantom {s}: " + ", ".join(
-                f"gate {g}: fallback {rows[g][-1]['fallback_rate']:.3f} dgcnr "
-                f"{max([abs(v) for v in rows[g][-1]['delta']['gcnr']] or [0]):.4f}" for g in gates))
-    return {g: summarize(r) for g, r in rows.items()}
+                f"{m.label}: fallback {rows[m.label][-1]['fallback_rate']:.3f} dgcnr "
+                f"{max([abs(v) for v in rows[m.label][-1]['delta']['gcnr']] or [0]):.4f}" for m in modes))
+    return {label: summarize(r) for label, r in rows.items()}
 
 
 def meets_bar(r: dict, max_dgcnr: float = 0.01, max_fwhm: float = 0.01) -> bool:
     """Held-out summary within the quality bar: every cyst's |delta gCNR| <=
-    max_dgcnr, and the median over wire targets of |delta FWHM| / FWHM within
-    max_fwhm of plain minimum variance, laterally and axially (a single
-    wire's half-maximum crossing can jump past a side lobe; the summaries also
-    carry the mean and the maximum)."""
+    max_dgcnr and every wire's lateral and axial FWHM within max_fwhm
+    (relative) of plain minimum variance."""
     if r.get("gcnr", {}).get("max_abs_delta", 1.0) > max_dgcnr:
         return False
     for k in ("lateral_fwhm_mm", "axial_fwhm_mm"):
         m = r.get(k)
-        if m and m.get("median_rel_delta", 0.0) > max_fwhm:
+        if m and m.get("max_rel_delta", 0.0) > max_fwhm:
             return False
     return True
 
 
-def choose_gate(results: dict, max_dgcnr: float = 0.01) -> float | None:
-    """The largest gate whose held-out summary meets the quality bar."""
-    ok = [g for g, r in results.items() if meets_bar(r, max_dgcnr)]
-    return max(ok) if ok else None
+def choose_mode(results: dict, modes, max_dgcnr: float = 0.01, max_fwhm: float = 0.01):
+    """The network-using mode with the lowest fallback rate among those that
+    meet the bar; if none does, the one closest to it (smallest worst relative
+    FWHM change, then gCNR change), marked as not meeting it. Returns
+    (mode, meets_bar)."""
+    cands = [m for m in modes if m.use_net and m.label in results]
+    ok = [m for m in cands if meets_bar(results[m.label], max_dgcnr, max_fwhm)]
+    if ok:
+        return min(ok, key=lambda m: results[m.label]["fallback_rate"]), True
+
+    def worst(m):
+        r = results[m.label]
+        f = max(r.get(k, {}).get("max_rel_delta", 0.0) for k in ("lateral_fwhm_mm", "axial_fwhm_mm"))
+        return (max(f / max_fwhm, r.get("gcnr", {}).get("max_abs_delta", 1.0) / max_dgcnr),
+                r["fallback_rate"])
+    return (min(cands, key=worst), False) if cands else (None, False)
 
 
 def summarize(rows) -> dict:
@@ -451,12 +494,17 @@ def main(argv=None) -> None:
     e.add_argument("--weights", default=str(DEFAULT_WEIGHTS))
     e.add_argument("--phantoms", type=int, default=16)
     for p in (t, e):
-        p.add_argument("--gates", default="0.01,0.03,0.1,0.3,1,inf")
+        p.add_argument("--gates", default="0.1,0.3,inf",
+                       help="gates on the network's distortionless residual (share gate off)")
+        p.add_argument("--shares", default="0.02,0.05,0.1,0.2,0.3,0.5",
+                       help="gates on the network direction's share of the power reduction (residual gate off)")
         p.add_argument("--refine", type=int, default=DEFAULT_REFINE,
                        help="DFT beams beside the network's direction (-1: no refinement)")
         p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
     a = ap.parse_args(argv)
-    gates = tuple(float(g) for g in a.gates.split(","))
+    modes = modes_for([float(g) for g in a.gates.split(",") if g],
+                      [float(x) for x in a.shares.split(",") if x] if a.refine >= 0 else [],
+                      ablation=a.refine >= 0)
     imager = Imager()
     report = {"dims": list(DIMS), "setup": imager.setup.__dict__}
     eval_seeds = np.arange(900_000, 900_000 + (a.eval_phantoms if a.cmd == "train" else a.phantoms))
@@ -482,15 +530,18 @@ def main(argv=None) -> None:
         prev = out.with_suffix(".json")
         if prev.exists():  # keep the training record, replace the evaluation
             report = {**json.loads(prev.read_text()), **report}
-    results = evaluate(imager, mlp, eval_seeds, gates, refine=a.refine)
+    results = evaluate(imager, mlp, eval_seeds, modes, refine=a.refine)
     report["refine"] = a.refine
-    report["eval"] = {str(g): {k: v for k, v in r.items() if k != "rows"} for g, r in results.items()}
-    report["gate"] = choose_gate(results)
+    report["eval"] = {label: {k: v for k, v in r.items() if k != "rows"} for label, r in results.items()}
+    chosen, ok = choose_mode(results, modes)
+    report.pop("share_gate", None)
+    if chosen is not None:
+        report.update(gate=chosen.gate, share_gate=chosen.share, chosen=chosen.label, meets_bar=ok)
     path = Path(a.report) if a.report else out.with_suffix(".json")
     path.write_text(json.dumps(report, indent=1, default=float))
-    if report["gate"] is not None:
-        out.with_suffix(".gate").write_text(f"{report['gate']} {a.refine}\n")
-    print(json.dumps({"gate": report["gate"], "eval": report["eval"]}, default=float))
+    if chosen is not None:
+        out.with_suffix(".gate").write_text(f"{chosen.gate} {a.refine} {chosen.share}\n")
+    print(json.dumps({"chosen": report.get("chosen"), "meets_bar": ok, "eval": report["eval"]}, default=float))
     imager.close()
 
 
@@ -502,6 +553,16 @@ def trained_gate(weights=DEFAULT_WEIGHTS) -> float:
         if g is not None:
             return float(g)
     return DEFAULT_GATE
+
+
+def trained_share_gate(weights=DEFAULT_WEIGHTS) -> float:
+    """The gate on the network direction's share chosen with the weights (+inf: none)."""
+    p = Path(weights).with_suffix(".json")
+    if p.exists():
+        g = json.loads(p.read_text()).get("share_gate")
+        if g is not None:
+            return float(g)
+    return math.inf
 
 
 def trained_refine(weights=DEFAULT_WEIGHTS) -> int:
