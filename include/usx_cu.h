@@ -162,12 +162,17 @@ int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, i
 
 /* Minimum-variance solver of a plan (no counterpart in the reference, whose
  * one solver is combine_mv_windowed, beamformer.cpp:137-214):
- *   USX_MV_EXACT   FP32, the reference's operation order (default);
- *   USX_MV_TENSOR  BF16 covariance on the tensor cores with FP32 accumulation,
- *                  FP32 Cholesky, one refinement step against the FP32
- *                  covariance, FP64 re-solve where the refined residual fails.
- * Results of the two agree within 1e-3 relative L2. */
-enum { USX_MV_EXACT = 0, USX_MV_TENSOR = 1 };
+ *   USX_MV_EXACT       FP32, the reference's operation order (default);
+ *   USX_MV_TENSOR      BF16 covariance on the tensor cores with FP32
+ *                      accumulation (full frames: a batched Hermitian rank-K
+ *                      update on tcgen05, accumulators in tensor memory),
+ *                      FP32 Cholesky, one refinement step against the FP32
+ *                      covariance, FP64 re-solve where the refined residual
+ *                      fails;
+ *   USX_MV_TENSOR_MMA  the same with the covariance formed by warp-level
+ *                      mma.sync inside the solve kernel.
+ * Results agree within 1e-3 relative L2. */
+enum { USX_MV_EXACT = 0, USX_MV_TENSOR = 1, USX_MV_TENSOR_MMA = 2 };
 int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode);
 /* Counts since the last call (synchronises): pixels re-solved in FP64 and
  * pixels whose factorisation failed (these take the DAS sum). */

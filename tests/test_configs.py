@@ -285,6 +285,12 @@ def test_cfg2_minimum_variance_l64_on_full_lines(cfg2_run, capi, ctx, torch, orc
                                    axes=axes)
     assert rel_l2(tc, want) < TOL_MV_TC
     assert failed == 0
+    # The same solver with the covariance on warp-level mma.sync: the two
+    # tensor-core covariances sum the same BF16 products in another order.
+    mma, (_, failed2) = gpu_frame(capi, ctx, torch, s, r["iq"], pts, len(CFG2_LINES), 1024, MV64, mv_mode=2,
+                                  axes=axes)
+    assert rel_l2(mma, want) < TOL_MV_TC and failed2 == 0
+    assert rel_l2(tc, mma) < 1e-4
 
 
 # ---------------------------------------------------------------- config 4

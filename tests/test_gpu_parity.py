@@ -182,16 +182,19 @@ def test_exact_precision_matches_reference_to_the_ulp(capi, ctx, torch, golden, 
     assert rel_l2(got, g[f"bf_{name}"]) < (1e-5 if name == "mv" else 1e-6)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("name", ["mv", "mv_l4", "mv_cf"])
-def test_mv_tensor_cores_match_reference(capi, ctx, torch, golden, name):
-    """BF16 tensor-core covariance + FP32 refinement: within 1e-3 of the reference."""
+def test_mv_tensor_cores_match_reference(capi, ctx, torch, golden, name, mode):
+    """BF16 tensor-core covariance (mode 1: batched rank-K update on tcgen05;
+    mode 2: warp-level mma.sync) + FP32 refinement: within 1e-3 of the
+    reference."""
     g = golden("bf")
     s = golden("sim")
     pr, med, acq = sim_setup(s)
     ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
     grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
     plan = ctx.plan(ch, grid, capi.bf_config(**BF_CASES[name]))
-    plan.set_mv_mode(1)
+    plan.set_mv_mode(mode)
     out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
     d = dev(torch, g["iq"])
     plan.execute(d.data_ptr(), out.data_ptr())

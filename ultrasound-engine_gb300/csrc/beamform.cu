@@ -1302,7 +1302,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
   int2* fb_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes));
   int2* ov_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes) + up(fb_bytes));
   int* fb_count = reinterpret_cast<int*>(wsb + up(y_bytes) + up(acc_bytes) + 2 * up(fb_bytes));  // [0] FP64, [1] overflow
-  const bool tensor = plan->mv_mode == USX_MV_TENSOR &&
+  const bool tensor = (plan->mv_mode == USX_MV_TENSOR || plan->mv_mode == USX_MV_TENSOR_MMA) &&
                       mv_tc_supported(a.n_ch, a.mv_subarray, a.mv_range_average);
   const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
   const size_t smem = sizeof(MvShared) * kMvWarps;
@@ -1316,6 +1316,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     if (int rc = launch_das(b, fast ? "das_fast_kernel(mv export)" : "das_kernel(mv export)")) return rc;
     if (tensor) {
       MvTcExtra ex;
+      ex.cov_engine = plan->mv_mode == USX_MV_TENSOR_MMA ? 0 : 1;
       if (plan->exp_feat) {
         // Training pairs: features of every pixel and its Capon weights.
         LmvLaunch l;
@@ -1476,9 +1477,9 @@ int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_fr
 
 int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode) {
   if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: null plan");
-  if (mode != USX_MV_EXACT && mode != USX_MV_TENSOR)
+  if (mode != USX_MV_EXACT && mode != USX_MV_TENSOR && mode != USX_MV_TENSOR_MMA)
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: unknown mode");
-  if (mode == USX_MV_TENSOR &&
+  if (mode != USX_MV_EXACT &&
       !mv_tc_supported(plan->cd.probe.n_elements, plan->cfg.mv_subarray, plan->cfg.mv_range_average))
     return fail(USX_ERR_UNSUPPORTED, "tensor-core minimum variance supports <= 128 channels, L <= 64, range +/-4");
   plan->mv_mode = mode;
@@ -1611,7 +1612,7 @@ int usx_cu_bf_plan_set_training_export(usx_bf_plan* plan, float* features, float
   const bool any = features || weights || valid;
   if (any && !(features && weights && valid))
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_training_export: give all three buffers or none");
-  if (any && (plan->cfg.combiner != USX_COMB_MV || plan->mv_mode != USX_MV_TENSOR ||
+  if (any && (plan->cfg.combiner != USX_COMB_MV || plan->mv_mode == USX_MV_EXACT ||
               plan->cfg.compounding == USX_COMP_INCOHERENT))
     return fail(USX_ERR_INVALID,
                 "usx_cu_bf_plan_set_training_export: needs a coherent minimum-variance plan in USX_MV_TENSOR mode");

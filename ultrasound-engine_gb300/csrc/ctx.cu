@@ -224,6 +224,7 @@ int usx_cu_ctx_destroy(usx_ctx* ctx) {
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->mv_cov) cudaFree(ctx->mv_cov);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;

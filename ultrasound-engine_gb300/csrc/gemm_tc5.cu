@@ -19,6 +19,7 @@
 
 #include <algorithm>
 
+#include "tc5.cuh"
 #include "usx_internal.cuh"
 
 namespace usxcu {
@@ -38,26 +39,6 @@ struct Tc5Args {
   int* status;
 };
 
-__device__ __forceinline__ unsigned su32(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
-// 1024 bytes apart (stride byte offset), version 1.
-__device__ __forceinline__ uint64_t smem_desc(unsigned addr) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFFu);          // start address
-  d |= static_cast<uint64_t>(1u) << 16;                       // leading byte offset (unused with swizzle)
-  d |= static_cast<uint64_t>((1024u >> 4) & 0x3FFFu) << 32;   // stride byte offset
-  d |= static_cast<uint64_t>(1u) << 46;                       // version
-  d |= static_cast<uint64_t>(2u) << 61;                       // SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, M x N.
-__host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
-         (static_cast<uint32_t>(M >> 4) << 24);
-}
-
 __device__ __forceinline__ void cp16(void* smem, const void* g) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(su32(smem)), "l"(g));
 }
@@ -74,19 +55,6 @@ __device__ __forceinline__ void load_swizzled(char* dst, const __nv_bfloat16* sr
     cp16(d, src + r * ld + q * 8);
   }
   asm volatile("cp.async.commit_group;\n" ::);
-}
-
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-  for (long spin = 0; spin < (1L << 24); ++spin) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
 }
 
 template <int N>

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 
+#include "tc5.cuh"
 #include "usx_internal.cuh"
 
 namespace usxcu {
@@ -613,6 +614,12 @@ struct MvWarpArgs {
   int* overflow_count;    // pixels beyond the class limits (solved by mv_tc_kernel)
   int2* overflow;
   int overflow_cap;
+  // Class mode in chunks: items [item_begin, item_end) (item_end 0: all), and
+  // their covariances R~ from mv_cov_tc5_kernel ([item - item_begin][r_stride],
+  // packed lower triangle), or null to form them here on mma.sync.
+  long item_begin, item_end;
+  const float2* r_pre;
+  int r_stride;
 };
 
 __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarpArgs wa) {
@@ -630,9 +637,9 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
   const int nmax = wa.nmax;
 
   const long n_items = wa.pair_list ? static_cast<long>(min(*wa.pair_count, wa.pair_cap))
-                                    : static_cast<long>(wa.n_list) * wa.n_frames;
-  for (long item = static_cast<long>(blockIdx.x) * kWarpMvWarps + warp; item < n_items;
-       item += static_cast<long>(gridDim.x) * kWarpMvWarps) {
+                                    : (wa.item_end > 0 ? wa.item_end : static_cast<long>(wa.n_list) * wa.n_frames);
+  for (long item = (wa.pair_list ? 0 : wa.item_begin) + static_cast<long>(blockIdx.x) * kWarpMvWarps + warp;
+       item < n_items; item += static_cast<long>(gridDim.x) * kWarpMvWarps) {
     int pix;
     long frame;
     if (wa.pair_list) {
@@ -742,6 +749,13 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     int e2;
     frexpf(amax, &e2);
     const float sc = ldexpf(1.0f, -e2), sc2 = ldexpf(1.0f, -2 * e2);
+    const float inv_k = 1.0f / static_cast<float>(K);
+    if (wa.r_pre) {
+      // R~ from the tensor-core stage (same scale, same packing).
+      const float2* src = wa.r_pre + (item - wa.item_begin) * wa.r_stride;
+      for (int e = lane; e < L * (L + 1) / 2; e += 32) Rl[e] = src[e];
+      __syncwarp();
+    } else {
     // BF16 pairs: word (p, par, d, w) = (v[2w+par], v[2w+par+1]) of part p, scaled.
     const int words = lay.words;
     for (int k = lane; k < 4 * n_d * words; k += 32) {
@@ -761,7 +775,6 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     const int two_l = 2 * L;
     const int MT = (two_l + 15) / 16, NT = (two_l + 7) / 8;
     const int n_kstep = (n_sub + 15) / 16;
-    const float inv_k = 1.0f / static_cast<float>(K);
     for (int mt = 0; mt < MT; ++mt) {
       for (int nt0 = 2 * mt; nt0 < NT; nt0 += 8) {
         float acc[8][4];
@@ -811,6 +824,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       }
     }
     __syncwarp();
+    }  // covariance on mma.sync
 
     // ---- exact trace: channel t of a row appears in c(t) subarrays -------
     float tr = 0.0f;
@@ -1047,6 +1061,284 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       finish(out, cre, cim, inc);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// The covariance stage on the fifth-generation tensor cores
+// (mv_cov_tc5_kernel<P>): every pixel of a class gets its spatially smoothed
+// covariance as one batched Hermitian rank-K update, G = A A^T, where A is the
+// real 2L x K form of the pixel's snapshot matrix (rows 2i and 2i + 1: real
+// and imaginary part of subarray element i; column k = d * S8 + s: snapshot s
+// of range row d, S8 = n_sub rounded up to 8, zero past n_sub), in BF16
+// scaled by the power of two of mv_warp_kernel, accumulated in FP32 in tensor
+// memory. P pixels share one M = N = 128 tile (pixel q's rows at
+// q * 128 / P; the blocks that mix two pixels are never read). One thread
+// issues the tile's K / 16 tcgen05.mma (M = N = 128, K = 16) with the same
+// shared-memory operand as A and B and commits them to an mbarrier (bounded
+// wait); the four warps then read their TMEM lanes back and write
+//   R~[a][b] = (G[2a][2b] + G[2a+1][2b+1] + i (G[2a+1][2b] - G[2a][2b+1])) / K
+// in the packed lower triangle mv_warp_kernel uses (tri(b, a) = conj R~[a][b]).
+// The solve kernel reads it back (r_pre) for the trace, Cholesky, solves and
+// refinement. A is built from the pixel's staged FP32 rows: for a column
+// chunk (8 snapshots) and 8 consecutive elements, one thread slides a 15-sample
+// window (the Hankel structure: element i + 1 at snapshot s is element i at
+// s + 1) and writes 16-byte chunks in the 128-byte-swizzled K-major layout.
+
+constexpr int kCovThreads = 128;
+
+struct MvCovArgs {
+  MvTcArgs base;
+  const int* pix_list;
+  int n_list, n_frames;
+  long item_begin, item_end;
+  int lmax, nmax, kcap;     // class limits; K capacity (multiple of 64)
+  float2* r_out;            // [item - item_begin][r_stride]
+  int r_stride;
+  int* status;              // set on an mbarrier timeout
+};
+
+struct CovItem {
+  int valid, L, n_sub, n_d, s8, kq;   // kq = n_d * s8
+  float sc, inv_k;
+};
+
+__host__ __device__ inline int cov_ystride(int nmax) { return nmax + 16; }
+
+__host__ __device__ inline size_t cov_smem_bytes(int P, int n_dmax, int nmax, int kcap) {
+  return 1024 + static_cast<size_t>(kcap) * 256 +
+         sizeof(float2) * static_cast<size_t>(P) * n_dmax * cov_ystride(nmax) + sizeof(int) * P * nmax +
+         sizeof(CovItem) * P + 64;
+}
+
+template <int P>
+__global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovArgs c) {
+  constexpr int R = 128 / P;   // rows of one pixel's slot
+  extern __shared__ __align__(1024) char cov_raw[];
+  char* sA = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(cov_raw) + 1023) & ~uintptr_t(1023));
+  const MvTcArgs& a = c.base;
+  const int ystride = cov_ystride(c.nmax);
+  float2* yst = reinterpret_cast<float2*>(sA + static_cast<size_t>(c.kcap) * 256);
+  int* act_all = reinterpret_cast<int*>(yst + static_cast<size_t>(P) * a.n_dmax * ystride);
+  CovItem* items = reinterpret_cast<CovItem*>(act_all + P * c.nmax);
+  uint64_t* bar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(items + P) + 15) & ~uintptr_t(15));
+  unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(tmem_slot)),
+                 "r"(128));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(su32(bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tmem = *tmem_slot;
+  const uint32_t idesc = instr_desc(128, 128);
+  unsigned phase = 0;
+  const long n_items = c.item_end - c.item_begin;
+  const long n_tiles = (n_items + P - 1) / P;
+
+  for (long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    // ---- per pixel (warp q): aperture, subarray, range rows, staged rows --
+    if (warp < P) {
+      const int q = warp;
+      const long rel = tile * P + q;
+      CovItem it{};
+      if (rel < n_items) {
+        const long item = c.item_begin + rel;
+        const long frame = item / c.n_list;
+        const int pix = c.pix_list[item - frame * c.n_list];
+        const int j = pix % a.n1;
+        const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+        int* act = act_all + q * c.nmax;
+        int n_act = 0;
+        for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+          const int ch = c0 + lane;
+          bool on = false;
+          if (ch < a.n_ch)
+            on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                                 a.tukey_alpha) > 0.0f;
+          const unsigned m = __ballot_sync(0xffffffffu, on);
+          const int slot = n_act + __popc(m & ((1u << lane) - 1u));
+          if (on && slot < c.nmax) act[slot] = ch;
+          n_act += __popc(m);
+        }
+        __syncwarp();
+        int L = a.mv_subarray;
+        const int hi = max(2, n_act / 2);
+        if (L < 2) L = 2;
+        if (L > hi) L = hi;
+        // The solve kernel's rules: past the class limits (overflow) or fewer
+        // than 4 active channels, no covariance.
+        if (!(n_act > c.nmax || L > c.lmax || n_act < 4)) {
+          int dlo = -a.range_avg, dhi = a.range_avg;
+          while (j + dlo < 0) ++dlo;
+          while (j + dhi >= a.n1) --dhi;
+          const int n_d = dhi - dlo + 1;
+          const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
+          float amax = 0.0f;
+          for (int k = lane; k < n_d * ystride; k += 32) {
+            const int d = k / ystride, t = k - d * ystride;
+            float2 v = make_float2(0.f, 0.f);
+            if (t < n_act) {
+              v = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[t]];
+              amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
+            }
+            yst[(q * a.n_dmax + d) * ystride + t] = v;
+          }
+          for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+          if (amax > 0.0f) {
+            int e2;
+            frexpf(amax, &e2);
+            it.valid = 1;
+            it.L = L;
+            it.n_sub = n_act - L + 1;
+            it.n_d = n_d;
+            it.s8 = (it.n_sub + 7) & ~7;
+            it.kq = n_d * it.s8;
+            it.sc = ldexpf(1.0f, -e2);
+            it.inv_k = 1.0f / static_cast<float>(n_d * it.n_sub);
+          }
+        }
+      }
+      if (lane == 0) items[q] = it;
+    }
+    __syncthreads();
+    int ktile = 0;
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+      if (items[q].valid) {
+        any = true;
+        ktile = max(ktile, items[q].kq);
+      }
+    ktile = (ktile + 15) & ~15;
+    if (!any) {
+      __syncthreads();
+      continue;
+    }
+    // ---- build A: window units (q, d, column chunk, element block of 8) --
+    int off[P + 1];
+    off[0] = 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      const CovItem& it = items[q];
+      off[q + 1] = off[q] + (it.valid ? it.n_d * (it.s8 >> 3) * ((it.L + 7) >> 3) : 0);
+    }
+    for (int f = threadIdx.x; f < off[P]; f += kCovThreads) {
+      int q = 0;
+#pragma unroll
+      for (int z = 1; z < P; ++z)
+        if (f >= off[z]) q = z;
+      const CovItem& it = items[q];
+      int u = f - off[q];
+      const int nib = (it.L + 7) >> 3, nc = it.s8 >> 3;
+      const int ib = u % nib;
+      u /= nib;
+      const int cc = u % nc, d = u / nc;
+      const float2* y = yst + (q * a.n_dmax + d) * ystride + 8 * cc + 8 * ib;
+      float2 win[15];
+#pragma unroll
+      for (int t = 0; t < 15; ++t) win[t] = y[t];
+      const int s0 = 8 * cc, k0 = d * it.s8 + s0;
+      bool in[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) in[t] = s0 + t < it.n_sub;
+#pragma unroll
+      for (int ii = 0; ii < 8; ++ii) {
+        const int i = 8 * ib + ii;
+        if (i < it.L) {
+          uint32_t re[4], im[4];
+#pragma unroll
+          for (int t = 0; t < 8; t += 2) {
+            const float2 v0 = in[t] ? win[ii + t] : make_float2(0.f, 0.f);
+            const float2 v1 = in[t + 1] ? win[ii + t + 1] : make_float2(0.f, 0.f);
+            re[t >> 1] = pack_bf16(v0.x * it.sc, v1.x * it.sc);
+            im[t >> 1] = pack_bf16(v0.y * it.sc, v1.y * it.sc);
+          }
+          const int row = q * R + 2 * i;
+          *reinterpret_cast<uint4*>(sA + sw128_offset(128, row, k0)) = make_uint4(re[0], re[1], re[2], re[3]);
+          *reinterpret_cast<uint4*>(sA + sw128_offset(128, row + 1, k0)) = make_uint4(im[0], im[1], im[2], im[3]);
+        }
+      }
+    }
+    // Zero columns [kq, ktile) of each pixel's rows.
+    int zoff[P + 1];
+    zoff[0] = 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      const CovItem& it = items[q];
+      zoff[q + 1] = zoff[q] + (it.valid ? 2 * it.L * ((ktile - it.kq) >> 3) : 0);
+    }
+    for (int f = threadIdx.x; f < zoff[P]; f += kCovThreads) {
+      int q = 0;
+#pragma unroll
+      for (int z = 1; z < P; ++z)
+        if (f >= zoff[z]) q = z;
+      const CovItem& it = items[q];
+      const int u = f - zoff[q], nz = (ktile - it.kq) >> 3;
+      const int row = q * R + u / nz, k0 = it.kq + 8 * (u % nz);
+      *reinterpret_cast<uint4*>(sA + sw128_offset(128, row, k0)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const unsigned a0 = su32(sA);
+      for (int ks = 0; ks < ktile / 16; ++ks) {
+        const uint64_t dsc = smem_desc(a0 + (ks >> 2) * 128 * 128 + (ks & 3) * 32);
+        tc5_mma(tmem, dsc, dsc, idesc, ks > 0 ? 1u : 0u);
+      }
+      tc5_commit(su32(bar));
+    }
+    const bool ok = mbar_wait(su32(bar), phase);
+    if (__syncthreads_or(!ok)) {
+      // Timed out: record it, give the tile's MMAs one more bounded wait so
+      // that none is in flight when the TMEM is released, and stop.
+      if (threadIdx.x == 0) {
+        if (c.status) atomicExch(c.status, 1);
+        mbar_wait(su32(bar), phase);
+      }
+      break;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // ---- epilogue: warp w holds rows 32 w .. 32 w + 31 -------------------
+    {
+      const int q = (warp * 32) / R;
+      const CovItem& it = items[q];
+      const int ml0 = warp * 32 - q * R;     // first local row of this warp
+      if (it.valid && ml0 < 2 * it.L) {
+        const long rel = tile * P + q;
+        float2* dst = c.r_out + rel * c.r_stride;
+        const int ml = ml0 + lane, a_el = ml >> 1;
+        const bool even = (ml & 1) == 0;
+        const unsigned taddr = tmem + (static_cast<unsigned>(warp * 32) << 16) + static_cast<unsigned>(q * R);
+        for (int j0 = 0; j0 < 2 * it.L; j0 += 32) {
+          uint32_t r[32];
+          tc5_ld32(taddr + static_cast<unsigned>(j0), r);
+#pragma unroll
+          for (int t = 0; t < 32; t += 2) {
+            // Odd row's G[2a+1][2b], G[2a+1][2b+1] from the neighbouring lane.
+            const float g0 = __uint_as_float(r[t]), g1 = __uint_as_float(r[t + 1]);
+            const float o0 = __shfl_xor_sync(0xffffffffu, g0, 1);
+            const float o1 = __shfl_xor_sync(0xffffffffu, g1, 1);
+            const int b = (j0 + t) >> 1;
+            if (even && a_el < it.L && b < it.L && b >= a_el)
+              dst[tri(b, a_el)] = make_float2((g0 + o1) * it.inv_k, -(o0 - g1) * it.inv_k);
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+  }
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(128));
 }
 
 // FP64 re-solve of the pixels whose refined FP32 residual failed: covariance
@@ -1375,7 +1667,71 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
       w.overflow_count = extra.overflow_count;
       w.overflow = extra.overflow;
       w.overflow_cap = extra.overflow_cap;
-      if (int rc = launch_warp(w, static_cast<long>(k.count) * n_frames, "mv_warp_kernel")) return rc;
+      const long items = static_cast<long>(k.count) * n_frames;
+      const int kcap = (a.n_dmax * ((k.nmax + 7) & ~7) + 63) & ~63;
+      const int P_cov = 2 * k.lmax <= 32 ? 4 : (2 * k.lmax <= 64 ? 2 : 1);
+      // Classes whose operand tile does not fit shared memory keep the mma.sync covariance.
+      if (extra.cov_engine == 1 && 2 * k.lmax <= 128 && cov_smem_bytes(P_cov, a.n_dmax, k.nmax, kcap) <= 227 * 1024) {
+        // Covariances on tcgen05 in chunks whose R~ (about 96 MB) stays in L2
+        // until the solve kernel reads it.
+        const int P = P_cov;
+        const int r_stride = k.lmax * (k.lmax + 1) / 2;
+        const long chunk = std::max(1024L, static_cast<long>((96u << 20) / (sizeof(float2) * r_stride)));
+        const size_t need = sizeof(float2) * static_cast<size_t>(r_stride) * static_cast<size_t>(std::min(chunk, items));
+        if (need > ctx->mv_cov_bytes) {
+          if (ctx->mv_cov) {
+            USX_CUDA(cudaStreamSynchronize(ctx->stream));
+            USX_CUDA(cudaFree(ctx->mv_cov));
+            ctx->mv_cov = nullptr;
+            ctx->mv_cov_bytes = 0;
+          }
+          USX_CUDA(cudaMalloc(&ctx->mv_cov, need));
+          ctx->mv_cov_bytes = need;
+        }
+        MvCovArgs cv{};
+        cv.base = a;
+        cv.pix_list = k.pixels;
+        cv.n_list = k.count;
+        cv.n_frames = n_frames;
+        cv.lmax = k.lmax;
+        cv.nmax = k.nmax;
+        cv.kcap = kcap;
+        cv.r_out = static_cast<float2*>(ctx->mv_cov);
+        cv.r_stride = r_stride;
+        cv.status = ctx->d_status + 14;
+        const size_t smem = cov_smem_bytes(P, a.n_dmax, k.nmax, cv.kcap);
+        const void* kern = P == 4 ? reinterpret_cast<const void*>(mv_cov_tc5_kernel<4>)
+                         : P == 2 ? reinterpret_cast<const void*>(mv_cov_tc5_kernel<2>)
+                                  : reinterpret_cast<const void*>(mv_cov_tc5_kernel<1>);
+        if (int rc_ = smem_limit(kern, smem)) return rc_;
+        int per_sm = 0;
+        if (int rc_ = occupancy(kern, kCovThreads, smem, &per_sm)) return rc_;
+        // At most four CTAs per SM: each holds 128 of the SM's 512 TMEM columns.
+        const long resident = static_cast<long>(std::max(1, std::min(per_sm, 4))) * ctx->sm_count;
+        w.r_pre = static_cast<const float2*>(ctx->mv_cov);
+        w.r_stride = r_stride;
+        for (long i0 = 0; i0 < items; i0 += chunk) {
+          const long i1 = std::min(items, i0 + chunk);
+          cv.item_begin = i0;
+          cv.item_end = i1;
+          const long tiles = (i1 - i0 + P - 1) / P;
+          const unsigned grid = static_cast<unsigned>(std::max(1L, std::min(tiles, resident)));
+          prof_begin(ctx, "mv_cov_tc5_kernel");
+          if (P == 4)
+            mv_cov_tc5_kernel<4><<<grid, kCovThreads, smem, ctx->stream>>>(cv);
+          else if (P == 2)
+            mv_cov_tc5_kernel<2><<<grid, kCovThreads, smem, ctx->stream>>>(cv);
+          else
+            mv_cov_tc5_kernel<1><<<grid, kCovThreads, smem, ctx->stream>>>(cv);
+          prof_end(ctx);
+          USX_CHECK_LAUNCH("mv_cov_tc5_kernel");
+          w.item_begin = i0;
+          w.item_end = i1;
+          if (int rc = launch_warp(w, i1 - i0, "mv_warp_kernel")) return rc;
+        }
+        continue;
+      }
+      if (int rc = launch_warp(w, items, "mv_warp_kernel")) return rc;
     }
     MvTcArgs b = a;
     b.list = extra.overflow;

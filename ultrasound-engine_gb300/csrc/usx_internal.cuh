@@ -54,6 +54,8 @@ struct usx_ctx {
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
   int* d_status = nullptr;     // device-side status word written by kernels
+  void* mv_cov = nullptr;      // minimum variance: covariances between the tcgen05 and solve stages
+  size_t mv_cov_bytes = 0;
   int sm_count = 0;
   bool profiling = false;      // record CUDA events around every launch
   std::vector<usx_prof_rec> prof;
@@ -273,6 +275,7 @@ struct MvClass {
   int lmax = 0, nmax = 0;
 };
 struct MvTcExtra {
+  int cov_engine = 1;                // class mode: 1 = covariance on tcgen05, 0 = mma.sync in the solve kernel
   const int2* list = nullptr;
   const int* list_count = nullptr;
   int list_cap = 0;

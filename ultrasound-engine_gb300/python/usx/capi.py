@@ -312,7 +312,8 @@ class Plan:
         check(lib().usx_cu_bf_plan_set_precision(self._h, int(precision)), "bf_plan_set_precision")
 
     def set_mv_mode(self, mode: int) -> None:
-        """0: FP32 in the reference's order; 1: BF16 tensor-core covariance + refinement."""
+        """0: FP32 in the reference's order; 1: BF16 covariance on tcgen05 + refinement;
+        2: the same with the covariance on warp-level mma.sync."""
         check(lib().usx_cu_bf_plan_set_mv_mode(self._h, int(mode)), "bf_plan_set_mv_mode")
 
     def mv_stats(self):

@@ -431,11 +431,15 @@ def meets_bar(r: dict, max_dgcnr: float = 0.01, max_fwhm: float = 0.01) -> bool:
     return True
 
 
-def choose_mode(results: dict, modes, max_dgcnr: float = 0.01, max_fwhm: float = 0.01):
+def choose_mode(results: dict, modes, max_dgcnr: float = 0.01, max_fwhm: float = 0.01,
+                max_fallback: float = 0.10):
     """The network-using mode with the lowest fallback rate among those that
-    meet the bar; if none does, the one closest to it (smallest worst relative
-    FWHM change, then gCNR change), marked as not meeting it. Returns
-    (mode, meets_bar)."""
+    meet the bar. If none does: among the modes with a finite gate whose
+    fallback rate is within `max_fallback` (beyond it the exact solver's share
+    of the frame takes most of the learned path's speed), the one closest to
+    the bar (smallest max(worst relative FWHM change / max_fwhm, worst |delta
+    gCNR| / max_dgcnr), then the lower fallback rate), marked as not meeting
+    it. Returns (mode, meets_bar)."""
     cands = [m for m in modes if m.use_net and m.label in results]
     ok = [m for m in cands if meets_bar(results[m.label], max_dgcnr, max_fwhm)]
     if ok:
@@ -446,7 +450,10 @@ def choose_mode(results: dict, modes, max_dgcnr: float = 0.01, max_fwhm: float =
         f = max(r.get(k, {}).get("max_rel_delta", 0.0) for k in ("lateral_fwhm_mm", "axial_fwhm_mm"))
         return (max(f / max_fwhm, r.get("gcnr", {}).get("max_abs_delta", 1.0) / max_dgcnr),
                 r["fallback_rate"])
-    return (min(cands, key=worst), False) if cands else (None, False)
+    finite = [m for m in cands if (math.isfinite(m.gate) or math.isfinite(m.share))
+              and results[m.label]["fallback_rate"] <= max_fallback]
+    pool = finite or cands
+    return (min(pool, key=worst), False) if pool else (None, False)
 
 
 def summarize(rows) -> dict:
