@@ -92,7 +92,7 @@ def gpu_frame(capi, ctx, torch, s, iq, grid_pts, n0, n1, kw, gtype=0, mv_mode=No
     out = torch.empty((n0, n1), dtype=torch.complex64, device="cuda")
     plan.execute(iq.data_ptr(), out.data_ptr())
     got = host(torch, out)
-    stats = plan.mv_stats() if mv_mode == 1 else None
+    stats = plan.mv_stats() if mv_mode in (1, 2) else None
     plan.close()
     return got, stats
 

@@ -101,6 +101,25 @@ def test_simulate_focused_and_no_diffraction_match_oracle(capi, ctx, torch, gold
         assert rel_l2(host(torch, rf), want) < TOL
 
 
+def test_simulate_is_deterministic(capi, ctx, torch, golden):
+    """No floating-point atomics: every RF sample sums its scatterers in the
+    same order, so two runs (and a run with the scatterers' memory reused)
+    give bit-identical RF, noise included."""
+    g = golden("sim")
+    pr, med, acq = sim_setup(g)
+    ch = c_channel(capi, pr, med, acq, txset(g, "pw"))
+    scat = dev(torch, np.concatenate([g["scat"]] * 20))  # 12,840 scatterers, many per RF sample
+    z = dev(torch, g["noise_z"])
+    out = []
+    for _ in range(2):
+        rf = torch.full(g["rf"].shape, float("nan"), dtype=torch.float32, device="cuda")
+        ctx.simulate(ch, capi.sim_config(noise_db=-60.0, noise_seed=7), scat.data_ptr(), scat.shape[0],
+                     z.data_ptr(), rf.data_ptr())
+        out.append(host(torch, rf))
+    assert np.isfinite(out[0]).all()
+    assert np.array_equal(out[0], out[1])
+
+
 def test_simulate_empty_phantom_and_zero_amplitudes(capi, ctx, torch, golden):
     g = golden("sim")
     pr, med, acq = sim_setup(g)

@@ -619,6 +619,7 @@ struct MvWarpArgs {
   // packed lower triangle), or null to form them here on mma.sync.
   long item_begin, item_end;
   const float2* r_pre;
+  const uint8_t* r_flag;  // [item - item_begin]: 1 where r_pre holds the pixel's R~
   int r_stride;
 };
 
@@ -750,7 +751,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     frexpf(amax, &e2);
     const float sc = ldexpf(1.0f, -e2), sc2 = ldexpf(1.0f, -2 * e2);
     const float inv_k = 1.0f / static_cast<float>(K);
-    if (wa.r_pre) {
+    if (wa.r_pre && wa.r_flag[item - wa.item_begin]) {
       // R~ from the tensor-core stage (same scale, same packing).
       const float2* src = wa.r_pre + (item - wa.item_begin) * wa.r_stride;
       for (int e = lane; e < L * (L + 1) / 2; e += 32) Rl[e] = src[e];
@@ -1093,21 +1094,151 @@ struct MvCovArgs {
   long item_begin, item_end;
   int lmax, nmax, kcap;     // class limits; K capacity (multiple of 64)
   float2* r_out;            // [item - item_begin][r_stride]
+  uint8_t* r_flag;          // [item - item_begin]: 1 where r_out holds the pixel's R~
   int r_stride;
   int* status;              // set on an mbarrier timeout
 };
 
 struct CovItem {
-  int valid, L, n_sub, n_d, s8, kq;   // kq = n_d * s8
+  int state;                // 0 none, 1 covariance here, 2 staged but amax unknown yet
+  int L, n_act, n_sub, n_d, dlo, pix, s8, kq;
+  long frame;
+  unsigned amax_bits;
   float sc, inv_k;
 };
 
 __host__ __device__ inline int cov_ystride(int nmax) { return nmax + 16; }
 
+// One buffer of per-tile pixel data (two are kept: the next tile's fills
+// while this tile's MMAs run).
+// Byte offsets within one buffer: staged rows, active channels, items (16-byte aligned).
+__host__ __device__ inline size_t cov_act_off(int P, int n_dmax, int nmax) {
+  return sizeof(float2) * static_cast<size_t>(P) * n_dmax * cov_ystride(nmax);
+}
+__host__ __device__ inline size_t cov_item_off(int P, int n_dmax, int nmax) {
+  return align16(cov_act_off(P, n_dmax, nmax) + sizeof(int) * P * nmax);
+}
+__host__ __device__ inline size_t cov_buf_bytes(int P, int n_dmax, int nmax) {
+  return align16(cov_item_off(P, n_dmax, nmax) + sizeof(CovItem) * P);
+}
+
 __host__ __device__ inline size_t cov_smem_bytes(int P, int n_dmax, int nmax, int kcap) {
-  return 1024 + static_cast<size_t>(kcap) * 256 +
-         sizeof(float2) * static_cast<size_t>(P) * n_dmax * cov_ystride(nmax) + sizeof(int) * P * nmax +
-         sizeof(CovItem) * P + 64;
+  return 1024 + static_cast<size_t>(kcap) * 256 + 2 * cov_buf_bytes(P, n_dmax, nmax) + 64;
+}
+
+template <int P>
+struct CovBuf {
+  float2* yst;   // [P][n_dmax][ystride]
+  int* act;      // [P][nmax]
+  CovItem* it;   // [P]
+};
+
+template <int P>
+__device__ __forceinline__ CovBuf<P> cov_buf(char* base, const MvCovArgs& c) {
+  CovBuf<P> b;
+  b.yst = reinterpret_cast<float2*>(base);
+  b.act = reinterpret_cast<int*>(base + cov_act_off(P, c.base.n_dmax, c.nmax));
+  b.it = reinterpret_cast<CovItem*>(base + cov_item_off(P, c.base.n_dmax, c.nmax));
+  return b;
+}
+
+// Pixel data of tile `tile` into buffer b: the aperture and subarray (warp q
+// for pixel q), then the range rows staged by all threads, then the scale.
+// Ends with a CTA barrier.
+template <int P>
+__device__ void cov_fill(const MvCovArgs& c, const CovBuf<P>& b, long tile, long n_items) {
+  const MvTcArgs& a = c.base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ystride = cov_ystride(c.nmax);
+  if (warp < P) {
+    const int q = warp;
+    const long rel = tile * P + q;
+    CovItem it{};
+    if (rel < n_items) {
+      const long item = c.item_begin + rel;
+      const long frame = item / c.n_list;
+      const int pix = c.pix_list[item - frame * c.n_list];
+      const int j = pix % a.n1;
+      const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
+      int* act = b.act + q * c.nmax;
+      int n_act = 0;
+      for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
+        const int ch = c0 + lane;
+        bool on = false;
+        if (ch < a.n_ch)
+          on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
+                               a.tukey_alpha) > 0.0f;
+        const unsigned m = __ballot_sync(0xffffffffu, on);
+        const int slot = n_act + __popc(m & ((1u << lane) - 1u));
+        if (on && slot < c.nmax) act[slot] = ch;
+        n_act += __popc(m);
+      }
+      int L = a.mv_subarray;
+      const int hi = max(2, n_act / 2);
+      if (L < 2) L = 2;
+      if (L > hi) L = hi;
+      // The solve kernel's rules (overflow, fewer than 4 channels) and the
+      // operand tile's capacity: otherwise no covariance here.
+      if (!(n_act > c.nmax || L > c.lmax || n_act < 4)) {
+        int dlo = -a.range_avg, dhi = a.range_avg;
+        while (j + dlo < 0) ++dlo;
+        while (j + dhi >= a.n1) --dhi;
+        const int n_sub = n_act - L + 1;
+        const int s8 = (n_sub + 7) & ~7;
+        const int n_d = dhi - dlo + 1;
+        if (n_d * s8 <= c.kcap) {
+          it.state = 2;
+          it.L = L;
+          it.n_act = n_act;
+          it.n_sub = n_sub;
+          it.n_d = n_d;
+          it.dlo = dlo;
+          it.pix = pix;
+          it.frame = frame;
+          it.s8 = s8;
+          it.kq = n_d * s8;
+        }
+      }
+    }
+    if (lane == 0) b.it[q] = it;
+  }
+  __syncthreads();
+  // Range rows of every staged pixel (zeros past n_act), all threads.
+  for (int q = 0; q < P; ++q) {
+    const CovItem& it = b.it[q];
+    if (it.state != 2) continue;   // uniform across the CTA
+    const float2* Y = a.y + it.frame * static_cast<long>(a.n_pix) * a.n_ch;
+    const int* act = b.act + q * c.nmax;
+    float m = 0.0f;
+    for (int k = threadIdx.x; k < it.n_d * ystride; k += kCovThreads) {
+      const int d = k / ystride, t = k - d * ystride;
+      float2 v = make_float2(0.f, 0.f);
+      if (t < it.n_act) {
+        v = Y[static_cast<long>(it.pix + it.dlo + d) * a.n_ch + act[t]];
+        m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+      }
+      b.yst[(q * a.n_dmax + d) * ystride + t] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m > 0.0f) atomicMax(&b.it[q].amax_bits, __float_as_uint(m));
+  }
+  __syncthreads();
+  if (threadIdx.x < P) {
+    CovItem& it = b.it[threadIdx.x];
+    if (it.state == 2) {
+      const float amax = __uint_as_float(it.amax_bits);
+      if (amax > 0.0f) {
+        int e2;
+        frexpf(amax, &e2);
+        it.sc = ldexpf(1.0f, -e2);
+        it.inv_k = 1.0f / static_cast<float>(it.n_d * it.n_sub);
+        it.state = 1;
+      } else {
+        it.state = 0;
+      }
+    }
+  }
+  __syncthreads();
 }
 
 template <int P>
@@ -1117,10 +1248,10 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
   char* sA = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(cov_raw) + 1023) & ~uintptr_t(1023));
   const MvTcArgs& a = c.base;
   const int ystride = cov_ystride(c.nmax);
-  float2* yst = reinterpret_cast<float2*>(sA + static_cast<size_t>(c.kcap) * 256);
-  int* act_all = reinterpret_cast<int*>(yst + static_cast<size_t>(P) * a.n_dmax * ystride);
-  CovItem* items = reinterpret_cast<CovItem*>(act_all + P * c.nmax);
-  uint64_t* bar = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(items + P) + 15) & ~uintptr_t(15));
+  const size_t buf_bytes = cov_buf_bytes(P, a.n_dmax, c.nmax);
+  char* buf0 = sA + static_cast<size_t>(c.kcap) * 256;
+  const CovBuf<P> bufs[2] = {cov_buf<P>(buf0, c), cov_buf<P>(buf0 + buf_bytes, c)};
+  uint64_t* bar = reinterpret_cast<uint64_t*>(buf0 + 2 * buf_bytes);
   unsigned* tmem_slot = reinterpret_cast<unsigned*>(bar + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -1142,83 +1273,28 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
   const long n_items = c.item_end - c.item_begin;
   const long n_tiles = (n_items + P - 1) / P;
 
-  for (long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    // ---- per pixel (warp q): aperture, subarray, range rows, staged rows --
-    if (warp < P) {
-      const int q = warp;
-      const long rel = tile * P + q;
-      CovItem it{};
-      if (rel < n_items) {
-        const long item = c.item_begin + rel;
-        const long frame = item / c.n_list;
-        const int pix = c.pix_list[item - frame * c.n_list];
-        const int j = pix % a.n1;
-        const float px = __ldg(a.points + 3 * pix), pz = __ldg(a.points + 3 * pix + 2);
-        int* act = act_all + q * c.nmax;
-        int n_act = 0;
-        for (int c0 = 0; c0 < a.n_ch; c0 += 32) {
-          const int ch = c0 + lane;
-          bool on = false;
-          if (ch < a.n_ch)
-            on = aperture_weight((static_cast<float>(ch) - a.half_nm1) * a.pitch, px, pz, a.f_number, a.rx_window,
-                                 a.tukey_alpha) > 0.0f;
-          const unsigned m = __ballot_sync(0xffffffffu, on);
-          const int slot = n_act + __popc(m & ((1u << lane) - 1u));
-          if (on && slot < c.nmax) act[slot] = ch;
-          n_act += __popc(m);
-        }
-        __syncwarp();
-        int L = a.mv_subarray;
-        const int hi = max(2, n_act / 2);
-        if (L < 2) L = 2;
-        if (L > hi) L = hi;
-        // The solve kernel's rules: past the class limits (overflow) or fewer
-        // than 4 active channels, no covariance.
-        if (!(n_act > c.nmax || L > c.lmax || n_act < 4)) {
-          int dlo = -a.range_avg, dhi = a.range_avg;
-          while (j + dlo < 0) ++dlo;
-          while (j + dhi >= a.n1) --dhi;
-          const int n_d = dhi - dlo + 1;
-          const float2* Y = a.y + frame * static_cast<long>(a.n_pix) * a.n_ch;
-          float amax = 0.0f;
-          for (int k = lane; k < n_d * ystride; k += 32) {
-            const int d = k / ystride, t = k - d * ystride;
-            float2 v = make_float2(0.f, 0.f);
-            if (t < n_act) {
-              v = Y[static_cast<long>(pix + dlo + d) * a.n_ch + act[t]];
-              amax = fmaxf(amax, fmaxf(fabsf(v.x), fabsf(v.y)));
-            }
-            yst[(q * a.n_dmax + d) * ystride + t] = v;
-          }
-          for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-          if (amax > 0.0f) {
-            int e2;
-            frexpf(amax, &e2);
-            it.valid = 1;
-            it.L = L;
-            it.n_sub = n_act - L + 1;
-            it.n_d = n_d;
-            it.s8 = (it.n_sub + 7) & ~7;
-            it.kq = n_d * it.s8;
-            it.sc = ldexpf(1.0f, -e2);
-            it.inv_k = 1.0f / static_cast<float>(n_d * it.n_sub);
-          }
-        }
-      }
-      if (lane == 0) items[q] = it;
-    }
-    __syncthreads();
+  long tile = blockIdx.x;
+  int cur = 0;
+  if (tile < n_tiles) cov_fill<P>(c, bufs[0], tile, n_items);
+  for (; tile < n_tiles; tile += gridDim.x, cur ^= 1) {
+    const CovBuf<P>& b = bufs[cur];
     int ktile = 0;
     bool any = false;
 #pragma unroll
-    for (int q = 0; q < P; ++q)
-      if (items[q].valid) {
+    for (int q = 0; q < P; ++q) {
+      const CovItem& it = b.it[q];
+      if (it.state == 1) {
         any = true;
-        ktile = max(ktile, items[q].kq);
+        ktile = max(ktile, it.kq);
       }
+      // Which items this tile covers (the solve kernel forms the rest itself).
+      const long rel = tile * P + q;
+      if (threadIdx.x == q && rel < n_items) c.r_flag[rel] = it.state == 1 ? 1 : 0;
+    }
     ktile = (ktile + 15) & ~15;
+    const long next = tile + gridDim.x;
     if (!any) {
-      __syncthreads();
+      if (next < n_tiles) cov_fill<P>(c, bufs[cur ^ 1], next, n_items);
       continue;
     }
     // ---- build A: window units (q, d, column chunk, element block of 8) --
@@ -1226,21 +1302,21 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
     off[0] = 0;
 #pragma unroll
     for (int q = 0; q < P; ++q) {
-      const CovItem& it = items[q];
-      off[q + 1] = off[q] + (it.valid ? it.n_d * (it.s8 >> 3) * ((it.L + 7) >> 3) : 0);
+      const CovItem& it = b.it[q];
+      off[q + 1] = off[q] + (it.state == 1 ? it.n_d * (it.s8 >> 3) * ((it.L + 7) >> 3) : 0);
     }
     for (int f = threadIdx.x; f < off[P]; f += kCovThreads) {
       int q = 0;
 #pragma unroll
       for (int z = 1; z < P; ++z)
         if (f >= off[z]) q = z;
-      const CovItem& it = items[q];
+      const CovItem& it = b.it[q];
       int u = f - off[q];
       const int nib = (it.L + 7) >> 3, nc = it.s8 >> 3;
       const int ib = u % nib;
       u /= nib;
       const int cc = u % nc, d = u / nc;
-      const float2* y = yst + (q * a.n_dmax + d) * ystride + 8 * cc + 8 * ib;
+      const float2* y = b.yst + (q * a.n_dmax + d) * ystride + 8 * cc + 8 * ib;
       float2 win[15];
 #pragma unroll
       for (int t = 0; t < 15; ++t) win[t] = y[t];
@@ -1271,15 +1347,15 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
     zoff[0] = 0;
 #pragma unroll
     for (int q = 0; q < P; ++q) {
-      const CovItem& it = items[q];
-      zoff[q + 1] = zoff[q] + (it.valid ? 2 * it.L * ((ktile - it.kq) >> 3) : 0);
+      const CovItem& it = b.it[q];
+      zoff[q + 1] = zoff[q] + (it.state == 1 ? 2 * it.L * ((ktile - it.kq) >> 3) : 0);
     }
     for (int f = threadIdx.x; f < zoff[P]; f += kCovThreads) {
       int q = 0;
 #pragma unroll
       for (int z = 1; z < P; ++z)
         if (f >= zoff[z]) q = z;
-      const CovItem& it = items[q];
+      const CovItem& it = b.it[q];
       const int u = f - zoff[q], nz = (ktile - it.kq) >> 3;
       const int row = q * R + u / nz, k0 = it.kq + 8 * (u % nz);
       *reinterpret_cast<uint4*>(sA + sw128_offset(128, row, k0)) = make_uint4(0u, 0u, 0u, 0u);
@@ -1295,6 +1371,8 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
       }
       tc5_commit(su32(bar));
     }
+    // The next tile's pixel data while the tensor core works.
+    if (next < n_tiles) cov_fill<P>(c, bufs[cur ^ 1], next, n_items);
     const bool ok = mbar_wait(su32(bar), phase);
     if (__syncthreads_or(!ok)) {
       // Timed out: record it, give the tile's MMAs one more bounded wait so
@@ -1310,9 +1388,9 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
     // ---- epilogue: warp w holds rows 32 w .. 32 w + 31 -------------------
     {
       const int q = (warp * 32) / R;
-      const CovItem& it = items[q];
+      const CovItem& it = b.it[q];
       const int ml0 = warp * 32 - q * R;     // first local row of this warp
-      if (it.valid && ml0 < 2 * it.L) {
+      if (it.state == 1 && ml0 < 2 * it.L) {
         const long rel = tile * P + q;
         float2* dst = c.r_out + rel * c.r_stride;
         const int ml = ml0 + lane, a_el = ml >> 1;
@@ -1327,9 +1405,9 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
             const float g0 = __uint_as_float(r[t]), g1 = __uint_as_float(r[t + 1]);
             const float o0 = __shfl_xor_sync(0xffffffffu, g0, 1);
             const float o1 = __shfl_xor_sync(0xffffffffu, g1, 1);
-            const int b = (j0 + t) >> 1;
-            if (even && a_el < it.L && b < it.L && b >= a_el)
-              dst[tri(b, a_el)] = make_float2((g0 + o1) * it.inv_k, -(o0 - g1) * it.inv_k);
+            const int bb = (j0 + t) >> 1;
+            if (even && a_el < it.L && bb < it.L && bb >= a_el)
+              dst[tri(bb, a_el)] = make_float2((g0 + o1) * it.inv_k, -(o0 - g1) * it.inv_k);
           }
         }
       }
@@ -1668,7 +1746,11 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
       w.overflow = extra.overflow;
       w.overflow_cap = extra.overflow_cap;
       const long items = static_cast<long>(k.count) * n_frames;
-      const int kcap = (a.n_dmax * ((k.nmax + 7) & ~7) + 63) & ~63;
+      // K capacity: a class's pixels have L >= its lower bound (less one at
+      // an aperture edge), so n_sub <= nmax - lmax + 18; pixels beyond it are
+      // flagged and the solve kernel forms their covariance itself.
+      const int nsub_cap = std::max(1, std::min(k.nmax, k.nmax - k.lmax + 18));
+      const int kcap = (a.n_dmax * ((nsub_cap + 7) & ~7) + 63) & ~63;
       const int P_cov = 2 * k.lmax <= 32 ? 4 : (2 * k.lmax <= 64 ? 2 : 1);
       // Classes whose operand tile does not fit shared memory keep the mma.sync covariance.
       if (extra.cov_engine == 1 && 2 * k.lmax <= 128 && cov_smem_bytes(P_cov, a.n_dmax, k.nmax, kcap) <= 227 * 1024) {
@@ -1677,7 +1759,9 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
         const int P = P_cov;
         const int r_stride = k.lmax * (k.lmax + 1) / 2;
         const long chunk = std::max(1024L, static_cast<long>((96u << 20) / (sizeof(float2) * r_stride)));
-        const size_t need = sizeof(float2) * static_cast<size_t>(r_stride) * static_cast<size_t>(std::min(chunk, items));
+        const size_t n_chunk = static_cast<size_t>(std::min(chunk, items));
+        const size_t flag_off = (sizeof(float2) * static_cast<size_t>(r_stride) * n_chunk + 255) / 256 * 256;
+        const size_t need = flag_off + n_chunk;
         if (need > ctx->mv_cov_bytes) {
           if (ctx->mv_cov) {
             USX_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1697,6 +1781,7 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
         cv.nmax = k.nmax;
         cv.kcap = kcap;
         cv.r_out = static_cast<float2*>(ctx->mv_cov);
+        cv.r_flag = static_cast<uint8_t*>(ctx->mv_cov) + flag_off;
         cv.r_stride = r_stride;
         cv.status = ctx->d_status + 14;
         const size_t smem = cov_smem_bytes(P, a.n_dmax, k.nmax, cv.kcap);
@@ -1709,6 +1794,7 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
         // At most four CTAs per SM: each holds 128 of the SM's 512 TMEM columns.
         const long resident = static_cast<long>(std::max(1, std::min(per_sm, 4))) * ctx->sm_count;
         w.r_pre = static_cast<const float2*>(ctx->mv_cov);
+        w.r_flag = cv.r_flag;
         w.r_stride = r_stride;
         for (long i0 = 0; i0 < items; i0 += chunk) {
           const long i1 = std::min(items, i0 + chunk);

@@ -1,23 +1,31 @@
-// simulate.cu — point-scatterer forward model (reference simulator.cpp:213-419).
+// simulate.cu — point-scatterer forward model (reference simulator.cpp:213-419),
+// in two stages per group of transmit events, with no floating-point atomics
+// (runs are bit-identical):
 //
-// One warp owns one (scatterer, transmit event) at a time:
-//   stage 1  the incident field at the scatterer, a sum over firing elements of
-//            the delayed, weighted two-way pulse linearly interpolated onto an
-//            oversampled time axis, built in the warp's shared-memory buffer.
-//            Per element the lanes split the buffer slots the pulse covers;
-//            each slot adds the "next sample" term of the previous tap and
-//            then the "this sample" term of its own tap, which is exactly the
-//            order in which the reference's serial tap loop updates each
-//            buffer position, so the buffer is bit-identical;
-//   trim     the buffer's -40 dB tails are cut (warp max + ballots);
-//   stage 2  for every receive element the lanes produce the delayed,
-//            weighted echo samples and add them into RF[event][element][n]
-//            with fire-and-forget reductions (red.global.add.f32).
-// Scatterers are independent, so the only cross-warp interaction is the
-// commutative RF accumulation, as in the reference's per-thread buffers
-// reduced under `omp critical`.
+//   incident_kernel  one warp per (scatterer, event): the incident field at
+//            the (moved) scatterer, a sum over firing elements of the delayed,
+//            weighted two-way pulse linearly interpolated onto an oversampled
+//            time axis, built in the warp's shared-memory buffer. Per element
+//            the lanes split the buffer slots the pulse covers; each slot adds
+//            the "next sample" term of the previous tap and then the "this
+//            sample" term of its own tap, which is exactly the order in which
+//            the reference's serial tap loop updates each buffer position, so
+//            the buffer is bit-identical. Its -40 dB tails are trimmed (warp
+//            max + ballots) and the trimmed field goes to global memory with a
+//            header (start time, length, position, amplitude);
+//   echo_kernel      one CTA per (group of elements, event), one warp per
+//            element, the element's RF row resident in shared memory: the warp
+//            walks every scatterer in order, sets up its echo on this element
+//            (distance, amplitude, delay, sample window) and the lanes add the
+//            echo samples (linear interpolation of the trimmed incident field)
+//            into the row, each sample owned by one lane, so every RF sample
+//            sums its scatterers in the same fixed order on every run. The row
+//            is then written once.
 //
-// Receive noise is added by a second kernel once an event's echoes are
+// The reference reduces per-thread buffers in `omp critical` order, which is
+// arbitrary; here the order is the scatterer order.
+//
+// Receive noise is added by a third kernel once an event's echoes are
 // complete: sigma = peak|RF| * 10^(noise_db/20), RF += z * sigma, with z the
 // host-generated standard normals of the reference's per-event generator.
 #include <algorithm>
@@ -29,10 +37,10 @@
 namespace usxcu {
 namespace {
 
-constexpr int kSimWarps = 4;
+constexpr int kSimWarps = 4;       // incident_kernel: warps (scatterers) per CTA
+constexpr int kEchoWarps = 8;      // echo_kernel: warps (elements) per CTA
 constexpr int kMaxElem = 256;
 constexpr int kMaxPulse = 1024;
-constexpr int kMaxTimeTable = 8192;
 
 struct SimArgs {
   const usx_scatterer* scat;
@@ -44,11 +52,13 @@ struct SimArgs {
   const float* pulse;      // [pulse_n]
   float* rf;               // [ev][n_el][n_smp]
   unsigned long long* counter;
-  int n_el, n_smp, n_ev, pulse_n, inc_cap, scat_per_block;
+  float* inc;              // [ev - ev0][n_scat][inc_cap] trimmed incident fields
+  float4* hdr;             // [ev - ev0][n_scat][2]: (t0, length bits, amplitude, -), (x, y, z, -)
+  int ev0;                 // first event of this group
+  int n_el, n_smp, n_ev, pulse_n, inc_cap;
   float c, fs, t0, fs_os, lambda, width, prf, half_nm1, pitch;
   float pulse_half, max_window_s, trim_amp, atten_db_per_m;
   int spreading, directivity_on, motion, full;
-  int t_table;             // the block holds the sample-time table (n_smp <= kMaxTimeTable)
 };
 
 __device__ __forceinline__ float elem_amp(const SimArgs& a, float base_amp, float px, float ex, float r) {
@@ -62,7 +72,7 @@ __device__ __forceinline__ float elem_amp(const SimArgs& a, float base_amp, floa
   return amp;
 }
 
-__global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs a) {
+__global__ void __launch_bounds__(32 * kSimWarps) incident_kernel(const SimArgs a) {
   extern __shared__ float4 sim_smem[];
   float* pulse = reinterpret_cast<float*>(sim_smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -74,176 +84,184 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
   float* e_ctr = e_amp + kMaxElem;              // stage-1 centre index (active order)
   int* e_base = reinterpret_cast<int*>(e_ctr + kMaxElem);
   for (int k = threadIdx.x; k < a.pulse_n; k += blockDim.x) pulse[k] = a.pulse[k];
-  // Sample times t0 + n / fs of the RF axis, each computed as the reference
-  // does (float division), once per block instead of once per echo sample.
-  float* t_axis = pulse + kMaxPulse + kSimWarps * (a.inc_cap + 4 * kMaxElem);
-  if (a.t_table)
-    for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
   __syncthreads();
 
-  const int ev = blockIdx.y;
+  const int evl = blockIdx.y, ev = a.ev0 + evl;
   const float event_time = static_cast<float>(ev) / a.prf;
   const int n_act = a.n_active[ev];
   const int* act = a.active + static_cast<long>(ev) * a.n_el;
   const float* dly = a.delays + static_cast<long>(ev) * a.n_el;
   const float* apd = a.apod + static_cast<long>(ev) * a.n_el;
-  float* rf_ev = a.rf + static_cast<long>(ev) * a.n_el * a.n_smp;
-  unsigned long long samples = 0;
 
-  const long s_begin = static_cast<long>(blockIdx.x) * a.scat_per_block;
-  const long s_end = min(a.n_scat, s_begin + a.scat_per_block);
-  for (long si = s_begin + warp; si < s_end; si += kSimWarps) {
+  for (long si = static_cast<long>(blockIdx.x) * kSimWarps + warp; si < a.n_scat;
+       si += static_cast<long>(gridDim.x) * kSimWarps) {
     __syncwarp();  // the previous scatterer's buffers are no longer read
+    float4* hd = a.hdr + 2 * (static_cast<long>(evl) * a.n_scat + si);
     const usx_scatterer sc = a.scat[si];
-    if (sc.amplitude == 0.0f) continue;
+    int trim_n = 0;
+    float trim_t0 = 0.0f;
     float px = sc.x, py = sc.y, pz = sc.z;
     if (a.motion) {
       px = px + sc.vx * event_time;
       py = py + sc.vy * event_time;
       pz = pz + sc.vz * event_time;
     }
-    if (pz <= 0.0f) continue;
-
-    // Distances to every element.
-    for (int e = lane; e < a.n_el; e += 32) {
-      const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
-      e_r[e] = dist3(px, py, pz, ex, 0.0f, 0.0f);
-    }
-    __syncwarp();
-
-    // ---- stage 1: arrival span over firing elements -----------------------
-    float t_min = INFINITY, t_max = -INFINITY;
-    for (int q = lane; q < n_act; q += 32) {
-      const int e = act[q];
-      const float t = dly[e] + e_r[e] / a.c;
-      t_min = fminf(t_min, t);
-      t_max = fmaxf(t_max, t);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      t_min = fminf(t_min, __shfl_xor_sync(0xffffffffu, t_min, o));
-      t_max = fmaxf(t_max, __shfl_xor_sync(0xffffffffu, t_max, o));
-    }
-    float span = (t_max - t_min) + 2.0f * a.pulse_half;
-    span = fminf(span, a.max_window_s + 2.0f * a.pulse_half);
-    const float inc_t0 = t_min - a.pulse_half;
-    const int inc_n = static_cast<int>(ceilf(span * a.fs_os)) + 2;
-    if (inc_n > a.inc_cap || inc_n <= 0) continue;  // cannot happen: cap bounds the window
-    for (int k = lane; k < inc_n; k += 32) inc[k] = 0.0f;
-
-    // Per firing element: amplitude and pulse placement.
-    for (int q = lane; q < n_act; q += 32) {
-      const int e = act[q];
-      const float r = e_r[e];
-      float amp = 0.0f;
-      float centre = 0.0f;
-      if (!(r < 1e-6f)) {
+    if (sc.amplitude != 0.0f && pz > 0.0f) {
+      // Distances to every element.
+      for (int e = lane; e < a.n_el; e += 32) {
         const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
-        amp = elem_amp(a, apd[e], px, ex, r);
-        const float t_arr = dly[e] + r / a.c;
-        centre = (t_arr - inc_t0) * a.fs_os;
-      } else {
-        amp = 0.0f;
-      }
-      e_amp[q] = (r < 1e-6f) ? 0.0f : amp;
-      e_ctr[q] = centre;
-      e_base[q] = static_cast<int>(floorf(centre)) - a.pulse_n / 2;
-    }
-    __syncwarp();
-    for (int q = 0; q < n_act; ++q) {
-      const float amp = e_amp[q];
-      if (amp == 0.0f) continue;
-      const float centre = e_ctr[q];
-      const int base = e_base[q];
-      const float frac = centre - floorf(centre);
-      const float omf = 1.0f - frac;
-      // One lane per buffer slot s = base + j: first the "next sample" term of
-      // tap j - 1, then the "this sample" term of tap j, which is the order in
-      // which the reference's serial tap loop updates slot s (see header).
-      for (int j = lane; j <= a.pulse_n; j += 32) {
-        const int s = base + j;
-        const bool nx = j >= 1 && s >= 1 && s < inc_n;          // tap j - 1 at index s - 1
-        const bool th = j < a.pulse_n && s >= 0 && s + 1 < inc_n; // tap j at index s
-        if (!nx && !th) continue;
-        float t = inc[s];
-        if (nx) t += (amp * pulse[j - 1]) * frac;
-        if (th) t += (amp * pulse[j]) * omf;
-        inc[s] = t;
+        e_r[e] = dist3(px, py, pz, ex, 0.0f, 0.0f);
       }
       __syncwarp();
-      if (!a.full) break;
-    }
-
-    // ---- trim ----------------------------------------------------------------
-    float peak = 0.0f;
-    for (int k = lane; k < inc_n; k += 32) peak = fmaxf(peak, fabsf(inc[k]));
-    for (int o = 16; o > 0; o >>= 1) peak = fmaxf(peak, __shfl_xor_sync(0xffffffffu, peak, o));
-    if (peak <= 0.0f) continue;
-    const float thr = peak * a.trim_amp;
-    int lo = inc_n, hi = -1;
-    for (int k0 = 0; k0 < inc_n; k0 += 32) {
-      const int k = k0 + lane;
-      const bool keep = k < inc_n && !(fabsf(inc[k]) < thr);
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (m) {
-        lo = min(lo, k0 + __ffs(m) - 1);
-        hi = max(hi, k0 + 31 - __clz(m));
+      // ---- arrival span over firing elements ------------------------------
+      float t_min = INFINITY, t_max = -INFINITY;
+      for (int q = lane; q < n_act; q += 32) {
+        const int e = act[q];
+        const float t = dly[e] + e_r[e] / a.c;
+        t_min = fminf(t_min, t);
+        t_max = fmaxf(t_max, t);
       }
-    }
-    if (lo >= inc_n || hi <= lo) continue;
-    const float trim_t0 = inc_t0 + static_cast<float>(lo) / a.fs_os;
-    const int trim_n = hi - lo + 1;
-    const float* tr = inc + lo;
-
-    // ---- stage 2: echo on every receive element ---------------------------------
-    // Per receive element, one lane each: amplitude, delay and the echo's
-    // sample window (the stage-1 tables are free again; e_r[e] is read by
-    // the lane that then overwrites it with the window's last sample).
-    const float span_t = static_cast<float>(trim_n - 1) / a.fs_os;
-    for (int e = lane; e < a.n_el; e += 32) {
-      const float r = e_r[e];
-      float amp = 0.0f, delay = 0.0f;
-      int n0 = 1, n1 = 0;
-      if (!(r < 1e-6f)) {
-        const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
-        amp = elem_amp(a, sc.amplitude, px, ex, r);
-        if (amp != 0.0f) {
-          delay = r / a.c;
-          const float t_start = trim_t0 + delay;
-          const float t_end = t_start + span_t;
-          n0 = max(static_cast<int>(ceilf((t_start - a.t0) * a.fs)), 0);
-          n1 = min(static_cast<int>(floorf((t_end - a.t0) * a.fs)), a.n_smp - 1);
+      for (int o = 16; o > 0; o >>= 1) {
+        t_min = fminf(t_min, __shfl_xor_sync(0xffffffffu, t_min, o));
+        t_max = fmaxf(t_max, __shfl_xor_sync(0xffffffffu, t_max, o));
+      }
+      float span = (t_max - t_min) + 2.0f * a.pulse_half;
+      span = fminf(span, a.max_window_s + 2.0f * a.pulse_half);
+      const float inc_t0 = t_min - a.pulse_half;
+      const int inc_n = static_cast<int>(ceilf(span * a.fs_os)) + 2;
+      if (inc_n <= a.inc_cap && inc_n > 0) {  // the cap bounds the window: always
+        for (int k = lane; k < inc_n; k += 32) inc[k] = 0.0f;
+        // Per firing element: amplitude and pulse placement.
+        for (int q = lane; q < n_act; q += 32) {
+          const int e = act[q];
+          const float r = e_r[e];
+          float amp = 0.0f;
+          float centre = 0.0f;
+          if (!(r < 1e-6f)) {
+            const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
+            amp = elem_amp(a, apd[e], px, ex, r);
+            const float t_arr = dly[e] + r / a.c;
+            centre = (t_arr - inc_t0) * a.fs_os;
+          }
+          e_amp[q] = (r < 1e-6f) ? 0.0f : amp;
+          e_ctr[q] = centre;
+          e_base[q] = static_cast<int>(floorf(centre)) - a.pulse_n / 2;
+        }
+        __syncwarp();
+        for (int q = 0; q < n_act; ++q) {
+          const float amp = e_amp[q];
+          if (amp == 0.0f) continue;
+          const float centre = e_ctr[q];
+          const int base = e_base[q];
+          const float frac = centre - floorf(centre);
+          const float omf = 1.0f - frac;
+          // One lane per buffer slot s = base + j: first the "next sample"
+          // term of tap j - 1, then the "this sample" term of tap j.
+          for (int j = lane; j <= a.pulse_n; j += 32) {
+            const int s = base + j;
+            const bool nx = j >= 1 && s >= 1 && s < inc_n;          // tap j - 1 at index s - 1
+            const bool th = j < a.pulse_n && s >= 0 && s + 1 < inc_n; // tap j at index s
+            if (!nx && !th) continue;
+            float t = inc[s];
+            if (nx) t += (amp * pulse[j - 1]) * frac;
+            if (th) t += (amp * pulse[j]) * omf;
+            inc[s] = t;
+          }
+          __syncwarp();
+          if (!a.full) break;
+        }
+        // ---- trim the -40 dB tails -----------------------------------------
+        float peak = 0.0f;
+        for (int k = lane; k < inc_n; k += 32) peak = fmaxf(peak, fabsf(inc[k]));
+        for (int o = 16; o > 0; o >>= 1) peak = fmaxf(peak, __shfl_xor_sync(0xffffffffu, peak, o));
+        if (peak > 0.0f) {
+          const float thr = peak * a.trim_amp;
+          int lo = inc_n, hi = -1;
+          for (int k0 = 0; k0 < inc_n; k0 += 32) {
+            const int k = k0 + lane;
+            const bool keep = k < inc_n && !(fabsf(inc[k]) < thr);
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (m) {
+              lo = min(lo, k0 + __ffs(m) - 1);
+              hi = max(hi, k0 + 31 - __clz(m));
+            }
+          }
+          if (lo < inc_n && hi > lo) {
+            trim_t0 = inc_t0 + static_cast<float>(lo) / a.fs_os;
+            trim_n = hi - lo + 1;
+            float* dst = a.inc + (static_cast<long>(evl) * a.n_scat + si) * a.inc_cap;
+            for (int k = lane; k < trim_n; k += 32) dst[k] = inc[lo + k];
+          }
         }
       }
-      if (n0 > n1) {
-        n0 = 1;
-        n1 = 0;
-      } else {
-        samples += static_cast<unsigned long long>(n1 - n0 + 1);
-      }
-      e_amp[e] = amp;
-      e_ctr[e] = delay;
-      e_base[e] = n0;
-      e_r[e] = __int_as_float(n1);
     }
-    __syncwarp();
-    for (int e = 0; e < a.n_el; ++e) {
-      const int n0 = e_base[e], n1 = __float_as_int(e_r[e]);
+    if (lane == 0) {
+      hd[0] = make_float4(trim_t0, __int_as_float(trim_n), sc.amplitude, 0.0f);
+      hd[1] = make_float4(px, py, pz, 0.0f);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(32 * kEchoWarps) echo_kernel(const SimArgs a) {
+  extern __shared__ float4 echo_smem[];
+  float* t_axis = reinterpret_cast<float*>(echo_smem);   // [n_smp]
+  float* rows = t_axis + a.n_smp;                        // [warps][n_smp]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  // Sample times t0 + n / fs of the RF axis, each computed as the reference
+  // does (float division).
+  for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
+  for (int k = threadIdx.x; k < n_warps * a.n_smp; k += blockDim.x) rows[k] = 0.0f;
+  __syncthreads();
+  const int evl = blockIdx.y, ev = a.ev0 + evl;
+  const int e = blockIdx.x * n_warps + warp;
+  unsigned long long samples = 0;
+  if (e < a.n_el) {
+    float* row = rows + warp * a.n_smp;
+    const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
+    const float4* hdr = a.hdr + 2 * static_cast<long>(evl) * a.n_scat;
+    const float* incs = a.inc + static_cast<long>(evl) * a.n_scat * a.inc_cap;
+    // The next scatterer's header is fetched while this one is processed.
+    float4 h0n = make_float4(0.f, 0.f, 0.f, 0.f), h1n = h0n;
+    if (a.n_scat > 0) {
+      h0n = __ldg(hdr);
+      h1n = __ldg(hdr + 1);
+    }
+    for (long si = 0; si < a.n_scat; ++si) {
+      const float4 h0 = h0n, h1 = h1n;
+      if (si + 1 < a.n_scat) {
+        h0n = __ldg(hdr + 2 * (si + 1));
+        h1n = __ldg(hdr + 2 * (si + 1) + 1);
+      }
+      const int trim_n = __float_as_int(h0.y);
+      if (trim_n <= 0) continue;
+      const float r = dist3(h1.x, h1.y, h1.z, ex, 0.0f, 0.0f);
+      if (r < 1e-6f) continue;
+      const float amp = elem_amp(a, h0.z, h1.x, ex, r);
+      if (amp == 0.0f) continue;
+      const float trim_t0 = h0.x;
+      const float delay = r / a.c;
+      const float span_t = static_cast<float>(trim_n - 1) / a.fs_os;
+      const float t_start = trim_t0 + delay;
+      const float t_end = t_start + span_t;
+      const int n0 = max(static_cast<int>(ceilf((t_start - a.t0) * a.fs)), 0);
+      const int n1 = min(static_cast<int>(floorf((t_end - a.t0) * a.fs)), a.n_smp - 1);
       if (n0 > n1) continue;
-      const float amp = e_amp[e], delay = e_ctr[e];
-      float* dst = rf_ev + static_cast<long>(e) * a.n_smp;
+      samples += static_cast<unsigned long long>(n1 - n0 + 1);
+      const float* tr = incs + si * a.inc_cap;
       for (int n = n0 + lane; n <= n1; n += 32) {
-        const float t = (a.t_table ? t_axis[n] : (a.t0 + static_cast<float>(n) / a.fs)) - delay;
+        const float t = t_axis[n] - delay;
         const float u = (t - trim_t0) * a.fs_os;
         const int k = static_cast<int>(u);
         if (k < 0 || k + 1 >= trim_n) continue;
         const float f = u - static_cast<float>(k);
-        const float va = tr[k], vb = tr[k + 1];
-        atomicAdd(dst + n, amp * (va + (vb - va) * f));
+        const float va = __ldg(tr + k), vb = __ldg(tr + k + 1);
+        row[n] += amp * (va + (vb - va) * f);
       }
     }
     __syncwarp();
+    float* dst = a.rf + (static_cast<long>(ev) * a.n_el + e) * a.n_smp;
+    for (int n = lane; n < a.n_smp; n += 32) dst[n] = row[n];
   }
-  for (int o = 16; o > 0; o >>= 1) samples += __shfl_xor_sync(0xffffffffu, samples, o);
   if (lane == 0 && samples) atomicAdd(a.counter, samples);
 }
 
@@ -286,7 +304,6 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   if (n_el > kMaxElem) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 256 elements");
   if (n_ev > 65535) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 65535 events");
   const long ev_size = static_cast<long>(n_el) * n_smp;
-  USX_CUDA(cudaMemsetAsync(rf, 0, sizeof(float) * ev_size * n_ev, ctx->stream));
 
   // Host-side constants with the reference's float arithmetic.
   int pulse_n = 0;
@@ -322,8 +339,13 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
     n_active[static_cast<size_t>(e)] = na;
   }
   const size_t tbl = delays.size();
+  // Event groups whose trimmed incident fields (inc_cap floats per scatterer
+  // and event, of which only the trimmed part is written) fit about 2 GB.
+  const long n_sc = std::max<long>(1, n_scat);
+  const size_t per_event = static_cast<size_t>(n_sc) * (static_cast<size_t>(inc_cap) * sizeof(float) + 2 * sizeof(float4));
+  const int group = static_cast<int>(std::max<size_t>(1, std::min<size_t>(n_ev, (size_t(2) << 30) / per_event)));
   const size_t bytes = sizeof(float) * (2 * tbl + pulse.size()) + sizeof(int) * (tbl + n_ev) +
-                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + 1024;
+                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + per_event * group + 4096;
   void* ws = nullptr;
   if (int rc = scratch(ctx, bytes, &ws)) return rc;
   char* w = static_cast<char*>(ws);
@@ -339,6 +361,8 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   int* d_active = reinterpret_cast<int*>(take(sizeof(int) * tbl));
   int* d_nact = reinterpret_cast<int*>(take(sizeof(int) * n_ev));
   float* d_pulse = reinterpret_cast<float*>(take(sizeof(float) * pulse.size()));
+  float4* d_hdr = reinterpret_cast<float4*>(take(sizeof(float4) * 2 * static_cast<size_t>(n_sc) * group));
+  float* d_inc = reinterpret_cast<float*>(take(sizeof(float) * static_cast<size_t>(inc_cap) * n_sc * group));
   if (static_cast<size_t>(w - static_cast<char*>(ws)) > ctx->scratch_bytes)
     return fail(USX_ERR_INVALID, "usx_cu_simulate: scratch layout overflow");
   USX_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), ctx->stream));
@@ -359,6 +383,9 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.pulse = d_pulse;
   a.rf = rf;
   a.counter = d_counter;
+  a.inc = d_inc;
+  a.hdr = d_hdr;
+  a.ev0 = 0;
   a.n_el = n_el;
   a.n_smp = n_smp;
   a.n_ev = n_ev;
@@ -381,21 +408,36 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.directivity_on = cfg->apply_directivity;
   a.motion = cfg->enable_motion;
   a.full = cfg->full_transmit_diffraction;
-  // Enough blocks per event to fill the GPU several times over.
-  const long target_blocks = std::max<long>(1, static_cast<long>(ctx->sm_count) * 8 / std::max(1, n_ev));
-  a.scat_per_block = static_cast<int>(std::max<long>(kSimWarps, (n_scat + target_blocks - 1) / target_blocks));
-  a.scat_per_block = std::min(a.scat_per_block, 256);
-  const long gx = std::max<long>(1, (n_scat + a.scat_per_block - 1) / a.scat_per_block);
-  a.t_table = n_smp <= kMaxTimeTable ? 1 : 0;
-  const size_t smem = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem) +
-                                       (a.t_table ? static_cast<size_t>(n_smp) : 0));
-  if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
-  if (int rc_ = smem_limit(reinterpret_cast<const void*>(simulate_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
+  const size_t smem_inc = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem));
+  if (smem_inc > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(incident_kernel), smem_inc)) return rc_;
+  // The echo stage keeps one RF row per warp plus the sample-time axis in shared memory.
+  const int echo_warps = static_cast<int>(std::min<long>(kEchoWarps, (227L * 1024) / (4L * n_smp) - 1));
+  if (echo_warps < 1) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 28,000 samples per trace");
+  const size_t smem_echo = sizeof(float) * static_cast<size_t>(echo_warps + 1) * n_smp;
+  if (int rc_ = smem_limit(reinterpret_cast<const void*>(echo_kernel), smem_echo)) return rc_;
   if (n_scat > 0) {
-    prof_begin(ctx, "simulate_kernel");
-    simulate_kernel<<<dim3(static_cast<unsigned>(gx), n_ev), 32 * kSimWarps, smem, ctx->stream>>>(a);
-    prof_end(ctx);
-    USX_CHECK_LAUNCH("simulate_kernel");
+    int per_sm = 0;
+    if (int rc_ = occupancy(reinterpret_cast<const void*>(incident_kernel), 32 * kSimWarps, smem_inc, &per_sm))
+      return rc_;
+    for (int e0 = 0; e0 < n_ev; e0 += group) {
+      const int ng = std::min(group, n_ev - e0);
+      a.ev0 = e0;
+      const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 4 / ng;
+      const long need = (n_scat + kSimWarps - 1) / kSimWarps;
+      const unsigned gx = static_cast<unsigned>(std::max(1L, std::min(want, need)));
+      prof_begin(ctx, "incident_kernel");
+      incident_kernel<<<dim3(gx, ng), 32 * kSimWarps, smem_inc, ctx->stream>>>(a);
+      prof_end(ctx);
+      USX_CHECK_LAUNCH("incident_kernel");
+      prof_begin(ctx, "echo_kernel");
+      echo_kernel<<<dim3(static_cast<unsigned>(ceil_div(n_el, echo_warps)), ng), 32 * echo_warps, smem_echo,
+                    ctx->stream>>>(a);
+      prof_end(ctx);
+      USX_CHECK_LAUNCH("echo_kernel");
+    }
+  } else {
+    USX_CUDA(cudaMemsetAsync(rf, 0, sizeof(float) * ev_size * n_ev, ctx->stream));
   }
   if (cfg->noise_db > -200.0f && noise_z) {
     USX_CUDA(cudaMemsetAsync(d_peak, 0, sizeof(unsigned) * n_ev, ctx->stream));
