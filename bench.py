@@ -432,6 +432,7 @@ def run_ours(args) -> None:
         gate = learned.trained_gate(WEIGHTS) if args.gate is None else args.gate
         refine = learned.trained_refine(WEIGHTS) if args.refine is None else args.refine
         share = learned.trained_share_gate(WEIGHTS) if args.share_gate is None else args.share_gate
+        level = learned.trained_level_gate(WEIGHTS) if args.level_gate is None else args.level_gate
         # Plain minimum variance (tensor-core solver) on the same frame, timed first.
         plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
         plain.set_mv_mode(1)
@@ -446,11 +447,13 @@ def run_ours(args) -> None:
         plan.set_learned(mlp, gate)
         plan.set_learned_refine(refine)
         plan.set_learned_subspace(True, share)
+        plan.set_learned_level_gate(level)
         extra["plain_mv"] = {"value": world * args.steps / (plain_ms / 1e3) * N0 / n0, "unit": "frames/s",
                              "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": "tensor"}
         extra["gate"] = gate
         extra["refine_beams"] = refine
         extra["share_gate"] = share
+        extra["level_gate"] = level
     else:
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         if args.workload == "mv":
@@ -488,7 +491,7 @@ def run_ours(args) -> None:
         rep = WEIGHTS.with_suffix(".json")
         if rep.exists():
             r = json.loads(rep.read_text())
-            label = learned.Mode(gate=float(gate), share=float(share)).label
+            label = learned.Mode(gate=float(gate), share=float(share), level=float(level)).label
             ev = r.get("eval", {}).get(label)
             if ev:
                 extra["held_out_quality"] = {
@@ -510,7 +513,7 @@ def run_ours(args) -> None:
     roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks, extra.get("refine_beams", -1))
 
     e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world,
-                                           (gate, refine, share) if args.workload == "learned" else None)
+                                           (gate, refine, share, level) if args.workload == "learned" else None)
     if bkw.get("combiner") == 2:
         fp64, failed = plan.mv_stats()
         roofline["mv_fp64_resolves_per_frame"] = fp64 / max(1, args.steps + args.warmup)
@@ -1221,6 +1224,7 @@ def run_mixed(args) -> None:
     lin.set_learned(mlp, learned.trained_gate(WEIGHTS))
     lin.set_learned_refine(learned.trained_refine(WEIGHTS))
     lin.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
+    lin.set_learned_level_gate(learned.trained_level_gate(WEIGHTS))
     f_lin = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
     lin.autotune(iq_lin.data_ptr(), f_lin.data_ptr(), repeats=1)
     # Sector: 64-element phased array.
@@ -1256,6 +1260,7 @@ def run_mixed(args) -> None:
     sec.set_learned(mlp, learned.trained_gate(WEIGHTS))
     sec.set_learned_refine(learned.trained_refine(WEIGHTS))
     sec.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
+    sec.set_learned_level_gate(learned.trained_level_gate(WEIGHTS))
     sec.autotune(iq_sec.data_ptr(), f_sec.data_ptr(), repeats=1)
     env, logi = torch.empty((256, 1024), device="cuda"), torch.empty((256, 1024), device="cuda")
     img = torch.empty((800, 800), device="cuda")
@@ -1337,7 +1342,7 @@ def run_e2e(usx, grid, raw, rf_host, args, world, learned=None):
     b = pcfg.beamformer
     b.mv_solver = usx.MvSolver.EXACT if args.workload == "mv_exact" else usx.MvSolver.TENSOR
     if learned is not None:
-        b.learned_gate, b.learned_refine, b.learned_share_gate = learned
+        b.learned_gate, b.learned_refine, b.learned_share_gate, b.learned_level_gate = learned
     kw = WORKLOADS[args.workload]
     b.f_number = kw["f_number"]
     b.combiner = usx.Combiner(kw.get("combiner", 0))
@@ -1375,6 +1380,8 @@ def main() -> int:
     ap.add_argument("--refine", type=int, default=None, help="learned workload: subspace beams (default: report)")
     ap.add_argument("--share-gate", type=float, default=None,
                     help="learned workload: gate on the network direction's share (default: report)")
+    ap.add_argument("--level-gate", type=float, default=None,
+                    help="learned workload: gate on tr(R) over its depth's level (default: report)")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -218,6 +218,13 @@ int usx_cu_bf_plan_set_learned_refine(usx_bf_plan* plan, int n_beams);
  * outside the beams' span). use_network = 0 solves within the beams alone.
  * Defaults: use_network = 1, max_network_share = +inf (no second gate). */
 int usx_cu_bf_plan_set_learned_subspace(usx_bf_plan* plan, int use_network, float max_network_share);
+/* The refinement's third gate (no counterpart in the reference): a pixel
+ * whose covariance trace tr(R) exceeds max_level_ratio times its depth's
+ * level, the geometric mean of tr(R) over the frame's lateral lines at that
+ * depth, goes to the exact minimum variance. Strong point targets raise tr(R)
+ * far above the speckle level around them, where minimum variance forms deep
+ * nulls that the refinement's subspace cannot. Default +inf (off); >= 1. */
+int usx_cu_bf_plan_set_learned_level_gate(usx_bf_plan* plan, float max_level_ratio);
 /* Pixels gated to the exact solver and pixels beamformed by the learned path
  * since the last call (synchronises). */
 int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels);

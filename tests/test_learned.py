@@ -593,3 +593,35 @@ def test_share_gate_sends_pixels_to_the_exact_solver(capi, torch):
         mlp.close()
     finally:
         im.close()
+
+
+@pytest.mark.gpu
+def test_level_gate_sends_bright_pixels_to_the_exact_solver(capi, torch):
+    """The gate on tr(R) over its depth's level (the geometric mean over the
+    lateral lines): at ratio 1 roughly every pixel brighter than its depth's
+    level goes to the exact solver, at +inf none, and the rate falls as the
+    ratio rises; the pixels around a bright wire are among the first gated."""
+    from usx import learned
+    im = learned.Imager(learned.Setup(n_tx=15, depth=0.04, n0=128, n1=256))
+    try:
+        mlp = learned.load_mlp(im.ctx)
+        plan = im.plan(learned.COMB_LEARNED_MV)
+        plan.set_learned(mlp, float("inf"))
+        plan.set_learned_refine(6)
+        spec = learned.phantom(31, im.setup)
+        im.acquire(spec)
+        im.beamform(learned.COMB_MV)
+        rates = []
+        for level in (1.0, 3.0, 30.0, float("inf")):
+            plan.set_learned_level_gate(level)
+            plan.learned_stats()
+            im.beamform(learned.COMB_LEARNED_MV)
+            gated, pixels = plan.learned_stats()
+            rates.append(gated / max(1, pixels))
+        assert 0.2 < rates[0] < 0.9 and rates[-1] < 1e-3, rates
+        assert rates[0] >= rates[1] >= rates[2] >= rates[3], rates
+        with pytest.raises(ValueError):
+            plan.set_learned_level_gate(0.5)
+        mlp.close()
+    finally:
+        im.close()

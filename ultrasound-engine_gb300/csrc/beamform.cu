@@ -1017,6 +1017,7 @@ struct usx_bf_plan {
   int lmv_beams = -1;   // < 0: the network's weights as predicted; >= 0: subspace refinement
   int lmv_use_net = 1;  // 0: the refinement's basis without the network's direction
   float lmv_share_gate = INFINITY;  // largest share of the refinement's power reduction from the network
+  float lmv_level_gate = INFINITY;  // largest tr(R) over its depth's geometric mean
   int64_t lmv_pixels = 0;      // pixels beamformed by the learned path since the last stats read
   // Training export (minimum variance plans): features, weights, valid flags.
   float* exp_feat = nullptr;
@@ -1188,20 +1189,21 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     const long rows = chunk * n_pix, padded = (rows + 127) / 128 * 128;
     const int widest = mlp_widest(plan->mlp);
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t sz[11] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
+    const size_t sz[12] = {up(sizeof(float2) * rows * a.n_ch), up(2 * padded * kLmvFeatures),
                           up(sizeof(float2) * rows * 64),       up(sizeof(float4) * rows),
                           up(2 * padded * widest),              up(2 * padded * widest),
                           up(sizeof(float) * padded * kLmvOutputs), up(sizeof(int2) * rows * kLmvGateClasses),
                           up(sizeof(int2) * rows), up(sizeof(int2) * rows),
                           plan->lmv_beams >= 0 ? up(static_cast<size_t>(lmv_subspace_record_bytes(plan->lmv_beams)) * rows)
-                                               : 0};
+                                               : 0,
+                          up(sizeof(float) * static_cast<size_t>(chunk) * plan->n1)};
     size_t total = 256;
     for (size_t b : sz) total += b;
     void* ws = nullptr;
     if (int rc = scratch(ctx, total, &ws)) return rc;
     char* q = static_cast<char*>(ws);
-    void* bufs[11];
-    for (int i = 0; i < 11; ++i) {
+    void* bufs[12];
+    for (int i = 0; i < 12; ++i) {
       bufs[i] = q;
       q += sz[i];
     }
@@ -1253,7 +1255,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       USX_CUDA(cudaMemsetAsync(counters, 0, (kLmvGateClasses + 2) * sizeof(int), ctx->stream));
       if (plan->lmv_beams >= 0) {
         if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate,
-                                         plan->lmv_use_net, plan->lmv_share_gate, counters,
+                                         plan->lmv_use_net, plan->lmv_share_gate, plan->lmv_level_gate,
+                                         static_cast<float*>(bufs[11]), counters,
                                          gated, static_cast<int>(nrows), plan->d_mv_stats + 2,
                                          static_cast<float*>(bufs[10])))
           return rc;
@@ -1604,6 +1607,14 @@ int usx_cu_bf_plan_set_learned_subspace(usx_bf_plan* plan, int use_network, floa
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_subspace: max_network_share must be >= 0");
   plan->lmv_use_net = use_network ? 1 : 0;
   plan->lmv_share_gate = max_network_share;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_learned_level_gate(usx_bf_plan* plan, float max_level_ratio) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_level_gate: null plan");
+  if (!(max_level_ratio >= 1.0f))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_level_gate: max_level_ratio must be >= 1");
+  plan->lmv_level_gate = max_level_ratio;
   return USX_OK;
 }
 

@@ -353,6 +353,8 @@ struct SubArgs {
   int rx_window;
   int use_net;            // 0: the beams alone (the network's direction left out)
   float share_gate;       // largest share of the power reduction the network's direction may carry
+  float log_level_gate;   // ln of the largest tr(R) over its depth's level (+inf: off)
+  float* level;           // [frame][n1]: mean over lines of ln tr(R) (the depth's level)
   int* gated_count;
   int2* gated;
   int gated_cap;
@@ -362,9 +364,9 @@ struct SubArgs {
 
 // Floats per pixel record between the two stages: the Gram matrix (upper
 // triangle, re/im), the projections of the subarray average, w_q^H 1, eps,
-// the snapshot count, the basis size, flags, L, valid.
+// the snapshot count, the basis size, flags, L, valid, tr(R).
 __host__ __device__ constexpr int lmv_rec_floats(int nb) {
-  return ((nb + 1) * (nb + 2) + 2 * (nb + 1) + 8 + 3) / 4 * 4;
+  return ((nb + 1) * (nb + 2) + 2 * (nb + 1) + 9 + 3) / 4 * 4;
 }
 
 // The beams' prefix sums are stored skewed, t at t + t / 16: conflict-free
@@ -432,7 +434,7 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
   extern __shared__ float4 sub_smem_raw[];
   constexpr int K1 = NB + 1;
   constexpr int kG = K1 * (K1 + 1);  // upper triangle of G, (re, im)
-  constexpr int kTail = kG + 2 * K1; // record: [G][Q^H abar][w_q^H 1, eps, K, nb, has_w, L, valid]
+  constexpr int kTail = kG + 2 * K1; // record: [G][Q^H abar][w_q^H 1, eps, K, nb, has_w, L, valid, tr R]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   SubWarpSmem<NB>& sm = *reinterpret_cast<SubWarpSmem<NB>*>(reinterpret_cast<char*>(sub_smem_raw) +
                                                            warp * sub_warp_bytes<NB>());
@@ -840,9 +842,36 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       tail[2 * K1 + 5] = has_w ? 1.f : 0.f;
       tail[2 * K1 + 6] = static_cast<float>(L);
       tail[2 * K1 + 7] = 1.f;   // record valid
+      tail[2 * K1 + 8] = tr / K;
     }
     __syncwarp();
   }
+}
+
+// The level of each depth: the mean over lateral lines of ln tr(R) of the
+// pixels with a record (the geometric mean of their covariance traces), one
+// thread per (frame, depth). A strong point target raises tr(R) far above its
+// depth's level in the pixels around it, where the subspace solve cannot form
+// the deep nulls of the exact minimum variance; the level gate sends those
+// pixels to the exact solver.
+template <int NB>
+__global__ void lmv_level_kernel(const SubArgs a) {
+  constexpr int K1 = NB + 1;
+  constexpr int kG = K1 * (K1 + 1);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const long frame = blockIdx.y;
+  if (j >= a.n1) return;
+  const int n0 = a.n_pix / a.n1;
+  float sum = 0.f;
+  int n = 0;
+  for (int i = 0; i < n0; ++i) {
+    const float* tail = a.rec + (frame * a.n_pix + static_cast<long>(i) * a.n1 + j) * lmv_rec_floats(NB) + kG;
+    if (tail[2 * K1 + 7] > 0.f && tail[2 * K1 + 8] > 0.f) {
+      sum += logf(tail[2 * K1 + 8]);
+      ++n;
+    }
+  }
+  a.level[frame * a.n1 + j] = n > 0 ? sum / static_cast<float>(n) : 0.f;
 }
 
 // Stage 2, one thread per pixel: (G / K + eps I) c = Q^H 1, then the output
@@ -858,6 +887,16 @@ __global__ void lmv_subspace_solve_kernel(const SubArgs a) {
   const float* tail = rec + kG;
   if (!(tail[2 * K1 + 7] > 0.f)) return;  // gated, or n_act < 4
   const float eps = tail[2 * K1 + 2], Kf = tail[2 * K1 + 3];
+  if (a.level && a.log_level_gate < INFINITY) {
+    const long frame = row / a.n_pix;
+    const int pix = static_cast<int>(row - frame * a.n_pix);
+    const float tr = tail[2 * K1 + 8];
+    if (tr > 0.f && logf(tr) - a.level[frame * a.n1 + pix % a.n1] > a.log_level_gate) {
+      push_gated(a.gated_count, a.gated, a.gated_cap, static_cast<int>(tail[2 * K1 + 6]), pix, frame);
+      if (a.stats) atomicAdd(a.stats, 1);
+      return;
+    }
+  }
   const int nb = static_cast<int>(tail[2 * K1 + 4]);
   const bool has_w = tail[2 * K1 + 5] > 0.f;
   const int L = static_cast<int>(tail[2 * K1 + 6]);
@@ -1045,8 +1084,8 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 
 
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int use_net, float share_gate, int* gated_count, int2* gated, int gated_cap,
-                        int* stats, float* rec) {
+                        float gate, int use_net, float share_gate, float level_gate, float* level,
+                        int* gated_count, int2* gated, int gated_cap, int* stats, float* rec) {
   SubArgs a;
   a.y = l.y;
   a.points = l.points;
@@ -1070,6 +1109,8 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.gate = gate;
   a.use_net = use_net;
   a.share_gate = share_gate;
+  a.log_level_gate = level_gate < INFINITY ? logf(std::max(level_gate, 1e-30f)) : INFINITY;
+  a.level = level_gate < INFINITY ? level : nullptr;
   a.rx_window = l.rx_window;
   a.gated_count = gated_count;
   a.gated = gated;
@@ -1078,7 +1119,7 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.rec = rec;
   if (l.n_ch > kSubMaxN || a.n_dmax > 9)
     return fail(USX_ERR_UNSUPPORTED, "learned-subspace refinement supports <= 128 channels, range average <= 4");
-  auto go = [&](auto gram, auto solve, size_t per_warp) -> int {
+  auto go = [&](auto gram, auto solve, auto level_k, size_t per_warp) -> int {
     const int smem = static_cast<int>(per_warp * kSubWarps);
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(gram), static_cast<size_t>(smem))) return rc_;
     int per_sm = 0;
@@ -1090,6 +1131,13 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
     gram<<<static_cast<unsigned>(std::max(1L, std::min(want, need))), 32 * kSubWarps, smem, ctx->stream>>>(a);
     prof_end(ctx);
     USX_CHECK_LAUNCH("lmv_subspace_gram_kernel");
+    if (a.level) {
+      prof_begin(ctx, "lmv_level_kernel");
+      level_k<<<dim3(static_cast<unsigned>(ceil_div(a.n1, 128)), static_cast<unsigned>(l.n_frames)), 128, 0,
+                ctx->stream>>>(a);
+      prof_end(ctx);
+      USX_CHECK_LAUNCH("lmv_level_kernel");
+    }
     prof_begin(ctx, "lmv_subspace_solve_kernel");
     solve<<<static_cast<unsigned>(ceil_div(a.n_rows, 128)), 128, 0, ctx->stream>>>(a);
     prof_end(ctx);
@@ -1097,10 +1145,10 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
     return USX_OK;
   };
   switch (std::min(kSubMaxBeams, 1 + n_beams)) {
-    case 1: return go(lmv_subspace_gram_kernel<1>, lmv_subspace_solve_kernel<1>, sub_warp_bytes<1>());
-    case 3: return go(lmv_subspace_gram_kernel<3>, lmv_subspace_solve_kernel<3>, sub_warp_bytes<3>());
-    case 5: return go(lmv_subspace_gram_kernel<5>, lmv_subspace_solve_kernel<5>, sub_warp_bytes<5>());
-    default: return go(lmv_subspace_gram_kernel<7>, lmv_subspace_solve_kernel<7>, sub_warp_bytes<7>());
+    case 1: return go(lmv_subspace_gram_kernel<1>, lmv_subspace_solve_kernel<1>, lmv_level_kernel<1>, sub_warp_bytes<1>());
+    case 3: return go(lmv_subspace_gram_kernel<3>, lmv_subspace_solve_kernel<3>, lmv_level_kernel<3>, sub_warp_bytes<3>());
+    case 5: return go(lmv_subspace_gram_kernel<5>, lmv_subspace_solve_kernel<5>, lmv_level_kernel<5>, sub_warp_bytes<5>());
+    default: return go(lmv_subspace_gram_kernel<7>, lmv_subspace_solve_kernel<7>, lmv_level_kernel<7>, sub_warp_bytes<7>());
   }
 }
 

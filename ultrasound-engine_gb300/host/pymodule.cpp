@@ -377,7 +377,8 @@ PYBIND11_MODULE(_usx, m) {
       .def_readwrite("mv_solver", &BeamformerConfig::mv_solver)
       .def_readwrite("learned_gate", &BeamformerConfig::learned_gate)
       .def_readwrite("learned_refine", &BeamformerConfig::learned_refine)
-      .def_readwrite("learned_share_gate", &BeamformerConfig::learned_share_gate);
+      .def_readwrite("learned_share_gate", &BeamformerConfig::learned_share_gate)
+      .def_readwrite("learned_level_gate", &BeamformerConfig::learned_level_gate);
 
   py::class_<Beamformer>(m, "Beamformer")
       .def(py::init<BeamformerConfig>(), py::arg("config") = BeamformerConfig{})

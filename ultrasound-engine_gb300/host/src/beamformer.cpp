@@ -40,8 +40,8 @@ namespace {
 // USX_LEARNED_MV_WEIGHTS, else the weights shipped beside the library
 // (<package>/weights/learned_mv_128ch_l64.bin), with the gates and subspace
 // refinement recorded in the ".gate" file written with the weights
-// ("<gate> [<beams> [<share gate>]]"); without it, gate 0.05, no refinement
-// and no share gate. BeamformerConfig's learned_* fields override these per
+// ("<gate> [<beams> [<share gate> [<level gate>]]]"); without it, gate 0.05,
+// no refinement and no share or level gate. BeamformerConfig's learned_* fields override these per
 // beamformer. The weights file is the trainer's raw format: "USXMLP1\0",
 // int32 n_layers, int32 dims[n_layers + 1], float32 parameters.
 struct LearnedNet {
@@ -49,6 +49,7 @@ struct LearnedNet {
   float gate = 0.05f;
   int refine = -1;   // DFT beams of the subspace refinement (< 0: none)
   float share_gate = INFINITY;
+  float level_gate = INFINITY;
 };
 
 std::string library_dir() {
@@ -89,13 +90,14 @@ LearnedNet learned_net(usx_ctx* ctx) {
   rt::check(usx_cu_mlp_create(ctx, n_layers, dims.data(), 0, &net.mlp), "learned network");
   rt::check(usx_cu_mlp_set_params(net.mlp, params.data()), "learned network weights");
   {
-    // "<gate> [<refine beams> [<share gate>]]", as written by the trainer's evaluation.
+    // "<gate> [<refine beams> [<share gate> [<level gate>]]]", as written by the trainer's evaluation.
     std::ifstream gf(path.substr(0, path.size() - 4) + ".gate");
     std::string gs;
     if (gf >> gs) net.gate = std::strtof(gs.c_str(), nullptr);
     int rv = 0;
     if (gf >> rv) net.refine = rv;
     if (gf >> gs) net.share_gate = std::strtof(gs.c_str(), nullptr);
+    if (gf >> gs) net.level_gate = std::strtof(gs.c_str(), nullptr);
   }
   nets.emplace(ctx, net);
   return net;
@@ -145,6 +147,7 @@ class PlanCache {
     put(&cfg.learned_gate, sizeof(real));
     put(&cfg.learned_refine, sizeof(int));
     put(&cfg.learned_share_gate, sizeof(real));
+    put(&cfg.learned_level_gate, sizeof(real));
     put(&data.demodulation_frequency, sizeof(real));
     put(&ev_begin, sizeof ev_begin);
     put(&ev_end, sizeof ev_end);
@@ -192,6 +195,8 @@ class PlanCache {
         rt::check(usx_cu_bf_plan_set_learned(plan, net.mlp, gate), "learned minimum variance");
         rt::check(usx_cu_bf_plan_set_learned_refine(plan, refine), "learned minimum variance refinement");
         rt::check(usx_cu_bf_plan_set_learned_subspace(plan, 1, share), "learned minimum variance share gate");
+        const float level = cfg.learned_level_gate >= 0.0f ? cfg.learned_level_gate : net.level_gate;
+        rt::check(usx_cu_bf_plan_set_learned_level_gate(plan, level), "learned minimum variance level gate");
       } catch (...) {
         usx_cu_bf_plan_destroy(plan);
         throw;

@@ -37,13 +37,14 @@ struct BeamformerConfig {
   // Fields below have no counterpart in the reference.
   MvSolver mv_solver = MvSolver::Tensor;
   // Learned minimum variance: the gate on the network's distortionless
-  // residual, the DFT beams of the subspace refinement (< 0: none) and the
-  // gate on the network direction's share of the power reduction. Negative
-  // gates and a refinement of -2 mean "as recorded with the weights" (their
-  // ".gate" file).
+  // residual, the DFT beams of the subspace refinement (< 0: none), the gate
+  // on the network direction's share of the power reduction and the gate on
+  // tr(R) over its depth's level. Negative gates and a refinement of -2 mean
+  // "as recorded with the weights" (their ".gate" file).
   real learned_gate = -1.0f;
   int learned_refine = -2;
   real learned_share_gate = -1.0f;
+  real learned_level_gate = -1.0f;
   void validate() const;
 };
 

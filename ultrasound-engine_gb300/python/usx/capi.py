@@ -357,6 +357,12 @@ class Plan:
                                                          C.c_float(max_network_share)),
               "bf_plan_set_learned_subspace")
 
+    def set_learned_level_gate(self, max_level_ratio: float = float("inf")) -> None:
+        """Pixels whose covariance trace exceeds this multiple of their depth's
+        geometric-mean trace go to the exact solver (+inf: off)."""
+        check(lib().usx_cu_bf_plan_set_learned_level_gate(self._h, C.c_float(max_level_ratio)),
+              "bf_plan_set_learned_level_gate")
+
     def learned_stats(self):
         """(pixels gated to the exact solver, pixels beamformed) since the last call."""
         a, b = C.c_int64(), C.c_int64()

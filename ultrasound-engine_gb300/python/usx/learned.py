@@ -366,16 +366,21 @@ class Mode:
     gate: float = math.inf
     share: float = math.inf
     use_net: bool = True
+    level: float = math.inf
 
     @property
     def label(self) -> str:
         if not self.use_net:
             return "beams_only"
-        return f"gate={self.gate:g},share={self.share:g}"
+        base = f"gate={self.gate:g},share={self.share:g}"
+        return base if math.isinf(self.level) else f"{base},level={self.level:g}"
 
 
-def modes_for(gates=(), shares=(), ablation: bool = True) -> list:
+def modes_for(gates=(), shares=(), ablation: bool = True, levels=(), level_shares=(math.inf,)) -> list:
+    """Modes of each single gate, and of every level gate combined with each of
+    `level_shares` (share gates)."""
     out = [Mode(gate=float(g)) for g in gates] + [Mode(share=float(x)) for x in shares]
+    out += [Mode(share=float(x), level=float(v)) for v in levels for x in level_shares]
     if ablation:
         out.append(Mode(use_net=False))
     seen, uniq = set(), []
@@ -401,6 +406,7 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, modes=(Mode(),), log=print,
         for m in modes:
             learned.set_learned(mlp, m.gate)
             learned.set_learned_subspace(m.use_net, m.share)
+            learned.set_learned_level_gate(m.level)
             learned.learned_stats()
             lf = imager.beamform(COMB_LEARNED_MV)
             gated, pixels = learned.learned_stats()
@@ -411,6 +417,7 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, modes=(Mode(),), log=print,
                                   "rel_l2": float((lf - ref).abs().pow(2).sum().sqrt()
                                                   / ref.abs().pow(2).sum().sqrt())})
         learned.set_learned_subspace(True, math.inf)
+        learned.set_learned_level_gate(math.inf)
         if log:
             log(f"phantom {s}: " + ", ".join(
                 f"{m.label}: fallback {rows[m.label][-1]['fallback_rate']:.3f} dgcnr "
@@ -450,7 +457,7 @@ def choose_mode(results: dict, modes, max_dgcnr: float = 0.01, max_fwhm: float =
         f = max(r.get(k, {}).get("max_rel_delta", 0.0) for k in ("lateral_fwhm_mm", "axial_fwhm_mm"))
         return (max(f / max_fwhm, r.get("gcnr", {}).get("max_abs_delta", 1.0) / max_dgcnr),
                 r["fallback_rate"])
-    finite = [m for m in cands if (math.isfinite(m.gate) or math.isfinite(m.share))
+    finite = [m for m in cands if (math.isfinite(m.gate) or math.isfinite(m.share) or math.isfinite(m.level))
               and results[m.label]["fallback_rate"] <= max_fallback]
     pool = finite or cands
     return (min(pool, key=worst), False) if pool else (None, False)
@@ -505,13 +512,19 @@ def main(argv=None) -> None:
                        help="gates on the network's distortionless residual (share gate off)")
         p.add_argument("--shares", default="0.02,0.05,0.1,0.2,0.3,0.5",
                        help="gates on the network direction's share of the power reduction (residual gate off)")
+        p.add_argument("--levels", default="3,10,30,100",
+                       help="gates on tr(R) over its depth's level, each alone and with every --level-shares")
+        p.add_argument("--level-shares", default="inf,0.2",
+                       help="share gates combined with each level gate")
         p.add_argument("--refine", type=int, default=DEFAULT_REFINE,
                        help="DFT beams beside the network's direction (-1: no refinement)")
         p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
     a = ap.parse_args(argv)
+    sub = a.refine >= 0
     modes = modes_for([float(g) for g in a.gates.split(",") if g],
-                      [float(x) for x in a.shares.split(",") if x] if a.refine >= 0 else [],
-                      ablation=a.refine >= 0)
+                      [float(x) for x in a.shares.split(",") if x] if sub else [], ablation=sub,
+                      levels=[float(v) for v in a.levels.split(",") if v] if sub else [],
+                      level_shares=[float(x) for x in a.level_shares.split(",") if x])
     imager = Imager()
     report = {"dims": list(DIMS), "setup": imager.setup.__dict__}
     eval_seeds = np.arange(900_000, 900_000 + (a.eval_phantoms if a.cmd == "train" else a.phantoms))
@@ -542,12 +555,14 @@ def main(argv=None) -> None:
     report["eval"] = {label: {k: v for k, v in r.items() if k != "rows"} for label, r in results.items()}
     chosen, ok = choose_mode(results, modes)
     report.pop("share_gate", None)
+    report.pop("level_gate", None)
     if chosen is not None:
-        report.update(gate=chosen.gate, share_gate=chosen.share, chosen=chosen.label, meets_bar=ok)
+        report.update(gate=chosen.gate, share_gate=chosen.share, level_gate=chosen.level, chosen=chosen.label,
+                      meets_bar=ok)
     path = Path(a.report) if a.report else out.with_suffix(".json")
     path.write_text(json.dumps(report, indent=1, default=float))
     if chosen is not None:
-        out.with_suffix(".gate").write_text(f"{chosen.gate} {a.refine} {chosen.share}\n")
+        out.with_suffix(".gate").write_text(f"{chosen.gate} {a.refine} {chosen.share} {chosen.level}\n")
     print(json.dumps({"chosen": report.get("chosen"), "meets_bar": ok, "eval": report["eval"]}, default=float))
     imager.close()
 
@@ -567,6 +582,16 @@ def trained_share_gate(weights=DEFAULT_WEIGHTS) -> float:
     p = Path(weights).with_suffix(".json")
     if p.exists():
         g = json.loads(p.read_text()).get("share_gate")
+        if g is not None:
+            return float(g)
+    return math.inf
+
+
+def trained_level_gate(weights=DEFAULT_WEIGHTS) -> float:
+    """The gate on tr(R) over its depth's level chosen with the weights (+inf: none)."""
+    p = Path(weights).with_suffix(".json")
+    if p.exists():
+        g = json.loads(p.read_text()).get("level_gate")
         if g is not None:
             return float(g)
     return math.inf
