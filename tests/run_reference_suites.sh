@@ -22,6 +22,8 @@ REF="${1:-${USX_REFERENCE_DIR:-/root/reference}}"
 WORK="${2:-$(mktemp -d)}"
 PKG="$ROOT/ultrasound-engine_gb300"
 mkdir -p "$WORK"
+WORK="$(cd "$WORK" && pwd)"
+REF="$(cd "$REF" 2>/dev/null && pwd || echo "$REF")"
 if [ ! -f "$REF/core/tests/test_main.cpp" ] || [ ! -f "$REF/tests/test_usx.py" ]; then
   echo "reference suites not found under $REF" >&2
   exit 3

@@ -1085,7 +1085,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
 // window (the Hankel structure: element i + 1 at snapshot s is element i at
 // s + 1) and writes 16-byte chunks in the 128-byte-swizzled K-major layout.
 
-constexpr int kCovThreads = 128;
+constexpr int kCovThreads = 256;   // eight warps: two per TMEM lane quarter in the epilogue
 
 struct MvCovArgs {
   MvTcArgs base;
@@ -1385,18 +1385,20 @@ __global__ void __launch_bounds__(kCovThreads, 1) mv_cov_tc5_kernel(const MvCovA
     }
     phase ^= 1u;
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // ---- epilogue: warp w holds rows 32 w .. 32 w + 31 -------------------
+    // ---- epilogue: warps w and w + 4 hold rows 32 (w % 4) .. + 31 (their
+    // TMEM lane quarter) and take alternate 32-column chunks --------------
     {
-      const int q = (warp * 32) / R;
+      const int quarter = warp & 3, half = warp >> 2;
+      const int q = (quarter * 32) / R;
       const CovItem& it = b.it[q];
-      const int ml0 = warp * 32 - q * R;     // first local row of this warp
+      const int ml0 = quarter * 32 - q * R;  // first local row of this warp
       if (it.state == 1 && ml0 < 2 * it.L) {
         const long rel = tile * P + q;
         float2* dst = c.r_out + rel * c.r_stride;
         const int ml = ml0 + lane, a_el = ml >> 1;
         const bool even = (ml & 1) == 0;
-        const unsigned taddr = tmem + (static_cast<unsigned>(warp * 32) << 16) + static_cast<unsigned>(q * R);
-        for (int j0 = 0; j0 < 2 * it.L; j0 += 32) {
+        const unsigned taddr = tmem + (static_cast<unsigned>(quarter * 32) << 16) + static_cast<unsigned>(q * R);
+        for (int j0 = 32 * half; j0 < 2 * it.L; j0 += 64) {
           uint32_t r[32];
           tc5_ld32(taddr + static_cast<unsigned>(j0), r);
 #pragma unroll

@@ -13,14 +13,17 @@
 //            the buffer is bit-identical. Its -40 dB tails are trimmed (warp
 //            max + ballots) and the trimmed field goes to global memory with a
 //            header (start time, length, position, amplitude);
-//   echo_kernel      one CTA per (group of elements, event), one warp per
-//            element, the element's RF row resident in shared memory: the warp
-//            walks every scatterer in order, sets up its echo on this element
-//            (distance, amplitude, delay, sample window) and the lanes add the
-//            echo samples (linear interpolation of the trimmed incident field)
-//            into the row, each sample owned by one lane, so every RF sample
-//            sums its scatterers in the same fixed order on every run. The row
-//            is then written once.
+//   echo_kernel      one CTA per (group of elements, event, slice of the
+//            scatterer list), one warp per element, the element's partial RF
+//            row resident in shared memory: the warp walks the slice's
+//            scatterers in order, sets up its echo on this element (distance,
+//            amplitude, delay, sample window) and the lanes add the echo
+//            samples (linear interpolation of the trimmed incident field) into
+//            the row, each sample owned by one lane. The partial row is
+//            written once;
+//   slice_sum_kernel sums the slices' partial rows in slice order into RF.
+//            Every RF sample therefore sums its scatterers in the same fixed
+//            order on every run.
 //
 // The reference reduces per-thread buffers in `omp critical` order, which is
 // arbitrary; here the order is the scatterer order.
@@ -53,6 +56,9 @@ struct SimArgs {
   float* rf;               // [ev][n_el][n_smp]
   unsigned long long* counter;
   float* inc;              // [ev - ev0][n_scat][inc_cap] trimmed incident fields
+  float* part;             // [ev - ev0][slice][n_el][n_smp] partial RF rows
+  int n_slices;
+  long slice_len;          // scatterers per slice
   float4* hdr;             // [ev - ev0][n_scat][2]: (t0, length bits, amplitude, -), (x, y, z, -)
   int ev0;                 // first event of this group
   int n_el, n_smp, n_ev, pulse_n, inc_cap;
@@ -212,8 +218,10 @@ __global__ void __launch_bounds__(32 * kEchoWarps) echo_kernel(const SimArgs a) 
   for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
   for (int k = threadIdx.x; k < n_warps * a.n_smp; k += blockDim.x) rows[k] = 0.0f;
   __syncthreads();
-  const int evl = blockIdx.y, ev = a.ev0 + evl;
+  const int evl = blockIdx.y, slice = blockIdx.z;
   const int e = blockIdx.x * n_warps + warp;
+  const long s_begin = static_cast<long>(slice) * a.slice_len;
+  const long s_end = min(a.n_scat, s_begin + a.slice_len);
   unsigned long long samples = 0;
   if (e < a.n_el) {
     float* row = rows + warp * a.n_smp;
@@ -222,13 +230,13 @@ __global__ void __launch_bounds__(32 * kEchoWarps) echo_kernel(const SimArgs a) 
     const float* incs = a.inc + static_cast<long>(evl) * a.n_scat * a.inc_cap;
     // The next scatterer's header is fetched while this one is processed.
     float4 h0n = make_float4(0.f, 0.f, 0.f, 0.f), h1n = h0n;
-    if (a.n_scat > 0) {
-      h0n = __ldg(hdr);
-      h1n = __ldg(hdr + 1);
+    if (s_begin < s_end) {
+      h0n = __ldg(hdr + 2 * s_begin);
+      h1n = __ldg(hdr + 2 * s_begin + 1);
     }
-    for (long si = 0; si < a.n_scat; ++si) {
+    for (long si = s_begin; si < s_end; ++si) {
       const float4 h0 = h0n, h1 = h1n;
-      if (si + 1 < a.n_scat) {
+      if (si + 1 < s_end) {
         h0n = __ldg(hdr + 2 * (si + 1));
         h1n = __ldg(hdr + 2 * (si + 1) + 1);
       }
@@ -259,10 +267,22 @@ __global__ void __launch_bounds__(32 * kEchoWarps) echo_kernel(const SimArgs a) 
       }
     }
     __syncwarp();
-    float* dst = a.rf + (static_cast<long>(ev) * a.n_el + e) * a.n_smp;
+    float* dst = a.part + ((static_cast<long>(evl) * a.n_slices + slice) * a.n_el + e) * a.n_smp;
     for (int n = lane; n < a.n_smp; n += 32) dst[n] = row[n];
   }
   if (lane == 0 && samples) atomicAdd(a.counter, samples);
+}
+
+// RF = the slices' partial rows summed in slice order (one thread per sample).
+__global__ void slice_sum_kernel(const SimArgs a, int n_ev_group) {
+  const long per_ev = static_cast<long>(a.n_el) * a.n_smp;
+  const long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+  if (i >= per_ev * n_ev_group) return;
+  const long evl = i / per_ev, k = i - evl * per_ev;
+  const float* p = a.part + evl * a.n_slices * per_ev + k;
+  float acc = 0.0f;
+  for (int sl = 0; sl < a.n_slices; ++sl) acc += p[sl * per_ev];
+  a.rf[(a.ev0 + evl) * per_ev + k] = acc;
 }
 
 __global__ void event_peak_kernel(const float* rf, long ev_size, unsigned* peak_bits) {
@@ -344,8 +364,18 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   const long n_sc = std::max<long>(1, n_scat);
   const size_t per_event = static_cast<size_t>(n_sc) * (static_cast<size_t>(inc_cap) * sizeof(float) + 2 * sizeof(float4));
   const int group = static_cast<int>(std::max<size_t>(1, std::min<size_t>(n_ev, (size_t(2) << 30) / per_event)));
+  // The echo stage in scatterer slices: enough CTAs for about four waves of
+  // the GPU, each slice's partial rows summed afterwards in slice order.
+  const int echo_warps = static_cast<int>(std::min<long>(kEchoWarps, (227L * 1024) / (4L * n_smp) - 1));
+  if (echo_warps < 1) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 28,000 samples per trace");
+  const long base_ctas = static_cast<long>(ceil_div(n_el, echo_warps)) * group;
+  const int n_slices = static_cast<int>(std::max<long>(1, std::min<long>({static_cast<long>(ctx->sm_count) * 12 /
+                                                                             std::max<long>(1, base_ctas),
+                                                                         n_sc, 256})));
+  const long slice_len = (n_sc + n_slices - 1) / n_slices;
+  const size_t part_bytes = sizeof(float) * static_cast<size_t>(group) * n_slices * n_el * n_smp;
   const size_t bytes = sizeof(float) * (2 * tbl + pulse.size()) + sizeof(int) * (tbl + n_ev) +
-                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + per_event * group + 4096;
+                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + per_event * group + part_bytes + 4096;
   void* ws = nullptr;
   if (int rc = scratch(ctx, bytes, &ws)) return rc;
   char* w = static_cast<char*>(ws);
@@ -363,6 +393,7 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   float* d_pulse = reinterpret_cast<float*>(take(sizeof(float) * pulse.size()));
   float4* d_hdr = reinterpret_cast<float4*>(take(sizeof(float4) * 2 * static_cast<size_t>(n_sc) * group));
   float* d_inc = reinterpret_cast<float*>(take(sizeof(float) * static_cast<size_t>(inc_cap) * n_sc * group));
+  float* d_part = reinterpret_cast<float*>(take(part_bytes));
   if (static_cast<size_t>(w - static_cast<char*>(ws)) > ctx->scratch_bytes)
     return fail(USX_ERR_INVALID, "usx_cu_simulate: scratch layout overflow");
   USX_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), ctx->stream));
@@ -384,6 +415,9 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.rf = rf;
   a.counter = d_counter;
   a.inc = d_inc;
+  a.part = d_part;
+  a.n_slices = n_slices;
+  a.slice_len = slice_len;
   a.hdr = d_hdr;
   a.ev0 = 0;
   a.n_el = n_el;
@@ -412,8 +446,6 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   if (smem_inc > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
   if (int rc_ = smem_limit(reinterpret_cast<const void*>(incident_kernel), smem_inc)) return rc_;
   // The echo stage keeps one RF row per warp plus the sample-time axis in shared memory.
-  const int echo_warps = static_cast<int>(std::min<long>(kEchoWarps, (227L * 1024) / (4L * n_smp) - 1));
-  if (echo_warps < 1) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 28,000 samples per trace");
   const size_t smem_echo = sizeof(float) * static_cast<size_t>(echo_warps + 1) * n_smp;
   if (int rc_ = smem_limit(reinterpret_cast<const void*>(echo_kernel), smem_echo)) return rc_;
   if (n_scat > 0) {
@@ -431,10 +463,15 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
       prof_end(ctx);
       USX_CHECK_LAUNCH("incident_kernel");
       prof_begin(ctx, "echo_kernel");
-      echo_kernel<<<dim3(static_cast<unsigned>(ceil_div(n_el, echo_warps)), ng), 32 * echo_warps, smem_echo,
-                    ctx->stream>>>(a);
+      echo_kernel<<<dim3(static_cast<unsigned>(ceil_div(n_el, echo_warps)), ng, n_slices), 32 * echo_warps,
+                    smem_echo, ctx->stream>>>(a);
       prof_end(ctx);
       USX_CHECK_LAUNCH("echo_kernel");
+      prof_begin(ctx, "slice_sum_kernel");
+      slice_sum_kernel<<<static_cast<unsigned>(ceil_div(static_cast<long>(ng) * n_el * n_smp, 256)), 256, 0,
+                         ctx->stream>>>(a, ng);
+      prof_end(ctx);
+      USX_CHECK_LAUNCH("slice_sum_kernel");
     }
   } else {
     USX_CUDA(cudaMemsetAsync(rf, 0, sizeof(float) * ev_size * n_ev, ctx->stream));
