@@ -854,24 +854,40 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
 // depth's level in the pixels around it, where the subspace solve cannot form
 // the deep nulls of the exact minimum variance; the level gate sends those
 // pixels to the exact solver.
+// One 128-thread block per (depth, frame): the threads stride over the
+// lines, then a fixed tree (warp shuffles, then the four warps in order).
 template <int NB>
-__global__ void lmv_level_kernel(const SubArgs a) {
+__global__ void __launch_bounds__(128) lmv_level_kernel(const SubArgs a) {
   constexpr int K1 = NB + 1;
   constexpr int kG = K1 * (K1 + 1);
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ float s_sum[4];
+  __shared__ int s_n[4];
+  const int j = blockIdx.x;
   const long frame = blockIdx.y;
-  if (j >= a.n1) return;
   const int n0 = a.n_pix / a.n1;
   float sum = 0.f;
   int n = 0;
-  for (int i = 0; i < n0; ++i) {
+  for (int i = threadIdx.x; i < n0; i += blockDim.x) {
     const float* tail = a.rec + (frame * a.n_pix + static_cast<long>(i) * a.n1 + j) * lmv_rec_floats(NB) + kG;
     if (tail[2 * K1 + 7] > 0.f && tail[2 * K1 + 8] > 0.f) {
       sum += logf(tail[2 * K1 + 8]);
       ++n;
     }
   }
-  a.level[frame * a.n1 + j] = n > 0 ? sum / static_cast<float>(n) : 0.f;
+  for (int o = 16; o > 0; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    n += __shfl_xor_sync(0xffffffffu, n, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_sum[threadIdx.x >> 5] = sum;
+    s_n[threadIdx.x >> 5] = n;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float t = ((s_sum[0] + s_sum[1]) + s_sum[2]) + s_sum[3];
+    const int c = s_n[0] + s_n[1] + s_n[2] + s_n[3];
+    a.level[frame * a.n1 + j] = c > 0 ? t / static_cast<float>(c) : 0.f;
+  }
 }
 
 // Stage 2, one thread per pixel: (G / K + eps I) c = Q^H 1, then the output
@@ -1133,8 +1149,7 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
     USX_CHECK_LAUNCH("lmv_subspace_gram_kernel");
     if (a.level) {
       prof_begin(ctx, "lmv_level_kernel");
-      level_k<<<dim3(static_cast<unsigned>(ceil_div(a.n1, 128)), static_cast<unsigned>(l.n_frames)), 128, 0,
-                ctx->stream>>>(a);
+      level_k<<<dim3(static_cast<unsigned>(a.n1), static_cast<unsigned>(l.n_frames)), 128, 0, ctx->stream>>>(a);
       prof_end(ctx);
       USX_CHECK_LAUNCH("lmv_level_kernel");
     }

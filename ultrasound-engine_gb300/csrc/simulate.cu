@@ -14,19 +14,22 @@
 //            max + ballots) and the trimmed field goes to global memory with a
 //            header (start time, length, position, amplitude);
 //   echo_kernel      one CTA per (group of elements, event, slice of the
-//            scatterer list), one warp per element, the element's partial RF
-//            row resident in shared memory: the warp walks the slice's
-//            scatterers in order, sets up its echo on this element (distance,
-//            amplitude, delay, sample window) and the lanes add the echo
-//            samples (linear interpolation of the trimmed incident field) into
-//            the row, each sample owned by one lane. The partial row is
-//            written once;
-//   slice_sum_kernel sums the slices' partial rows in slice order into RF.
-//            Every RF sample therefore sums its scatterers in the same fixed
-//            order on every run.
+//            scatterer list), one warp per element: the lanes take 32
+//            scatterers at a time, each setting up its echo on the warp's
+//            element (distance, amplitude, delay, sample window) and adding
+//            its echo samples (linear interpolation of the trimmed incident
+//            field) into the element's row in shared memory. The row holds
+//            64-bit fixed-point integers (the samples times 2^s, s chosen from
+//            a bound on every sum so nothing overflows), so the additions are
+//            exact and their order does not matter: every run gives the same
+//            bits. Rows are added (as integers) into a global accumulator;
+//   fixed_to_float_kernel converts the accumulator to the float RF.
 //
 // The reference reduces per-thread buffers in `omp critical` order, which is
-// arbitrary; here the order is the scatterer order.
+// arbitrary; here each RF sample is the exact sum of its contributions, each
+// rounded to the fixed-point step (2^-61 of the bound on any sum: for 100,000
+// scatterers about 1e-13 of one scatterer's largest echo, far below the float
+// rounding of a sample).
 //
 // Receive noise is added by a third kernel once an event's echoes are
 // complete: sigma = peak|RF| * 10^(noise_db/20), RF += z * sigma, with z the
@@ -41,7 +44,7 @@ namespace usxcu {
 namespace {
 
 constexpr int kSimWarps = 4;       // incident_kernel: warps (scatterers) per CTA
-constexpr int kEchoWarps = 8;      // echo_kernel: warps (elements) per CTA
+constexpr int kEchoWarps = 4;      // echo_kernel: warps (elements) per CTA
 constexpr int kMaxElem = 256;
 constexpr int kMaxPulse = 1024;
 
@@ -56,8 +59,8 @@ struct SimArgs {
   float* rf;               // [ev][n_el][n_smp]
   unsigned long long* counter;
   float* inc;              // [ev - ev0][n_scat][inc_cap] trimmed incident fields
-  float* part;             // [ev - ev0][slice][n_el][n_smp] partial RF rows
-  int n_slices;
+  unsigned long long* acc; // [ev - ev0][n_el][n_smp] 64-bit fixed-point RF of the group
+  unsigned* bound_bits;    // bound on one scatterer's contribution to any sample (float bits)
   long slice_len;          // scatterers per slice
   float4* hdr;             // [ev - ev0][n_scat][2]: (t0, length bits, amplitude, -), (x, y, z, -)
   int ev0;                 // first event of this group
@@ -197,6 +200,15 @@ __global__ void __launch_bounds__(32 * kSimWarps) incident_kernel(const SimArgs 
             trim_n = hi - lo + 1;
             float* dst = a.inc + (static_cast<long>(evl) * a.n_scat + si) * a.inc_cap;
             for (int k = lane; k < trim_n; k += 32) dst[k] = inc[lo + k];
+            // Largest contribution of this scatterer to any RF sample:
+            // |amplitude| x peak of the field x the largest element factor
+            // (directivity and attenuation are at most 1; spreading 1 / r).
+            float r_min = INFINITY;
+            for (int e = lane; e < a.n_el; e += 32) r_min = fminf(r_min, e_r[e]);
+            for (int o = 16; o > 0; o >>= 1) r_min = fminf(r_min, __shfl_xor_sync(0xffffffffu, r_min, o));
+            const float spread = a.spreading ? 1.0f / fmaxf(r_min, 1e-6f) : 1.0f;
+            const float bnd = fabsf(sc.amplitude) * peak * spread * 1.001f;
+            if (lane == 0 && bnd > 0.0f) atomicMax(a.bound_bits, __float_as_uint(bnd));
           }
         }
       }
@@ -208,81 +220,98 @@ __global__ void __launch_bounds__(32 * kSimWarps) incident_kernel(const SimArgs 
   }
 }
 
+// Fixed-point shift of a group: samples are stored times 2^(61 - e) with
+// n_scat x bound < 2^e, so no sum of contributions reaches 2^61 in
+// magnitude. The same on every thread.
+__device__ __forceinline__ int fixed_shift(const SimArgs& a) {
+  const float bound = __uint_as_float(*a.bound_bits);
+  int e = 0;
+  frexp(static_cast<double>(bound) * static_cast<double>(a.n_scat), &e);
+  return 61 - e;
+}
+
 __global__ void __launch_bounds__(32 * kEchoWarps) echo_kernel(const SimArgs a) {
   extern __shared__ float4 echo_smem[];
-  float* t_axis = reinterpret_cast<float*>(echo_smem);   // [n_smp]
-  float* rows = t_axis + a.n_smp;                        // [warps][n_smp]
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  unsigned long long* rows = reinterpret_cast<unsigned long long*>(echo_smem);   // [warps][n_smp]
+  float* t_axis = reinterpret_cast<float*>(rows + kEchoWarps * a.n_smp);       // [n_smp]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Sample times t0 + n / fs of the RF axis, each computed as the reference
   // does (float division).
   for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
-  for (int k = threadIdx.x; k < n_warps * a.n_smp; k += blockDim.x) rows[k] = 0.0f;
+  for (int k = threadIdx.x; k < kEchoWarps * a.n_smp; k += blockDim.x) rows[k] = 0ull;
   __syncthreads();
+  // 2^shift as two float factors, each within float range whatever the bound.
+  const int shift = fixed_shift(a);
+  const float scale1 = ldexpf(1.0f, shift / 2), scale2 = ldexpf(1.0f, shift - shift / 2);
   const int evl = blockIdx.y, slice = blockIdx.z;
-  const int e = blockIdx.x * n_warps + warp;
+  const int e = blockIdx.x * kEchoWarps + warp;
   const long s_begin = static_cast<long>(slice) * a.slice_len;
   const long s_end = min(a.n_scat, s_begin + a.slice_len);
   unsigned long long samples = 0;
   if (e < a.n_el) {
-    float* row = rows + warp * a.n_smp;
+    unsigned long long* row = rows + warp * a.n_smp;
     const float ex = (static_cast<float>(e) - a.half_nm1) * a.pitch;
     const float4* hdr = a.hdr + 2 * static_cast<long>(evl) * a.n_scat;
     const float* incs = a.inc + static_cast<long>(evl) * a.n_scat * a.inc_cap;
-    // The next scatterer's header is fetched while this one is processed.
-    float4 h0n = make_float4(0.f, 0.f, 0.f, 0.f), h1n = h0n;
-    if (s_begin < s_end) {
-      h0n = __ldg(hdr + 2 * s_begin);
-      h1n = __ldg(hdr + 2 * s_begin + 1);
-    }
-    for (long si = s_begin; si < s_end; ++si) {
-      const float4 h0 = h0n, h1 = h1n;
-      if (si + 1 < s_end) {
-        h0n = __ldg(hdr + 2 * (si + 1));
-        h1n = __ldg(hdr + 2 * (si + 1) + 1);
+    for (long s0 = s_begin; s0 < s_end; s0 += 32) {
+      // Lane = scatterer: its echo on this element.
+      const long si = s0 + lane;
+      int n0 = 1, n1 = 0;
+      float amp = 0.0f, delay = 0.0f, trim_t0 = 0.0f;
+      int trim_n = 0;
+      if (si < s_end) {
+        const float4 h0 = __ldg(hdr + 2 * si);
+        trim_n = __float_as_int(h0.y);
+        if (trim_n > 0) {
+          const float4 h1 = __ldg(hdr + 2 * si + 1);
+          const float r = dist3(h1.x, h1.y, h1.z, ex, 0.0f, 0.0f);
+          if (!(r < 1e-6f)) {
+            amp = elem_amp(a, h0.z, h1.x, ex, r);
+            if (amp != 0.0f) {
+              trim_t0 = h0.x;
+              delay = r / a.c;
+              const float span_t = static_cast<float>(trim_n - 1) / a.fs_os;
+              const float t_start = trim_t0 + delay;
+              const float t_end = t_start + span_t;
+              n0 = max(static_cast<int>(ceilf((t_start - a.t0) * a.fs)), 0);
+              n1 = min(static_cast<int>(floorf((t_end - a.t0) * a.fs)), a.n_smp - 1);
+            }
+          }
+        }
       }
-      const int trim_n = __float_as_int(h0.y);
-      if (trim_n <= 0) continue;
-      const float r = dist3(h1.x, h1.y, h1.z, ex, 0.0f, 0.0f);
-      if (r < 1e-6f) continue;
-      const float amp = elem_amp(a, h0.z, h1.x, ex, r);
-      if (amp == 0.0f) continue;
-      const float trim_t0 = h0.x;
-      const float delay = r / a.c;
-      const float span_t = static_cast<float>(trim_n - 1) / a.fs_os;
-      const float t_start = trim_t0 + delay;
-      const float t_end = t_start + span_t;
-      const int n0 = max(static_cast<int>(ceilf((t_start - a.t0) * a.fs)), 0);
-      const int n1 = min(static_cast<int>(floorf((t_end - a.t0) * a.fs)), a.n_smp - 1);
-      if (n0 > n1) continue;
-      samples += static_cast<unsigned long long>(n1 - n0 + 1);
-      const float* tr = incs + si * a.inc_cap;
-      for (int n = n0 + lane; n <= n1; n += 32) {
-        const float t = t_axis[n] - delay;
-        const float u = (t - trim_t0) * a.fs_os;
-        const int k = static_cast<int>(u);
-        if (k < 0 || k + 1 >= trim_n) continue;
-        const float f = u - static_cast<float>(k);
-        const float va = __ldg(tr + k), vb = __ldg(tr + k + 1);
-        row[n] += amp * (va + (vb - va) * f);
+      if (n0 <= n1) {
+        samples += static_cast<unsigned long long>(n1 - n0 + 1);
+        const float* tr = incs + si * a.inc_cap;
+        for (int n = n0; n <= n1; ++n) {
+          const float t = t_axis[n] - delay;
+          const float u = (t - trim_t0) * a.fs_os;
+          const int k = static_cast<int>(u);
+          if (k < 0 || k + 1 >= trim_n) continue;
+          const float f = u - static_cast<float>(k);
+          const float va = __ldg(tr + k), vb = __ldg(tr + k + 1);
+          const float v = amp * (va + (vb - va) * f);
+          atomicAdd(row + n, static_cast<unsigned long long>(__float2ll_rn((v * scale1) * scale2)));
+        }
       }
     }
     __syncwarp();
-    float* dst = a.part + ((static_cast<long>(evl) * a.n_slices + slice) * a.n_el + e) * a.n_smp;
-    for (int n = lane; n < a.n_smp; n += 32) dst[n] = row[n];
+    unsigned long long* dst = a.acc + (static_cast<long>(evl) * a.n_el + e) * a.n_smp;
+    for (int n = lane; n < a.n_smp; n += 32)
+      if (row[n]) atomicAdd(dst + n, row[n]);
   }
+  for (int o = 16; o > 0; o >>= 1) samples += __shfl_xor_sync(0xffffffffu, samples, o);
   if (lane == 0 && samples) atomicAdd(a.counter, samples);
 }
 
-// RF = the slices' partial rows summed in slice order (one thread per sample).
-__global__ void slice_sum_kernel(const SimArgs a, int n_ev_group) {
+// RF of the group's events from the fixed-point accumulator.
+__global__ void fixed_to_float_kernel(const SimArgs a, int n_ev_group) {
   const long per_ev = static_cast<long>(a.n_el) * a.n_smp;
   const long i = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
   if (i >= per_ev * n_ev_group) return;
+  const double inv = ldexp(1.0, -fixed_shift(a));
   const long evl = i / per_ev, k = i - evl * per_ev;
-  const float* p = a.part + evl * a.n_slices * per_ev + k;
-  float acc = 0.0f;
-  for (int sl = 0; sl < a.n_slices; ++sl) acc += p[sl * per_ev];
-  a.rf[(a.ev0 + evl) * per_ev + k] = acc;
+  const long long v = static_cast<long long>(a.acc[i]);
+  a.rf[(a.ev0 + evl) * per_ev + k] = static_cast<float>(static_cast<double>(v) * inv);
 }
 
 __global__ void event_peak_kernel(const float* rf, long ev_size, unsigned* peak_bits) {
@@ -365,17 +394,21 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   const size_t per_event = static_cast<size_t>(n_sc) * (static_cast<size_t>(inc_cap) * sizeof(float) + 2 * sizeof(float4));
   const int group = static_cast<int>(std::max<size_t>(1, std::min<size_t>(n_ev, (size_t(2) << 30) / per_event)));
   // The echo stage in scatterer slices: enough CTAs for about four waves of
-  // the GPU, each slice's partial rows summed afterwards in slice order.
-  const int echo_warps = static_cast<int>(std::min<long>(kEchoWarps, (227L * 1024) / (4L * n_smp) - 1));
-  if (echo_warps < 1) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 28,000 samples per trace");
-  const long base_ctas = static_cast<long>(ceil_div(n_el, echo_warps)) * group;
+  // the GPU; the slices' fixed-point rows add exactly into one accumulator.
+  // Each CTA keeps kEchoWarps fixed-point rows and the sample-time axis in
+  // shared memory.
+  const size_t smem_echo = sizeof(unsigned long long) * kEchoWarps * static_cast<size_t>(n_smp) +
+                           sizeof(float) * static_cast<size_t>(n_smp);
+  if (smem_echo > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: more than 6,900 samples per trace");
+  const long base_ctas = static_cast<long>(ceil_div(n_el, kEchoWarps)) * group;
   const int n_slices = static_cast<int>(std::max<long>(1, std::min<long>({static_cast<long>(ctx->sm_count) * 12 /
                                                                              std::max<long>(1, base_ctas),
-                                                                         n_sc, 256})));
-  const long slice_len = (n_sc + n_slices - 1) / n_slices;
-  const size_t part_bytes = sizeof(float) * static_cast<size_t>(group) * n_slices * n_el * n_smp;
+                                                                         (n_sc + 31) / 32, 4096})));
+  const long slice_len = ((n_sc + n_slices - 1) / n_slices + 31) / 32 * 32;
+  const size_t acc_bytes = sizeof(unsigned long long) * static_cast<size_t>(group) * n_el * n_smp;
   const size_t bytes = sizeof(float) * (2 * tbl + pulse.size()) + sizeof(int) * (tbl + n_ev) +
-                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + per_event * group + part_bytes + 4096;
+                       sizeof(unsigned long long) + sizeof(unsigned) * (n_ev + 1) + per_event * group + acc_bytes +
+                       4096;
   void* ws = nullptr;
   if (int rc = scratch(ctx, bytes, &ws)) return rc;
   char* w = static_cast<char*>(ws);
@@ -393,7 +426,8 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   float* d_pulse = reinterpret_cast<float*>(take(sizeof(float) * pulse.size()));
   float4* d_hdr = reinterpret_cast<float4*>(take(sizeof(float4) * 2 * static_cast<size_t>(n_sc) * group));
   float* d_inc = reinterpret_cast<float*>(take(sizeof(float) * static_cast<size_t>(inc_cap) * n_sc * group));
-  float* d_part = reinterpret_cast<float*>(take(part_bytes));
+  unsigned long long* d_acc = reinterpret_cast<unsigned long long*>(take(acc_bytes));
+  unsigned* d_bound = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
   if (static_cast<size_t>(w - static_cast<char*>(ws)) > ctx->scratch_bytes)
     return fail(USX_ERR_INVALID, "usx_cu_simulate: scratch layout overflow");
   USX_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), ctx->stream));
@@ -415,8 +449,8 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.rf = rf;
   a.counter = d_counter;
   a.inc = d_inc;
-  a.part = d_part;
-  a.n_slices = n_slices;
+  a.acc = d_acc;
+  a.bound_bits = d_bound;
   a.slice_len = slice_len;
   a.hdr = d_hdr;
   a.ev0 = 0;
@@ -445,8 +479,6 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   const size_t smem_inc = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem));
   if (smem_inc > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
   if (int rc_ = smem_limit(reinterpret_cast<const void*>(incident_kernel), smem_inc)) return rc_;
-  // The echo stage keeps one RF row per warp plus the sample-time axis in shared memory.
-  const size_t smem_echo = sizeof(float) * static_cast<size_t>(echo_warps + 1) * n_smp;
   if (int rc_ = smem_limit(reinterpret_cast<const void*>(echo_kernel), smem_echo)) return rc_;
   if (n_scat > 0) {
     int per_sm = 0;
@@ -458,20 +490,23 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
       const long want = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count * 4 / ng;
       const long need = (n_scat + kSimWarps - 1) / kSimWarps;
       const unsigned gx = static_cast<unsigned>(std::max(1L, std::min(want, need)));
+      USX_CUDA(cudaMemsetAsync(d_bound, 0, sizeof(unsigned), ctx->stream));
+      USX_CUDA(cudaMemsetAsync(d_acc, 0, sizeof(unsigned long long) * static_cast<size_t>(ng) * n_el * n_smp,
+                               ctx->stream));
       prof_begin(ctx, "incident_kernel");
       incident_kernel<<<dim3(gx, ng), 32 * kSimWarps, smem_inc, ctx->stream>>>(a);
       prof_end(ctx);
       USX_CHECK_LAUNCH("incident_kernel");
       prof_begin(ctx, "echo_kernel");
-      echo_kernel<<<dim3(static_cast<unsigned>(ceil_div(n_el, echo_warps)), ng, n_slices), 32 * echo_warps,
+      echo_kernel<<<dim3(static_cast<unsigned>(ceil_div(n_el, kEchoWarps)), ng, n_slices), 32 * kEchoWarps,
                     smem_echo, ctx->stream>>>(a);
       prof_end(ctx);
       USX_CHECK_LAUNCH("echo_kernel");
-      prof_begin(ctx, "slice_sum_kernel");
-      slice_sum_kernel<<<static_cast<unsigned>(ceil_div(static_cast<long>(ng) * n_el * n_smp, 256)), 256, 0,
-                         ctx->stream>>>(a, ng);
+      prof_begin(ctx, "fixed_to_float_kernel");
+      fixed_to_float_kernel<<<static_cast<unsigned>(ceil_div(static_cast<long>(ng) * n_el * n_smp, 256)), 256, 0,
+                              ctx->stream>>>(a, ng);
       prof_end(ctx);
-      USX_CHECK_LAUNCH("slice_sum_kernel");
+      USX_CHECK_LAUNCH("fixed_to_float_kernel");
     }
   } else {
     USX_CUDA(cudaMemsetAsync(rf, 0, sizeof(float) * ev_size * n_ev, ctx->stream));
