@@ -1189,6 +1189,90 @@ def run_sector(args) -> None:
     ctx.close()
 
 
+def run_queue(args) -> None:
+    """Mixed probe geometries in one persistent launch: 4 linear frames (128
+    elements, 75 plane waves, 512 x 1024, DAS) and 4 phased-array sector
+    frames (64 elements, 31 diverging waves, 256 x 1024, DAS), beamformed by
+    usx_cu_bf_execute_queue in one launch per step, with the same 8 frames as
+    one launch per frame (each plan's autotuned shape) timed beside it."""
+    import torch
+    import usx
+    from usx import capi
+    torch.cuda.set_device(0)
+    ctx = capi.Context(0)
+    _, probe, medium, acq, sim, txs, ph, grid = workload_setup()
+    ch_rf = _capi_channel(capi, probe, medium, acq, txs)
+    ch_iq = _capi_channel(capi, probe, medium, acq, txs, is_iq=True, fdem=F0)
+    d_sc = torch.from_numpy(_scatterers(ph)).cuda()
+    rf = torch.empty((N_TX, N_EL, N_SMP), device="cuda")
+    lin_iq = torch.empty((N_TX, N_EL, N_SMP), dtype=torch.complex64, device="cuda")
+    torch.cuda.synchronize()
+    ctx.simulate(ch_rf, capi.sim_config(), d_sc.data_ptr(), d_sc.shape[0], None, rf.data_ptr())
+    ctx.demodulate(ch_rf, capi.demod_config(), rf.data_ptr(), lin_iq.data_ptr())
+    sprobe = usx.Probe()
+    sprobe.n_elements, sprobe.pitch, sprobe.element_width = 64, 200e-6, 180e-6
+    sprobe.center_frequency, sprobe.bandwidth = 2.5e6, 0.6
+    sacq = usx.presets.acquisition(sprobe, depth=0.082, medium=medium, samples_per_wavelength=4.0)
+    ssim = usx.Simulator(sprobe, medium, sacq, usx.SimulatorConfig())
+    stxs = ssim.make_diverging_waves(usx.angles_deg(-45, 45, 31), 0.01)
+    sph = usx.Phantom.speckle_box(-0.06, 0.06, 0.004, 0.084, 0.0, 100_000, 2027)
+    sch_rf = _capi_channel(capi, sprobe, medium, sacq, stxs)
+    sch_iq = _capi_channel(capi, sprobe, medium, sacq, stxs, is_iq=True, fdem=2.5e6)
+    d_ssc = torch.from_numpy(_scatterers(sph)).cuda()
+    srf = torch.empty((31, 64, sacq.n_samples), device="cuda")
+    sec_iq = torch.empty((31, 64, sacq.n_samples), dtype=torch.complex64, device="cuda")
+    ctx.simulate(sch_rf, capi.sim_config(), d_ssc.data_ptr(), d_ssc.shape[0], None, srf.data_ptr())
+    ctx.demodulate(sch_rf, capi.demod_config(), srf.data_ptr(), sec_iq.data_ptr())
+    del rf, srf
+    sgrid = usx.ScanGrid.sector(float(np.deg2rad(-45.0)), float(np.deg2rad(45.0)), 256, 0.005, 0.08, 1024,
+                                usx.Vec3(0.0, 0.0, 0.0))
+    lin = ctx.plan(ch_iq, capi.Grid(0, np.asarray(grid.axis0), np.asarray(grid.axis1),
+                                    np.asarray(grid.points).reshape(-1, 3)), capi.bf_config(f_number=1.5))
+    sec = ctx.plan(sch_iq, capi.Grid(1, np.asarray(sgrid.axis0), np.asarray(sgrid.axis1),
+                                     np.asarray(sgrid.points).reshape(-1, 3)), capi.bf_config(f_number=1.5))
+    lin_out = [torch.empty((N0, N1), dtype=torch.complex64, device="cuda") for _ in range(4)]
+    sec_out = [torch.empty((256, 1024), dtype=torch.complex64, device="cuda") for _ in range(4)]
+    lin.autotune(lin_iq.data_ptr(), lin_out[0].data_ptr(), repeats=1)
+    sec.autotune(sec_iq.data_ptr(), sec_out[0].data_ptr(), repeats=1)
+    plans = [lin, sec] * 4
+    data = [lin_iq.data_ptr(), sec_iq.data_ptr()] * 4
+    outs = [o.data_ptr() for pair in zip(lin_out, sec_out) for o in pair]
+
+    def separate():
+        for p_, d_, o_ in zip(plans, data, outs):
+            p_.execute(d_, o_)
+
+    def queued():
+        ctx.execute_queue(plans, data, outs)
+
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(args.warmup):
+        separate()
+        queued()
+    ctx.synchronize()
+    sep_ms = timed(stream, separate, args.steps)
+    capi.profile(ctx, True)
+    capi.profile_reset(ctx)
+    with ClockSampler(0) as clocks:
+        ms = timed(stream, queued, args.steps)
+    prof = capi.profile_read(ctx)
+    capi.profile(ctx, False)
+    per = {k: v[0] / args.steps for k, v in prof.items()}
+    line = _stage_line("mixed-probe frames/s in one persistent launch (4 x 128-el 75-PW 512x1024 + 4 x 64-el "
+                       "31-DW sector 256x1024, DAS)", "frames/s", 8 * args.steps / (ms / 1e3), args, ms, prof,
+                       clocks, {"workload": "queue_4x_linear_512x1024_4x_sector_256x1024", "frames_per_step": 8,
+                                "launch": "one das_queue_kernel per step"},
+                       {"kernel": "das_queue_kernel", "bound": None, "achieved": None, "peak": None, "unit": None,
+                        "frac": None, "traffic": None},
+                       {"one_launch_per_frame": {"value": 8 * args.steps / (sep_ms / 1e3), "unit": "frames/s",
+                                                 "ms_per_step": sep_ms / args.steps},
+                        "kernels_ms_per_step": per})
+    print(json.dumps(line))
+    lin.close()
+    sec.close()
+    ctx.close()
+
+
 def run_mixed(args) -> None:
     """Mixed-probe streaming: per step one 128-element linear frame (75 plane
     waves, 512 x 1024) and one 64-element phased-array sector frame (31
@@ -1373,7 +1457,7 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="learned",
-                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "post", "batch", "sector",
+                    choices=sorted(WORKLOADS) + ["simulate", "demod", "doppler", "strain", "post", "batch", "sector", "queue",
                                                    "mixed"])
     ap.add_argument("--scatterers", type=int, default=100_000, help="simulate workload: phantom size")
     ap.add_argument("--gate", type=float, default=None, help="learned workload: gate (default: the weights' report)")
@@ -1400,6 +1484,8 @@ def main() -> int:
         run_batch(args)
     elif args.workload == "sector":
         run_sector(args)
+    elif args.workload == "queue":
+        run_queue(args)
     elif args.workload == "mixed":
         run_mixed(args)
     else:

@@ -293,6 +293,17 @@ int usx_cu_mlp_set_gemm_path(usx_mlp* mlp, int path);
 int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_frames,
                                const void* data, float* frames, int64_t frame_stride);
 
+/* Frames of many plans in one persistent launch (reference: Beamformer::beamform,
+ * beamformer.cpp:297-549, once per frame): entry i beamforms data[i] with
+ * plans[i] into frames[i] (one frame each; any probe, grid, transmit set and
+ * plain combiner — DAS, DMAS, coherence factor — coherent or select
+ * compounding, all IQ or all RF). The CTAs take tiles of all entries from one
+ * work counter, so frames of uneven size share the GPU without a tail per
+ * frame; each frame equals its plan's own execution bit for bit. Up to 48
+ * entries per launch (more are split); the plans must belong to ctx. */
+int usx_cu_bf_execute_queue(usx_ctx* ctx, int n, usx_bf_plan* const* plans, const void* const* data,
+                            float* const* frames);
+
 /* One-shot convenience: plan, execute, destroy (not graph-capturable). */
 int usx_cu_beamform(usx_ctx* ctx, const usx_channel_desc* cd, const void* data,
                     const usx_grid_desc* grid, const float* points_host,

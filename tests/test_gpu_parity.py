@@ -323,6 +323,65 @@ def test_das_variants_ragged_grid(capi, ctx, torch, golden, cfg_kw):
     plan.close()
 
 
+def test_execute_queue_equals_each_plans_own_execution(capi, ctx, torch, golden):
+    """Frames of different plans (probe geometry, grid, transmit set, combiner,
+    compounding) in one persistent launch: every frame equals its plan's own
+    execution bit for bit, including a 75-plane-wave 128-channel frame beside
+    the 32-element golden ones, and more entries than one launch takes (the
+    call splits them)."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    grid = capi.Grid(0, g["ax0"], g["ax1"], g["pts"])
+    sgrid = capi.Grid(1, g["sax0"], g["sax1"], g["spts"])
+    ch_pw = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    ch_foc = c_channel(capi, pr, med, acq, txset(g, "foc"), is_iq=True, fdem=5e6)
+    ch_div = c_channel(capi, pr, med, acq, txset(g, "div"), is_iq=True, fdem=5e6)
+    # A large frame of another probe: 128 channels, 75 plane waves, random IQ, 24 x 1024 pixels.
+    big_pr = O.probe()
+    big_acq = O.acquisition(fs=20e6, n_samples=2073, prf=5000.0)
+    ang = np.deg2rad(np.linspace(-16, 16, 75)).astype(np.float32)
+    ex = ((np.arange(128, dtype=np.float32) - np.float32(63.5)) * np.float32(300e-6)).astype(np.float32)
+    big_tx = O.TxSet(np.ones(75, np.int32), ang, np.tile([0, 0, 0.03], (75, 1)).astype(np.float32),
+                     np.zeros((75, 3), np.float32), (ex[None, :] * np.sin(ang)[:, None] / np.float32(1540.0)),
+                     np.ones((75, 128), np.float32))
+    ch_big = c_channel(capi, big_pr, med, big_acq, big_tx, is_iq=True, fdem=5e6)
+    rng = np.random.default_rng(9)
+    big_iq = (rng.standard_normal((75, 128, 2073), dtype=np.float32)
+              + 1j * rng.standard_normal((75, 128, 2073), dtype=np.float32)).astype(np.complex64)
+    bax0 = np.linspace(-0.01, 0.01, 24).astype(np.float32)
+    bax1 = np.linspace(0.005, 0.060, 1024).astype(np.float32)
+    bpts = np.stack(np.meshgrid(bax0, [0.0], bax1, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    big_grid = capi.Grid(0, bax0, bax1, bpts)
+    d_iq, d_foc, d_div, d_big = dev(torch, g["iq"]), dev(torch, g["foc_iq"]), dev(torch, g["div_iq"]), dev(torch, big_iq)
+    entries = [(ch_pw, grid, dict(f_number=1.5), d_iq), (ch_pw, grid, dict(f_number=1.5, coherence_factor=1), d_iq),
+               (ch_pw, grid, dict(f_number=1.5, combiner=1), d_iq),
+               (ch_foc, grid, dict(f_number=1.5, compounding=2), d_foc),
+               (ch_div, sgrid, dict(f_number=1.5), d_div), (ch_big, big_grid, dict(f_number=1.5), d_big)]
+    plans = [ctx.plan(ch, gr, capi.bf_config(**kw)) for ch, gr, kw, _ in entries]
+    want = []
+    for p, (_, gr, _, d) in zip(plans, entries):
+        out = torch.empty(gr.shape, dtype=torch.complex64, device="cuda")
+        p.execute(d.data_ptr(), out.data_ptr())
+        want.append(host(torch, out))
+    order = list(range(len(plans))) * 9          # 54 entries: two launches
+    outs = [torch.full(entries[i][1].shape, float("nan"), dtype=torch.complex64, device="cuda") for i in order]
+    ctx.execute_queue([plans[i] for i in order], [entries[i][3].data_ptr() for i in order],
+                      [o.data_ptr() for o in outs])
+    for i, o in zip(order, outs):
+        assert np.array_equal(host(torch, o), want[i]), i
+    mv = ctx.plan(ch_pw, grid, capi.bf_config(f_number=1.5, combiner=2))
+    with pytest.raises(RuntimeError, match="DAS, DMAS and coherence-factor"):
+        ctx.execute_queue([mv], [d_iq.data_ptr()], [outs[0].data_ptr()])
+    ch_rf = c_channel(capi, pr, med, acq, txset(s, "pw"))
+    rf_plan = ctx.plan(ch_rf, grid, capi.bf_config(f_number=1.5))
+    with pytest.raises(ValueError, match="mixed IQ and RF"):
+        ctx.execute_queue([plans[0], rf_plan], [d_iq.data_ptr(), d_iq.data_ptr()],
+                          [outs[0].data_ptr(), outs[1].data_ptr()])
+    for p in plans + [mv, rf_plan]:
+        p.close()
+
+
 def test_batch_and_sequence_equal_single_frames(capi, ctx, torch, golden):
     g = golden("bf")
     s = golden("sim")

@@ -233,6 +233,7 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
   a.out[frame * a.out_stride + pix] = make_float2(result.re, result.im);
 }
 
+
 // ------------------------------------------------------------------------
 // das_fast_kernel: the default beamformer (USX_BF_FAST).
 //
@@ -259,16 +260,14 @@ __global__ void __launch_bounds__(kBfThreads) das_kernel(const BfArgs a) {
 // are template parameters; every variant computes the same sums in the same
 // order (bit-identical frames), and the plan's autotuner picks the fastest
 // for its geometry.
-template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1,
-          bool kDeepFirst = false>
-__global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
+// One CTA tile (`tile` of frame `frame`) of the plan `a`: the body of
+// das_fast_kernel, also run by das_queue_kernel for the tiles of many plans.
+// rt_s: kRtShared's per-thread receive delays in shared memory.
+template <bool IQ, int kFastGroup, int kTileLines, bool kRtShared, int kWarpLines, bool kDeepFirst>
+__device__ __forceinline__ void das_fast_tile(const BfArgs& a, int tile, long frame, float* rt_s) {
   static_assert(kTileLines % kWarpLines == 0 && 32 % kWarpLines == 0, "warp shape must tile the CTA");
-  // kRtShared: the group's receive delays live in shared memory instead of
-  // registers, so that a larger group fits the register cap.
-  __shared__ float rt_s[kRtShared ? 32 * kTileLines * kFastGroup : 1];
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
-  const int tile = blockIdx.x;
   constexpr int kWarpDepths = 32 / kWarpLines;
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
   // Tile order. Default: depth tiles of a group of lines, then the next lines.
@@ -284,7 +283,6 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
   const int depth = depth_tile * 32 + (w % kWarpLines) * kWarpDepths + ln % kWarpDepths;
   if (line >= n0 || depth >= a.n1) return;
   const int pix = line * a.n1 + depth;
-  const long frame = blockIdx.y;
   const float px = __ldg(a.points + 3 * pix), py = __ldg(a.points + 3 * pix + 1),
               pz = __ldg(a.points + 3 * pix + 2);
   int ev_first = a.ev_begin, ev_last = a.ev_end;
@@ -438,6 +436,52 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
   if (a.is_mv) return;
   if (incoherent) result = mk(sqrtf(inc_acc), 0.0f);
   a.out[frame * a.out_stride + pix] = make_float2(result.re, result.im);
+}
+
+template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1,
+          bool kDeepFirst = false>
+__global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const BfArgs a) {
+  // kRtShared: the group's receive delays live in shared memory instead of
+  // registers, so that a larger group fits the register cap.
+  __shared__ float rt_s[kRtShared ? 32 * kTileLines * kFastGroup : 1];
+  das_fast_tile<IQ, kFastGroup, kTileLines, kRtShared, kWarpLines, kDeepFirst>(a, blockIdx.x, blockIdx.y, rt_s);
+}
+
+// ------------------------------------------------------------------------
+// das_queue_kernel: frames of many plans (any probe, grid, transmit set and
+// plain combiner) in one persistent launch. Each CTA takes the next tile
+// from a device counter, finds its (plan, frame) from the entries' tile
+// prefix, and runs das_fast_tile with that plan's arguments (kernel
+// parameters, indexed by entry). Tiles of every entry are the same as in the
+// plan's own launch, so each frame equals its plan's execution bit for bit.
+constexpr int kQueueMax = 48;
+
+struct DasQueueArgs {
+  BfArgs args[kQueueMax];
+  int tiles[kQueueMax];        // tiles per frame
+  int first[kQueueMax + 1];    // first work item of each entry (tiles x frames)
+  int n;
+  unsigned* next;              // work counter (zero at launch)
+};
+
+template <bool IQ, int kFastGroup, int kTileLines, int MINB, bool kRtShared = false, int kWarpLines = 1,
+          bool kDeepFirst = false>
+__global__ void __launch_bounds__(32 * kTileLines, MINB) das_queue_kernel(const DasQueueArgs q) {
+  __shared__ float rt_s[kRtShared ? 32 * kTileLines * kFastGroup : 1];
+  __shared__ int s_item;
+  const int total = q.first[q.n];
+  for (;;) {
+    if (threadIdx.x == 0) s_item = static_cast<int>(atomicAdd(q.next, 1u));
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    int e = 0;
+    while (e + 1 < q.n && item >= q.first[e + 1]) ++e;
+    const int local = item - q.first[e];
+    const int frame = local / q.tiles[e], tile = local - frame * q.tiles[e];
+    das_fast_tile<IQ, kFastGroup, kTileLines, kRtShared, kWarpLines, kDeepFirst>(q.args[e], tile, frame, rt_s);
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -1647,6 +1691,73 @@ int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pix
 
 int usx_cu_bf_execute(usx_bf_plan* plan, const void* data, float* frame) {
   return usx_cu_bf_execute_batch(plan, 1, data, 0, frame, 0);
+}
+
+int usx_cu_bf_execute_queue(usx_ctx* ctx, int n, usx_bf_plan* const* plans, const void* const* data,
+                            float* const* frames) {
+  if (!ctx || (n > 0 && (!plans || !data || !frames)))
+    return fail(USX_ERR_INVALID, "usx_cu_bf_execute_queue: null argument");
+  if (n <= 0) return USX_OK;
+  bool iq = false;
+  for (int i = 0; i < n; ++i) {
+    const usx_bf_plan* p = plans[i];
+    if (!p || !data[i] || !frames[i]) return fail(USX_ERR_INVALID, "usx_cu_bf_execute_queue: null entry");
+    if (p->ctx != ctx) return fail(USX_ERR_INVALID, "usx_cu_bf_execute_queue: a plan of another context");
+    if (p->cfg.combiner == USX_COMB_MV || p->cfg.combiner == USX_COMB_LEARNED_MV)
+      return fail(USX_ERR_UNSUPPORTED, "usx_cu_bf_execute_queue: DAS, DMAS and coherence-factor plans only");
+    if (p->precision != USX_BF_FAST)
+      return fail(USX_ERR_UNSUPPORTED, "usx_cu_bf_execute_queue: plans in the reference's operation order run alone");
+    if (p->cfg.compounding == USX_COMP_INCOHERENT)
+      return fail(USX_ERR_UNSUPPORTED, "usx_cu_bf_execute_queue: incoherent compounding runs alone");
+    if (i == 0) iq = p->cd.is_iq;
+    if (p->cd.is_iq != iq) return fail(USX_ERR_INVALID, "usx_cu_bf_execute_queue: mixed IQ and RF plans");
+  }
+  unsigned* next = reinterpret_cast<unsigned*>(ctx->d_status + 15);
+  for (int i0 = 0; i0 < n; i0 += kQueueMax) {
+    const int m = std::min(kQueueMax, n - i0);
+    DasQueueArgs q;
+    std::memset(&q, 0, sizeof(q));
+    q.n = 0;
+    q.first[0] = 0;
+    for (int k = 0; k < m; ++k) {
+      const usx_bf_plan* p = plans[i0 + k];
+      BfArgs a = make_args(p);
+      if (iq)
+        a.iq = static_cast<const float2*>(data[i0 + k]);
+      else
+        a.rf = static_cast<const float*>(data[i0 + k]);
+      a.out = reinterpret_cast<float2*>(frames[i0 + k]);
+      a.out_stride = 0;
+      a.data_stride = 0;
+      if (a.ev_end <= a.ev_begin) {  // no events: the reference's all-zero frame
+        USX_CUDA(cudaMemsetAsync(frames[i0 + k], 0, sizeof(float2) * a.n_pix, ctx->stream));
+        continue;
+      }
+      const int tiles = ceil_div(p->n0, 4) * ceil_div(p->n1, 32);
+      q.args[q.n] = a;
+      q.tiles[q.n] = tiles;
+      q.first[q.n + 1] = q.first[q.n] + tiles;
+      ++q.n;
+    }
+    if (q.n == 0) continue;
+    q.next = next;
+    USX_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), ctx->stream));
+    // IQ: the 4-channel, 4-line, 12-CTA shape with 4-line warps and the
+    // deepest tiles first (the autotuner's usual choice); RF: the RF shape.
+    const void* kern = iq ? reinterpret_cast<const void*>(das_queue_kernel<true, 4, 4, 12, false, 4, true>)
+                          : reinterpret_cast<const void*>(das_queue_kernel<false, 16, 4, 1>);
+    int per_sm = 0;
+    if (int rc = occupancy(kern, 32 * 4, 0, &per_sm)) return rc;
+    const unsigned grid = static_cast<unsigned>(std::max(1, per_sm) * ctx->sm_count);
+    prof_begin(ctx, "das_queue_kernel");
+    if (iq)
+      das_queue_kernel<true, 4, 4, 12, false, 4, true><<<grid, 32 * 4, 0, ctx->stream>>>(q);
+    else
+      das_queue_kernel<false, 16, 4, 1><<<grid, 32 * 4, 0, ctx->stream>>>(q);
+    prof_end(ctx);
+    USX_CHECK_LAUNCH("das_queue_kernel");
+  }
+  return USX_OK;
 }
 
 int usx_cu_beamform(usx_ctx* ctx, const usx_channel_desc* cd, const void* data,

@@ -273,6 +273,14 @@ class Context:
                                             C.byref(cfg), vp(vel), vp(pw), vp(var), vp(valid)),
               "color_flow_batch")
 
+    def execute_queue(self, plans, data_ptrs, frame_ptrs) -> None:
+        """One frame per (plan, data, frame) entry, all in one persistent launch."""
+        n = len(plans)
+        P = (vp * n)(*[p._h for p in plans])
+        D = (vp * n)(*[vp(x) for x in data_ptrs])
+        F = (vp * n)(*[vp(x) for x in frame_ptrs])
+        check(lib().usx_cu_bf_execute_queue(self._h, n, P, D, F), "bf_execute_queue")
+
     def axial_displacement(self, a_ptr, b_ptr, n0, n1, axis1, fdem, c, ka, kl, max_lag, axial_ptr, corr_ptr):
         ax = np.ascontiguousarray(axis1, dtype=np.float32)
         check(lib().usx_cu_axial_displacement(self._h, vp(a_ptr), vp(b_ptr), n0, n1, ax.ctypes.data_as(f32p),
