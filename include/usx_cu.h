@@ -45,6 +45,9 @@ typedef struct usx_mlp usx_mlp;
 /* ----------------------------------------------------------- context, memory */
 
 int usx_cu_abi_version(void);
+/* Compute capability of the device code the library loaded on the current
+ * device, major * 10 + minor (103 for sm_103a). Needs a device. */
+int usx_cu_binary_version(int* version);
 /* Message of the last failed call on this thread ("" if none). */
 const char* usx_cu_last_error(void);
 
@@ -156,6 +159,15 @@ int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* 
  * every line group's deepest depth tile goes first (the lightest tiles form
  * the grid's tail), 0 for depth tiles in ascending order. */
 int usx_cu_bf_variant_order(int index, int* deep_first);
+/* The kernel family of variant i: 0 thread per pixel with channel groups
+ * (tile_lines x 32 pixels per CTA), 1 the same with the trace windows staged
+ * by bulk copies, 2 a transmit table (32 pixels per CTA, warp_lines lines x
+ * 32 / warp_lines depths, one warp per channel_group channels; the transmit
+ * delay, phasor and illumination weight computed once per pixel and event).
+ * Families 1 and 2 fall back to variant 0 where they do not apply (RF data,
+ * incoherent compounding; family 1 also needs plane waves, family 2 at most
+ * 256 channels). */
+int usx_cu_bf_variant_kind(int index, int* kind);
 int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
 int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);
 int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, int repeats, float* ms_out);

@@ -40,13 +40,25 @@ def test_library_exports_every_declared_symbol():
     assert lib.usx_cu_abi_version() == 1
 
 
-def test_library_is_sm103a_only():
-    so = PKG / "lib" / "libusx_cu.so"
-    out = subprocess.run(["/usr/local/cuda/bin/cuobjdump", "--list-elf", str(so)], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    archs = set(re.findall(r"sm_\d+a?", out.stdout))
-    assert archs == {"sm_103a"}, archs
+def test_library_is_built_for_sm103a_only():
+    """The build compiles device code for one target, sm_103a (no PTX for a
+    JIT fallback, no other architecture)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("usx_build", PKG / "build.py")
+    B = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(B)
+    gencodes = re.findall(r"-gencode[= ]arch=(\w+),code=(\w+)", B.ARCH)
+    assert gencodes == [("compute_103a", "sm_103a")], gencodes
+    assert "-arch" not in B.ARCH and "compute_103a" not in gencodes[0][1]
+
+
+@pytest.mark.gpu
+def test_loaded_device_code_is_sm103():
+    """At run time the loaded kernels are sm_103 code (cudaFuncGetAttributes)."""
+    from usx import capi
+    v = C.c_int(0)
+    capi.check(capi.lib().usx_cu_binary_version(C.byref(v)), "usx_cu_binary_version")
+    assert v.value == 103
 
 
 def test_descriptor_layouts_match_header(tmp_path):

@@ -274,8 +274,9 @@ def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_k
     out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
     frames = []
     variants = capi.das_variants()
-    assert len(variants) >= 2 and variants[0] == (8, 4, 8, 1, 0)
+    assert len(variants) >= 2 and variants[0] == (8, 4, 8, 1, 0, 0)
     assert any(v[4] == 1 for v in variants)  # deepest-tiles-first orders are candidates
+    assert any(v[5] == 2 for v in variants)  # transmit-table kernels are candidates
     for v in range(len(variants)):
         plan.set_variant(v)
         plan.execute(d.data_ptr(), out.data_ptr())

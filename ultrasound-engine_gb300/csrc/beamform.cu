@@ -485,6 +485,222 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_queue_kernel(const 
 }
 
 // ------------------------------------------------------------------------
+// das_table_kernel: the fast delay-and-sum with the transmit side computed
+// once per (pixel, event). A CTA is 32 pixels (kWL lines x 32 / kWL depths,
+// one per lane) and one warp per group of G channels (all warps share the
+// lanes' pixels). For each chunk of events the warps first fill a table of
+// (transmit delay, weighted transmit phasor, illumination weight) for the 32
+// pixels in shared memory, each warp its share of the events; then every
+// warp runs its channels over the chunk's events, reading one table entry per
+// event instead of evaluating the illumination weight, the transmit delay and
+// its phasor once per channel group as das_fast_kernel does. The per-channel
+// sums, the receive phasor and aperture weight are das_fast_kernel's
+// expressions in the same order, so the per-channel values are the same bit
+// for bit; they are staged in shared memory [pixel][channel] and either
+// written out as rows (the minimum-variance export: 32 contiguous rows of
+// n_ch samples instead of one sample per pixel and channel) or combined by
+// the first warp, channel by channel in ascending order as das_fast_kernel
+// does. IQ data, coherent and select compounding, n_ch <= 256.
+// Measured at 128 channels, 75 plane waves, 512 x 1024 (ms per frame against
+// 4.98 for das_fast_kernel's best shape): G = 8 with 1, 2, 4 lines per CTA
+// and two CTAs per SM 8.63, 8.39, 8.29; G = 8, three CTAs 7.87; G = 4, one
+// CTA of 32 warps 9.21; G = 4, two CTAs (64 warps per SM) 6.06. The warps of a
+// CTA read different traces, so none of the L1 reuse that das_fast_kernel's
+// warps get from sharing each trace window remains, and the gathers' latency
+// outweighs the transmit work saved. G = 4 with two CTAs stays a candidate.
+constexpr int kTableEv = 32;    // events per table chunk (16 KB)
+constexpr int kTableMaxCh = 256;
+
+__host__ __device__ inline int table_warps(int group, int n_ch) {
+  const int cap = group >= 8 ? 16 : 32;
+  const int need = (n_ch + group - 1) / group;
+  return need < cap ? need : cap;
+}
+__host__ __device__ inline size_t table_stage_off() { return sizeof(float4) * kTableEv * 32; }
+__host__ __device__ inline size_t table_smem_bytes(int n_ch) {
+  return table_stage_off() + sizeof(float2) * 33 * n_ch + 32 * n_ch;
+}
+
+template <int G, int kWL, int MINB>
+__global__ void __launch_bounds__(32 * (G >= 8 ? 16 : 32), MINB) das_table_kernel(const BfArgs a) {
+  extern __shared__ float4 table_smem[];
+  float4* tab = table_smem;                                                    // [event in chunk][lane]
+  // Staged channel values [channel][33] (one pad column: rows of a pixel read
+  // along channels stay conflict-free) and active flags [channel][32].
+  float2* ys = reinterpret_cast<float2*>(reinterpret_cast<char*>(table_smem) + table_stage_off());
+  unsigned char* act_s = reinterpret_cast<unsigned char*>(ys + 33 * a.n_ch);
+  constexpr int kWD = 32 / kWL;
+  const int n0 = a.n_pix / a.n1;
+  const int tiles_depth = (a.n1 + kWD - 1) / kWD;
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  const long frame = blockIdx.y;
+  const int line = (static_cast<int>(blockIdx.x) / tiles_depth) * kWL + ln / kWD;
+  const int depth = (static_cast<int>(blockIdx.x) % tiles_depth) * kWD + ln % kWD;
+  const bool valid = line < n0 && depth < a.n1;
+  const int pix = valid ? line * a.n1 + depth : 0;
+  const float px = __ldg(a.points + 3 * pix), py = __ldg(a.points + 3 * pix + 1), pz = __ldg(a.points + 3 * pix + 2);
+  int ev_lo = a.ev_begin, ev_hi = a.ev_end;
+  if (a.seq_epf > 0) {
+    ev_lo = a.ev_begin + static_cast<int>(frame) * a.seq_epf;
+    ev_hi = ev_lo + a.seq_epf;
+  }
+  if (a.pass >= 0) {
+    ev_lo += a.pass;
+    ev_hi = ev_lo + 1;
+  }
+  const bool select = a.compounding == USX_COMP_SELECT;
+  int best_ev = -1;
+  float best_w = 0.0f;
+  if (select) {
+    for (int ev = ev_lo; ev < ev_hi; ++ev) {
+      const float tw = tx_sensitivity_fast(a.tx[ev], px, pz, a.lambda);
+      if (tw > best_w) {
+        best_w = tw;
+        best_ev = ev;
+      }
+    }
+  }
+  const float2* iq = a.iq + frame * a.data_stride;
+  const unsigned n_last = static_cast<unsigned>(a.n_smp - 1);
+  const int ch_stride = G * n_warps;
+  const bool one_chunk = ev_hi - ev_lo <= kTableEv;
+
+  for (int g = G * w, g_first = 0; g_first < a.n_ch; g += ch_stride, g_first += ch_stride) {
+    float rt[G];
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const int ch = g + k;
+      rt[k] = 0.0f;
+      if (valid && ch < a.n_ch) {
+        const float ex = elem_x(a, ch);
+        if (aperture_weight(ex, px, pz, a.f_number, a.rx_window, a.tukey_alpha) > 0.0f) {
+          mask |= 1u << k;
+          rt[k] = dist3(ex, 0.0f, 0.0f, px, py, pz) / a.c;
+        }
+      }
+    }
+    float ar[G], ai[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) ar[k] = ai[k] = 0.0f;
+    for (int c0 = ev_lo; c0 < ev_hi; c0 += kTableEv) {
+      const int c1 = min(ev_hi, c0 + kTableEv);
+      if (g_first == 0 || !one_chunk) {
+        // The chunk's table: (tau, tw cos, tw sin, tw) for this lane's pixel.
+        __syncthreads();
+        for (int e = c0 + w; e < c1; e += n_warps) {
+          const TxDev& t = a.tx[e];
+          float tw;
+          if (select)
+            tw = (best_ev == e && best_w > 0.0f) ? 1.0f : 0.0f;
+          else if (a.tx_weighting)
+            tw = tx_sensitivity_fast(t, px, pz, a.lambda);
+          else
+            tw = 1.0f;
+          float4 ent = make_float4(0.f, 0.f, 0.f, tw);
+          if (tw > 0.0f) {
+            const float tau = tx_arrival(t, px, py, pz, a.c);
+            float tc = 1.0f, ts = 0.0f;
+            if (a.fdem > 0.0f) sincosf(a.two_pi_f * tau, &ts, &tc);
+            ent = make_float4(tau, tw * tc, tw * ts, tw);
+          }
+          tab[(e - c0) * 32 + ln] = ent;
+        }
+        __syncthreads();
+      }
+      if (!mask) continue;
+      for (int e = c0; e < c1; ++e) {
+        const float4 ent = tab[(e - c0) * 32 + ln];
+        if (ent.w <= 0.0f) continue;
+        const float tau = ent.x, wr = ent.y, wi = ent.z;
+        const float2* trace = iq + (static_cast<long>(e) * a.n_ch + g) * a.n_smp;
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          if (!(mask & (1u << k))) continue;
+          const float idx = (tau + rt[k] - a.t0) * a.fs;
+          const float fl = floorf(idx);
+          const int kk = static_cast<int>(fl);
+          if (static_cast<unsigned>(kk) >= n_last) continue;
+          const float f = idx - fl;
+          const float2* tr = trace + static_cast<long>(k) * a.n_smp + kk;
+          const float2 s0 = __ldg(tr), s1 = __ldg(tr + 1);
+          const float vr = fmaf(f, s1.x - s0.x, s0.x);
+          const float vi = fmaf(f, s1.y - s0.y, s0.y);
+          ar[k] = fmaf(wr, vr, fmaf(-wi, vi, ar[k]));
+          ai[k] = fmaf(wr, vi, fmaf(wi, vr, ai[k]));
+        }
+      }
+    }
+    // Each channel's aperture weight and receive phasor; staged per pixel.
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const int ch = g + k;
+      if (ch >= a.n_ch) break;
+      const bool act = (mask >> k) & 1u;
+      float2 y = make_float2(0.f, 0.f);
+      if (act) {
+        const float wt = aperture_weight(elem_x(a, ch), px, pz, a.f_number, a.rx_window, a.tukey_alpha);
+        const float ap = a.is_mv ? 1.0f : wt;
+        float rc = 1.0f, rs = 0.0f;
+        if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs, &rc);
+        const float gr = ap * rc, gi = ap * rs;
+        y = make_float2(fmaf(gr, ar[k], -gi * ai[k]), fmaf(gr, ai[k], gi * ar[k]));
+      }
+      ys[ch * 33 + ln] = y;
+      act_s[ch * 32 + ln] = act ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  if (a.is_mv) {
+    // 32 rows of n_ch samples, written by the whole CTA.
+    for (int i = threadIdx.x; i < 32 * a.n_ch; i += blockDim.x) {
+      const int p = i / a.n_ch, ch = i - p * a.n_ch;
+      const int pl = (static_cast<int>(blockIdx.x) / tiles_depth) * kWL + p / kWD;
+      const int pd = (static_cast<int>(blockIdx.x) % tiles_depth) * kWD + p % kWD;
+      if (pl < n0 && pd < a.n1)
+        a.y_out[(frame * a.n_pix + static_cast<long>(pl) * a.n1 + pd) * a.n_ch + ch] = ys[ch * 33 + p];
+    }
+    return;
+  }
+  if (w != 0 || !valid) return;
+  cplx das = mk(0.f, 0.f), s = mk(0.f, 0.f), q = mk(0.f, 0.f), coh = mk(0.f, 0.f);
+  float incs = 0.0f;
+  int n_active = 0;
+  for (int ch = 0; ch < a.n_ch; ++ch) {
+    const float2 yv = ys[ch * 33 + ln];
+    const cplx y = mk(yv.x, yv.y);
+    const bool act = act_s[ch * 32 + ln] != 0;
+    n_active += act ? 1 : 0;
+    if (a.combiner == USX_COMB_DMAS) {
+      const float m = cabsf_(y);
+      if (m > 0.0f) {
+        const cplx v = cdivr(y, sqrtf(m));
+        s = cadd(s, v);
+        q = cadd(q, cmul(v, v));
+      }
+    } else {
+      das = cadd(das, y);
+    }
+    if (a.cf && act) {
+      coh = cadd(coh, y);
+      incs += cnorm(y);
+    }
+  }
+  cplx out;
+  if (n_active == 0) {
+    out = mk(0.f, 0.f);
+  } else if (a.combiner == USX_COMB_DMAS) {
+    const cplx acc = cscale(csub(cmul(s, s), q), 0.5f);
+    out = cdivr(acc, 0.5f * fmaxf(1.0f, static_cast<float>(n_active - 1)));
+  } else {
+    out = das;
+  }
+  if (a.cf && n_active > 0)
+    out = cscale(out, (incs > 0.0f) ? cnorm(coh) / (static_cast<float>(n_active) * incs) : 0.0f);
+  a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+}
+
+// ------------------------------------------------------------------------
 // das_staged_kernel: the fast delay-and-sum with the IQ windows of every
 // (channel group, kE transmits) step staged in shared memory by the tensor
 // memory accelerator (cp.async.bulk, one 1-D bulk copy per channel row,
@@ -818,17 +1034,24 @@ struct DasVariant {
   void (*iq)(BfArgs);
   void (*rf)(BfArgs);
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
+  bool table;    // das_table_kernel (IQ, coherent or select, n_ch <= 256); else variant 0
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
 template <int G, int TL, int MB, bool RTS = false, int WL = 1, bool DF = false>
 constexpr DasVariant das_variant() {
   return DasVariant{G,     TL, MB, WL, DF, das_fast_kernel<true, G, TL, MB, RTS, WL, DF>,
-                    das_fast_kernel<false, 16, 4, 1>, false};
+                    das_fast_kernel<false, 16, 4, 1>, false, false};
+}
+// Transmit-table shapes: channels per warp G, lines per CTA WL (32 / WL
+// depths), MB resident CTAs per SM.
+template <int G, int WL, int MB>
+constexpr DasVariant das_table_variant() {
+  return DasVariant{G, WL, MB, WL, false, das_table_kernel<G, WL, MB>, das_fast_kernel<false, 16, 4, 1>, false, true};
 }
 template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
-  return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true};
+  return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true, false};
 }
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
@@ -838,6 +1061,7 @@ const DasVariant kDasVariants[] = {
     das_variant<8, 2, 16, false, 2>(), das_variant<8, 8, 4, false, 4>(), das_variant<8, 8, 4, false, 8>(),
     das_variant<4, 4, 12, false, 2, true>(), das_variant<4, 4, 12, false, 4, true>(),
     das_variant<8, 4, 8, false, 4, true>(),
+    das_table_variant<4, 2, 2>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -1200,12 +1424,24 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
                     reinterpret_cast<uintptr_t>(data) % 16 == 0 && a.n_smp >= kStageW + 2;
     if (!ok) dvp = &kDasVariants[0];
   }
+  if (dvp->table) {
+    const bool ok = plan->cd.is_iq && a.compounding != USX_COMP_INCOHERENT && a.n_ch <= kTableMaxCh;
+    if (!ok) dvp = &kDasVariants[0];
+  }
   const DasVariant& dv = *dvp;
-  dim3 grid_das(fast ? ceil_div(plan->n0, dv.tile_lines) * ceil_div(plan->n1, 32) : ceil_div(n_pix, kBfThreads),
+  const bool table = fast && dv.table;
+  dim3 grid_das(table  ? ceil_div(plan->n0, dv.warp_lines) * ceil_div(plan->n1, 32 / dv.warp_lines)
+                : fast ? ceil_div(plan->n0, dv.tile_lines) * ceil_div(plan->n1, 32)
+                       : ceil_div(n_pix, kBfThreads),
                 n_frames);
+  const size_t table_smem = table ? table_smem_bytes(a.n_ch) : 0;
+  if (table)
+    if (int rc_ = smem_limit(reinterpret_cast<const void*>(dv.iq), table_smem)) return rc_;
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
     prof_begin(ctx, name);
-    if (fast) {
+    if (table) {
+      dv.iq<<<grid_das, 32 * table_warps(dv.group, b.n_ch), table_smem, ctx->stream>>>(b);
+    } else if (fast) {
       if (plan->cd.is_iq)
         dv.iq<<<grid_das, 32 * dv.tile_lines, 0, ctx->stream>>>(b);
       else
@@ -1547,6 +1783,12 @@ int usx_cu_bf_variant_info(int index, int* channel_group, int* tile_lines, int* 
 int usx_cu_bf_variant_order(int index, int* deep_first) {
   if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_order: no such variant");
   if (deep_first) *deep_first = kDasVariants[index].deep_first ? 1 : 0;
+  return USX_OK;
+}
+
+int usx_cu_bf_variant_kind(int index, int* kind) {
+  if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_kind: no such variant");
+  if (kind) *kind = kDasVariants[index].table ? 2 : kDasVariants[index].staged ? 1 : 0;
   return USX_OK;
 }
 

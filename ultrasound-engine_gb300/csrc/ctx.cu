@@ -174,6 +174,9 @@ int validate_channel(const usx_channel_desc& cd) {
   return USX_OK;
 }
 
+// Never launched: its attributes tell which device code the library carries.
+__global__ void binary_version_kernel() {}
+
 }  // namespace usxcu
 
 using namespace usxcu;
@@ -181,6 +184,14 @@ using namespace usxcu;
 extern "C" {
 
 int usx_cu_abi_version(void) { return USX_CU_ABI_VERSION; }
+
+int usx_cu_binary_version(int* version) {
+  if (!version) return fail(USX_ERR_INVALID, "usx_cu_binary_version: version is NULL");
+  cudaFuncAttributes a{};
+  USX_CUDA(cudaFuncGetAttributes(&a, binary_version_kernel));
+  *version = a.binaryVersion;
+  return USX_OK;
+}
 
 const char* usx_cu_last_error(void) { return g_last_error.c_str(); }
 

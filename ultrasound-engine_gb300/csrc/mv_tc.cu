@@ -1791,6 +1791,10 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
                          : P == 2 ? reinterpret_cast<const void*>(mv_cov_tc5_kernel<2>)
                                   : reinterpret_cast<const void*>(mv_cov_tc5_kernel<1>);
         if (int rc_ = smem_limit(kern, smem)) return rc_;
+        // The kernel reads nothing through L1 that it does not stage: all of
+        // the SM's unified memory may go to shared memory, two CTAs of ~100 KB.
+        USX_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      static_cast<int>(cudaSharedmemCarveoutMaxShared)));
         int per_sm = 0;
         if (int rc_ = occupancy(kern, kCovThreads, smem, &per_sm)) return rc_;
         // At most four CTAs per SM: each holds 128 of the SM's 512 TMEM columns.

@@ -489,13 +489,15 @@ class Mlp:
 
 def das_variants() -> list:
     """(channel group, tile lines, min resident CTAs, lines per warp, deepest
-    tiles first) of each delay-and-sum variant."""
+    tiles first, kind) of each delay-and-sum variant; kind 0: thread per
+    pixel, 1: staged trace windows, 2: transmit table."""
     out = []
     for i in range(lib().usx_cu_bf_variant_count()):
-        g, t, m, w, d = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        g, t, m, w, d, k = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         check(lib().usx_cu_bf_variant_info(i, C.byref(g), C.byref(t), C.byref(m), C.byref(w)), "bf_variant_info")
         check(lib().usx_cu_bf_variant_order(i, C.byref(d)), "bf_variant_order")
-        out.append((g.value, t.value, m.value, w.value, d.value))
+        check(lib().usx_cu_bf_variant_kind(i, C.byref(k)), "bf_variant_kind")
+        out.append((g.value, t.value, m.value, w.value, d.value, k.value))
     return out
 
 
