@@ -332,7 +332,7 @@ def subspace_flops_per_frame(grid_pts: np.ndarray, nb: int) -> float:
 
 
 def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks: dict,
-                    refine_beams: int = -1) -> dict:
+                    refine_beams: int = -1, mv_mode: int = 1) -> dict:
     """Roofline of the dominant kernel of the timed region: algorithmic work
     per frame over that kernel's device time per frame (CUDA events on the
     launching stream)."""
@@ -346,7 +346,15 @@ def kernel_roofline(prof: dict, frames: int, pts: np.ndarray, txs, probe, peaks:
            "kernels_ms_per_frame": per_frame,
            "launches_per_frame": {k: v[1] / frames for k, v in prof.items()}}
     base = kname.split("(")[0]
-    if base.startswith("mv"):
+    if base.startswith("mv") and mv_mode == 3:
+        flops = mv_flops_per_frame(pts, MV_KW)
+        achieved = flops / (kms / 1e3) / 1e12
+        out.update(bound="fp32", achieved=achieved, peak=FP32_NOMINAL_TFLOPS, unit="TFLOP/s",
+                   algorithmic_gflop_per_frame=flops / 1e9,
+                   note="the reference formulation's flops (covariance 4 L^2 n_snap + Cholesky 4/3 L^3 + "
+                        "solves 16 L^2 per pixel; the lag recurrence forms the covariance with fewer); "
+                        "peak = nominal FP32")
+    elif base.startswith("mv"):
         flops = mv_flops_per_frame(pts, MV_KW)
         achieved = flops / (kms / 1e3) / 1e12
         out.update(bound="tensor", achieved=achieved, peak=peaks["bf16_tflops_sustained"], unit="TFLOP/s",
@@ -435,7 +443,7 @@ def run_ours(args) -> None:
         level = learned.trained_level_gate(WEIGHTS) if args.level_gate is None else args.level_gate
         # Plain minimum variance (tensor-core solver) on the same frame, timed first.
         plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
-        plain.set_mv_mode(1)
+        plain.set_mv_mode(args.mv_mode)
         plain.autotune(d_iq.data_ptr(), frame.data_ptr(), repeats=1)
         for _ in range(args.warmup):
             plain.execute(d_iq.data_ptr(), frame.data_ptr())
@@ -448,8 +456,11 @@ def run_ours(args) -> None:
         plan.set_learned_refine(refine)
         plan.set_learned_subspace(True, share)
         plan.set_learned_level_gate(level)
+        if args.mv_mode == 3:
+            plan.set_mv_mode(3)   # the gated pixels take the same solver
+        solver = {1: "tensor", 2: "tensor_mma", 3: "fp32_recurrence"}[args.mv_mode]
         extra["plain_mv"] = {"value": world * args.steps / (plain_ms / 1e3) * N0 / n0, "unit": "frames/s",
-                             "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": "tensor"}
+                             "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": solver}
         extra["gate"] = gate
         extra["refine_beams"] = refine
         extra["share_gate"] = share
@@ -457,7 +468,7 @@ def run_ours(args) -> None:
     else:
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         if args.workload == "mv":
-            plan.set_mv_mode(1)
+            plan.set_mv_mode(args.mv_mode)
 
     # The plan's autotuner picks the delay-and-sum launch shape on this acquisition.
     best, tune_ms = plan.autotune(d_iq.data_ptr(), frame.data_ptr(), repeats=2)
@@ -510,7 +521,8 @@ def run_ours(args) -> None:
 
     peaks = load_peaks()
     launches_in_region = sum(n for _, n in prof.values())
-    roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks, extra.get("refine_beams", -1))
+    roofline = kernel_roofline(prof, args.steps, pts, txs, probe, peaks, extra.get("refine_beams", -1),
+                               args.mv_mode)
 
     e2e = None if args.no_e2e else run_e2e(usx, grid, raw, rf_host, args, world,
                                            (gate, refine, share, level) if args.workload == "learned" else None)
@@ -1467,6 +1479,10 @@ def main() -> int:
     ap.add_argument("--level-gate", type=float, default=None,
                     help="learned workload: gate on tr(R) over its depth's level (default: report)")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
+    ap.add_argument("--mv-mode", type=int, default=1, choices=[1, 2, 3],
+                    help="plain MV solver (mv workload, the headline's plain MV and the learned plan's gated "
+                         "pixels): 1 tcgen05 BF16 covariance + refinement, 2 the same on mma.sync, "
+                         "3 FP32 lag-recurrence covariance")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -182,9 +182,14 @@ int usx_cu_bf_plan_autotune(usx_bf_plan* plan, const void* data, float* frame, i
  *                      covariance, FP64 re-solve where the refined residual
  *                      fails;
  *   USX_MV_TENSOR_MMA  the same with the covariance formed by warp-level
- *                      mma.sync inside the solve kernel.
+ *                      mma.sync inside the solve kernel;
+ *   USX_MV_FP32        FP32 covariance formed inside the solve kernel from
+ *                      the range rows by the lag recurrence (each entry
+ *                      from its diagonal predecessor with 2 products per
+ *                      range row instead of K), FP32 Cholesky and one solve:
+ *                      the reference's precision, summed in another order.
  * Results agree within 1e-3 relative L2. */
-enum { USX_MV_EXACT = 0, USX_MV_TENSOR = 1, USX_MV_TENSOR_MMA = 2 };
+enum { USX_MV_EXACT = 0, USX_MV_TENSOR = 1, USX_MV_TENSOR_MMA = 2, USX_MV_FP32 = 3 };
 int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode);
 /* Counts since the last call (synchronises): pixels re-solved in FP64 and
  * pixels whose factorisation failed (these take the DAS sum). */

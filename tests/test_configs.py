@@ -92,7 +92,7 @@ def gpu_frame(capi, ctx, torch, s, iq, grid_pts, n0, n1, kw, gtype=0, mv_mode=No
     out = torch.empty((n0, n1), dtype=torch.complex64, device="cuda")
     plan.execute(iq.data_ptr(), out.data_ptr())
     got = host(torch, out)
-    stats = plan.mv_stats() if mv_mode in (1, 2) else None
+    stats = plan.mv_stats() if mv_mode in (1, 2, 3) else None
     plan.close()
     return got, stats
 
@@ -291,6 +291,11 @@ def test_cfg2_minimum_variance_l64_on_full_lines(cfg2_run, capi, ctx, torch, orc
                                   axes=axes)
     assert rel_l2(mma, want) < TOL_MV_TC and failed2 == 0
     assert rel_l2(tc, mma) < 1e-4
+    # FP32 covariance by the lag recurrence and one FP32 solve: the exact
+    # solver's bar.
+    f32, (fp64_3, failed3) = gpu_frame(capi, ctx, torch, s, r["iq"], pts, len(CFG2_LINES), 1024, MV64, mv_mode=3,
+                                       axes=axes)
+    assert rel_l2(f32, want) < TOL_MV and failed3 == 0 and fp64_3 == 0
 
 
 # ---------------------------------------------------------------- config 4

@@ -408,6 +408,19 @@ def test_gate_zero_falls_back_to_plain_mv_everywhere(capi, torch):
         assert pixels == setup.n0 * setup.n1
         assert gated > 0.9 * pixels
         assert rel_l2(out, mv) < 1e-6
+        # With the plan in the FP32 mode its gated pixels take the FP32
+        # solver: gate 0 gives that solver's frame.
+        mv32_plan = im.ctx.plan(im.ch_iq, im.grid, setup.bf(learned.COMB_MV))
+        mv32_plan.set_mv_mode(3)
+        mv32 = torch.empty((setup.n0, setup.n1), dtype=torch.complex64, device="cuda")
+        mv32_plan.execute(im.iq.data_ptr(), mv32.data_ptr())
+        plan.set_mv_mode(3)
+        out32 = im.beamform(learned.COMB_LEARNED_MV).cpu().numpy()
+        plan.set_mv_mode(0)
+        plan.learned_stats()
+        mv32_plan.close()
+        assert rel_l2(out32, mv32.cpu().numpy()) < 1e-6
+        assert rel_l2(out32, mv) < 1e-3
         # An infinite gate takes every network output (no fallback).
         plan.set_learned(mlp, float("inf"))
         im.beamform(learned.COMB_LEARNED_MV)

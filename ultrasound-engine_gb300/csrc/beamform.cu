@@ -1552,6 +1552,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
         const int lmax = std::min(kLmvClassWidth * (c + 1), plan_lmax);
         if (c > 0 && kLmvClassWidth * c >= plan_lmax) break;
         MvTcExtra ex;
+        // The plan's FP32 mode also serves its gated pixels.
+        ex.cov_engine = plan->mv_mode == USX_MV_FP32 ? 2 : 0;
         ex.list = gated + static_cast<long>(c) * nrows;
         ex.list_count = counters + c;
         ex.list_cap = static_cast<int>(nrows);
@@ -1585,7 +1587,8 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
   int2* fb_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes));
   int2* ov_list = reinterpret_cast<int2*>(wsb + up(y_bytes) + up(acc_bytes) + up(fb_bytes));
   int* fb_count = reinterpret_cast<int*>(wsb + up(y_bytes) + up(acc_bytes) + 2 * up(fb_bytes));  // [0] FP64, [1] overflow
-  const bool tensor = (plan->mv_mode == USX_MV_TENSOR || plan->mv_mode == USX_MV_TENSOR_MMA) &&
+  const bool tensor = (plan->mv_mode == USX_MV_TENSOR || plan->mv_mode == USX_MV_TENSOR_MMA ||
+                       plan->mv_mode == USX_MV_FP32) &&
                       mv_tc_supported(a.n_ch, a.mv_subarray, a.mv_range_average);
   const bool incoherent = a.compounding == USX_COMP_INCOHERENT;
   const size_t smem = sizeof(MvShared) * kMvWarps;
@@ -1599,7 +1602,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     if (int rc = launch_das(b, fast ? "das_fast_kernel(mv export)" : "das_kernel(mv export)")) return rc;
     if (tensor) {
       MvTcExtra ex;
-      ex.cov_engine = plan->mv_mode == USX_MV_TENSOR_MMA ? 0 : 1;
+      ex.cov_engine = plan->mv_mode == USX_MV_TENSOR_MMA ? 0 : plan->mv_mode == USX_MV_FP32 ? 2 : 1;
       if (plan->exp_feat) {
         // Training pairs: features of every pixel and its Capon weights.
         LmvLaunch l;
@@ -1760,7 +1763,7 @@ int usx_cu_bf_execute_sequence(usx_bf_plan* plan, int events_per_frame, int n_fr
 
 int usx_cu_bf_plan_set_mv_mode(usx_bf_plan* plan, int mode) {
   if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: null plan");
-  if (mode != USX_MV_EXACT && mode != USX_MV_TENSOR && mode != USX_MV_TENSOR_MMA)
+  if (mode != USX_MV_EXACT && mode != USX_MV_TENSOR && mode != USX_MV_TENSOR_MMA && mode != USX_MV_FP32)
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_mv_mode: unknown mode");
   if (mode != USX_MV_EXACT &&
       !mv_tc_supported(plan->cd.probe.n_elements, plan->cfg.mv_subarray, plan->cfg.mv_range_average))

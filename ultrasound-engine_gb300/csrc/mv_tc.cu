@@ -587,20 +587,91 @@ constexpr int kWarpMvWarps = 4;
 
 struct MvWarpLayout {
   int words;
-  size_t off_act, off_yf, off_yb, off_r, off_w, bytes;  // per warp
+  size_t off_act, off_yf, off_yb, off_r, off_w, off_p, bytes;  // per warp
 };
 
-__host__ __device__ inline MvWarpLayout mv_warp_layout(int nmax, int n_dmax, int lmax) {
+// recur: the covariance by lags from the FP32 rows (no BF16 staging, no
+// refinement, so no t_k either).
+__host__ __device__ inline MvWarpLayout mv_warp_layout(int nmax, int n_dmax, int lmax, bool recur = false) {
   MvWarpLayout l;
   l.words = nmax / 2 + 10;
   size_t o = 0;
   l.off_act = o; o = align16(o + sizeof(int) * nmax);
   l.off_yf = o;  o = align16(o + sizeof(float2) * n_dmax * nmax);
-  l.off_yb = o;  o = align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);  // also t_k after the covariance
+  l.off_yb = o;  o = recur ? o : align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);  // also t_k after the covariance
   l.off_r = o;   o = align16(o + sizeof(float2) * (lmax * (lmax + 1) / 2));
   l.off_w = o;   o = align16(o + sizeof(float2) * 2 * lmax);
+  l.off_p = o;   o = align16(o + sizeof(float2) * 4 * lmax);   // the Cholesky's panel, transposed
   l.bytes = o;
   return l;
+}
+
+// Cholesky of the packed lower triangle Rl (L <= 64) by one warp, blocked
+// right-looking: each block of four columns is factored as a panel (columns
+// in turn, lanes over rows), copied transposed into P[k][0..3], and the
+// trailing triangle takes one rank-4 update, R[i][k] -= sum_c l_ic conj(l_kc),
+// with lanes over rows: lane l walks row k0 + l and, when the trailing part
+// has more than 32 rows, row L - 1 - l, so that every lane updates about
+// n + 1 entries (n trailing rows). Against one trailing row per step with
+// lanes over columns, a quarter of the passes over the triangle and no lane
+// idles on short rows. False on a non-positive pivot.
+__device__ bool chol_blocked(float2* Rl, float2* P, int L, int lane) {
+  for (int c0 = 0; c0 < L; c0 += 4) {
+    const int nb = min(4, L - c0);
+    for (int c = c0; c < c0 + nb; ++c) {
+      const float dgl = Rl[tri(c, c)].x;
+      if (!(dgl > 0.0f)) return false;
+      const float ljj = sqrtf(dgl), inv = 1.0f / ljj;
+      for (int i = c + 1 + lane; i < L; i += 32) {
+        const float2 v = Rl[tri(i, c)];
+        Rl[tri(i, c)] = make_float2(v.x * inv, v.y * inv);
+      }
+      __syncwarp();
+      if (lane == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
+      for (int cc = c + 1; cc < c0 + nb; ++cc) {
+        const float2 lk = Rl[tri(cc, c)];
+        for (int i = cc + lane; i < L; i += 32) {
+          const float2 li = Rl[tri(i, c)];
+          float2 v = Rl[tri(i, cc)];
+          v.x = fmaf(-li.x, lk.x, fmaf(-li.y, lk.y, v.x));
+          v.y = fmaf(-li.y, lk.x, fmaf(li.x, lk.y, v.y));
+          Rl[tri(i, cc)] = v;
+        }
+      }
+      __syncwarp();
+    }
+    const int k0 = c0 + nb;
+    if (k0 >= L) break;
+    for (int k = k0 + lane; k < L; k += 32)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) P[4 * k + j] = Rl[tri(k, c0 + j)];
+    __syncwarp();
+    const int n = L - k0;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      const int i = h == 0 ? k0 + lane : L - 1 - lane;
+      if (h == 0 ? lane >= n : lane > n - 33) continue;
+      const float4* pi = reinterpret_cast<const float4*>(P + 4 * i);
+      const float4 ia = pi[0], ib = pi[1];
+      float2* row = Rl + tri(i, 0);
+      for (int k = k0; k <= i; ++k) {
+        const float4* pk = reinterpret_cast<const float4*>(P + 4 * k);
+        const float4 ka = pk[0], kb = pk[1];
+        float2 v = row[k];
+        v.x = fmaf(-ia.x, ka.x, fmaf(-ia.y, ka.y, v.x));
+        v.y = fmaf(-ia.y, ka.x, fmaf(ia.x, ka.y, v.y));
+        v.x = fmaf(-ia.z, ka.z, fmaf(-ia.w, ka.w, v.x));
+        v.y = fmaf(-ia.w, ka.z, fmaf(ia.z, ka.w, v.y));
+        v.x = fmaf(-ib.x, kb.x, fmaf(-ib.y, kb.y, v.x));
+        v.y = fmaf(-ib.y, kb.x, fmaf(ib.x, kb.y, v.y));
+        v.x = fmaf(-ib.z, kb.z, fmaf(-ib.w, kb.w, v.x));
+        v.y = fmaf(-ib.w, kb.z, fmaf(ib.z, kb.w, v.y));
+        row[k] = v;
+      }
+    }
+    __syncwarp();
+  }
+  return true;
 }
 
 struct MvWarpArgs {
@@ -621,13 +692,16 @@ struct MvWarpArgs {
   const float2* r_pre;
   const uint8_t* r_flag;  // [item - item_begin]: 1 where r_pre holds the pixel's R~
   int r_stride;
+  // 1: R~ in FP32 from the rows by the lag recurrence and one FP32 solve (no
+  // refinement, no FP64 re-solve: the reference's precision).
+  int cov_recur;
 };
 
 __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarpArgs wa) {
   extern __shared__ float4 mvw_smem_raw[];
   const MvTcArgs& a = wa.base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const MvWarpLayout lay = mv_warp_layout(wa.nmax, a.n_dmax, wa.lmax);
+  const MvWarpLayout lay = mv_warp_layout(wa.nmax, a.n_dmax, wa.lmax, wa.cov_recur != 0);
   char* base = reinterpret_cast<char*>(mvw_smem_raw) + warp * lay.bytes;
   int* act = reinterpret_cast<int*>(base + lay.off_act);
   float2* yf = reinterpret_cast<float2*>(base + lay.off_yf);
@@ -751,7 +825,43 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     frexpf(amax, &e2);
     const float sc = ldexpf(1.0f, -e2), sc2 = ldexpf(1.0f, -2 * e2);
     const float inv_k = 1.0f / static_cast<float>(K);
-    if (wa.r_pre && wa.r_flag[item - wa.item_begin]) {
+    if (wa.cov_recur) {
+      // R~[i][k] = sum_d sum_{s < n_sub} x_d[s + i] conj(x_d[s + k]) by
+      // diagonals (lag m = i - k): the first entry of a diagonal in full,
+      // then R~[i + 1][k + 1] = R~[i][k] - x[i] conj(x[k]) + x[n_sub + i]
+      // conj(x[n_sub + k]) summed over the rows, 2 n_d products per entry
+      // instead of K. Lane l takes m = l and, for L > 32, m = 63 - l (every
+      // lane then walks about L entries).
+      const float f = sc2 * inv_k;
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        const int m = h == 0 ? lane : 63 - lane;
+        if (m >= L || (h == 1 && m < 32)) continue;
+        float re = 0.f, im = 0.f;
+        for (int d = 0; d < n_d; ++d) {
+          const float2* x = yf + d * nmax;
+          for (int s = 0; s < n_sub; ++s) {
+            const float2 p = x[s + m], q = x[s];
+            re = fmaf(p.x, q.x, fmaf(p.y, q.y, re));
+            im = fmaf(p.y, q.x, fmaf(-p.x, q.y, im));
+          }
+        }
+        Rl[tri(m, 0)] = make_float2(re * f, im * f);
+        for (int j = 1; j + m < L; ++j) {
+          for (int d = 0; d < n_d; ++d) {
+            const float2* x = yf + d * nmax;
+            const float2 p1 = x[n_sub + m + j - 1], q1 = x[n_sub + j - 1];
+            const float2 p0 = x[m + j - 1], q0 = x[j - 1];
+            re = fmaf(p1.x, q1.x, fmaf(p1.y, q1.y, re));
+            im = fmaf(p1.y, q1.x, fmaf(-p1.x, q1.y, im));
+            re = fmaf(-p0.x, q0.x, fmaf(-p0.y, q0.y, re));
+            im = fmaf(-p0.y, q0.x, fmaf(p0.x, q0.y, im));
+          }
+          Rl[tri(m + j, j)] = make_float2(re * f, im * f);
+        }
+      }
+      __syncwarp();
+    } else if (wa.r_pre && wa.r_flag[item - wa.item_begin]) {
       // R~ from the tensor-core stage (same scale, same packing).
       const float2* src = wa.r_pre + (item - wa.item_begin) * wa.r_stride;
       for (int e = lane; e < L * (L + 1) / 2; e += 32) Rl[e] = src[e];
@@ -841,52 +951,8 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     for (int i = lane; i < L; i += 32) Rl[tri(i, i)].x += eps;
     __syncwarp();
 
-    // ---- Cholesky, right-looking; pivot column in registers ---------------
-    bool ok = true;
-    for (int c = 0; c < L; ++c) {
-      const float dgl = Rl[tri(c, c)].x;
-      if (!(dgl > 0.0f)) {
-        ok = false;
-        break;
-      }
-      const float ljj = sqrtf(dgl), inv = 1.0f / ljj;
-      float2 lc[2];
-#pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
-        const int i = c + 1 + lane + 32 * s2;
-        lc[s2] = make_float2(0.f, 0.f);
-        if (i < L) {
-          const float2 v = Rl[tri(i, c)];
-          lc[s2] = make_float2(v.x * inv, v.y * inv);
-        }
-      }
-      __syncwarp();
-      if (lane == 0) Rl[tri(c, c)] = make_float2(ljj, 0.0f);
-#pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
-        const int i = c + 1 + lane + 32 * s2;
-        if (i < L) Rl[tri(i, c)] = lc[s2];
-      }
-      // Row i of the trailing matrix: R[i][k] -= l_ic conj(l_kc), k = c+1..i.
-      for (int i = c + 1; i < L; ++i) {
-        const int ii = i - c - 1, src = ii & 31;
-        const float lix = __shfl_sync(0xffffffffu, ii >> 5 ? lc[1].x : lc[0].x, src);
-        const float liy = __shfl_sync(0xffffffffu, ii >> 5 ? lc[1].y : lc[0].y, src);
-        float2* rowp = Rl + i * (i + 1) / 2;
-#pragma unroll
-        for (int s2 = 0; s2 < 2; ++s2) {
-          const int k = c + 1 + lane + 32 * s2;
-          if (k <= i) {
-            const float2 lk = lc[s2];
-            float2 v = rowp[k];
-            v.x -= fmaf(lix, lk.x, liy * lk.y);
-            v.y -= fmaf(liy, lk.x, -lix * lk.y);
-            rowp[k] = v;
-          }
-        }
-      }
-      __syncwarp();
-    }
+    // ---- Cholesky (blocked, rank-4 trailing updates) ---------------------
+    const bool ok = chol_blocked(Rl, reinterpret_cast<float2*>(base + lay.off_p), L, lane);
     if (!ok) {
       export_invalid(a, row, lane);
       if (lane == 0) {
@@ -977,6 +1043,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     w[0] = lane < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
     w[1] = lane + 32 < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
     solve(w);
+    if (!wa.cov_recur) {
 #pragma unroll
     for (int s2 = 0; s2 < 2; ++s2)
       if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
@@ -1020,6 +1087,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       }
       continue;
     }
+    }  // refinement
     // out = n_act * sum conj(w_i) avg_i / sum w, avg from the centre row.
     float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
     const float inv_nsub = 1.0f / static_cast<float>(n_sub);
@@ -1690,7 +1758,8 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
     return USX_OK;
   };
   auto launch_warp = [&](MvWarpArgs& w, long items, const char* name) -> int {
-    const MvWarpLayout l = mv_warp_layout(w.nmax, a.n_dmax, w.lmax);
+    w.cov_recur = extra.cov_engine == 2 ? 1 : 0;
+    const MvWarpLayout l = mv_warp_layout(w.nmax, a.n_dmax, w.lmax, w.cov_recur != 0);
     const size_t smem = l.bytes * kWarpMvWarps;
     if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "minimum variance: class too large for shared memory");
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_warp_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;

@@ -275,7 +275,9 @@ struct MvClass {
   int lmax = 0, nmax = 0;
 };
 struct MvTcExtra {
-  int cov_engine = 1;                // class mode: 1 = covariance on tcgen05, 0 = mma.sync in the solve kernel
+  // 1 = covariance on tcgen05 (class mode; lists as 0), 0 = mma.sync in the
+  // solve kernel, 2 = FP32 by the lag recurrence in the solve kernel.
+  int cov_engine = 1;
   const int2* list = nullptr;
   const int* list_count = nullptr;
   int list_cap = 0;

@@ -66,7 +66,10 @@ PYBIND11_MODULE(_usx, m) {
       .value("PLANE_WAVE", TransmitType::PlaneWave)
       .value("DIVERGING", TransmitType::Diverging);
   py::enum_<GridType>(m, "GridType").value("CARTESIAN", GridType::Cartesian).value("SECTOR", GridType::Sector);
-  py::enum_<MvSolver>(m, "MvSolver").value("TENSOR", MvSolver::Tensor).value("EXACT", MvSolver::Exact);
+  py::enum_<MvSolver>(m, "MvSolver")
+      .value("TENSOR", MvSolver::Tensor)
+      .value("EXACT", MvSolver::Exact)
+      .value("FP32", MvSolver::FP32);
 
   py::enum_<Combiner>(m, "Combiner")
       .value("DAS", Combiner::DAS)

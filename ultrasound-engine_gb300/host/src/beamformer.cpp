@@ -186,6 +186,8 @@ class PlanCache {
     // reference's FP32 operation order.
     if (cfg.combiner == Combiner::MV && cfg.mv_solver == MvSolver::Tensor)
       usx_cu_bf_plan_set_mv_mode(plan, USX_MV_TENSOR);  // unsupported shapes stay exact
+    if ((cfg.combiner == Combiner::MV || cfg.combiner == Combiner::LearnedMV) && cfg.mv_solver == MvSolver::FP32)
+      usx_cu_bf_plan_set_mv_mode(plan, USX_MV_FP32);
     if (cfg.combiner == Combiner::LearnedMV) {
       try {
         const LearnedNet net = learned_net(key.ctx);

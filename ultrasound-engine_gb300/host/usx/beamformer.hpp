@@ -20,8 +20,11 @@ enum class Compounding : std::uint8_t { Coherent = 0, Incoherent = 1, Select = 2
 // solver is its FP32 Cholesky): Tensor = BF16 covariance on the tensor cores
 // with FP32 accumulation, one refinement step against the FP32 covariance and
 // an FP64 re-solve where it fails (within 1e-3 of the reference); Exact = the
-// reference's FP32 operation order (within 1e-4, several times slower).
-enum class MvSolver { Tensor = 0, Exact = 1 };
+// reference's FP32 operation order (within 1e-4, several times slower); FP32 =
+// FP32 covariance by the lag recurrence and one FP32 solve (the reference's
+// precision in another summation order). For LearnedMV the solver of the
+// gated pixels: FP32, else the tensor-core one.
+enum class MvSolver { Tensor = 0, Exact = 1, FP32 = 2 };
 
 struct BeamformerConfig {
   real f_number = 1.75f;

@@ -321,7 +321,8 @@ class Plan:
 
     def set_mv_mode(self, mode: int) -> None:
         """0: FP32 in the reference's order; 1: BF16 covariance on tcgen05 + refinement;
-        2: the same with the covariance on warp-level mma.sync."""
+        2: the same with the covariance on warp-level mma.sync; 3: FP32 covariance by
+        the lag recurrence in the solve kernel, one FP32 solve."""
         check(lib().usx_cu_bf_plan_set_mv_mode(self._h, int(mode)), "bf_plan_set_mv_mode")
 
     def mv_stats(self):
