@@ -46,7 +46,7 @@ MV_KW = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01,
 LEARNED_KW = dict(MV_KW, combiner=3)
 WORKLOADS = {
     "learned": LEARNED_KW,   # learned MV with plain-MV fallback (the headline), plain MV timed beside it
-    "mv": MV_KW,             # tensor-core covariance (the fast plain MV)
+    "mv": MV_KW,             # the fast plain MV (--mv-mode: FP32 lag recurrence by default, or tensor cores)
     "mv_exact": MV_KW,       # FP32 in the reference's operation order
     "das": dict(f_number=1.5),
     "cf": dict(f_number=1.5, coherence_factor=1),
@@ -1436,7 +1436,8 @@ def run_e2e(usx, grid, raw, rf_host, args, world, learned=None):
     import torch
     pcfg = usx.PipelineConfig()
     b = pcfg.beamformer
-    b.mv_solver = usx.MvSolver.EXACT if args.workload == "mv_exact" else usx.MvSolver.TENSOR
+    b.mv_solver = (usx.MvSolver.EXACT if args.workload == "mv_exact" else
+                   {1: usx.MvSolver.TENSOR, 2: usx.MvSolver.TENSOR, 3: usx.MvSolver.FP32}[args.mv_mode])
     if learned is not None:
         b.learned_gate, b.learned_refine, b.learned_share_gate, b.learned_level_gate = learned
     kw = WORKLOADS[args.workload]
@@ -1479,7 +1480,7 @@ def main() -> int:
     ap.add_argument("--level-gate", type=float, default=None,
                     help="learned workload: gate on tr(R) over its depth's level (default: report)")
     ap.add_argument("--lines", type=int, default=N0, help="lateral lines timed (profiling cases use fewer)")
-    ap.add_argument("--mv-mode", type=int, default=1, choices=[1, 2, 3],
+    ap.add_argument("--mv-mode", type=int, default=3, choices=[1, 2, 3],
                     help="plain MV solver (mv workload, the headline's plain MV and the learned plan's gated "
                          "pixels): 1 tcgen05 BF16 covariance + refinement, 2 the same on mma.sync, "
                          "3 FP32 lag-recurrence covariance")

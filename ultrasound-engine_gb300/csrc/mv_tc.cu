@@ -576,12 +576,13 @@ __global__ void __launch_bounds__(32 * kTcWarps) mv_tc_kernel(const MvTcArgs a) 
 // subarrays, the common case, pack many warps per SM.
 //
 // Per pixel: the active channels of the range rows in the smoothing window
-// are staged once in FP32 (yf) and as BF16 pairs (yb, scaled by a power of
-// two); G = A A^T on the tensor cores gives R~; the exact trace comes from
-// the FP32 rows with each channel's subarray multiplicity; the Cholesky runs
-// right-looking with the pivot column held in registers (one row of the
-// trailing update per step, lanes over columns); the solves, the refinement
-// step and the refined-residual gate are those of mv_tc_kernel.
+// are staged once in FP32 (yf); R~ comes from the tcgen05 stage (r_pre), or
+// from G = A A^T on mma.sync over BF16 pairs (yb, scaled by a power of two),
+// or in FP32 from yf by the lag recurrence (cov_recur); the exact trace comes
+// from the FP32 rows with each channel's subarray multiplicity; the Cholesky
+// is blocked (chol_blocked); with a BF16 covariance the solves are followed
+// by the refinement step and the refined-residual gate of mv_tc_kernel, with
+// the FP32 one by nothing (one solve, as the reference).
 
 constexpr int kWarpMvWarps = 4;
 
@@ -837,26 +838,52 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       for (int h = 0; h < 2; ++h) {
         const int m = h == 0 ? lane : 63 - lane;
         if (m >= L || (h == 1 && m < 32)) continue;
-        float re = 0.f, im = 0.f;
+        // Four independent partial sums (snapshot parity x real/imaginary)
+        // keep the FMA chains short.
+        float re0 = 0.f, im0 = 0.f, re1 = 0.f, im1 = 0.f;
         for (int d = 0; d < n_d; ++d) {
           const float2* x = yf + d * nmax;
-          for (int s = 0; s < n_sub; ++s) {
+          int s = 0;
+          for (; s + 1 < n_sub; s += 2) {
+            const float2 p = x[s + m], q = x[s], pb = x[s + 1 + m], qb = x[s + 1];
+            re0 = fmaf(p.x, q.x, fmaf(p.y, q.y, re0));
+            im0 = fmaf(p.y, q.x, fmaf(-p.x, q.y, im0));
+            re1 = fmaf(pb.x, qb.x, fmaf(pb.y, qb.y, re1));
+            im1 = fmaf(pb.y, qb.x, fmaf(-pb.x, qb.y, im1));
+          }
+          if (s < n_sub) {
             const float2 p = x[s + m], q = x[s];
-            re = fmaf(p.x, q.x, fmaf(p.y, q.y, re));
-            im = fmaf(p.y, q.x, fmaf(-p.x, q.y, im));
+            re0 = fmaf(p.x, q.x, fmaf(p.y, q.y, re0));
+            im0 = fmaf(p.y, q.x, fmaf(-p.x, q.y, im0));
           }
         }
+        float re = re0 + re1, im = im0 + im1;
         Rl[tri(m, 0)] = make_float2(re * f, im * f);
         for (int j = 1; j + m < L; ++j) {
-          for (int d = 0; d < n_d; ++d) {
-            const float2* x = yf + d * nmax;
+          // The step's row sums (entering minus leaving product), rows in
+          // two interleaved partial sums.
+          float ar = 0.f, ai = 0.f, br = 0.f, bi = 0.f;
+          const float2* x = yf;
+          int d = 0;
+          for (; d + 1 < n_d; d += 2, x += 2 * nmax) {
             const float2 p1 = x[n_sub + m + j - 1], q1 = x[n_sub + j - 1];
             const float2 p0 = x[m + j - 1], q0 = x[j - 1];
-            re = fmaf(p1.x, q1.x, fmaf(p1.y, q1.y, re));
-            im = fmaf(p1.y, q1.x, fmaf(-p1.x, q1.y, im));
-            re = fmaf(-p0.x, q0.x, fmaf(-p0.y, q0.y, re));
-            im = fmaf(-p0.y, q0.x, fmaf(p0.x, q0.y, im));
+            const float2* y = x + nmax;
+            const float2 r1 = y[n_sub + m + j - 1], s1 = y[n_sub + j - 1];
+            const float2 r0 = y[m + j - 1], s0 = y[j - 1];
+            ar += fmaf(p1.x, q1.x, p1.y * q1.y) - fmaf(p0.x, q0.x, p0.y * q0.y);
+            ai += fmaf(p1.y, q1.x, -p1.x * q1.y) - fmaf(p0.y, q0.x, -p0.x * q0.y);
+            br += fmaf(r1.x, s1.x, r1.y * s1.y) - fmaf(r0.x, s0.x, r0.y * s0.y);
+            bi += fmaf(r1.y, s1.x, -r1.x * s1.y) - fmaf(r0.y, s0.x, -r0.x * s0.y);
           }
+          if (d < n_d) {
+            const float2 p1 = x[n_sub + m + j - 1], q1 = x[n_sub + j - 1];
+            const float2 p0 = x[m + j - 1], q0 = x[j - 1];
+            ar += fmaf(p1.x, q1.x, p1.y * q1.y) - fmaf(p0.x, q0.x, p0.y * q0.y);
+            ai += fmaf(p1.y, q1.x, -p1.x * q1.y) - fmaf(p0.y, q0.x, -p0.x * q0.y);
+          }
+          re += ar + br;
+          im += ai + bi;
           Rl[tri(m + j, j)] = make_float2(re * f, im * f);
         }
       }

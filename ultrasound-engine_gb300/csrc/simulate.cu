@@ -23,6 +23,13 @@
 // fixed-point step is 2^-61 of the bound on any sum (for realistic phantoms
 // well below the float rounding of a sample).
 //
+// Measured and dropped (100,000 scatterers, 75 events x 128 elements, 509 ms
+// for this kernel): the incident waveforms of a batch written to a pool and
+// an echo kernel whose warps each own one element's RF row in shared memory
+// and add every scatterer's echo in ascending order (no atomics, bit-exact
+// order): 834 ms, the waveform reads going to L2 once per element because
+// the rows leave little L1.
+//
 // Receive noise is added by a second kernel once an event's echoes are
 // complete: sigma = peak|RF| * 10^(noise_db/20), RF += z * sigma, with z the
 // host-generated standard normals of the reference's per-event generator.

@@ -38,7 +38,7 @@ struct BeamformerConfig {
   real mv_diagonal_loading = 1e-2f;
   int mv_range_average = 2;
   // Fields below have no counterpart in the reference.
-  MvSolver mv_solver = MvSolver::Tensor;
+  MvSolver mv_solver = MvSolver::FP32;
   // Learned minimum variance: the gate on the network's distortionless
   // residual, the DFT beams of the subspace refinement (< 0: none), the gate
   // on the network direction's share of the power reduction and the gate on
