@@ -451,6 +451,20 @@ def run_ours(args) -> None:
         plain_ms = timed(stream, lambda: plain.execute(d_iq.data_ptr(), frame.data_ptr()), args.steps)
         ref_frame = frame.clone()
         plain.close()
+        # The tensor-core plain MV (tcgen05 BF16 covariance + refinement) on the
+        # same frame, for reference beside the default solver.
+        alt = None
+        if args.mv_mode != 1:
+            tc = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
+            tc.set_mv_mode(1)
+            tc.autotune(d_iq.data_ptr(), frame.data_ptr(), repeats=1)
+            for _ in range(args.warmup):
+                tc.execute(d_iq.data_ptr(), frame.data_ptr())
+            ctx.synchronize()
+            tc_ms = timed(stream, lambda: tc.execute(d_iq.data_ptr(), frame.data_ptr()), args.steps)
+            tc.close()
+            alt = {"value": world * args.steps / (tc_ms / 1e3) * N0 / n0, "unit": "frames/s",
+                   "ms_per_step": tc_ms / args.steps * N0 / n0, "solver": "tensor"}
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         plan.set_learned(mlp, gate)
         plan.set_learned_refine(refine)
@@ -461,6 +475,8 @@ def run_ours(args) -> None:
         solver = {1: "tensor", 2: "tensor_mma", 3: "fp32_recurrence"}[args.mv_mode]
         extra["plain_mv"] = {"value": world * args.steps / (plain_ms / 1e3) * N0 / n0, "unit": "frames/s",
                              "ms_per_step": plain_ms / args.steps * N0 / n0, "solver": solver}
+        if alt is not None:
+            extra["plain_mv_tensor"] = alt
         extra["gate"] = gate
         extra["refine_beams"] = refine
         extra["share_gate"] = share
@@ -497,6 +513,8 @@ def run_ours(args) -> None:
         gated, pixels = plan.learned_stats()
         extra["fallback_rate"] = gated / max(1, pixels)
         extra["speedup_vs_plain_mv"] = (extra["plain_mv"]["ms_per_step"] / (ms_per_step * N0 / n0))
+        if "plain_mv_tensor" in extra:
+            extra["speedup_vs_plain_mv_tensor"] = (extra["plain_mv_tensor"]["ms_per_step"] / (ms_per_step * N0 / n0))
         extra["rel_l2_vs_plain_mv"] = float((frame - ref_frame).abs().pow(2).sum().sqrt()
                                             / ref_frame.abs().pow(2).sum().sqrt())
         rep = WEIGHTS.with_suffix(".json")
