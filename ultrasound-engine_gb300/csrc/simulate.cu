@@ -1,6 +1,7 @@
 // simulate.cu — point-scatterer forward model (reference simulator.cpp:213-419).
 //
-// One warp owns one (scatterer, transmit event) at a time:
+// One warp owns one (scatterer, transmit event) at a time (eight warps per
+// CTA):
 //   stage 1  the incident field at the scatterer, a sum over firing elements of
 //            the delayed, weighted two-way pulse linearly interpolated onto an
 //            oversampled time axis, built in the warp's shared-memory buffer.
@@ -23,8 +24,18 @@
 // fixed-point step is 2^-61 of the bound on any sum (for realistic phantoms
 // well below the float rounding of a sample).
 //
+// Occupancy: a warp keeps a 1,536-sample incident buffer and element tables
+// sized to the probe in shared memory (8 KB at 128 elements), so that eight
+// warps per CTA and three CTAs per SM fit; windows longer than the buffer
+// (up to the 30 us clamp) use the warp's slot of a global buffer through the
+// same generic pointer, and the grid is persistent over (event, block of
+// scatterers) items so that there is one slot per resident warp. Against
+// buffers sized for the clamp (10 warps per SM): 509 -> 311 ms for 100,000
+// scatterers. The fixed-point scale (a power of two) is folded into each
+// element's amplitude, which gives the same scaled samples exactly.
+//
 // Measured and dropped (100,000 scatterers, 75 events x 128 elements, 509 ms
-// for this kernel): the incident waveforms of a batch written to a pool and
+// for the kernel at the time): the incident waveforms of a batch written to a pool and
 // an echo kernel whose warps each own one element's RF row in shared memory
 // and add every scatterer's echo in ascending order (no atomics, bit-exact
 // order): 834 ms, the waveform reads going to L2 once per element because
@@ -42,10 +53,13 @@
 namespace usxcu {
 namespace {
 
-constexpr int kSimWarps = 4;
+constexpr int kSimWarps = 8;
 constexpr int kMaxElem = 256;
 constexpr int kMaxPulse = 1024;
 constexpr int kMaxTimeTable = 8192;
+// Incident samples a warp keeps in shared memory; a longer window (up to the
+// clamp) uses the warp's slot of a global-memory buffer instead.
+constexpr int kIncSmall = 1536;
 
 struct SimArgs {
   const usx_scatterer* scat;
@@ -62,6 +76,9 @@ struct SimArgs {
   float apod_sum_max;      // largest sum of transmit apodisation over the events
   float pulse_max;         // largest |pulse tap|
   int n_el, n_smp, n_ev, pulse_n, inc_cap, scat_per_block;
+  int pulse_pad, tbl_pad, inc_small;  // shared-memory layout (floats)
+  long n_sblocks, n_items;  // scatterer blocks per event; work items (events x blocks)
+  float* inc_global;       // [block][warp][inc_cap] incident buffers for long windows
   float c, fs, t0, fs_os, lambda, width, prf, half_nm1, pitch;
   float pulse_half, max_window_s, trim_amp, atten_db_per_m;
   int spreading, directivity_on, motion, full;
@@ -107,36 +124,43 @@ __device__ __forceinline__ int fixed_shift(const SimArgs& a) {
 
 __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs a) {
   extern __shared__ float4 sim_smem[];
+  // Shared memory: the pulse, the sample-time table, then per warp a small
+  // incident buffer and four element tables (sized to the probe).
   float* pulse = reinterpret_cast<float*>(sim_smem);
+  float* t_axis = pulse + a.pulse_pad;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int per_warp = a.inc_cap + 4 * kMaxElem;
-  float* mine = pulse + kMaxPulse + warp * per_warp;
-  float* inc = mine;                            // [inc_cap]
-  float* e_r = inc + a.inc_cap;                 // distance to each element
-  float* e_amp = e_r + kMaxElem;                // stage-1 amplitude (active order)
-  float* e_ctr = e_amp + kMaxElem;              // stage-1 centre index (active order)
-  int* e_base = reinterpret_cast<int*>(e_ctr + kMaxElem);
+  const int per_warp = a.inc_small + 4 * a.tbl_pad;
+  float* mine = t_axis + (a.t_table ? a.n_smp + (4 - a.n_smp % 4) % 4 : 0) + warp * per_warp;
+  float* inc_smem = mine;                       // [inc_small]
+  float* inc_glob = a.inc_global + (static_cast<long>(blockIdx.x) * kSimWarps + warp) * a.inc_cap;
+  float* e_r = inc_smem + a.inc_small;          // distance to each element
+  float* e_amp = e_r + a.tbl_pad;               // stage-1 amplitude (active order)
+  float* e_ctr = e_amp + a.tbl_pad;             // stage-1 centre index (active order)
+  int* e_base = reinterpret_cast<int*>(e_ctr + a.tbl_pad);
   for (int k = threadIdx.x; k < a.pulse_n; k += blockDim.x) pulse[k] = a.pulse[k];
   // Sample times t0 + n / fs of the RF axis, each computed as the reference
   // does (float division), once per block instead of once per echo sample.
-  float* t_axis = pulse + kMaxPulse + kSimWarps * (a.inc_cap + 4 * kMaxElem);
   if (a.t_table)
     for (int n = threadIdx.x; n < a.n_smp; n += blockDim.x) t_axis[n] = a.t0 + static_cast<float>(n) / a.fs;
   __syncthreads();
 
-  const int ev = blockIdx.y;
-  const float event_time = static_cast<float>(ev) / a.prf;
   // 2^shift as two float factors, each within float range whatever the bound.
   const int shift = fixed_shift(a);
   const float scale1 = ldexpf(1.0f, shift / 2), scale2 = ldexpf(1.0f, shift - shift / 2);
+  unsigned long long samples = 0;
+
+  // Work items (event, block of scatterers), the grid persistent over them
+  // (so that the global incident buffers are per resident CTA).
+  for (long item = blockIdx.x; item < a.n_items; item += gridDim.x) {
+  const int ev = static_cast<int>(item / a.n_sblocks);
+  const long sb = item - static_cast<long>(ev) * a.n_sblocks;
+  const float event_time = static_cast<float>(ev) / a.prf;
   const int n_act = a.n_active[ev];
   const int* act = a.active + static_cast<long>(ev) * a.n_el;
   const float* dly = a.delays + static_cast<long>(ev) * a.n_el;
   const float* apd = a.apod + static_cast<long>(ev) * a.n_el;
   unsigned long long* acc_ev = a.acc + static_cast<long>(ev) * a.n_el * a.n_smp;
-  unsigned long long samples = 0;
-
-  const long s_begin = static_cast<long>(blockIdx.x) * a.scat_per_block;
+  const long s_begin = sb * a.scat_per_block;
   const long s_end = min(a.n_scat, s_begin + a.scat_per_block);
   for (long si = s_begin + warp; si < s_end; si += kSimWarps) {
     __syncwarp();  // the previous scatterer's buffers are no longer read
@@ -174,6 +198,9 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
     const float inc_t0 = t_min - a.pulse_half;
     const int inc_n = static_cast<int>(ceilf(span * a.fs_os)) + 2;
     if (inc_n > a.inc_cap || inc_n <= 0) continue;  // cannot happen: cap bounds the window
+    // The window in shared memory when it fits, else in the warp's global slot
+    // (the same code through a generic pointer).
+    float* inc = inc_n <= a.inc_small ? inc_smem : inc_glob;
     for (int k = lane; k < inc_n; k += 32) inc[k] = 0.0f;
 
     // Per firing element: amplitude and pulse placement.
@@ -266,7 +293,9 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
       } else {
         samples += static_cast<unsigned long long>(n1 - n0 + 1);
       }
-      e_amp[e] = amp;
+      // The fixed-point scale is a power of two, so scaling the amplitude
+      // gives the scaled sample exactly: amp 2^s x lerp = (amp x lerp) 2^s.
+      e_amp[e] = (amp * scale1) * scale2;
       e_ctr[e] = delay;
       e_base[e] = n0;
       e_r[e] = __int_as_float(n1);
@@ -285,11 +314,12 @@ __global__ void __launch_bounds__(32 * kSimWarps) simulate_kernel(const SimArgs 
         const float f = u - static_cast<float>(k);
         const float va = tr[k], vb = tr[k + 1];
         const float v = amp * (va + (vb - va) * f);
-        atomicAdd(dst + n, static_cast<unsigned long long>(__float2ll_rn((v * scale1) * scale2)));
+        atomicAdd(dst + n, static_cast<unsigned long long>(__float2ll_rn(v)));
       }
     }
     __syncwarp();
   }
+  }  // work items
   for (int o = 16; o > 0; o >>= 1) samples += __shfl_xor_sync(0xffffffffu, samples, o);
   if (lane == 0 && samples) atomicAdd(a.counter, samples);
 }
@@ -377,8 +407,18 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   }
   const size_t tbl = delays.size();
   const size_t acc_bytes = sizeof(unsigned long long) * static_cast<size_t>(ev_size) * n_ev;
-  const size_t bytes = acc_bytes + 256 + sizeof(float) * (2 * tbl + pulse.size()) + sizeof(int) * (tbl + n_ev) +
-                       sizeof(unsigned long long) + sizeof(unsigned) * n_ev + 1024;
+  // Work items: blocks of scatterers per event, enough to fill the GPU several
+  // times over; the grid is persistent over them (at most eight CTAs per SM).
+  const long target_blocks = std::max<long>(1, static_cast<long>(ctx->sm_count) * 8 / std::max(1, n_ev));
+  const int scat_per_block = static_cast<int>(
+      std::min<long>(256, std::max<long>(kSimWarps, (n_scat + target_blocks - 1) / target_blocks)));
+  const long gx = std::max<long>(1, (n_scat + scat_per_block - 1) / scat_per_block);
+  const long grid_max = std::max<long>(1, std::min<long>(gx * n_ev, 8L * ctx->sm_count));
+  // Incident buffers for windows longer than the shared-memory one: one per
+  // warp of the persistent grid.
+  const size_t incg_bytes = sizeof(float) * static_cast<size_t>(grid_max) * kSimWarps * inc_cap;
+  const size_t bytes = acc_bytes + incg_bytes + 512 + sizeof(float) * (2 * tbl + pulse.size()) +
+                       sizeof(int) * (tbl + n_ev) + sizeof(unsigned long long) + sizeof(unsigned) * n_ev + 1024;
   void* ws = nullptr;
   if (int rc = scratch(ctx, bytes, &ws)) return rc;
   char* w = static_cast<char*>(ws);
@@ -391,6 +431,7 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   unsigned* d_peak = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * (n_ev + 1)));
   unsigned* d_bound = d_peak + n_ev;
   unsigned long long* d_acc = reinterpret_cast<unsigned long long*>(take(acc_bytes));
+  float* d_incg = reinterpret_cast<float*>(take(incg_bytes));
   float* d_delays = reinterpret_cast<float*>(take(sizeof(float) * tbl));
   float* d_apod = reinterpret_cast<float*>(take(sizeof(float) * tbl));
   int* d_active = reinterpret_cast<int*>(take(sizeof(int) * tbl));
@@ -452,23 +493,29 @@ extern "C" int usx_cu_simulate(usx_ctx* ctx, const usx_channel_desc* cd,
   a.directivity_on = cfg->apply_directivity;
   a.motion = cfg->enable_motion;
   a.full = cfg->full_transmit_diffraction;
-  // Enough blocks per event to fill the GPU several times over.
-  const long target_blocks = std::max<long>(1, static_cast<long>(ctx->sm_count) * 8 / std::max(1, n_ev));
-  a.scat_per_block = static_cast<int>(std::max<long>(kSimWarps, (n_scat + target_blocks - 1) / target_blocks));
-  a.scat_per_block = std::min(a.scat_per_block, 256);
-  const long gx = std::max<long>(1, (n_scat + a.scat_per_block - 1) / a.scat_per_block);
+  a.scat_per_block = scat_per_block;
+  a.inc_global = d_incg;
+  a.n_sblocks = gx;
+  a.n_items = gx * n_ev;
   a.t_table = n_smp <= kMaxTimeTable ? 1 : 0;
-  const size_t smem = sizeof(float) * (kMaxPulse + static_cast<size_t>(kSimWarps) * (inc_cap + 4 * kMaxElem) +
-                                       (a.t_table ? static_cast<size_t>(n_smp) : 0));
+  a.pulse_pad = (pulse_n + 3) / 4 * 4;
+  a.tbl_pad = (n_el + 3) / 4 * 4;
+  a.inc_small = std::min(kIncSmall, (inc_cap + 3) / 4 * 4);
+  const size_t smem = sizeof(float) * (a.pulse_pad + (a.t_table ? (n_smp + 3) / 4 * 4 : 0) +
+                                       static_cast<size_t>(kSimWarps) * (a.inc_small + 4 * a.tbl_pad));
   if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "usx_cu_simulate: incident window too long");
   if (int rc_ = smem_limit(reinterpret_cast<const void*>(simulate_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
+  int per_sm = 0;
+  if (int rc_ = occupancy(reinterpret_cast<const void*>(simulate_kernel), 32 * kSimWarps, smem, &per_sm)) return rc_;
+  const long grid = std::max<long>(1, std::min<long>(grid_max, static_cast<long>(std::max(1, per_sm)) * ctx->sm_count));
+
   if (n_scat > 0) {
     prof_begin(ctx, "simulate_kernel");
     USX_CUDA(cudaMemsetAsync(d_bound, 0, sizeof(unsigned), ctx->stream));
     USX_CUDA(cudaMemsetAsync(d_acc, 0, acc_bytes, ctx->stream));
     sim_bound_kernel<<<static_cast<unsigned>(ceil_div(n_scat, 256)), 256, 0, ctx->stream>>>(a);
     USX_CHECK_LAUNCH("sim_bound_kernel");
-    simulate_kernel<<<dim3(static_cast<unsigned>(gx), n_ev), 32 * kSimWarps, smem, ctx->stream>>>(a);
+    simulate_kernel<<<static_cast<unsigned>(grid), 32 * kSimWarps, smem, ctx->stream>>>(a);
     prof_end(ctx);
     USX_CHECK_LAUNCH("simulate_kernel");
     fixed_to_float_kernel<<<static_cast<unsigned>(ceil_div(ev_size * n_ev, 256)), 256, 0, ctx->stream>>>(
