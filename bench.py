@@ -509,6 +509,39 @@ def run_ours(args) -> None:
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = world * args.steps / (ms / 1e3)
+    if args.workload == "learned" and args.two_streams:
+        # Two frames in flight: a second plan (same settings, same network) on
+        # its own context and stream; frame i goes to plan i % 2.
+        ctx2 = capi.Context(local)
+        plan2 = ctx2.plan(ch_iq, cgrid, capi.bf_config(**bkw))
+        plan2.set_learned(mlp, gate)
+        plan2.set_learned_refine(refine)
+        plan2.set_learned_subspace(True, share)
+        plan2.set_learned_level_gate(level)
+        if args.mv_mode == 3:
+            plan2.set_mv_mode(3)
+        plan2.set_variant(best)
+        frame2 = torch.empty_like(frame)
+        for _ in range(args.warmup):
+            plan2.execute(d_iq.data_ptr(), frame2.data_ptr())
+        ctx2.synchronize()
+        s1, s2 = stream, torch.cuda.ExternalStream(ctx2.stream())
+        ev0, ev_b, ev1 = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(), torch.cuda.Event(enable_timing=True))
+        torch.cuda.synchronize()
+        ev0.record(s1)
+        s2.wait_event(ev0)
+        for i in range(args.steps):
+            (plan if i % 2 == 0 else plan2).execute(d_iq.data_ptr(), (frame if i % 2 == 0 else frame2).data_ptr())
+        ev_b.record(s2)
+        s1.wait_event(ev_b)
+        ev1.record(s1)
+        ev1.synchronize()
+        ms2 = ev0.elapsed_time(ev1)
+        extra["two_frames_in_flight"] = {"value": world * args.steps / (ms2 / 1e3) * N0 / n0, "unit": "frames/s",
+                                         "ms_per_step": ms2 / args.steps * N0 / n0,
+                                         "streams": 2, "note": "frames alternate between two plans on two streams"}
+        plan2.close()
+        ctx2.close()
     if args.workload == "learned":
         gated, pixels = plan.learned_stats()
         extra["fallback_rate"] = gated / max(1, pixels)
@@ -1503,6 +1536,8 @@ def main() -> int:
                          "pixels): 1 tcgen05 BF16 covariance + refinement, 2 the same on mma.sync, "
                          "3 FP32 lag-recurrence covariance")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-two-streams", dest="two_streams", action="store_false",
+                    help="learned workload: skip the two-frames-in-flight timing (two plans on two streams)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
