@@ -163,10 +163,12 @@ int usx_cu_bf_variant_order(int index, int* deep_first);
  * (tile_lines x 32 pixels per CTA), 1 the same with the trace windows staged
  * by bulk copies, 2 a transmit table (32 pixels per CTA, warp_lines lines x
  * 32 / warp_lines depths, one warp per channel_group channels; the transmit
- * delay, phasor and illumination weight computed once per pixel and event).
- * Families 1 and 2 fall back to variant 0 where they do not apply (RF data,
- * incoherent compounding; family 1 also needs plane waves, family 2 at most
- * 256 channels). */
+ * delay, phasor and illumination weight computed once per pixel and event),
+ * 3 the staged windows in a ring of shared-memory stages filled by a producer
+ * warp (bulk copies on mbarriers, no CTA-wide barrier in the loop).
+ * Families 1-3 fall back to variant 0 where they do not apply (RF data,
+ * incoherent compounding; families 1 and 3 also need plane waves, family 2
+ * at most 256 channels). */
 int usx_cu_bf_variant_kind(int index, int* kind);
 int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
 int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);

@@ -1025,6 +1025,337 @@ __global__ void __launch_bounds__(32 * kTL) das_staged_kernel(const BfArgs a) {
   a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
 }
 
+// ------------------------------------------------------------------------
+// das_ring_kernel: the staged delay-and-sum with a producer warp. The CTA is
+// kTL consumer warps (one lateral line x 32 depths each, as das_staged_kernel)
+// and one producer warp. Steps are (channel group of kG, transmit) in
+// das_fast_kernel's order; the producer stages each step's channel windows
+// (kStageW samples per channel, bounded analytically from the tile's extent
+// for plane waves) into a ring of kS shared-memory stages with cp.async.bulk,
+// each stage completing on its "full" mbarrier (transaction bytes), and
+// reuses a stage once all consumer warps have arrived on its "empty"
+// mbarrier. The consumers never meet at a CTA barrier inside the loop: each
+// waits for its step's stage, computes, and releases it. Samples outside a
+// staged window (rounding at its edge, a channel the tile's bound left out)
+// are read from global memory, so the frame is das_fast_kernel's bit for bit.
+// All waits are bounded; after a timeout the consumers read every sample
+// from global memory, the context's status word records it, and the producer
+// waits (bounded) for its copies in flight before it exits.
+// Measured at 128 channels, 75 plane waves, 512 x 1024 (ms per frame against
+// 4.98 for das_fast_kernel's best shape): (kG, kTL, kS) = (4, 4, 8) 12.1,
+// (8, 4, 8) 9.9, (8, 8, 8) 8.1, (16, 4, 4) 9.7; with the producer's bounds
+// per event and per channel group precomputed, (4, 4, 12) 11.5 and (8, 8, 8)
+// 7.75. The consumers still evaluate each event's transmit terms once per
+// channel group and now also wait on a stage per step; das_fast_kernel's L1
+// already serves most gathers. (8, 8, 8) stays an autotuner candidate.
+constexpr int kRingMaxEv = 128;   // events whose tile bound is kept in shared memory
+
+__device__ __forceinline__ bool ring_wait(uint64_t* bar, unsigned parity) {
+  for (long spin = 0; spin < (1L << 24); ++spin)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int kG, int kTL, int kS>
+__global__ void __launch_bounds__(32 * (kTL + 1)) das_ring_kernel(const BfArgs a) {
+  __shared__ __align__(16) float2 win[kS][kG][kStageW];
+  __shared__ __align__(8) uint64_t full[kS], empty[kS];
+  __shared__ int s_lo[kS][kG];
+  __shared__ float bnd[4][kTL];   // per consumer warp: x min, x max, z min, z max
+  __shared__ float s_tmin[kRingMaxEv];
+  const int n0 = a.n_pix / a.n1;
+  const int tiles_depth = (a.n1 + 31) / 32;
+  const int tile = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool producer = warp == kTL;
+  const int line = (tile / tiles_depth) * kTL + warp;
+  const int depth = (tile % tiles_depth) * 32 + lane;
+  const bool live = !producer && line < n0 && depth < a.n1;
+  const int pix = live ? line * a.n1 + depth : 0;
+  const long frame = blockIdx.y;
+  const float px = live ? __ldg(a.points + 3 * pix) : 0.f, py = live ? __ldg(a.points + 3 * pix + 1) : 0.f,
+              pz = live ? __ldg(a.points + 3 * pix + 2) : 0.f;
+  if (!producer) {
+    float xl = live ? px : INFINITY, xh = live ? px : -INFINITY, zl = live ? pz : INFINITY,
+          zh = live ? pz : -INFINITY;
+    for (int o = 16; o > 0; o >>= 1) {
+      xl = fminf(xl, __shfl_xor_sync(0xffffffffu, xl, o));
+      xh = fmaxf(xh, __shfl_xor_sync(0xffffffffu, xh, o));
+      zl = fminf(zl, __shfl_xor_sync(0xffffffffu, zl, o));
+      zh = fmaxf(zh, __shfl_xor_sync(0xffffffffu, zh, o));
+    }
+    if (lane == 0) {
+      bnd[0][warp] = xl;
+      bnd[1][warp] = xh;
+      bnd[2][warp] = zl;
+      bnd[3][warp] = zh;
+    }
+  }
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < kS; ++st) {
+      mbar_init(&full[st], 1);
+      mbar_init(&empty[st], kTL);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  float x_min = bnd[0][0], x_max = bnd[1][0], z_min = bnd[2][0], z_max = bnd[3][0];
+#pragma unroll
+  for (int w = 1; w < kTL; ++w) {
+    x_min = fminf(x_min, bnd[0][w]);
+    x_max = fmaxf(x_max, bnd[1][w]);
+    z_min = fminf(z_min, bnd[2][w]);
+    z_max = fmaxf(z_max, bnd[3][w]);
+  }
+  int ev_first = a.ev_begin, ev_last = a.ev_end;
+  if (a.seq_epf > 0) {
+    ev_first = a.ev_begin + static_cast<int>(frame) * a.seq_epf;
+    ev_last = ev_first + a.seq_epf;
+  }
+  if (a.pass >= 0) {
+    ev_first += a.pass;
+    ev_last = ev_first + 1;
+  }
+  const float2* iq = a.iq + frame * a.data_stride;
+  const int n_ev = max(0, ev_last - ev_first);
+  const int n_groups = (a.n_ch + kG - 1) / kG;
+  const int n_steps = x_min <= x_max ? n_groups * n_ev : 0;   // no live pixel: no steps
+
+  if (producer) {
+    // Lane k < kG stages channel g + k of each step. The earliest transmit
+    // arrival over the tile, per event, once (in shared memory).
+    float* tmin_ev = reinterpret_cast<float*>(&s_tmin[0]);
+    for (int e = lane; e < n_ev && e < kRingMaxEv; e += 32) {
+      const TxDev& t = a.tx[ev_first + e];
+      const float tx0 = ((x_min - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+      const float tx1 = ((x_max - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+      const float tx2 = ((x_min - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+      const float tx3 = ((x_max - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+      tmin_ev[e] = fminf(fminf(tx0, tx1), fminf(tx2, tx3));
+    }
+    __syncwarp();
+    const float half_ap = 0.5f * z_max / fmaxf(a.f_number, 1e-3f) + a.pitch;
+    const long row_base = frame * a.data_stride;
+    bool ok = true;
+    int issued = 0;
+    float rmin = 0.0f;
+    bool in_ap = false;
+    for (int i = 0; i < n_steps; ++i) {
+      const int st = i % kS;
+      if (i >= kS) {
+        bool got = true;
+        if (lane == 0) got = ring_wait(&empty[st], static_cast<unsigned>((i / kS) - 1) & 1u);
+        if (!__shfl_sync(0xffffffffu, got, 0)) {
+          ok = false;
+          break;
+        }
+      }
+      const int g = (i / n_ev) * kG, e_rel = i % n_ev, ev = ev_first + e_rel;
+      if (e_rel == 0 && lane < kG) {
+        // A new channel group: this lane's channel, in the tile's aperture?
+        const int ch = g + lane;
+        in_ap = false;
+        if (ch < a.n_ch) {
+          const float ex = elem_x(a, ch);
+          if (ex >= x_min - half_ap && ex <= x_max + half_ap) {
+            const float xc = fminf(fmaxf(ex, x_min), x_max);
+            rmin = sqrtf((ex - xc) * (ex - xc) + z_min * z_min) / a.c;
+            in_ap = true;
+          }
+        }
+      }
+      float tmin;
+      if (e_rel < kRingMaxEv) {
+        tmin = tmin_ev[e_rel];
+      } else {
+        const TxDev& t = a.tx[ev];
+        const float tx0 = ((x_min - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+        const float tx1 = ((x_max - t.ox) * t.sin_a + (z_min - 0.0f) * t.cos_a) / a.c;
+        const float tx2 = ((x_min - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+        const float tx3 = ((x_max - t.ox) * t.sin_a + (z_max - 0.0f) * t.cos_a) / a.c;
+        tmin = fminf(fminf(tx0, tx1), fminf(tx2, tx3));
+      }
+      int lo = -1;
+      if (lane < kG) {
+        const int ch = g + lane;
+        if (in_ap) {
+          {
+            lo = static_cast<int>(floorf((tmin + rmin - a.t0) * a.fs)) - 2;
+            lo = max(0, min(lo, a.n_smp - kStageW - 1));
+            const long el = row_base + (static_cast<long>(ev) * a.n_ch + ch) * a.n_smp + lo;
+            if (el & 1L) lo = lo > 0 ? lo - 1 : lo + 1;   // 16-byte aligned source
+          }
+        }
+        s_lo[st][lane] = lo;
+      }
+      unsigned bytes = lo >= 0 ? static_cast<unsigned>(kStageW * sizeof(float2)) : 0u;
+      for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+      __syncwarp();
+      if (lane == 0) {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_arrive_expect_tx(&full[st], bytes);
+      }
+      __syncwarp();
+      if (lo >= 0) {
+        const float2* src = iq + (static_cast<long>(ev) * a.n_ch + g + lane) * a.n_smp + lo;
+        bulk_copy_g2s(&win[st][lane][0], src, kStageW * sizeof(float2), &full[st]);
+      }
+      ++issued;
+    }
+    if (lane == 0) {
+      if (!ok && a.status) atomicExch(a.status, 1);
+      // No copy may still be in flight when the CTA exits.
+      for (int i = max(0, issued - kS); i < issued; ++i) ring_wait(&full[i % kS], static_cast<unsigned>(i / kS) & 1u);
+    }
+    return;
+  }
+
+  // ---- consumers ----------------------------------------------------------
+  const bool select = a.compounding == USX_COMP_SELECT;
+  int best_ev = -1;
+  float best_w = 0.0f;
+  if (select && live) {
+    for (int ev = ev_first; ev < ev_last; ++ev) {
+      const float tw = tx_sensitivity_fast(a.tx[ev], px, pz, a.lambda);
+      if (tw > best_w) {
+        best_w = tw;
+        best_ev = ev;
+      }
+    }
+  }
+  const unsigned n_last = static_cast<unsigned>(a.n_smp - 1);
+  cplx das = mk(0.f, 0.f), s = mk(0.f, 0.f), q = mk(0.f, 0.f), coh = mk(0.f, 0.f);
+  float incs = 0.0f;
+  int n_active = 0;
+  float rt[kG], ar[kG], ai[kG];
+  unsigned mask = 0u;
+  bool timed_out = false;
+  for (int i = 0; i < n_steps; ++i) {
+    const int g = (i / n_ev) * kG, ev = ev_first + i % n_ev;
+    const int st = i % kS;
+    if (i % n_ev == 0) {
+      mask = 0u;
+#pragma unroll
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        rt[k] = 0.0f;
+        ar[k] = ai[k] = 0.0f;
+        if (live && ch < a.n_ch) {
+          const float ex = elem_x(a, ch);
+          if (aperture_weight(ex, px, pz, a.f_number, a.rx_window, a.tukey_alpha) > 0.0f) {
+            mask |= 1u << k;
+            rt[k] = dist3(ex, 0.0f, 0.0f, px, py, pz) / a.c;
+          }
+        }
+      }
+    }
+    if (!timed_out && !ring_wait(&full[st], static_cast<unsigned>(i / kS) & 1u)) timed_out = true;
+    if (mask) {
+      const TxDev& t = a.tx[ev];
+      float tw;
+      if (select) {
+        tw = (best_ev == ev && best_w > 0.0f) ? 1.0f : 0.0f;
+      } else if (a.tx_weighting) {
+        tw = tx_sensitivity_fast(t, px, pz, a.lambda);
+      } else {
+        tw = 1.0f;
+      }
+      if (tw > 0.0f) {
+        const float tau = tx_arrival(t, px, py, pz, a.c);
+        float tc = 1.0f, ts = 0.0f;
+        if (a.fdem > 0.0f) sincosf(a.two_pi_f * tau, &ts, &tc);
+        const float wr = tw * tc, wi = tw * ts;
+        const long trace0 = (static_cast<long>(ev) * a.n_ch + g) * a.n_smp;
+#pragma unroll
+        for (int k = 0; k < kG; ++k) {
+          if (!(mask & (1u << k))) continue;
+          const float idx = (tau + rt[k] - a.t0) * a.fs;
+          const float fl = floorf(idx);
+          const int kk = static_cast<int>(fl);
+          if (static_cast<unsigned>(kk) >= n_last) continue;
+          const float f = idx - fl;
+          const int lo = s_lo[st][k];
+          const int loc = kk - lo;
+          float2 s0, s1;
+          if (!timed_out && lo >= 0 && loc >= 0 && loc + 1 < kStageW) {
+            s0 = win[st][k][loc];
+            s1 = win[st][k][loc + 1];
+          } else {
+            const float2* tr = iq + trace0 + static_cast<long>(k) * a.n_smp + kk;
+            s0 = __ldg(tr);
+            s1 = __ldg(tr + 1);
+          }
+          const float vr = fmaf(f, s1.x - s0.x, s0.x);
+          const float vi = fmaf(f, s1.y - s0.y, s0.y);
+          ar[k] = fmaf(wr, vr, fmaf(-wi, vi, ar[k]));
+          ai[k] = fmaf(wr, vi, fmaf(wi, vr, ai[k]));
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+    if ((i + 1) % n_ev == 0) {
+      // The group is complete: receive phasor and aperture weight, combine.
+#pragma unroll
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        if (ch >= a.n_ch || !live) continue;
+        const bool act = (mask >> k) & 1u;
+        cplx y = mk(0.f, 0.f);
+        if (act) {
+          const float w = aperture_weight(elem_x(a, ch), px, pz, a.f_number, a.rx_window, a.tukey_alpha);
+          const float ap = a.is_mv ? 1.0f : w;
+          float rc = 1.0f, rs = 0.0f;
+          if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs, &rc);
+          const float gr = ap * rc, gi = ap * rs;
+          y = mk(fmaf(gr, ar[k], -gi * ai[k]), fmaf(gr, ai[k], gi * ar[k]));
+        }
+        if (a.is_mv) {
+          a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = make_float2(y.re, y.im);
+          continue;
+        }
+        n_active += act ? 1 : 0;
+        if (a.combiner == USX_COMB_DMAS) {
+          const float m = cabsf_(y);
+          if (m > 0.0f) {
+            const cplx v = cdivr(y, sqrtf(m));
+            s = cadd(s, v);
+            q = cadd(q, cmul(v, v));
+          }
+        } else {
+          das = cadd(das, y);
+        }
+        if (a.cf && act) {
+          coh = cadd(coh, y);
+          incs += cnorm(y);
+        }
+      }
+    }
+  }
+  if (timed_out && lane == 0 && a.status) atomicExch(a.status, 1);
+  if (!live) return;
+  if (a.is_mv) {
+    if (n_steps == 0)
+      for (int ch = 0; ch < a.n_ch; ++ch) a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = make_float2(0.f, 0.f);
+    return;
+  }
+  cplx out;
+  if (n_active == 0) {
+    out = mk(0.f, 0.f);
+  } else if (a.combiner == USX_COMB_DMAS) {
+    const cplx acc = cscale(csub(cmul(s, s), q), 0.5f);
+    out = cdivr(acc, 0.5f * fmaxf(1.0f, static_cast<float>(n_active - 1)));
+  } else {
+    out = das;
+  }
+  if (a.cf && n_active > 0)
+    out = cscale(out, (incs > 0.0f) ? cnorm(coh) / (static_cast<float>(n_active) * incs) : 0.0f);
+  a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+}
+
 // The delay-and-sum variants the autotuner chooses from (index 0 is the
 // default): (channel group, tile lines, minimum resident CTAs per SM, lines
 // per warp).
@@ -1035,6 +1366,7 @@ struct DasVariant {
   void (*rf)(BfArgs);
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
   bool table;    // das_table_kernel (IQ, coherent or select, n_ch <= 256); else variant 0
+  int producer_warps = 0;   // das_ring_kernel: one warp beside the tile's warps
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
@@ -1053,6 +1385,11 @@ template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
   return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true, false};
 }
+// The producer-warp ring (same applicability as the staged kernel).
+template <int G, int TL, int S>
+constexpr DasVariant das_ring_variant() {
+  return DasVariant{G, TL, 0, 1, false, das_ring_kernel<G, TL, S>, das_fast_kernel<false, 16, 4, 1>, true, false, 1};
+}
 const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8>(),  das_variant<16, 4, 1>(), das_variant<16, 8, 2>(), das_variant<32, 4, 1>(),
     das_variant<8, 8, 4>(),  das_variant<16, 2, 8>(), das_variant<4, 4, 12>(), das_variant<8, 2, 16>(),
@@ -1062,6 +1399,7 @@ const DasVariant kDasVariants[] = {
     das_variant<4, 4, 12, false, 2, true>(), das_variant<4, 4, 12, false, 4, true>(),
     das_variant<8, 4, 8, false, 4, true>(),
     das_table_variant<4, 2, 2>(),
+    das_ring_variant<8, 8, 8>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -1443,7 +1781,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       dv.iq<<<grid_das, 32 * table_warps(dv.group, b.n_ch), table_smem, ctx->stream>>>(b);
     } else if (fast) {
       if (plan->cd.is_iq)
-        dv.iq<<<grid_das, 32 * dv.tile_lines, 0, ctx->stream>>>(b);
+        dv.iq<<<grid_das, 32 * (dv.tile_lines + dv.producer_warps), 0, ctx->stream>>>(b);
       else
         dv.rf<<<grid_das, 32 * dv.tile_lines, 0, ctx->stream>>>(b);
     } else {
@@ -1791,7 +2129,11 @@ int usx_cu_bf_variant_order(int index, int* deep_first) {
 
 int usx_cu_bf_variant_kind(int index, int* kind) {
   if (index < 0 || index >= kNumDasVariants) return fail(USX_ERR_INVALID, "usx_cu_bf_variant_kind: no such variant");
-  if (kind) *kind = kDasVariants[index].table ? 2 : kDasVariants[index].staged ? 1 : 0;
+  if (kind)
+    *kind = kDasVariants[index].table            ? 2
+            : kDasVariants[index].producer_warps ? 3
+            : kDasVariants[index].staged         ? 1
+                                                 : 0;
   return USX_OK;
 }
 
