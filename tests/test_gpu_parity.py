@@ -297,6 +297,38 @@ def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_k
     plan.close()
 
 
+def test_mv_export_variants_bit_identical(capi, ctx, torch, golden):
+    """Minimum variance through every delay-and-sum shape, including the
+    export-only tabulated kernels: the exported channel samples are the same
+    bit for bit, so the FP32 minimum-variance frames are identical; on a ragged
+    grid too."""
+    g = golden("bf")
+    s = golden("sim")
+    pr, med, acq = sim_setup(s)
+    ch = c_channel(capi, pr, med, acq, txset(s, "pw"), is_iq=True, fdem=5e6)
+    ax0, ax1 = np.asarray(g["ax0"]), np.asarray(g["ax1"])
+    pts = np.asarray(g["pts"], dtype=np.float32).reshape(len(ax0), len(ax1), 3)
+    d = dev(torch, g["iq"])
+    variants = capi.das_variants()
+    assert any(v[5] == 4 for v in variants)  # export-only shapes are candidates
+    grids = (capi.Grid(0, ax0, ax1, pts.reshape(-1, 3)), capi.Grid(0, ax0[:13], ax1[:37], pts[:13, :37].reshape(-1, 3)))
+    for gi, grid in enumerate(grids):
+        plan = ctx.plan(ch, grid, capi.bf_config(**BF_CASES["mv"]))
+        plan.set_mv_mode(3)
+        out = torch.empty(grid.shape, dtype=torch.complex64, device="cuda")
+        frames = []
+        for v in range(len(variants)):
+            plan.set_variant(v)
+            out.fill_(float("nan"))
+            plan.execute(d.data_ptr(), out.data_ptr())
+            frames.append(host(torch, out))
+        for v, f in enumerate(frames[1:], 1):
+            assert np.array_equal(f, frames[0]), f"variant {v}"
+        if gi == 0:  # the ragged grid's edge pixels average other range rows
+            assert rel_l2(frames[0], g["bf_mv"]) < 1e-5
+        plan.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("cfg_kw", [dict(f_number=1.5), dict(f_number=1.5, combiner=1, coherence_factor=1)])
 def test_das_variants_ragged_grid(capi, ctx, torch, golden, cfg_kw):

@@ -448,6 +448,155 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 }
 
 // ------------------------------------------------------------------------
+// das_export_kernel: the minimum-variance export (compounded channel samples
+// y[frame][pixel][channel]) with the transmit side tabulated per pixel. A
+// CTA is kPW pixel warps x kCQ channel warps: the tile is kPW x 32 pixels
+// (das_fast_kernel's tile: kPW lines x 32 depths, warps of kWL lines x 32 /
+// kWL depths), and channel warp cq takes channels cq, cq + kCQ, ... in groups
+// of kG, so the kPW pixel warps that share a channel read the same trace
+// windows through L1. Per pass (one group of kG channels per channel warp)
+// the events go in chunks of kExpEv: the CTA first tabulates (transmit delay,
+// weighted transmit phasor, illumination weight) for its pixels and the
+// chunk's events, each thread for its own pixel, then every thread runs its
+// kG channels over the chunk. The transmit side is evaluated once per pixel,
+// event and pass instead of once per channel group; the per-channel sums are
+// das_fast_kernel's expressions in the same order, so the exported samples
+// are the same bit for bit. Export launches only (no channel combine).
+// Measured on the learned frame (128 ch, 75 plane waves, 512 x 1024): export
+// 4.83 ms with (kG, kPW, kCQ, kWL) = (4, 4, 4, 4) against 5.08 for
+// das_fast_kernel's best shape; (8, 4, 4, 4) 5.1, (8, 4, 4, 1) 5.6,
+// (8, 4, 2, 4) 5.3. The gathers' latency, not the transmit terms, bounds it.
+constexpr int kExpEv = 16;
+
+template <int kG, int kPW, int kCQ, int kWL>
+__global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs a) {
+  static_assert(32 % kWL == 0 && kPW % kWL == 0, "warp shape must tile the CTA");
+  __shared__ float4 tab[kExpEv][32 * kPW];
+  constexpr int kWD = 32 / kWL;
+  const int n0 = a.n_pix / a.n1;
+  const int tiles_depth = (a.n1 + 31) / 32;
+  const int tile = blockIdx.x;
+  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  const int pw = w % kPW, cq = w / kPW;
+  const int pl = pw * 32 + ln;   // pixel slot in the tile
+  const int line = (tile / tiles_depth) * kPW + (pw / kWL) * kWL + ln / kWD;
+  const int depth = (tile % tiles_depth) * 32 + (pw % kWL) * kWD + ln % kWD;
+  const bool valid = line < n0 && depth < a.n1;
+  const int pix = valid ? line * a.n1 + depth : 0;
+  const long frame = blockIdx.y;
+  const float px = __ldg(a.points + 3 * pix), py = __ldg(a.points + 3 * pix + 1), pz = __ldg(a.points + 3 * pix + 2);
+  int ev_lo = a.ev_begin, ev_hi = a.ev_end;
+  if (a.seq_epf > 0) {
+    ev_lo = a.ev_begin + static_cast<int>(frame) * a.seq_epf;
+    ev_hi = ev_lo + a.seq_epf;
+  }
+  if (a.pass >= 0) {
+    ev_lo += a.pass;
+    ev_hi = ev_lo + 1;
+  }
+  const bool select = a.compounding == USX_COMP_SELECT;
+  int best_ev = -1;
+  float best_w = 0.0f;
+  if (select && valid) {
+    for (int ev = ev_lo; ev < ev_hi; ++ev) {
+      const float tw = tx_sensitivity_fast(a.tx[ev], px, pz, a.lambda);
+      if (tw > best_w) {
+        best_w = tw;
+        best_ev = ev;
+      }
+    }
+  }
+  const float2* iq = a.iq + frame * a.data_stride;
+  const unsigned n_last = static_cast<unsigned>(a.n_smp - 1);
+  const int n_groups = (a.n_ch + kG - 1) / kG;
+  const int n_pass = (n_groups + kCQ - 1) / kCQ;
+  for (int pass = 0; pass < n_pass; ++pass) {
+    const int grp = pass * kCQ + cq;
+    const int g = grp * kG;
+    float rt[kG];
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < kG; ++k) {
+      const int ch = g + k;
+      rt[k] = 0.0f;
+      if (valid && ch < a.n_ch) {
+        const float ex = elem_x(a, ch);
+        if (aperture_weight(ex, px, pz, a.f_number, a.rx_window, a.tukey_alpha) > 0.0f) {
+          mask |= 1u << k;
+          rt[k] = dist3(ex, 0.0f, 0.0f, px, py, pz) / a.c;
+        }
+      }
+    }
+    float ar[kG], ai[kG];
+#pragma unroll
+    for (int k = 0; k < kG; ++k) ar[k] = ai[k] = 0.0f;
+    for (int c0 = ev_lo; c0 < ev_hi; c0 += kExpEv) {
+      const int c1 = min(ev_hi, c0 + kExpEv);
+      // The chunk's table: (tau, tw cos, tw sin, tw) for this thread's pixel.
+      __syncthreads();
+      for (int e = c0 + cq; e < c1; e += kCQ) {
+        const TxDev& t = a.tx[e];
+        float tw;
+        if (!valid)
+          tw = 0.0f;
+        else if (select)
+          tw = (best_ev == e && best_w > 0.0f) ? 1.0f : 0.0f;
+        else if (a.tx_weighting)
+          tw = tx_sensitivity_fast(t, px, pz, a.lambda);
+        else
+          tw = 1.0f;
+        float4 ent = make_float4(0.f, 0.f, 0.f, tw);
+        if (tw > 0.0f) {
+          const float tau = tx_arrival(t, px, py, pz, a.c);
+          float tc = 1.0f, ts = 0.0f;
+          if (a.fdem > 0.0f) sincosf(a.two_pi_f * tau, &ts, &tc);
+          ent = make_float4(tau, tw * tc, tw * ts, tw);
+        }
+        tab[e - c0][pl] = ent;
+      }
+      __syncthreads();
+      if (!mask) continue;
+      for (int e = c0; e < c1; ++e) {
+        const float4 ent = tab[e - c0][pl];
+        if (ent.w <= 0.0f) continue;
+        const float tau = ent.x, wr = ent.y, wi = ent.z;
+        const float2* trace = iq + (static_cast<long>(e) * a.n_ch + g) * a.n_smp;
+#pragma unroll
+        for (int k = 0; k < kG; ++k) {
+          if (!(mask & (1u << k))) continue;
+          const float idx = (tau + rt[k] - a.t0) * a.fs;
+          const float fl = floorf(idx);
+          const int kk = static_cast<int>(fl);
+          if (static_cast<unsigned>(kk) >= n_last) continue;
+          const float f = idx - fl;
+          const float2* tr = trace + static_cast<long>(k) * a.n_smp + kk;
+          const float2 s0 = __ldg(tr), s1 = __ldg(tr + 1);
+          const float vr = fmaf(f, s1.x - s0.x, s0.x);
+          const float vi = fmaf(f, s1.y - s0.y, s0.y);
+          ar[k] = fmaf(wr, vr, fmaf(-wi, vi, ar[k]));
+          ai[k] = fmaf(wr, vi, fmaf(wi, vr, ai[k]));
+        }
+      }
+    }
+    if (!valid) continue;
+#pragma unroll
+    for (int k = 0; k < kG; ++k) {
+      const int ch = g + k;
+      if (ch >= a.n_ch) break;
+      const bool act = (mask >> k) & 1u;
+      float2 y = make_float2(0.f, 0.f);
+      if (act) {
+        float rc = 1.0f, rs = 0.0f;
+        if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs, &rc);
+        const float gr = 1.0f * rc, gi = 1.0f * rs;   // the export carries no aperture weight
+        y = make_float2(fmaf(gr, ar[k], -gi * ai[k]), fmaf(gr, ai[k], gi * ar[k]));
+      }
+      a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = y;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
 // das_queue_kernel: frames of many plans (any probe, grid, transmit set and
 // plain combiner) in one persistent launch. Each CTA takes the next tile
 // from a device counter, finds its (plan, frame) from the entries' tile
@@ -1367,6 +1516,7 @@ struct DasVariant {
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
   bool table;    // das_table_kernel (IQ, coherent or select, n_ch <= 256); else variant 0
   int producer_warps = 0;   // das_ring_kernel: one warp beside the tile's warps
+  int channel_warps = 1;    // das_export_kernel: warps per pixel warp (export launches only; else variant 0)
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
@@ -1385,6 +1535,12 @@ template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
   return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true, false};
 }
+// The tabulated export (minimum-variance export launches; others use variant 0).
+template <int G, int PW, int CQ, int WL>
+constexpr DasVariant das_export_variant() {
+  return DasVariant{G, PW, 0, WL, false, das_export_kernel<G, PW, CQ, WL>, das_fast_kernel<false, 16, 4, 1>, false,
+                    false, 0, CQ};
+}
 // The producer-warp ring (same applicability as the staged kernel).
 template <int G, int TL, int S>
 constexpr DasVariant das_ring_variant() {
@@ -1400,6 +1556,7 @@ const DasVariant kDasVariants[] = {
     das_variant<8, 4, 8, false, 4, true>(),
     das_table_variant<4, 2, 2>(),
     das_ring_variant<8, 8, 8>(),
+    das_export_variant<4, 4, 4, 4>(), das_export_variant<8, 4, 4, 4>(),
 };
 constexpr int kNumDasVariants = static_cast<int>(sizeof(kDasVariants) / sizeof(kDasVariants[0]));
 
@@ -1777,7 +1934,17 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(dv.iq), table_smem)) return rc_;
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
     prof_begin(ctx, name);
-    if (table) {
+    if (fast && dv.channel_warps > 1 && !(b.is_mv && plan->cd.is_iq)) {
+      // An export-only shape on a launch that is not an export: variant 0.
+      const DasVariant& d0 = kDasVariants[0];
+      const dim3 g0(ceil_div(plan->n0, d0.tile_lines) * ceil_div(plan->n1, 32), grid_das.y);
+      if (plan->cd.is_iq)
+        d0.iq<<<g0, 32 * d0.tile_lines, 0, ctx->stream>>>(b);
+      else
+        d0.rf<<<g0, 32 * d0.tile_lines, 0, ctx->stream>>>(b);
+    } else if (fast && dv.channel_warps > 1) {
+      dv.iq<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, 0, ctx->stream>>>(b);
+    } else if (table) {
       dv.iq<<<grid_das, 32 * table_warps(dv.group, b.n_ch), table_smem, ctx->stream>>>(b);
     } else if (fast) {
       if (plan->cd.is_iq)
@@ -2132,6 +2299,7 @@ int usx_cu_bf_variant_kind(int index, int* kind) {
   if (kind)
     *kind = kDasVariants[index].table            ? 2
             : kDasVariants[index].producer_warps ? 3
+            : kDasVariants[index].channel_warps > 1 ? 4
             : kDasVariants[index].staged         ? 1
                                                  : 0;
   return USX_OK;
