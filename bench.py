@@ -1002,7 +1002,7 @@ def run_batch(args) -> None:
     for name, kw in BATCH_BEAMFORMERS.items():
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**kw))
         if name == "mv":
-            plan.set_mv_mode(1)
+            plan.set_mv_mode(args.mv_mode)
         with torch.cuda.stream(stream):
             plan.autotune(iq[0].data_ptr(), frames[0].data_ptr(), repeats=1)
 
@@ -1077,7 +1077,8 @@ def run_batch(args) -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (64 GPU-simulated 100k-scatterer cyst phantoms, seeds 2026-2089)",
             "config": {"workload": "batch_64x_75pw_512x1024", "beamformers": BATCH_BEAMFORMERS,
-                       "mv_solver": "tensor", "frames": n_frames, "iq_bytes": int(iq.numel() * 8),
+                       "mv_solver": {1: "tensor", 2: "tensor_mma", 3: "fp32_recurrence"}[args.mv_mode],
+                       "frames": n_frames, "iq_bytes": int(iq.numel() * 8),
                        "l2": "inputs larger than L2 (10.2 GB IQ), no flush"},
             "gpu_launches": launches, "graph_replays_per_step": len(graphs), "beamformers": per_bf,
             "roofline": roof, "cpu_baseline": cpu, "e2e": None, "clocks": clocks.summary(),
@@ -1206,7 +1207,7 @@ def run_sector(args) -> None:
     def make(kw, mv=False):
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**kw))
         if mv:
-            plan.set_mv_mode(1)
+            plan.set_mv_mode(args.mv_mode)
         plan.autotune(iq.data_ptr(), frame.data_ptr(), repeats=1)
         return plan
 
@@ -1397,7 +1398,7 @@ def run_mixed(args) -> None:
     sector_mv = dict(f_number=1.5, mv_subarray=32, mv_diagonal_loading=0.01, mv_range_average=2)
     f_sec = torch.empty((256, 1024), dtype=torch.complex64, device="cuda")
     plain = ctx.plan(sch_iq, scg, capi.bf_config(combiner=2, **sector_mv))
-    plain.set_mv_mode(1)
+    plain.set_mv_mode(args.mv_mode)
     plain.execute(iq_sec.data_ptr(), f_sec.data_ptr())
     ctx.synchronize()                    # the plan ran on the context's stream
     f_sec_plain = f_sec.clone()

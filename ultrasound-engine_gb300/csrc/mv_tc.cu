@@ -616,6 +616,7 @@ __host__ __device__ inline MvWarpLayout mv_warp_layout(int nmax, int n_dmax, int
 // n + 1 entries (n trailing rows). Against one trailing row per step with
 // lanes over columns, a quarter of the passes over the triangle and no lane
 // idles on short rows. False on a non-positive pivot.
+template <int kSlots>
 __device__ bool chol_blocked(float2* Rl, float2* P, int L, int lane) {
   for (int c0 = 0; c0 < L; c0 += 4) {
     const int nb = min(4, L - c0);
@@ -649,7 +650,7 @@ __device__ bool chol_blocked(float2* Rl, float2* P, int L, int lane) {
     __syncwarp();
     const int n = L - k0;
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < kSlots; ++h) {
       const int i = h == 0 ? k0 + lane : L - 1 - lane;
       if (h == 0 ? lane >= n : lane > n - 33) continue;
       const float4* pi = reinterpret_cast<const float4*>(P + 4 * i);
@@ -698,11 +699,12 @@ struct MvWarpArgs {
   int cov_recur;
 };
 
+template <int kSlots, bool kRecur>
 __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarpArgs wa) {
   extern __shared__ float4 mvw_smem_raw[];
   const MvTcArgs& a = wa.base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const MvWarpLayout lay = mv_warp_layout(wa.nmax, a.n_dmax, wa.lmax, wa.cov_recur != 0);
+  const MvWarpLayout lay = mv_warp_layout(wa.nmax, a.n_dmax, wa.lmax, kRecur);
   char* base = reinterpret_cast<char*>(mvw_smem_raw) + warp * lay.bytes;
   int* act = reinterpret_cast<int*>(base + lay.off_act);
   float2* yf = reinterpret_cast<float2*>(base + lay.off_yf);
@@ -826,7 +828,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     frexpf(amax, &e2);
     const float sc = ldexpf(1.0f, -e2), sc2 = ldexpf(1.0f, -2 * e2);
     const float inv_k = 1.0f / static_cast<float>(K);
-    if (wa.cov_recur) {
+    if constexpr (kRecur) {
       // R~[i][k] = sum_d sum_{s < n_sub} x_d[s + i] conj(x_d[s + k]) by
       // diagonals (lag m = i - k): the first entry of a diagonal in full,
       // then R~[i + 1][k + 1] = R~[i][k] - x[i] conj(x[k]) + x[n_sub + i]
@@ -835,7 +837,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       // lane then walks about L entries).
       const float f = sc2 * inv_k;
 #pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
+      for (int h = 0; h < kSlots; ++h) {
         const int m = h == 0 ? lane : 63 - lane;
         if (m >= L || (h == 1 && m < 32)) continue;
         // Four independent partial sums (snapshot parity x real/imaginary)
@@ -888,7 +890,8 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
         }
       }
       __syncwarp();
-    } else if (wa.r_pre && wa.r_flag[item - wa.item_begin]) {
+    } else {
+    if (wa.r_pre && wa.r_flag[item - wa.item_begin]) {
       // R~ from the tensor-core stage (same scale, same packing).
       const float2* src = wa.r_pre + (item - wa.item_begin) * wa.r_stride;
       for (int e = lane; e < L * (L + 1) / 2; e += 32) Rl[e] = src[e];
@@ -963,6 +966,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     }
     __syncwarp();
     }  // covariance on mma.sync
+    }  // BF16 covariances
 
     // ---- exact trace: channel t of a row appears in c(t) subarrays -------
     float tr = 0.0f;
@@ -979,7 +983,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     __syncwarp();
 
     // ---- Cholesky (blocked, rank-4 trailing updates) ---------------------
-    const bool ok = chol_blocked(Rl, reinterpret_cast<float2*>(base + lay.off_p), L, lane);
+    const bool ok = chol_blocked<kSlots>(Rl, reinterpret_cast<float2*>(base + lay.off_p), L, lane);
     if (!ok) {
       export_invalid(a, row, lane);
       if (lane == 0) {
@@ -991,17 +995,17 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       continue;
     }
 
-    auto solve = [&](float2 (&v)[2]) {
+    auto solve = [&](float2 (&v)[kSlots]) {
       for (int c = 0; c < L; ++c) {
         const int own = c & 31, sl = c >> 5;
         if (lane == own) {
           const float ljj = Rl[tri(c, c)].x;
-          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+          v[kSlots == 1 ? 0 : sl] = make_float2(v[kSlots == 1 ? 0 : sl].x / ljj, v[kSlots == 1 ? 0 : sl].y / ljj);
         }
-        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
-        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        const float vx = __shfl_sync(0xffffffffu, (kSlots > 1 && sl) ? v[kSlots - 1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, (kSlots > 1 && sl) ? v[kSlots - 1].y : v[0].y, own);
 #pragma unroll
-        for (int s2 = 0; s2 < 2; ++s2) {
+        for (int s2 = 0; s2 < kSlots; ++s2) {
           const int i = lane + 32 * s2;
           if (i > c && i < L) {
             const float2 l = Rl[tri(i, c)];
@@ -1014,13 +1018,13 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
         const int own = c & 31, sl = c >> 5;
         if (lane == own) {
           const float ljj = Rl[tri(c, c)].x;
-          v[sl] = make_float2(v[sl].x / ljj, v[sl].y / ljj);
+          v[kSlots == 1 ? 0 : sl] = make_float2(v[kSlots == 1 ? 0 : sl].x / ljj, v[kSlots == 1 ? 0 : sl].y / ljj);
         }
-        const float vx = __shfl_sync(0xffffffffu, sl ? v[1].x : v[0].x, own);
-        const float vy = __shfl_sync(0xffffffffu, sl ? v[1].y : v[0].y, own);
+        const float vx = __shfl_sync(0xffffffffu, (kSlots > 1 && sl) ? v[kSlots - 1].x : v[0].x, own);
+        const float vy = __shfl_sync(0xffffffffu, (kSlots > 1 && sl) ? v[kSlots - 1].y : v[0].y, own);
         const int rowc = c * (c + 1) / 2;
 #pragma unroll
-        for (int s2 = 0; s2 < 2; ++s2) {
+        for (int s2 = 0; s2 < kSlots; ++s2) {
           const int i = lane + 32 * s2;
           if (i < c) {
             const float2 l = Rl[rowc + i];
@@ -1045,7 +1049,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       }
       __syncwarp();
 #pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
+      for (int s2 = 0; s2 < kSlots; ++s2) {
         const int i = lane + 32 * s2;
         if (i < L) {
           float are = 0.f, aim = 0.f;
@@ -1066,39 +1070,39 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
       __syncwarp();
     };
 
-    float2 w[2];
+    float2 w[kSlots];
     w[0] = lane < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
-    w[1] = lane + 32 < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+    if (kSlots > 1) w[kSlots - 1] = lane + 32 < L ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
     solve(w);
-    if (!wa.cov_recur) {
+    if constexpr (!kRecur) {
 #pragma unroll
-    for (int s2 = 0; s2 < 2; ++s2)
+    for (int s2 = 0; s2 < kSlots; ++s2)
       if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
     __syncwarp();
     residual();
     {
-      float2 r[2];
+      float2 r[kSlots];
 #pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
+      for (int s2 = 0; s2 < kSlots; ++s2) {
         const int i = lane + 32 * s2;
         r[s2] = i < L ? wv[L + i] : make_float2(0.f, 0.f);
       }
       solve(r);
 #pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
+      for (int s2 = 0; s2 < kSlots; ++s2) {
         w[s2].x += r[s2].x;
         w[s2].y += r[s2].y;
       }
       __syncwarp();
 #pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2)
+      for (int s2 = 0; s2 < kSlots; ++s2)
         if (lane + 32 * s2 < L) wv[lane + 32 * s2] = w[s2];
       __syncwarp();
     }
     residual();
     float rn = 0.f;
 #pragma unroll
-    for (int s2 = 0; s2 < 2; ++s2) {
+    for (int s2 = 0; s2 < kSlots; ++s2) {
       const int i = lane + 32 * s2;
       if (i < L) {
         const float2 r = wv[L + i];
@@ -1119,7 +1123,7 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
     const float inv_nsub = 1.0f / static_cast<float>(n_sub);
 #pragma unroll
-    for (int s2 = 0; s2 < 2; ++s2) {
+    for (int s2 = 0; s2 < kSlots; ++s2) {
       const int i = lane + 32 * s2;
       if (i < L) {
         dre += w[s2].x;
@@ -1145,7 +1149,10 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     if (hypotf(dre, dim) < 1e-30f)
       export_invalid(a, row, lane);
     else
-      export_weights(a, row, lane, L, w, dre, dim);
+      {
+        const float2 w2[2] = {w[0], kSlots > 1 ? w[kSlots - 1] : make_float2(0.f, 0.f)};
+        export_weights(a, row, lane, L, w2, dre, dim);
+      }
     if (lane == 0) {
       cplx out;
       if (hypotf(dre, dim) < 1e-30f) {
@@ -1789,14 +1796,23 @@ int launch_mv_tc(usx_ctx* ctx, const float2* y, const float* points, float2* out
     const MvWarpLayout l = mv_warp_layout(w.nmax, a.n_dmax, w.lmax, w.cov_recur != 0);
     const size_t smem = l.bytes * kWarpMvWarps;
     if (smem > 227 * 1024) return fail(USX_ERR_UNSUPPORTED, "minimum variance: class too large for shared memory");
-    if (int rc_ = smem_limit(reinterpret_cast<const void*>(mv_warp_kernel), static_cast<size_t>(static_cast<int>(smem)))) return rc_;
+    // The FP32 instance compiles only the lag recurrence and one solve (64
+    // registers against 124 with the BF16 paths: twice the resident warps).
+    const bool recur = w.cov_recur != 0;
+    const void* kern = recur ? reinterpret_cast<const void*>(mv_warp_kernel<2, true>)
+                             : reinterpret_cast<const void*>(mv_warp_kernel<2, false>);
+    if (int rc_ = smem_limit(kern, static_cast<size_t>(static_cast<int>(smem)))) return rc_;
     int per_sm = 0;
-    if (int rc_ = occupancy(reinterpret_cast<const void*>(mv_warp_kernel), 32 * kWarpMvWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
+    if (int rc_ = occupancy(kern, 32 * kWarpMvWarps, static_cast<size_t>(smem), &per_sm)) return rc_;
     const long resident = static_cast<long>(std::max(1, per_sm)) * ctx->sm_count;
     const long need = (items + kWarpMvWarps - 1) / kWarpMvWarps;
     const long blocks = items < 0 ? resident : std::max(1L, std::min(need, resident * 8));
     prof_begin(ctx, name);
-    mv_warp_kernel<<<static_cast<unsigned>(blocks), 32 * kWarpMvWarps, smem, ctx->stream>>>(w);
+    const dim3 gr(static_cast<unsigned>(blocks));
+    if (recur)
+      mv_warp_kernel<2, true><<<gr, 32 * kWarpMvWarps, smem, ctx->stream>>>(w);
+    else
+      mv_warp_kernel<2, false><<<gr, 32 * kWarpMvWarps, smem, ctx->stream>>>(w);
     prof_end(ctx);
     USX_CHECK_LAUNCH(name);
     return USX_OK;
