@@ -441,6 +441,7 @@ def run_ours(args) -> None:
         refine = learned.trained_refine(WEIGHTS) if args.refine is None else args.refine
         share = learned.trained_share_gate(WEIGHTS) if args.share_gate is None else args.share_gate
         level = learned.trained_level_gate(WEIGHTS) if args.level_gate is None else args.level_gate
+        window = learned.trained_level_window(WEIGHTS)
         # Plain minimum variance (tensor-core solver) on the same frame, timed first.
         plain = ctx.plan(ch_iq, cgrid, capi.bf_config(**MV_KW))
         plain.set_mv_mode(args.mv_mode)
@@ -470,6 +471,7 @@ def run_ours(args) -> None:
         plan.set_learned_refine(refine)
         plan.set_learned_subspace(True, share)
         plan.set_learned_level_gate(level)
+        plan.set_learned_level_window(*window)
         if args.mv_mode == 3:
             plan.set_mv_mode(3)   # the gated pixels take the same solver
         solver = {1: "tensor", 2: "tensor_mma", 3: "fp32_recurrence"}[args.mv_mode]
@@ -481,6 +483,7 @@ def run_ours(args) -> None:
         extra["refine_beams"] = refine
         extra["share_gate"] = share
         extra["level_gate"] = level
+        extra["level_window"] = list(window)
     else:
         plan = ctx.plan(ch_iq, cgrid, capi.bf_config(**bkw))
         if args.workload == "mv":
@@ -518,6 +521,7 @@ def run_ours(args) -> None:
         plan2.set_learned_refine(refine)
         plan2.set_learned_subspace(True, share)
         plan2.set_learned_level_gate(level)
+        plan2.set_learned_level_window(*window)
         if args.mv_mode == 3:
             plan2.set_mv_mode(3)
         plan2.set_variant(best)
@@ -553,7 +557,8 @@ def run_ours(args) -> None:
         rep = WEIGHTS.with_suffix(".json")
         if rep.exists():
             r = json.loads(rep.read_text())
-            label = learned.Mode(gate=float(gate), share=float(share), level=float(level)).label
+            label = learned.Mode(gate=float(gate), share=float(share), level=float(level),
+                                 window=tuple(window)).label
             ev = r.get("eval", {}).get(label)
             if ev:
                 extra["held_out_quality"] = {
@@ -1373,6 +1378,7 @@ def run_mixed(args) -> None:
     lin.set_learned_refine(learned.trained_refine(WEIGHTS))
     lin.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
     lin.set_learned_level_gate(learned.trained_level_gate(WEIGHTS))
+    lin.set_learned_level_window(*learned.trained_level_window(WEIGHTS))
     f_lin = torch.empty((N0, N1), dtype=torch.complex64, device="cuda")
     lin.autotune(iq_lin.data_ptr(), f_lin.data_ptr(), repeats=1)
     # Sector: 64-element phased array.
@@ -1409,6 +1415,7 @@ def run_mixed(args) -> None:
     sec.set_learned_refine(learned.trained_refine(WEIGHTS))
     sec.set_learned_subspace(True, learned.trained_share_gate(WEIGHTS))
     sec.set_learned_level_gate(learned.trained_level_gate(WEIGHTS))
+    sec.set_learned_level_window(*learned.trained_level_window(WEIGHTS))
     sec.autotune(iq_sec.data_ptr(), f_sec.data_ptr(), repeats=1)
     env, logi = torch.empty((256, 1024), device="cuda"), torch.empty((256, 1024), device="cuda")
     img = torch.empty((800, 800), device="cuda")

@@ -246,6 +246,12 @@ int usx_cu_bf_plan_set_learned_subspace(usx_bf_plan* plan, int use_network, floa
  * far above the speckle level around them, where minimum variance forms deep
  * nulls that the refinement's subspace cannot. Default +inf (off); >= 1. */
 int usx_cu_bf_plan_set_learned_level_gate(usx_bf_plan* plan, float max_level_ratio);
+/* The level gate's neighbourhood: a pixel goes to the exact minimum variance
+ * when any pixel within +/- half_lines lateral lines and +/- half_depths
+ * depths exceeds its own depth's level by the gate, so that the flanks of a
+ * strong target's response are solved with its peak. Default 0, 0 (the pixel
+ * itself); each in [0, 16]. */
+int usx_cu_bf_plan_set_learned_level_window(usx_bf_plan* plan, int half_lines, int half_depths);
 /* Pixels gated to the exact solver and pixels beamformed by the learned path
  * since the last call (synchronises). */
 int usx_cu_bf_plan_learned_stats(usx_bf_plan* plan, int64_t* gated, int64_t* pixels);

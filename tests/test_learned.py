@@ -633,6 +633,20 @@ def test_level_gate_sends_bright_pixels_to_the_exact_solver(capi, torch):
             rates.append(gated / max(1, pixels))
         assert 0.2 < rates[0] < 0.9 and rates[-1] < 1e-3, rates
         assert rates[0] >= rates[1] >= rates[2] >= rates[3], rates
+        # A neighbourhood gates the flanks with the hot pixels: more pixels
+        # at the same ratio, growing with the window.
+        wrates = []
+        plan.set_learned_level_gate(3.0)
+        for win in ((0, 0), (1, 2), (3, 6)):
+            plan.set_learned_level_window(*win)
+            plan.learned_stats()
+            im.beamform(learned.COMB_LEARNED_MV)
+            gated, pixels = plan.learned_stats()
+            wrates.append(gated / max(1, pixels))
+        assert wrates[0] == pytest.approx(rates[1]) and wrates[0] < wrates[1] < wrates[2] < 1.0, wrates
+        with pytest.raises(ValueError):
+            plan.set_learned_level_window(-1, 0)
+        plan.set_learned_level_window(0, 0)
         with pytest.raises(ValueError):
             plan.set_learned_level_gate(0.5)
         mlp.close()

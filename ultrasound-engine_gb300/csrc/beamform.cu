@@ -1781,6 +1781,7 @@ struct usx_bf_plan {
   int lmv_use_net = 1;  // 0: the refinement's basis without the network's direction
   float lmv_share_gate = INFINITY;  // largest share of the refinement's power reduction from the network
   float lmv_level_gate = INFINITY;  // largest tr(R) over its depth's geometric mean
+  int lmv_level_lines = 0, lmv_level_depths = 0;  // the level gate's neighbourhood (half widths)
   int64_t lmv_pixels = 0;      // pixels beamformed by the learned path since the last stats read
   // Training export (minimum variance plans): features, weights, valid flags.
   float* exp_feat = nullptr;
@@ -2041,6 +2042,7 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       if (plan->lmv_beams >= 0) {
         if (int rc = launch_lmv_subspace(ctx, l, net, plan->lmv_beams, b.mv_loading, plan->lmv_gate,
                                          plan->lmv_use_net, plan->lmv_share_gate, plan->lmv_level_gate,
+                                         plan->lmv_level_lines, plan->lmv_level_depths,
                                          static_cast<float*>(bufs[11]), counters,
                                          gated, static_cast<int>(nrows), plan->d_mv_stats + 2,
                                          static_cast<float*>(bufs[10])))
@@ -2414,6 +2416,15 @@ int usx_cu_bf_plan_set_learned_level_gate(usx_bf_plan* plan, float max_level_rat
   if (!(max_level_ratio >= 1.0f))
     return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_level_gate: max_level_ratio must be >= 1");
   plan->lmv_level_gate = max_level_ratio;
+  return USX_OK;
+}
+
+int usx_cu_bf_plan_set_learned_level_window(usx_bf_plan* plan, int half_lines, int half_depths) {
+  if (!plan) return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_level_window: null plan");
+  if (half_lines < 0 || half_depths < 0 || half_lines > 16 || half_depths > 16)
+    return fail(USX_ERR_INVALID, "usx_cu_bf_plan_set_learned_level_window: half widths must be in [0, 16]");
+  plan->lmv_level_lines = half_lines;
+  plan->lmv_level_depths = half_depths;
   return USX_OK;
 }
 

@@ -355,6 +355,7 @@ struct SubArgs {
   float share_gate;       // largest share of the power reduction the network's direction may carry
   float log_level_gate;   // ln of the largest tr(R) over its depth's level (+inf: off)
   float* level;           // [frame][n1]: mean over lines of ln tr(R) (the depth's level)
+  int level_lines, level_depths;  // the level gate's neighbourhood: +/- lines, +/- depths
   int* gated_count;
   int2* gated;
   int gated_cap;
@@ -904,10 +905,29 @@ __global__ void lmv_subspace_solve_kernel(const SubArgs a) {
   if (!(tail[2 * K1 + 7] > 0.f)) return;  // gated, or n_act < 4
   const float eps = tail[2 * K1 + 2], Kf = tail[2 * K1 + 3];
   if (a.level && a.log_level_gate < INFINITY) {
+    // Any pixel of the neighbourhood (the pixel itself by default) whose
+    // tr(R) is above its depth's level by the gate sends this one to the
+    // exact solver: with a neighbourhood, the flanks of a strong target's
+    // response go with its peak.
     const long frame = row / a.n_pix;
     const int pix = static_cast<int>(row - frame * a.n_pix);
-    const float tr = tail[2 * K1 + 8];
-    if (tr > 0.f && logf(tr) - a.level[frame * a.n1 + pix % a.n1] > a.log_level_gate) {
+    const int n0 = a.n_pix / a.n1, line = pix / a.n1, depth = pix - line * a.n1;
+    bool hot = false;
+    for (int dl = -a.level_lines; dl <= a.level_lines && !hot; ++dl) {
+      const int ln = line + dl;
+      if (ln < 0 || ln >= n0) continue;
+      for (int dd = -a.level_depths; dd <= a.level_depths; ++dd) {
+        const int dp = depth + dd;
+        if (dp < 0 || dp >= a.n1) continue;
+        const float* nt = a.rec + (frame * a.n_pix + static_cast<long>(ln) * a.n1 + dp) * lmv_rec_floats(NB) + kG;
+        const float tr = nt[2 * K1 + 8];
+        if (nt[2 * K1 + 7] > 0.f && tr > 0.f && logf(tr) - a.level[frame * a.n1 + dp] > a.log_level_gate) {
+          hot = true;
+          break;
+        }
+      }
+    }
+    if (hot) {
       push_gated(a.gated_count, a.gated, a.gated_cap, static_cast<int>(tail[2 * K1 + 6]), pix, frame);
       if (a.stats) atomicAdd(a.stats, 1);
       return;
@@ -1100,7 +1120,8 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 
 
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int use_net, float share_gate, float level_gate, float* level,
+                        float gate, int use_net, float share_gate, float level_gate, int level_lines,
+                        int level_depths, float* level,
                         int* gated_count, int2* gated, int gated_cap, int* stats, float* rec) {
   SubArgs a;
   a.y = l.y;
@@ -1127,6 +1148,8 @@ int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int 
   a.share_gate = share_gate;
   a.log_level_gate = level_gate < INFINITY ? logf(std::max(level_gate, 1e-30f)) : INFINITY;
   a.level = level_gate < INFINITY ? level : nullptr;
+  a.level_lines = std::max(0, level_lines);
+  a.level_depths = std::max(0, level_depths);
   a.rx_window = l.rx_window;
   a.gated_count = gated_count;
   a.gated = gated;

@@ -330,7 +330,7 @@ int launch_lmv_apply(usx_ctx* ctx, const float* net, const float2* avg, const fl
 // tr(R) over the lateral lines at their depth also go to the exact solver
 // (+inf: off); `level` holds one float per (frame, depth).
 int launch_lmv_subspace(usx_ctx* ctx, const LmvLaunch& l, const float* net, int n_beams, float loading,
-                        float gate, int use_net, float share_gate, float level_gate, float* level,
+                        float gate, int use_net, float share_gate, float level_gate, int level_lines, int level_depths, float* level,
                         int* gated_count, int2* gated, int gated_cap, int* stats, float* rec);
 // Bytes per pixel of the scratch record launch_lmv_subspace passes between its two stages.
 int lmv_subspace_record_bytes(int n_beams);

@@ -50,6 +50,7 @@ struct LearnedNet {
   int refine = -1;   // DFT beams of the subspace refinement (< 0: none)
   float share_gate = INFINITY;
   float level_gate = INFINITY;
+  int level_lines = 0, level_depths = 0;  // the level gate's neighbourhood
 };
 
 std::string library_dir() {
@@ -98,6 +99,8 @@ LearnedNet learned_net(usx_ctx* ctx) {
     if (gf >> rv) net.refine = rv;
     if (gf >> gs) net.share_gate = std::strtof(gs.c_str(), nullptr);
     if (gf >> gs) net.level_gate = std::strtof(gs.c_str(), nullptr);
+    if (gf >> gs) net.level_lines = std::atoi(gs.c_str());
+    if (gf >> gs) net.level_depths = std::atoi(gs.c_str());
   }
   nets.emplace(ctx, net);
   return net;
@@ -199,6 +202,8 @@ class PlanCache {
         rt::check(usx_cu_bf_plan_set_learned_subspace(plan, 1, share), "learned minimum variance share gate");
         const float level = cfg.learned_level_gate >= 0.0f ? cfg.learned_level_gate : net.level_gate;
         rt::check(usx_cu_bf_plan_set_learned_level_gate(plan, level), "learned minimum variance level gate");
+        rt::check(usx_cu_bf_plan_set_learned_level_window(plan, net.level_lines, net.level_depths),
+                  "learned minimum variance level window");
       } catch (...) {
         usx_cu_bf_plan_destroy(plan);
         throw;

@@ -372,6 +372,12 @@ class Plan:
         check(lib().usx_cu_bf_plan_set_learned_level_gate(self._h, C.c_float(max_level_ratio)),
               "bf_plan_set_learned_level_gate")
 
+    def set_learned_level_window(self, half_lines: int = 0, half_depths: int = 0) -> None:
+        """The level gate's neighbourhood (+/- lines, +/- depths): a pixel goes to
+        the exact solver when any pixel of it is above its depth's level."""
+        check(lib().usx_cu_bf_plan_set_learned_level_window(self._h, int(half_lines), int(half_depths)),
+              "bf_plan_set_learned_level_window")
+
     def learned_stats(self):
         """(pixels gated to the exact solver, pixels beamformed) since the last call."""
         a, b = C.c_int64(), C.c_int64()

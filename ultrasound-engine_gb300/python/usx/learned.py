@@ -367,20 +367,27 @@ class Mode:
     share: float = math.inf
     use_net: bool = True
     level: float = math.inf
+    window: tuple = (0, 0)   # the level gate's neighbourhood: +/- lateral lines, +/- depths
 
     @property
     def label(self) -> str:
         if not self.use_net:
             return "beams_only"
         base = f"gate={self.gate:g},share={self.share:g}"
-        return base if math.isinf(self.level) else f"{base},level={self.level:g}"
+        if math.isinf(self.level):
+            return base
+        base = f"{base},level={self.level:g}"
+        return base if tuple(self.window) == (0, 0) else f"{base},win={self.window[0]}x{self.window[1]}"
 
 
-def modes_for(gates=(), shares=(), ablation: bool = True, levels=(), level_shares=(math.inf,)) -> list:
+def modes_for(gates=(), shares=(), ablation: bool = True, levels=(), level_shares=(math.inf,),
+              windows=((0, 0),)) -> list:
     """Modes of each single gate, and of every level gate combined with each of
-    `level_shares` (share gates)."""
+    `level_shares` (share gates) and each of `windows` (the level gate's
+    neighbourhood)."""
     out = [Mode(gate=float(g)) for g in gates] + [Mode(share=float(x)) for x in shares]
-    out += [Mode(share=float(x), level=float(v)) for v in levels for x in level_shares]
+    out += [Mode(share=float(x), level=float(v), window=tuple(w))
+            for v in levels for x in level_shares for w in windows]
     if ablation:
         out.append(Mode(use_net=False))
     seen, uniq = set(), []
@@ -407,6 +414,7 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, modes=(Mode(),), log=print,
             learned.set_learned(mlp, m.gate)
             learned.set_learned_subspace(m.use_net, m.share)
             learned.set_learned_level_gate(m.level)
+            learned.set_learned_level_window(*m.window)
             learned.learned_stats()
             lf = imager.beamform(COMB_LEARNED_MV)
             gated, pixels = learned.learned_stats()
@@ -418,6 +426,7 @@ def evaluate(imager: Imager, mlp: capi.Mlp, seeds, modes=(Mode(),), log=print,
                                                   / ref.abs().pow(2).sum().sqrt())})
         learned.set_learned_subspace(True, math.inf)
         learned.set_learned_level_gate(math.inf)
+        learned.set_learned_level_window(0, 0)
         if log:
             log(f"phantom {s}: " + ", ".join(
                 f"{m.label}: fallback {rows[m.label][-1]['fallback_rate']:.3f} dgcnr "
@@ -516,6 +525,8 @@ def main(argv=None) -> None:
                        help="gates on tr(R) over its depth's level, each alone and with every --level-shares")
         p.add_argument("--level-shares", default="inf,0.2",
                        help="share gates combined with each level gate")
+        p.add_argument("--windows", default="0x0",
+                       help="level-gate neighbourhoods, +/- lines x +/- depths, combined with each level gate")
         p.add_argument("--refine", type=int, default=DEFAULT_REFINE,
                        help="DFT beams beside the network's direction (-1: no refinement)")
         p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
@@ -524,7 +535,8 @@ def main(argv=None) -> None:
     modes = modes_for([float(g) for g in a.gates.split(",") if g],
                       [float(x) for x in a.shares.split(",") if x] if sub else [], ablation=sub,
                       levels=[float(v) for v in a.levels.split(",") if v] if sub else [],
-                      level_shares=[float(x) for x in a.level_shares.split(",") if x])
+                      level_shares=[float(x) for x in a.level_shares.split(",") if x],
+                      windows=[tuple(int(v) for v in w.split("x")) for w in a.windows.split(",") if w])
     imager = Imager()
     report = {"dims": list(DIMS), "setup": imager.setup.__dict__}
     eval_seeds = np.arange(900_000, 900_000 + (a.eval_phantoms if a.cmd == "train" else a.phantoms))
@@ -556,13 +568,15 @@ def main(argv=None) -> None:
     chosen, ok = choose_mode(results, modes)
     report.pop("share_gate", None)
     report.pop("level_gate", None)
+    report.pop("level_window", None)
     if chosen is not None:
-        report.update(gate=chosen.gate, share_gate=chosen.share, level_gate=chosen.level, chosen=chosen.label,
-                      meets_bar=ok)
+        report.update(gate=chosen.gate, share_gate=chosen.share, level_gate=chosen.level,
+                      level_window=list(chosen.window), chosen=chosen.label, meets_bar=ok)
     path = Path(a.report) if a.report else out.with_suffix(".json")
     path.write_text(json.dumps(report, indent=1, default=float))
     if chosen is not None:
-        out.with_suffix(".gate").write_text(f"{chosen.gate} {a.refine} {chosen.share} {chosen.level}\n")
+        out.with_suffix(".gate").write_text(
+            f"{chosen.gate} {a.refine} {chosen.share} {chosen.level} {chosen.window[0]} {chosen.window[1]}\n")
     print(json.dumps({"chosen": report.get("chosen"), "meets_bar": ok, "eval": report["eval"]}, default=float))
     imager.close()
 
@@ -595,6 +609,16 @@ def trained_level_gate(weights=DEFAULT_WEIGHTS) -> float:
         if g is not None:
             return float(g)
     return math.inf
+
+
+def trained_level_window(weights=DEFAULT_WEIGHTS) -> tuple:
+    """The level gate's neighbourhood chosen with the weights ((0, 0): the pixel itself)."""
+    p = Path(weights).with_suffix(".json")
+    if p.exists():
+        w = json.loads(p.read_text()).get("level_window")
+        if w is not None:
+            return int(w[0]), int(w[1])
+    return 0, 0
 
 
 def trained_refine(weights=DEFAULT_WEIGHTS) -> int:
