@@ -527,10 +527,16 @@ def main(argv=None) -> None:
                        help="share gates combined with each level gate")
         p.add_argument("--windows", default="0x0",
                        help="level-gate neighbourhoods, +/- lines x +/- depths, combined with each level gate")
-        p.add_argument("--refine", type=int, default=DEFAULT_REFINE,
-                       help="DFT beams beside the network's direction (-1: no refinement)")
+        p.add_argument("--refine", type=int, default=None,
+                       help="DFT beams beside the network's direction (-1: no refinement; default: "
+                            "the refinement recorded with the weights when evaluating, else 4)")
         p.add_argument("--report", default=None, help="JSON report (default: beside the weights)")
     a = ap.parse_args(argv)
+    if a.refine is None:
+        a.refine = DEFAULT_REFINE
+        if a.cmd == "evaluate" and Path(a.weights).with_suffix(".json").exists():
+            recorded = trained_refine(a.weights)
+            a.refine = recorded if recorded >= 0 else DEFAULT_REFINE
     sub = a.refine >= 0
     modes = modes_for([float(g) for g in a.gates.split(",") if g],
                       [float(x) for x in a.shares.split(",") if x] if sub else [], ablation=sub,
