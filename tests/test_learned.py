@@ -110,6 +110,28 @@ def test_weights_file_roundtrip(tmp_path):
         learned.load_weights(f)
 
 
+def test_mode_selection_respects_the_fallback_budget():
+    """The shipped setting is the lowest-fallback mode that meets the quality
+    bar within the fallback budget, else the mode closest to the bar within
+    it; the mode that meets the bar at any cost is recorded beside it."""
+    from usx import learned
+    M = learned.Mode
+
+    def res(fb, dg, lat, ax):
+        return {"fallback_rate": fb, "gcnr": {"max_abs_delta": dg},
+                "lateral_fwhm_mm": {"max_rel_delta": lat}, "axial_fwhm_mm": {"max_rel_delta": ax}}
+    modes = [M(), M(level=10.0), M(level=3.0, share=0.02), M(use_net=False)]
+    results = {modes[0].label: res(0.0, 0.008, 0.80, 0.018), modes[1].label: res(0.055, 0.008, 0.027, 0.018),
+               modes[2].label: res(0.70, 0.008, 0.0, 0.005), modes[3].label: res(0.0, 0.014, 0.09, 0.80)}
+    chosen, ok = learned.choose_mode(results, modes)
+    assert chosen == modes[1] and not ok            # the bar is met only beyond the budget
+    assert learned.at_bar_mode(results, modes) == modes[2]
+    chosen, ok = learned.choose_mode(results, modes, max_fallback=0.8)
+    assert chosen == modes[2] and ok
+    assert M(level=10.0, window=(1, 2)).label.endswith(",level=10,win=1x2")
+    assert M(level=10.0).label == "gate=inf,share=inf,level=10"
+
+
 def _golden_mv_case(golden, name="mv"):
     g = golden("bf")
     s = golden("sim")
