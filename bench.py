@@ -85,28 +85,82 @@ def workload_setup(n_scat: int = 100_000):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+    """SM clocks and clock-event (throttle) reasons sampled in the background
+    during the timed region: through NVML (read-only queries, every 20 ms)
+    where libnvidia-ml loads, else by running nvidia-smi every 200 ms."""
 
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    # NVML clock-event reason bits, in the order of the names in summary().
+    BITS = (0x8, 0x40, 0x20, 0x4)
 
     def __init__(self, device: int = 0):
         self.device = device
         self.rows = []
+        self.source = None
         self._stop = threading.Event()
         self._t = None
+        self._nvml = self._open_nvml()
+
+    def _open_nvml(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = ctypes.c_void_p()
+            # The CUDA device's own PCI address (NVML's indices need not follow
+            # CUDA_VISIBLE_DEVICES), else NVML's index.
+            bus = None
+            try:
+                import torch
+                p = torch.cuda.get_device_properties(self.device)
+                bus = "%04x:%02x:%02x.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+            except Exception:
+                bus = None
+            if bus is None or lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(h)) != 0:
+                if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.device), ctypes.byref(h)) != 0:
+                    return None
+            fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            return lib, h, fn
+        except (OSError, AttributeError):
+            return None
+
+    def _sample_nvml(self):
+        import ctypes
+        lib, h, reasons_fn = self._nvml
+        sm, mx, mw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        if lib.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) != 0:        # NVML_CLOCK_SM
+            return None
+        lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        lib.nvmlDeviceGetPowerUsage(h, ctypes.byref(mw))
+        reasons_fn(h, ctypes.byref(rs))
+        flags = ["Active" if rs.value & b else "Not Active" for b in self.BITS]
+        return [str(sm.value), str(mx.value), f"{mw.value / 1000:.1f}"] + flags
 
     def _run(self):
         while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.rows.append([v.strip() for v in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+            row = None
+            if self._nvml is not None:
+                try:
+                    row = self._sample_nvml()
+                    self.source = "nvml"
+                except Exception:
+                    row = None
+            if row is None:
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                    if out.returncode == 0 and out.stdout.strip():
+                        row = [v.strip() for v in out.stdout.strip().split(",")]
+                        self.source = "nvidia-smi"
+                except Exception:
+                    pass
+            if row is not None:
+                self.rows.append(row)
+            self._stop.wait(0.02 if self.source == "nvml" else 0.2)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
@@ -126,7 +180,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 3 + i and r[3 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(self.rows), "source": self.source}
 
 
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
