@@ -267,11 +267,11 @@ MV64 = dict(f_number=1.5, combiner=2, mv_subarray=64, mv_diagonal_loading=0.01, 
 
 def test_cfg2_minimum_variance_l64_on_full_lines(cfg2_run, capi, ctx, torch, orc):
     """Minimum variance at subarray 64, diagonal loading tr(R)/(100 L), range
-    averaging +/-2 on 16 full-depth lines of the 75-PW acquisition: the FP32
-    solver within 1e-4 and the BF16 tensor-core covariance with refinement
-    within 1e-3 of the oracle (the reference's combine_mv_windowed,
-    core/src/beamformer.cpp:137-214), with no failed refinement; the public
-    usx.Beamformer gives the tensor-core frame."""
+    averaging +/-2 on 16 full-depth lines of the 75-PW acquisition against the
+    oracle (the reference's combine_mv_windowed, core/src/beamformer.cpp:
+    137-214): the reference-order FP32 solver and the FP32 lag-recurrence
+    solver within 1e-4, the BF16 tensor-core covariances (tcgen05 and
+    mma.sync) with refinement within 1e-3, with no failed refinement."""
     r = cfg2_run
     s = r["s"]
     pts = np.asarray(s.grid.points, np.float32).reshape(512, 1024, 3)[CFG2_LINES].reshape(-1, 3)
