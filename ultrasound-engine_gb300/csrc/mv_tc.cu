@@ -601,8 +601,16 @@ __host__ __device__ inline MvWarpLayout mv_warp_layout(int nmax, int n_dmax, int
   l.off_yf = o;  o = align16(o + sizeof(float2) * n_dmax * nmax);
   l.off_yb = o;  o = recur ? o : align16(o + sizeof(uint32_t) * 4 * n_dmax * l.words);  // also t_k after the covariance
   l.off_r = o;   o = align16(o + sizeof(float2) * (lmax * (lmax + 1) / 2));
-  l.off_w = o;   o = align16(o + sizeof(float2) * 2 * lmax);
-  l.off_p = o;   o = align16(o + sizeof(float2) * 4 * lmax);   // the Cholesky's panel, transposed
+  if (recur && n_dmax * nmax >= 4 * lmax) {
+    // FP32: no refinement buffer, and the rows are dead once the covariance,
+    // the trace and the centre row's average are formed, so the Cholesky's
+    // panel takes their place.
+    l.off_w = o;
+    l.off_p = l.off_yf;
+  } else {
+    l.off_w = o;   o = recur ? o : align16(o + sizeof(float2) * 2 * lmax);  // refinement (BF16 only)
+    l.off_p = o;   o = align16(o + sizeof(float2) * 4 * lmax);   // the Cholesky's panel, transposed
+  }
   l.bytes = o;
   return l;
 }
@@ -983,6 +991,29 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     __syncwarp();
 
     // ---- Cholesky (blocked, rank-4 trailing updates) ---------------------
+    // The centre row's subarray average, before the Cholesky may reuse the
+    // rows' space (FP32 instance).
+    float avg_re[kSlots], avg_im[kSlots];
+    {
+      const float inv_nsub = 1.0f / static_cast<float>(n_sub);
+#pragma unroll
+      for (int s2 = 0; s2 < kSlots; ++s2) {
+        const int i = lane + 32 * s2;
+        float are = 0.f, aim = 0.f;
+        if (i < L) {
+          const float2* yr = yf + dc * nmax + i;
+          for (int s = 0; s < n_sub; ++s) {
+            are += yr[s].x;
+            aim += yr[s].y;
+          }
+          are *= inv_nsub;
+          aim *= inv_nsub;
+        }
+        avg_re[s2] = are;
+        avg_im[s2] = aim;
+      }
+    }
+    __syncwarp();
     const bool ok = chol_blocked<kSlots>(Rl, reinterpret_cast<float2*>(base + lay.off_p), L, lane);
     if (!ok) {
       export_invalid(a, row, lane);
@@ -1121,21 +1152,13 @@ __global__ void __launch_bounds__(32 * kWarpMvWarps) mv_warp_kernel(const MvWarp
     }  // refinement
     // out = n_act * sum conj(w_i) avg_i / sum w, avg from the centre row.
     float dre = 0.f, dim = 0.f, ore = 0.f, oim = 0.f;
-    const float inv_nsub = 1.0f / static_cast<float>(n_sub);
 #pragma unroll
     for (int s2 = 0; s2 < kSlots; ++s2) {
       const int i = lane + 32 * s2;
       if (i < L) {
         dre += w[s2].x;
         dim += w[s2].y;
-        float are = 0.f, aim = 0.f;
-        const float2* yr = yf + dc * nmax + i;
-        for (int s = 0; s < n_sub; ++s) {
-          are += yr[s].x;
-          aim += yr[s].y;
-        }
-        are *= inv_nsub;
-        aim *= inv_nsub;
+        const float are = avg_re[s2], aim = avg_im[s2];
         ore += w[s2].x * are + w[s2].y * aim;
         oim += w[s2].x * aim - w[s2].y * are;
       }
