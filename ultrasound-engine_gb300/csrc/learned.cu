@@ -138,36 +138,37 @@ __global__ void __launch_bounds__(32 * kLmvWarps, 5) lmv_features_kernel(const L
       continue;
     }
 
-    // Diagonal sums rho[m] for m = lane, lane + 32.
+    // Diagonal sums rho[m] for the lags m1 = lane and m2 = 63 - lane, in one
+    // loop of (n_act - m1) + (n_act - m2) steps: lag m has n_act - m terms, so
+    // when L > 32 every lane runs about the same count (as two loops the
+    // warp would run lane 0's n_act steps, then lane 31's n_act - 32).
     float rre[2] = {0.f, 0.f}, rim[2] = {0.f, 0.f};
-#pragma unroll
-    for (int s2 = 0; s2 < 2; ++s2) {
-      const int m = lane + 32 * s2;
-      if (m >= L) continue;
-      const int lm1 = L - m - 1;
-      // The trapezoid weight depends on t only: sum the range rows first.
-      float are = 0.f, aim = 0.f;
-      const float2* pp = rows + m;
-      if (kND > 0 && n_d == kND) {
-        // The full window with a compile-time row stride: immediate offsets.
-        for (int t = 0; t < n_act - m; ++t) {
-          const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
-          float sre = 0.f, sim = 0.f;
-#pragma unroll
-          for (int d = 0; d < kND; ++d) {
-            const float2 pv = pp[d * rs + t], q = rows[d * rs + t];
-            sre = fmaf(pv.x, q.x, fmaf(pv.y, q.y, sre));
-            sim = fmaf(pv.y, q.x, fmaf(-pv.x, q.y, sim));
+    {
+      const int m1 = lane, m2 = 63 - lane;
+      const int len1 = m1 < L ? n_act - m1 : 0;
+      const int len = len1 + (m2 < L ? n_act - m2 : 0);   // len1 == 0 implies len == 0
+      auto lags = [&](auto nd_c) {
+        // ND > 0: the full window with a compile-time row count (and, with
+        // kStride, immediate row offsets); 0: n_d rows at run time.
+        constexpr int ND = decltype(nd_c)::value;
+        const int nd = ND > 0 ? ND : n_d;
+        int m = m1, t = 0;
+        float are = 0.f, aim = 0.f;
+        for (int it = 0; it < len; ++it, ++t) {
+          if (it == len1) {   // on to the second lag
+            rre[0] = are;
+            rim[0] = aim;
+            are = 0.f;
+            aim = 0.f;
+            m = m2;
+            t = 0;
           }
-          are = fmaf(w, sre, are);
-          aim = fmaf(w, sim, aim);
-        }
-      } else {
-        for (int t = 0; t < n_act - m; ++t) {
-          const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - lm1) + 1);
+          // The trapezoid weight depends on t only: sum the range rows first.
+          const float w = static_cast<float>(min(t, n_sub - 1) - max(0, t - (L - m - 1)) + 1);
+          const float2* pp = rows + m;
           float sre = 0.f, sim = 0.f;
 #pragma unroll 5
-          for (int d = 0; d < n_d; ++d) {
+          for (int d = 0; d < nd; ++d) {
             const float2 pv = pp[d * rs + t], q = rows[d * rs + t];
             sre = fmaf(pv.x, q.x, fmaf(pv.y, q.y, sre));
             sim = fmaf(pv.y, q.x, fmaf(-pv.x, q.y, sim));
@@ -175,12 +176,30 @@ __global__ void __launch_bounds__(32 * kLmvWarps, 5) lmv_features_kernel(const L
           are = fmaf(w, sre, are);
           aim = fmaf(w, sim, aim);
         }
+        if (len > len1) {
+          rre[1] = are;
+          rim[1] = aim;
+        } else if (len > 0) {
+          rre[0] = are;
+          rim[0] = aim;
+        }
+      };
+      if (kND > 0 && n_d == kND)
+        lags(std::integral_constant<int, kND>{});
+      else
+        lags(std::integral_constant<int, 0>{});
+      if (m1 < L) {
+        rre[0] /= static_cast<float>(L - m1);
+        rim[0] /= static_cast<float>(L - m1);
       }
-      rre[s2] += are;
-      rim[s2] += aim;
-      rre[s2] /= static_cast<float>(L - m);
-      rim[s2] /= static_cast<float>(L - m);
+      if (m2 < L) {
+        rre[1] /= static_cast<float>(L - m2);
+        rim[1] /= static_cast<float>(L - m2);
+      }
     }
+    // Lag 32 + lane from lane 31 - lane, for the feature writes below.
+    rre[1] = __shfl_sync(0xffffffffu, rre[1], 31 - lane);
+    rim[1] = __shfl_sync(0xffffffffu, rim[1], 31 - lane);
     const float r0 = __shfl_sync(0xffffffffu, rre[0], 0);
     const float inv_r0 = r0 > 0.f ? 1.0f / r0 : 0.f;
 
