@@ -165,12 +165,13 @@ int usx_cu_bf_variant_order(int index, int* deep_first);
  * 32 / warp_lines depths, one warp per channel_group channels; the transmit
  * delay, phasor and illumination weight computed once per pixel and event),
  * 3 the staged windows in a ring of shared-memory stages filled by a producer
- * warp (bulk copies on mbarriers, no CTA-wide barrier in the loop), 4 the
- * minimum-variance export with channel warps beside the pixel warps and the
- * transmit terms tabulated per pixel and event.
+ * warp (bulk copies on mbarriers, no CTA-wide barrier in the loop), 4
+ * channel warps beside the pixel warps with the transmit terms tabulated per
+ * pixel and event (the minimum-variance export, and the sums with the
+ * channel combine in shared memory, in ascending channel order).
  * Families 1-4 fall back to variant 0 where they do not apply (RF data,
  * incoherent compounding; families 1 and 3 also need plane waves, family 2
- * at most 256 channels, family 4 serves export launches only). */
+ * at most 256 channels). */
 int usx_cu_bf_variant_kind(int index, int* kind);
 int usx_cu_bf_plan_set_variant(usx_bf_plan* plan, int index);
 int usx_cu_bf_plan_get_variant(const usx_bf_plan* plan, int* index);

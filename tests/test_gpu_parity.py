@@ -266,8 +266,10 @@ def test_beamform_geometries_match_reference(capi, ctx, torch, golden):
 @pytest.mark.parametrize("cfg_kw", [dict(f_number=1.5), dict(f_number=1.5, combiner=1),
                                     dict(f_number=1.5, coherence_factor=1), dict(f_number=1.5, compounding=2)])
 def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_kw):
-    """Every delay-and-sum launch shape gives the same frame bit for bit; the
-    autotuner keeps one of them and leaves its frame in the output."""
+    """Every delay-and-sum launch shape gives the same frame bit for bit
+    (the channel-warp kernels combine the channels in shared memory in the
+    same order); the autotuner keeps one of them and leaves its frame in the
+    output."""
     g = golden("bf")
     s = golden("sim")
     pr, med, acq = sim_setup(s)
@@ -281,6 +283,7 @@ def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_k
     assert len(variants) >= 2 and variants[0] == (8, 4, 8, 1, 0, 0)
     assert any(v[4] == 1 for v in variants)  # deepest-tiles-first orders are candidates
     assert any(v[5] == 2 for v in variants)  # transmit-table kernels are candidates
+    assert any(v[5] == 4 for v in variants)  # channel-warp kernels are candidates
     for v in range(len(variants)):
         plan.set_variant(v)
         plan.execute(d.data_ptr(), out.data_ptr())
@@ -299,7 +302,7 @@ def test_das_variants_bit_identical_and_autotune(capi, ctx, torch, golden, cfg_k
 
 def test_mv_export_variants_bit_identical(capi, ctx, torch, golden):
     """Minimum variance through every delay-and-sum shape, including the
-    export-only tabulated kernels: the exported channel samples are the same
+    channel-warp tabulated kernels: the exported channel samples are the same
     bit for bit, so the FP32 minimum-variance frames are identical; on a ragged
     grid too."""
     g = golden("bf")
@@ -310,7 +313,7 @@ def test_mv_export_variants_bit_identical(capi, ctx, torch, golden):
     pts = np.asarray(g["pts"], dtype=np.float32).reshape(len(ax0), len(ax1), 3)
     d = dev(torch, g["iq"])
     variants = capi.das_variants()
-    assert any(v[5] == 4 for v in variants)  # export-only shapes are candidates
+    assert any(v[5] == 4 for v in variants)  # channel-warp shapes are candidates
     grids = (capi.Grid(0, ax0, ax1, pts.reshape(-1, 3)), capi.Grid(0, ax0[:13], ax1[:37], pts[:13, :37].reshape(-1, 3)))
     for gi, grid in enumerate(grids):
         plan = ctx.plan(ch, grid, capi.bf_config(**BF_CASES["mv"]))

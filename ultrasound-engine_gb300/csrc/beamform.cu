@@ -461,7 +461,16 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 // kG channels over the chunk. The transmit side is evaluated once per pixel,
 // event and pass instead of once per channel group; the per-channel sums are
 // das_fast_kernel's expressions in the same order, so the exported samples
-// are the same bit for bit. Export launches only (no channel combine).
+// are the same bit for bit.
+// das_csum_kernel is the same body for the plain sums (delay-and-sum, DMAS,
+// coherence factor): after each pass the channel warps stage their channel
+// values in the table's shared memory and channel warp 0's thread of each
+// pixel combines the pass's channels in ascending order, exactly as
+// das_fast_kernel's channel loop, so its frames are the same bit for bit;
+// the combine state lives in shared memory between passes. At 128 channels,
+// 75 plane waves, 512 x 1024: 4.20 ms per frame against 4.97 for
+// das_fast_kernel's best shape (three CTAs per SM; two, at 64 registers,
+// measured 5.6).
 // Measured on the learned frame (128 ch, 75 plane waves, 512 x 1024): export
 // 4.83 ms with (kG, kPW, kCQ, kWL) = (4, 4, 4, 4) against 5.08 for
 // das_fast_kernel's best shape; (8, 4, 4, 4) 5.1, (8, 4, 4, 1) 5.6,
@@ -470,10 +479,19 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 // deepest tiles first: 4.38 -> 4.13 ms.
 constexpr int kExpEv = 16;
 
-template <int kG, int kPW, int kCQ, int kWL>
-__global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs a) {
+template <int kG, int kPW, int kCQ, int kWL, bool kSum>
+__device__ __forceinline__ void das_export_body(const BfArgs& a) {
   static_assert(32 % kWL == 0 && kPW % kWL == 0, "warp shape must tile the CTA");
+  static_assert(sizeof(float2) * kCQ * kG <= sizeof(float4) * kExpEv, "a pass's channel values fit the table");
   __shared__ float4 tab[kExpEv][32 * kPW];
+  // kSum: a pass's channel values [channel of the pass][pixel slot] in the
+  // table's space once the pass's events are done, and each channel warp's
+  // aperture mask per pixel.
+  __shared__ unsigned act_s[kSum ? kCQ : 1][32 * kPW];
+  // kSum: each pixel's combine state (das, s, q, coh, incs, n_active), kept
+  // in shared memory rather than in registers through the event loops.
+  __shared__ float cs[kSum ? 10 : 1][32 * kPW];
+  float2* ys = reinterpret_cast<float2*>(&tab[0][0]);
   constexpr int kWD = 32 / kWL;
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
@@ -516,6 +534,11 @@ __global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs
   const unsigned n_last = static_cast<unsigned>(a.n_smp - 1);
   const int n_groups = (a.n_ch + kG - 1) / kG;
   const int n_pass = (n_groups + kCQ - 1) / kCQ;
+  // kSum: the channel combine of das_fast_tile, run by channel warp 0's
+  // thread of each pixel over the channels in ascending order.
+  if (kSum && cq == 0)
+#pragma unroll
+    for (int i = 0; i < 10; ++i) cs[i][pl] = 0.0f;
   for (int pass = 0; pass < n_pass; ++pass) {
     const int grp = pass * kCQ + cq;
     const int g = grp * kG;
@@ -588,6 +611,65 @@ __global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs
         }
       }
     }
+    if (kSum) {
+      __syncthreads();   // the table is read for the last time
+#pragma unroll
+      for (int k = 0; k < kG; ++k) {
+        const int ch = g + k;
+        float2 y = make_float2(0.f, 0.f);
+        if ((mask >> k) & 1u) {
+          const float ap = aperture_weight(elem_x(a, ch), px, pz, a.f_number, a.rx_window, a.tukey_alpha);
+          float rc = 1.0f, rs = 0.0f;
+          if (a.fdem > 0.0f) sincosf(a.two_pi_f * rt[k], &rs, &rc);
+          const float gr = ap * rc, gi = ap * rs;
+          y = make_float2(fmaf(gr, ar[k], -gi * ai[k]), fmaf(gr, ai[k], gi * ar[k]));
+        }
+        ys[(cq * kG + k) * (32 * kPW) + pl] = y;
+      }
+      act_s[cq][pl] = mask;
+      __syncthreads();
+      // (The next pass's __syncthreads_or keeps the table's writers out of
+      // these values until the combine is done.)
+      if (cq == 0 && valid) {
+        cplx das = mk(cs[0][pl], cs[1][pl]), s = mk(cs[2][pl], cs[3][pl]), q = mk(cs[4][pl], cs[5][pl]),
+             coh = mk(cs[6][pl], cs[7][pl]);
+        float incs = cs[8][pl];
+        int n_active = __float_as_int(cs[9][pl]);
+        for (int c = 0; c < kCQ * kG; ++c) {
+          const int ch = pass * kCQ * kG + c;
+          if (ch >= a.n_ch) break;
+          const bool act = (act_s[c / kG][pl] >> (c % kG)) & 1u;
+          const float2 yv = ys[c * (32 * kPW) + pl];
+          const cplx y = mk(yv.x, yv.y);
+          n_active += act ? 1 : 0;
+          if (a.combiner == USX_COMB_DMAS) {
+            const float m = cabsf_(y);
+            if (m > 0.0f) {
+              const cplx v = cdivr(y, sqrtf(m));
+              s = cadd(s, v);
+              q = cadd(q, cmul(v, v));
+            }
+          } else {
+            das = cadd(das, y);
+          }
+          if (a.cf && act) {
+            coh = cadd(coh, y);
+            incs += cnorm(y);
+          }
+        }
+        cs[0][pl] = das.re;
+        cs[1][pl] = das.im;
+        cs[2][pl] = s.re;
+        cs[3][pl] = s.im;
+        cs[4][pl] = q.re;
+        cs[5][pl] = q.im;
+        cs[6][pl] = coh.re;
+        cs[7][pl] = coh.im;
+        cs[8][pl] = incs;
+        cs[9][pl] = __int_as_float(n_active);
+      }
+      continue;
+    }
     if (!valid) continue;
 #pragma unroll
     for (int k = 0; k < kG; ++k) {
@@ -604,6 +686,35 @@ __global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs
       a.y_out[(frame * a.n_pix + pix) * a.n_ch + ch] = y;
     }
   }
+  if (kSum && cq == 0 && valid) {
+    const cplx das = mk(cs[0][pl], cs[1][pl]), s = mk(cs[2][pl], cs[3][pl]), q = mk(cs[4][pl], cs[5][pl]),
+               coh = mk(cs[6][pl], cs[7][pl]);
+    const float incs = cs[8][pl];
+    const int n_active = __float_as_int(cs[9][pl]);
+    cplx out;
+    if (n_active == 0) {
+      out = mk(0.f, 0.f);
+    } else if (a.combiner == USX_COMB_DMAS) {
+      const cplx acc = cscale(csub(cmul(s, s), q), 0.5f);
+      out = cdivr(acc, 0.5f * fmaxf(1.0f, static_cast<float>(n_active - 1)));
+    } else {
+      out = das;
+    }
+    if (a.cf && n_active > 0)
+      out = cscale(out, (incs > 0.0f) ? cnorm(coh) / (static_cast<float>(n_active) * incs) : 0.0f);
+    a.out[frame * a.out_stride + pix] = make_float2(out.re, out.im);
+  }
+}
+
+template <int kG, int kPW, int kCQ, int kWL>
+__global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs a) {
+  das_export_body<kG, kPW, kCQ, kWL, false>(a);
+}
+// The channel-combining instance (delay-and-sum, DMAS, coherence factor):
+// three CTAs per SM, as the export's fastest shape runs.
+template <int kG, int kPW, int kCQ, int kWL>
+__global__ void __launch_bounds__(32 * kPW * kCQ, 3) das_csum_kernel(const BfArgs a) {
+  das_export_body<kG, kPW, kCQ, kWL, true>(a);
 }
 
 // ------------------------------------------------------------------------
@@ -1526,7 +1637,8 @@ struct DasVariant {
   bool staged;   // das_staged_kernel (plane waves, IQ, 16-byte aligned data); else variant 0
   bool table;    // das_table_kernel (IQ, coherent or select, n_ch <= 256); else variant 0
   int producer_warps = 0;   // das_ring_kernel: one warp beside the tile's warps
-  int channel_warps = 1;    // das_export_kernel: warps per pixel warp (export launches only; else variant 0)
+  int channel_warps = 1;    // das_export_kernel: warps per pixel warp (IQ: MV exports, coherent sums; else variant 0)
+  void (*sum)(BfArgs) = nullptr;   // das_csum_kernel, the channel-combining instance (plain IQ launches)
 };
 // RF input (the reference's interp_rf path) keeps the default shape in
 // every variant.
@@ -1545,11 +1657,13 @@ template <int G, int TL, int E>
 constexpr DasVariant das_staged_variant() {
   return DasVariant{G, TL, 0, 1, false, das_staged_kernel<G, TL, E>, das_fast_kernel<false, 16, 4, 1>, true, false};
 }
-// The tabulated export (minimum-variance export launches; others use variant 0).
+// The channel-warp kernel: minimum-variance exports, and coherent or select
+// IQ delay-and-sum, DMAS and coherence factor with the channel combine in
+// shared memory; RF and incoherent launches use variant 0.
 template <int G, int PW, int CQ, int WL>
 constexpr DasVariant das_export_variant() {
-  return DasVariant{G, PW, 0, WL, false, das_export_kernel<G, PW, CQ, WL>, das_fast_kernel<false, 16, 4, 1>, false,
-                    false, 0, CQ};
+  return DasVariant{G, PW, 0, WL, false, das_export_kernel<G, PW, CQ, WL>, das_fast_kernel<false, 16, 4, 1>,
+                    false, false, 0, CQ, das_csum_kernel<G, PW, CQ, WL>};
 }
 // The producer-warp ring (same applicability as the staged kernel).
 template <int G, int TL, int S>
@@ -1944,9 +2058,15 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
   if (table)
     if (int rc_ = smem_limit(reinterpret_cast<const void*>(dv.iq), table_smem)) return rc_;
   auto launch_das = [&](const BfArgs& b, const char* name) -> int {
-    prof_begin(ctx, name);
-    if (fast && dv.channel_warps > 1 && !(b.is_mv && plan->cd.is_iq)) {
-      // An export-only shape on a launch that is not an export: variant 0.
+    const bool csum = fast && dv.channel_warps > 1 && !b.is_mv && plan->cd.is_iq &&
+                      !(b.compounding == USX_COMP_INCOHERENT && b.pass < 0);
+    const bool cexport = fast && dv.channel_warps > 1 && b.is_mv && plan->cd.is_iq;
+    // The profiling label names the kernel that runs.
+    prof_begin(ctx, csum ? "das_csum_kernel" : cexport ? "das_export_kernel(mv export)" : name);
+    if (csum) {
+      dv.sum<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, 0, ctx->stream>>>(b);
+    } else if (fast && dv.channel_warps > 1 && !(b.is_mv && plan->cd.is_iq)) {
+      // A channel-warp shape on an RF or incoherent launch: variant 0.
       const DasVariant& d0 = kDasVariants[0];
       const dim3 g0(ceil_div(plan->n0, d0.tile_lines) * ceil_div(plan->n1, 32), grid_das.y);
       if (plan->cd.is_iq)
