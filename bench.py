@@ -1408,8 +1408,8 @@ def run_queue(args) -> None:
     line = _stage_line("mixed-probe frames/s in one persistent launch (4 x 128-el 75-PW 512x1024 + 4 x 64-el "
                        "31-DW sector 256x1024, DAS)", "frames/s", 8 * args.steps / (ms / 1e3), args, ms, prof,
                        clocks, {"workload": "queue_4x_linear_512x1024_4x_sector_256x1024", "frames_per_step": 8,
-                                "launch": "one das_queue_kernel per step"},
-                       {"kernel": "das_queue_kernel", "bound": None, "achieved": None, "peak": None, "unit": None,
+                                "launch": "one das_csum_queue_kernel per step (IQ)"},
+                       {"kernel": "das_csum_queue_kernel", "bound": None, "achieved": None, "peak": None, "unit": None,
                         "frac": None, "traffic": None},
                        {"one_launch_per_frame": {"value": 8 * args.steps / (sep_ms / 1e3), "unit": "frames/s",
                                                  "ms_per_step": sep_ms / args.steps},

@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 constexpr int kExpEv = 16;
 
 template <int kG, int kPW, int kCQ, int kWL, bool kSum>
-__device__ __forceinline__ void das_export_body(const BfArgs& a) {
+__device__ __forceinline__ void das_export_body(const BfArgs& a, int tile, long frame) {
   static_assert(32 % kWL == 0 && kPW % kWL == 0, "warp shape must tile the CTA");
   static_assert(sizeof(float2) * kCQ * kG <= sizeof(float4) * kExpEv, "a pass's channel values fit the table");
   __shared__ float4 tab[kExpEv][32 * kPW];
@@ -495,7 +495,6 @@ __device__ __forceinline__ void das_export_body(const BfArgs& a) {
   constexpr int kWD = 32 / kWL;
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
-  const int tile = blockIdx.x;
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
   const int pw = w % kPW, cq = w / kPW;
   const int pl = pw * 32 + ln;   // pixel slot in the tile
@@ -507,7 +506,6 @@ __device__ __forceinline__ void das_export_body(const BfArgs& a) {
   const int depth = depth_tile * 32 + (pw % kWL) * kWD + ln % kWD;
   const bool valid = line < n0 && depth < a.n1;
   const int pix = valid ? line * a.n1 + depth : 0;
-  const long frame = blockIdx.y;
   const float px = __ldg(a.points + 3 * pix), py = __ldg(a.points + 3 * pix + 1), pz = __ldg(a.points + 3 * pix + 2);
   int ev_lo = a.ev_begin, ev_hi = a.ev_end;
   if (a.seq_epf > 0) {
@@ -708,13 +706,13 @@ __device__ __forceinline__ void das_export_body(const BfArgs& a) {
 
 template <int kG, int kPW, int kCQ, int kWL>
 __global__ void __launch_bounds__(32 * kPW * kCQ) das_export_kernel(const BfArgs a) {
-  das_export_body<kG, kPW, kCQ, kWL, false>(a);
+  das_export_body<kG, kPW, kCQ, kWL, false>(a, blockIdx.x, blockIdx.y);
 }
 // The channel-combining instance (delay-and-sum, DMAS, coherence factor):
 // three CTAs per SM, as the export's fastest shape runs.
 template <int kG, int kPW, int kCQ, int kWL>
 __global__ void __launch_bounds__(32 * kPW * kCQ, 3) das_csum_kernel(const BfArgs a) {
-  das_export_body<kG, kPW, kCQ, kWL, true>(a);
+  das_export_body<kG, kPW, kCQ, kWL, true>(a, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------------------
@@ -751,6 +749,25 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_queue_kernel(const 
     const int local = item - q.first[e];
     const int frame = local / q.tiles[e], tile = local - frame * q.tiles[e];
     das_fast_tile<IQ, kFastGroup, kTileLines, kRtShared, kWarpLines, kDeepFirst>(q.args[e], tile, frame, rt_s);
+  }
+}
+
+// The same queue over das_csum_kernel's body (IQ plans): CTAs of 4 pixel
+// warps x 4 channel warps on the same 4-line x 32-depth tiles.
+__global__ void __launch_bounds__(512, 3) das_csum_queue_kernel(const DasQueueArgs q) {
+  __shared__ int s_item;
+  const int total = q.first[q.n];
+  for (;;) {
+    if (threadIdx.x == 0) s_item = static_cast<int>(atomicAdd(q.next, 1u));
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= total) break;
+    int e = 0;
+    while (e + 1 < q.n && item >= q.first[e + 1]) ++e;
+    const int local = item - q.first[e];
+    const int frame = local / q.tiles[e], tile = local - frame * q.tiles[e];
+    das_export_body<4, 4, 4, 4, true>(q.args[e], tile, frame);
   }
 }
 
@@ -2638,18 +2655,20 @@ int usx_cu_bf_execute_queue(usx_ctx* ctx, int n, usx_bf_plan* const* plans, cons
     if (q.n == 0) continue;
     q.next = next;
     USX_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), ctx->stream));
-    // IQ: the 4-channel, 4-line, 12-CTA shape with 4-line warps and the
-    // deepest tiles first (the autotuner's usual choice); RF: the RF shape.
-    const void* kern = iq ? reinterpret_cast<const void*>(das_queue_kernel<true, 4, 4, 12, false, 4, true>)
+    // IQ: das_csum_kernel's body (4 pixel warps x 4 channel warps, the
+    // transmit table, the in-order channel combine; the autotuner's usual
+    // choice); RF: das_fast_kernel's RF shape.
+    const void* kern = iq ? reinterpret_cast<const void*>(das_csum_queue_kernel)
                           : reinterpret_cast<const void*>(das_queue_kernel<false, 16, 4, 1>);
+    const int threads = iq ? 512 : 32 * 4;
     int per_sm = 0;
-    if (int rc = occupancy(kern, 32 * 4, 0, &per_sm)) return rc;
+    if (int rc = occupancy(kern, threads, 0, &per_sm)) return rc;
     const unsigned grid = static_cast<unsigned>(std::max(1, per_sm) * ctx->sm_count);
-    prof_begin(ctx, "das_queue_kernel");
+    prof_begin(ctx, iq ? "das_csum_queue_kernel" : "das_queue_kernel");
     if (iq)
-      das_queue_kernel<true, 4, 4, 12, false, 4, true><<<grid, 32 * 4, 0, ctx->stream>>>(q);
+      das_csum_queue_kernel<<<grid, threads, 0, ctx->stream>>>(q);
     else
-      das_queue_kernel<false, 16, 4, 1><<<grid, 32 * 4, 0, ctx->stream>>>(q);
+      das_queue_kernel<false, 16, 4, 1><<<grid, threads, 0, ctx->stream>>>(q);
     prof_end(ctx);
     USX_CHECK_LAUNCH("das_queue_kernel");
   }
