@@ -477,14 +477,21 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 // das_fast_kernel's best shape; (8, 4, 4, 4) 5.1, (8, 4, 4, 1) 5.6,
 // (8, 4, 2, 4) 5.3. The gathers' latency, not the transmit terms, bounds it.
 // Skipping the passes outside every pixel's aperture: 4.83 -> 4.38 ms; the
-// deepest tiles first: 4.38 -> 4.13 ms.
-constexpr int kExpEv = 16;
+// deepest tiles first: 4.38 -> 4.13 ms; chunks of 32 events instead of 16
+// (half the table barriers, the table in 64 KB of dynamic shared memory):
+// 4.13 -> 4.10 ms, and 4.21 -> 4.18 ms for das_csum_kernel.
+constexpr int kExpEv = 32;
+// Dynamic shared memory of the channel-warp kernels (the transmit table).
+__host__ __device__ constexpr size_t exp_table_bytes(int pixel_warps) {
+  return sizeof(float4) * kExpEv * 32 * pixel_warps;
+}
 
 template <int kG, int kPW, int kCQ, int kWL, bool kSum>
 __device__ __forceinline__ void das_export_body(const BfArgs& a, int tile, long frame) {
   static_assert(32 % kWL == 0 && kPW % kWL == 0, "warp shape must tile the CTA");
   static_assert(sizeof(float2) * kCQ * kG <= sizeof(float4) * kExpEv, "a pass's channel values fit the table");
-  __shared__ float4 tab[kExpEv][32 * kPW];
+  extern __shared__ float4 das_exp_smem[];
+  float4 (*tab)[32 * kPW] = reinterpret_cast<float4 (*)[32 * kPW]>(das_exp_smem);   // [kExpEv][pixel slot]
   // kSum: a pass's channel values [channel of the pass][pixel slot] in the
   // table's space once the pass's events are done, and each channel warp's
   // aperture mask per pixel.
@@ -492,7 +499,7 @@ __device__ __forceinline__ void das_export_body(const BfArgs& a, int tile, long 
   // kSum: each pixel's combine state (das, s, q, coh, incs, n_active), kept
   // in shared memory rather than in registers through the event loops.
   __shared__ float cs[kSum ? 10 : 1][32 * kPW];
-  float2* ys = reinterpret_cast<float2*>(&tab[0][0]);
+  float2* ys = reinterpret_cast<float2*>(das_exp_smem);
   constexpr int kWD = 32 / kWL;
   const int n0 = a.n_pix / a.n1;
   const int tiles_depth = (a.n1 + 31) / 32;
@@ -2082,7 +2089,9 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
     // The profiling label names the kernel that runs.
     prof_begin(ctx, csum ? "das_csum_kernel" : cexport ? "das_export_kernel(mv export)" : name);
     if (csum) {
-      dv.sum<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, 0, ctx->stream>>>(b);
+      const size_t tb = exp_table_bytes(dv.tile_lines);
+      if (int rc_ = smem_limit(reinterpret_cast<const void*>(dv.sum), tb)) return rc_;
+      dv.sum<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, tb, ctx->stream>>>(b);
     } else if (fast && dv.channel_warps > 1 && !(b.is_mv && plan->cd.is_iq)) {
       // A channel-warp shape on an RF or incoherent launch: variant 0.
       const DasVariant& d0 = kDasVariants[0];
@@ -2092,7 +2101,9 @@ int bf_execute(usx_bf_plan* plan, int n_frames, const void* data, int64_t data_s
       else
         d0.rf<<<g0, 32 * d0.tile_lines, 0, ctx->stream>>>(b);
     } else if (fast && dv.channel_warps > 1) {
-      dv.iq<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, 0, ctx->stream>>>(b);
+      const size_t tb = exp_table_bytes(dv.tile_lines);
+      if (int rc_ = smem_limit(reinterpret_cast<const void*>(dv.iq), tb)) return rc_;
+      dv.iq<<<grid_das, 32 * dv.tile_lines * dv.channel_warps, tb, ctx->stream>>>(b);
     } else if (table) {
       dv.iq<<<grid_das, 32 * table_warps(dv.group, b.n_ch), table_smem, ctx->stream>>>(b);
     } else if (fast) {
@@ -2662,12 +2673,15 @@ int usx_cu_bf_execute_queue(usx_ctx* ctx, int n, usx_bf_plan* const* plans, cons
     const void* kern = iq ? reinterpret_cast<const void*>(das_csum_queue_kernel)
                           : reinterpret_cast<const void*>(das_queue_kernel<false, 16, 4, 1>);
     const int threads = iq ? 512 : 32 * 4;
+    const size_t tb = iq ? exp_table_bytes(4) : 0;
+    if (iq)
+      if (int rc = smem_limit(kern, tb)) return rc;
     int per_sm = 0;
-    if (int rc = occupancy(kern, threads, 0, &per_sm)) return rc;
+    if (int rc = occupancy(kern, threads, tb, &per_sm)) return rc;
     const unsigned grid = static_cast<unsigned>(std::max(1, per_sm) * ctx->sm_count);
     prof_begin(ctx, iq ? "das_csum_queue_kernel" : "das_queue_kernel");
     if (iq)
-      das_csum_queue_kernel<<<grid, threads, 0, ctx->stream>>>(q);
+      das_csum_queue_kernel<<<grid, threads, tb, ctx->stream>>>(q);
     else
       das_queue_kernel<false, 16, 4, 1><<<grid, threads, 0, ctx->stream>>>(q);
     prof_end(ctx);
