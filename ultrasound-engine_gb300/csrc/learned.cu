@@ -636,9 +636,9 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
       }
 
       // The beams' prefix sums P_b[t + 1] = sum_{t' <= t} tw_b[t'] y[t']: lane
-      // l sums its run of C samples t = C l .. C l + C - 1 (C = 2 when the
-      // aperture fits 64 channels, else 4; the row is zero past n_act), then
-      // a warp scan of the run totals, beam by beam.
+      // l sums its run of C samples t = C l .. C l + C - 1 (C = 1, 2 or 4 for
+      // apertures of at most 32, 64 or 128 channels; the row is zero past
+      // n_act), then a warp scan of the run totals, beam by beam.
       auto scan_row = [&](auto run_len) {
         constexpr int C = decltype(run_len)::value;
         float2 yv[C], t1v[C];
@@ -670,7 +670,9 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
           for (int c = 0; c < C; ++c) sm.pre[k][skw(C * lane + c + 1)] = make_float2(ex.x + loc[c].x, ex.y + loc[c].y);
         }
       };
-      if (n_act <= 64)
+      if (n_act <= 32)
+        scan_row(std::integral_constant<int, 1>{});
+      else if (n_act <= 64)
         scan_row(std::integral_constant<int, 2>{});
       else
         scan_row(std::integral_constant<int, 4>{});
@@ -777,7 +779,12 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
 
     // G, reduced across the warp by a reduce-scatter: after five halvings each
     // lane holds kPad / 32 finished entries, written straight to the record.
+    // The projections of the subarray average and of 1 onto the basis ride
+    // in the padding of the same reduce-scatter (the record keeps them right
+    // after G).
     constexpr int kPad = (kG + 31) / 32 * 32;
+    constexpr int kRed = kG + 2 * K1 + 2;
+    static_assert(kRed <= kPad, "the projections fit the reduce-scatter's padding");
     float v[kPad];
     {
       // The beams' 1 / sqrt(L) per factor; entries of beams past nb are
@@ -792,7 +799,33 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
           v[e + 1] = g[e + 1] * f;
         }
 #pragma unroll
-      for (int e2 = kG; e2 < kPad; ++e2) v[e2] = 0.f;
+      for (int k = 0; k < K1; ++k) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int i = 2 * lane + h;
+          const float mi = i < L ? 1.f : 0.f;   // the average is defined for i < L
+          const float ax = (h ? av4.z : av4.x) * mi, ay = (h ? av4.w : av4.y) * mi;
+          float2 q;   // basis vector k at i (beams past nb are unused by stage 2)
+          if (k < NB) {
+            const float2 t = beam_twiddle(sm.tw1[i], k);
+            q = make_float2(t.x * rs, -t.y * rs);
+          } else {
+            q = wv[h];
+          }
+          acc.x += q.x * ax + q.y * ay;   // conj(q) abar
+          acc.y += q.x * ay - q.y * ax;
+        }
+        v[kG + 2 * k] = acc.x;
+        v[kG + 2 * k + 1] = acc.y;
+      }
+      float2 bw = make_float2(0.f, 0.f);   // w_q^H 1
+      if (2 * lane < L) bw = make_float2(wv[0].x, -wv[0].y);
+      if (2 * lane + 1 < L) bw = make_float2(bw.x + wv[1].x, bw.y - wv[1].y);
+      v[kG + 2 * K1] = bw.x;
+      v[kG + 2 * K1 + 1] = bw.y;
+#pragma unroll
+      for (int e2 = kRed; e2 < kPad; ++e2) v[e2] = 0.f;
     }
     int base = 0;
 #pragma unroll
@@ -811,52 +844,9 @@ __global__ void __launch_bounds__(32 * kSubWarps, 3) lmv_subspace_gram_kernel(co
     }
 #pragma unroll
     for (int i = 0; i < kPad / 32; ++i)
-      if (base + i < kG) rec[base + i] = v[i];
-    // Projections of the subarray average and of 1 onto the basis, reduced
-    // together.
-    float2 ak[K1];
-#pragma unroll
-    for (int k = 0; k < K1; ++k) {
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int i = 2 * lane + h;
-        const float mi = i < L ? 1.f : 0.f;   // the average is defined for i < L
-        const float ax = (h ? av4.z : av4.x) * mi, ay = (h ? av4.w : av4.y) * mi;
-        float2 q;   // basis vector k at i (beams past nb are unused by stage 2)
-        if (k < NB) {
-          const float2 t = beam_twiddle(sm.tw1[i], k);
-          q = make_float2(t.x * rs, -t.y * rs);
-        } else {
-          q = wv[h];
-        }
-        acc.x += q.x * ax + q.y * ay;   // conj(q) abar
-        acc.y += q.x * ay - q.y * ax;
-      }
-      ak[k] = acc;
-    }
-    float2 bw = make_float2(0.f, 0.f);
-    if (2 * lane < L) bw = make_float2(wv[0].x, -wv[0].y);
-    if (2 * lane + 1 < L) bw = make_float2(bw.x + wv[1].x, bw.y - wv[1].y);
-#pragma unroll
-    for (int o2 = 16; o2 > 0; o2 >>= 1) {
-#pragma unroll
-      for (int k = 0; k < K1; ++k) {
-        ak[k].x += __shfl_xor_sync(0xffffffffu, ak[k].x, o2);
-        ak[k].y += __shfl_xor_sync(0xffffffffu, ak[k].y, o2);
-      }
-      bw.x += __shfl_xor_sync(0xffffffffu, bw.x, o2);   // w_q^H 1
-      bw.y += __shfl_xor_sync(0xffffffffu, bw.y, o2);
-    }
+      if (base + i < kRed) rec[base + i] = v[i];
     if (lane == 0) {
       float* tail = rec + kG;
-#pragma unroll
-      for (int k = 0; k < K1; ++k) {
-        tail[2 * k] = ak[k].x;
-        tail[2 * k + 1] = ak[k].y;
-      }
-      tail[2 * K1 + 0] = bw.x;
-      tail[2 * K1 + 1] = bw.y;
       tail[2 * K1 + 2] = fmaxf(a.loading * (tr / K) * inv_l, 1e-20f);   // eps
       tail[2 * K1 + 3] = K;
       tail[2 * K1 + 4] = static_cast<float>(nb);
