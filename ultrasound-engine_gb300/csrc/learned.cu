@@ -57,7 +57,8 @@ struct LmvArgs {
 // (n_ch <= 128: 128), else 0 (n_ch); kND: the full smoothing window's row
 // count that gets an unrolled lag loop (5 for range averaging 2), else 0.
 // Five CTAs per SM (48 registers) measured faster than the four that 59
-// registers allow.
+// registers allow. Staging the rows with the range rows in an inner loop
+// (no integer division in the index) measured the same (2.60 ms per frame).
 template <int kStride, int kND>
 __global__ void __launch_bounds__(32 * kLmvWarps, 5) lmv_features_kernel(const LmvArgs a) {
   extern __shared__ float2 lmv_smem[];
