@@ -471,7 +471,8 @@ __global__ void __launch_bounds__(32 * kTileLines, MINB) das_fast_kernel(const B
 // 75 plane waves, 512 x 1024: 4.20 ms per frame against 4.97 for
 // das_fast_kernel's best shape (three CTAs per SM; two, at 64 registers,
 // measured 5.6). Warps of 2 or 1 lines (x 16 or 32 depths) instead of 4:
-// 4.26 and 4.34 ms.
+// 4.26 and 4.34 ms; 2 pixel warps x 8 channel warps (32 channels per pass,
+// half the passes and tables, half the pixel warps sharing a trace): 4.43.
 // Measured on the learned frame (128 ch, 75 plane waves, 512 x 1024): export
 // 4.83 ms with (kG, kPW, kCQ, kWL) = (4, 4, 4, 4) against 5.08 for
 // das_fast_kernel's best shape; (8, 4, 4, 4) 5.1, (8, 4, 4, 1) 5.6,
