@@ -114,3 +114,20 @@ def test_validation_maps_to_value_error():
         usx.Simulator(p, usx.Medium(), usx.Acquisition())
     with pytest.raises(ValueError):
         usx.ScanGrid.cartesian(0, 1, 0, 0, 1, 4)
+
+
+def test_launch_shape_table_without_gpu():
+    """The autotuner's launch-shape table is host metadata: 24 shapes in five
+    kernel families, variant 0 the default thread-per-pixel shape, the
+    channel-warp family (kind 4) with 4 pixel warps x 4 channel warps among
+    them, and an index past the table rejected."""
+    from usx import capi
+    v = capi.das_variants()
+    assert len(v) == 24
+    assert v[0] == (8, 4, 8, 1, 0, 0)
+    assert sorted({x[5] for x in v}) == [0, 1, 2, 3, 4]
+    assert (4, 4, 0, 4, 0, 4) in v      # das_export_kernel / das_csum_kernel <4, 4, 4, 4>
+    assert any(x[4] == 1 for x in v)    # deepest depth tiles first
+    lib = capi.lib()
+    kind = C.c_int(-1)
+    assert lib.usx_cu_bf_variant_kind(len(v), C.byref(kind)) != 0

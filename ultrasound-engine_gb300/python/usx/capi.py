@@ -497,7 +497,9 @@ class Mlp:
 def das_variants() -> list:
     """(channel group, tile lines, min resident CTAs, lines per warp, deepest
     tiles first, kind) of each delay-and-sum variant; kind 0: thread per
-    pixel, 1: staged trace windows, 2: transmit table."""
+    pixel, 1: staged trace windows, 2: transmit table, 3: producer-warp ring,
+    4: channel warps with a per-pixel transmit table (tile lines = pixel
+    warps)."""
     out = []
     for i in range(lib().usx_cu_bf_variant_count()):
         g, t, m, w, d, k = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
